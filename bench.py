@@ -1,0 +1,363 @@
+"""Benchmark of the MCL sensor update: scored particle*points per second.
+
+Workload (default): one filter of 100,000 particles (Gaussian, sigma 0.3 m / 5 deg)
+x 8,192 scan points (64x2048 ray-cast, sigma 0.02 m, 1 % dropouts, reduced and
+subsampled) in a seeded 100x100x10 m building mapped at 0.05 m.  One step = one
+sensor update (transform, lookup, score, per-particle sum, normalisation, mean
+pose) plus one systematic resampling, on the same particle poses every step as
+the reference's own timing loop does (num_particles_eval.cpp:237-257).
+
+Arms:
+  default            libtsdfl on cuda (device-resident inputs) + e2e through the
+                     host C ABI + roofline of the scoring kernel + CPU baseline
+  --impl reference   the reference's CPU sensor update (its own sources where
+                     they were compiled on this machine, else the CPU
+                     restatement) on a bounded sample of the same workload
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "scored particle*points/s at 100k x 8k"
+UNIT = "particle*points/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="building", choices=["building", "room"])
+    ap.add_argument("--particles", type=int, default=None)
+    ap.add_argument("--points", type=int, default=None)
+    ap.add_argument("--layout", default="dense", choices=["dense", "brick"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload(args):
+    from tsdf_localization_gb300 import synth
+    if args.workload == "room":
+        wl = synth.room_workload(seed=1, n_particles=args.particles or 1000, n_points=args.points or 2048)
+    else:
+        wl = synth.building_workload(seed=2, n_particles=args.particles or 100_000, n_points=args.points or 8192)
+    return wl
+
+
+def roofline_bytes(P: int, N: int, layout: str) -> float:
+    """Algorithmic bytes of one scoring launch: per particle*point the slot
+    reads (brick reference 4 B + 2 B code, or 2 B in the dense layout), per
+    particle 56 B (pose in, weight, index, pose out), per point 12 B."""
+    bpp = 2 if layout == "dense" else 6
+    return float(bpp) * P * N + 56.0 * P + 12.0 * N
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(wl, target_s: float = 10.0) -> dict:
+    """The reference CPU sensor update + resampling on a bounded particle sample."""
+    from oracle import oracle_py as O
+    kind = "reference" if O.reference_available() else "port"
+    om = O.OracleMap(O.coef_from(wl.coef), wl.grid_occ, wl.float_data())
+    N = wl.points.shape[0]
+    if kind == "reference":
+        rm = _reference_map(O, wl)
+    P_s = min(wl.particles.shape[0], 512)
+    rate = None
+    while True:
+        parts = wl.particles[:P_s].copy()
+        t0 = time.perf_counter()
+        if kind == "reference":
+            r = rm.evaluate(parts, wl.points, wl.tf, serial=False)
+            O.ref_resample_systematic(parts[:, 6], 1)
+        else:
+            r = O.evaluate(om, parts, wl.points, wl.tf)
+            O.resample_systematic(parts[:, 6], float(np.float32(0.5 / P_s)))
+        dt = time.perf_counter() - t0
+        rate = P_s * N / dt
+        if dt * 4 > target_s or P_s >= wl.particles.shape[0]:
+            break
+        P_s = min(wl.particles.shape[0], int(P_s * max(2.0, target_s / max(dt, 1e-3) / 2)))
+    cores = os.cpu_count() or 1
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"{P_s} particles x {N} points, one update + resample, {dt:.2f} s"}, (P_s, kind, om,
+                                                                                             rm if kind == "reference" else None)
+
+
+def _reference_map(O, wl):
+    """The map loaded into the reference's own CudaSubVoxelMap."""
+    return O.RefMap.from_slots(wl.coef, wl.grid_occ, wl.float_data())
+
+
+def run_reference_arm(args, rank: int) -> None:
+    if rank != 0:
+        return
+    wl = make_workload(args)
+    base, (P_s, kind, om, rm) = cpu_baseline(wl, target_s=5.0)
+    N = wl.points.shape[0]
+    times = []
+    for i in range(args.warmup + args.steps):
+        parts = wl.particles[:P_s].copy()
+        t0 = time.perf_counter()
+        if kind == "reference":
+            rm.evaluate(parts, wl.points, wl.tf, serial=False)
+            from oracle import oracle_py as O
+            O.ref_resample_systematic(parts[:, 6], 1 + i)
+        else:
+            from oracle import oracle_py as O
+            O.evaluate(om, parts, wl.points, wl.tf)
+            O.resample_systematic(parts[:, 6], float(np.float32(0.5 / P_s)))
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    t = float(np.sum(times))
+    value = P_s * N * len(times) / t
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t / len(times),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": wl.name, "particles": int(wl.particles.shape[0]), "points": int(N),
+                      "sample_particles": int(P_s)},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": kind,
+                            "sample": f"{P_s} particles x {N} points per step"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    from tsdf_localization_gb300 import Context, DeviceMap
+    from tsdf_localization_gb300 import _native as N
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    wl = make_workload(args)
+    P = int(wl.particles.shape[0])
+    Npts = int(wl.points.shape[0])
+    lib = N.lib()
+    ctx = Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=(args.layout == "dense"))
+    info = dmap.info()
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    tf = np.ascontiguousarray(wl.tf, np.float32)
+    tfp = tf.ctypes.data_as(C.c_void_p)
+    cap = 2 * P + 16
+    d_part = torch.from_numpy(wl.particles).to(f"cuda:{local}")
+    d_pts = torch.from_numpy(wl.points).to(f"cuda:{local}")
+    d_out = torch.empty((cap, 7), dtype=torch.float32, device=f"cuda:{local}")
+    d_cnt = torch.zeros(4, dtype=torch.int32, device=f"cuda:{local}")
+    d_pose = torch.zeros(8, dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    ctx.reserve(P, Npts)
+    rng = np.random.default_rng(1234 + rank)
+    vp = C.c_void_p
+
+    def step():
+        N.check(lib.tsdfl_evaluate_device(ctx.handle, dmap.handle, C.byref(model), vp(d_part.data_ptr()), P,
+                                          vp(d_pts.data_ptr()), Npts, tfp, N.TSDFL_SUM_EXACT,
+                                          vp(d_pose.data_ptr())))
+        u0 = float(np.float32(rng.random() / P))
+        N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(d_part.data_ptr()), P, u0,
+                                                     vp(d_out.data_ptr()), cap, vp(d_cnt.data_ptr())))
+
+    lib.tsdfl_ctx_set_timing(ctx.handle, 1)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        ctx.sync()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.tsdfl_launch_count()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kern_ms = []
+        with ClockSampler(local) as clk:
+            for i in range(args.steps):
+                flush.zero_()                       # L2 flush outside the timed step
+                starts[i].record(stream)
+                step()
+                ends[i].record(stream)
+                ends[i].synchronize()
+                k = C.c_float()
+                N.check(lib.tsdfl_ctx_last_timing(ctx.handle, C.byref(k)))
+                kern_ms.append(k.value)
+            ctx.sync()
+            torch.cuda.synchronize()
+        launches = lib.tsdfl_launch_count() - l0
+        clocks = clk.summary()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    value = P * Npts * args.steps * world / (total_ms / 1000.0)
+    lib.tsdfl_ctx_set_timing(ctx.handle, 0)
+
+    # roofline of the scoring kernel
+    kmed = float(np.median(kern_ms))
+    alg = roofline_bytes(P, Npts, args.layout)
+    peak, peak_src = measured_peaks()
+    achieved = alg / (kmed / 1000.0) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "eval_exact_kernel", "kernel_ms": kmed, "peak_source": peak_src,
+            "algorithmic_bytes": alg}
+
+    # end to end through the host C ABI, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_part = torch.empty((P, 7), dtype=torch.float32).pin_memory().numpy()
+        h_pts = torch.empty((Npts, 3), dtype=torch.float32).pin_memory().numpy()
+        h_w = torch.empty(P, dtype=torch.float32).pin_memory().numpy()
+        h_idx = torch.empty(cap, dtype=torch.int32).pin_memory().numpy()
+        h_pts[:] = wl.points
+        pose = np.zeros(6, np.float32)
+        cnt = C.c_size_t()
+
+        def e2e_step(i):
+            h_part[:] = wl.particles
+            N.check(lib.tsdfl_evaluate(ctx.handle, dmap.handle, C.byref(model), h_part.ctypes.data_as(vp), P,
+                                       h_pts.ctypes.data_as(vp), Npts, tfp, N.TSDFL_SUM_EXACT,
+                                       pose.ctypes.data_as(vp)))
+            h_w[:] = h_part[:, 6]
+            N.check(lib.tsdfl_resample_systematic(ctx.handle, h_w.ctypes.data_as(vp), P,
+                                                  np.float32(rng.random() / P), h_idx.ctypes.data_as(vp), cap,
+                                                  C.byref(cnt)))
+            return cnt.value
+
+        with torch.cuda.stream(stream):
+            for i in range(args.warmup):
+                e2e_step(i)
+            tt = []
+            counts = []
+            for i in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                counts.append(e2e_step(i))
+                tt.append(time.perf_counter() - t0)
+        e2e_s = float(np.sum(tt))
+        h2d = 28 * P + 12 * Npts + 4 * P
+        d2h = 28 * P + 4 * 6 + 4 + 4 * cap
+        e2e = {"value": P * Npts * args.steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s / args.steps}
+
+    base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        base, _ = cpu_baseline(wl)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": wl.name, "particles": P, "points": Npts, "voxel_m": wl.voxel_mm / 1000.0,
+                          "layout": args.layout, "map_bricks": int(info["bricks"]),
+                          "map_device_bytes": int(info["device_bytes"]), "sums": "exact fixed point",
+                          "l2": "flushed (512 MB write) before every timed step",
+                          "step": "sensor update + normalise + mean pose + systematic resample",
+                          "parallelism": f"replicas x{world}"},
+               "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
+               "clocks": clocks}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

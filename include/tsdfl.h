@@ -1,0 +1,178 @@
+/*
+ * tsdfl -- GB300-native MCL sensor update for TSDF maps (C ABI).
+ *
+ * Drop-in for the sensor-update path of uos/tsdf_localization:
+ *   transform the scan by every particle's pose, look each point up in the
+ *   likelihood map built from the TSDF, score, sum per particle, normalise,
+ *   mean pose, systematic resampling.
+ * Every entry point names the reference interface it replaces.  All functions
+ * return a tsdfl status; tsdfl_last_error() gives the message of the last
+ * failure on the calling thread.  Sizes are element counts.  Pointers named
+ * d_* are device pointers; all other array pointers are host memory.
+ */
+#ifndef TSDFL_H
+#define TSDFL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference throws std::runtime_error instead) ---- */
+#define TSDFL_OK 0
+#define TSDFL_ERR_INVALID_ARG 1
+#define TSDFL_ERR_OUT_OF_MEMORY 2
+#define TSDFL_ERR_DEGENERATE 3   /* weight sum 0 or not finite: "No particle is valid!" */
+#define TSDFL_ERR_DEVICE 4       /* CUDA error (cudaCheck, cuda_util.cu:8-17) */
+#define TSDFL_ERR_TIMEOUT 5      /* a bounded device wait ran out */
+#define TSDFL_ERR_CAPACITY 6     /* an output buffer is too small */
+#define TSDFL_ERR_UNSUPPORTED 7
+
+/* Same field order, types and size (120 bytes on LP64) as
+ * CudaSubVoxelMap<float,float>::MapCoef (include/tsdf_localization/cuda/
+ * cuda_sub_voxel_map.h:22-50), so &map.coef() can be passed directly. */
+typedef struct tsdfl_map_coef {
+    uint64_t dim_x, dim_y, dim_z;
+    float min_x, min_y, min_z;
+    float max_x, max_y, max_z;
+    float resolution;
+    float init_value;
+    uint64_t up_dim_x, up_dim_y, up_dim_z, up_dim_2;
+    uint64_t sub_dim, sub_dim_2;
+    uint64_t grid_occ_size, data_size;
+} tsdfl_map_coef;
+
+/* Sensor model of TSDFEvaluator / CudaEvaluator
+ * (tsdf_evaluator.h:72-80, cuda_evaluator.h:112). */
+typedef struct tsdfl_model {
+    float a_hit, a_range, a_max, max_range;
+} tsdfl_model;
+
+typedef struct tsdfl_ctx tsdfl_ctx;
+typedef struct tsdfl_map tsdfl_map;
+
+const char* tsdfl_last_error(void);
+const char* tsdfl_version(void);
+
+/* ---- context: one device, one stream, a growable workspace ----
+ * Replaces the device-buffer ownership of CudaEvaluator
+ * (cuda_evaluator.cu:136-209, 239-261); unlike the reference, nothing is
+ * process-global, so several maps and contexts can coexist. */
+int tsdfl_ctx_create(int device, tsdfl_ctx** out);
+int tsdfl_ctx_destroy(tsdfl_ctx* ctx);
+/* Use the caller's cudaStream_t (NULL = the context's own stream). */
+int tsdfl_ctx_set_stream(tsdfl_ctx* ctx, void* cuda_stream);
+void* tsdfl_ctx_stream(tsdfl_ctx* ctx);
+/* Waits for the stream and returns the status raised by device work since the
+ * last sync (e.g. TSDFL_ERR_DEGENERATE from tsdfl_evaluate_device). */
+int tsdfl_ctx_sync(tsdfl_ctx* ctx);
+/* Pre-sizes the workspace for P particles and N points so that later calls
+ * allocate nothing (needed before capturing calls into a CUDA graph). */
+int tsdfl_ctx_reserve(tsdfl_ctx* ctx, size_t P, size_t N);
+
+/* Device timing of the scoring kernels of the next evaluations (CUDA events
+ * on the context stream) and the number of kernels this library launched in
+ * the process so far. */
+int tsdfl_ctx_set_timing(tsdfl_ctx* ctx, int enable);
+int tsdfl_ctx_last_timing(tsdfl_ctx* ctx, float* eval_kernel_ms);
+uint64_t tsdfl_launch_count(void);
+
+/* ---- map ----
+ * Uploads a built CudaSubVoxelMap<float,float> (coef(), rawGridOcc(),
+ * rawData(); replaces the map upload in the CudaEvaluator ctor,
+ * cuda_evaluator.cu:21-59).  When every slot equals one of the likelihood
+ * values of createTSDFMap for `sigma` (map_util.h:68-71,124-127), slots are
+ * stored as 16-bit codes, losslessly; otherwise as float.  flags: TSDFL_MAP_*. */
+#define TSDFL_MAP_DENSE 1u        /* also build the one-gather dense brick layout */
+#define TSDFL_MAP_FORCE_F32 2u    /* keep float slots */
+int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
+                     float sigma, uint32_t flags, tsdfl_map** out);
+/* Same map from 16-bit slot codes (code c < 600: likelihood of |tsdf| = c mm;
+ * 600: the init value), as tsdfl_build_map_codes produces them. */
+int tsdfl_map_create_codes(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ,
+                           const uint16_t* codes, float sigma, uint32_t flags, tsdfl_map** out);
+int tsdfl_map_destroy(tsdfl_map* map);
+
+typedef struct tsdfl_map_info {
+    uint64_t grid_occ_size, data_size, bricks;
+    uint64_t device_bytes;     /* all device memory the map holds */
+    int32_t storage;           /* 0 = 16-bit codes, 1 = float */
+    int32_t dense;             /* dense layout present */
+} tsdfl_map_info;
+int tsdfl_map_get_info(const tsdfl_map* map, tsdfl_map_info* info);
+
+/* Likelihood-map construction of createTSDFMap (map_util.h:17-154) from TSDF
+ * cells, without HDF5: n_chunks chunks of edge^3 raw cells (low int16 = value
+ * in mm, high int16 = weight, tsdf.h:11-33; cell index edge*edge*i+edge*j+k),
+ * chunk coordinates in chunk_pos (3 ints each), in the order the map file lists
+ * them.  edge = 64 and voxel_mm = 64 give the reference's map exactly.
+ * Outputs (malloc'd, free with tsdfl_free): grid_occ[coef.grid_occ_size],
+ * slot codes[coef.data_size] and the free-space cell positions (xyz). */
+int tsdfl_build_map_codes(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
+                          int voxel_mm, float sigma, tsdfl_map_coef* coef, int32_t** grid_occ,
+                          uint16_t** codes, float** free_xyz, size_t* n_free);
+/* The float value of every code for sigma (601 entries: codes 0..600). */
+int tsdfl_code_values(float sigma, float init_value, float* out601);
+void tsdfl_free(void* p);
+
+/* ---- sensor update ----
+ * TSDFEvaluator::evaluate(particles, points, tf, use_cuda)
+ * (tsdf_evaluator.cpp:78-245) / CudaEvaluator::evaluate
+ * (cuda_evaluator.cu:118-428).
+ * particles: P x 7 floats (x, y, z, roll, pitch, yaw, weight) -- the layout of
+ *   struct Particle (particle.h:26-55); weights are overwritten with the
+ *   normalised weights, as the reference does.
+ * points: N x 3 floats (struct CudaPoint, cuda_evaluator.h:22-39).
+ * tf: the 4x4 row-major sensor-to-base transform (tsdf_evaluator.cpp:271-284).
+ * pose_out (optional): weighted mean x, y, z and circular-mean roll, pitch, yaw.
+ * N == 0 returns TSDFL_OK and leaves everything untouched
+ * (cuda_evaluator.cu:122-125).  Weight sum 0 -> TSDFL_ERR_DEGENERATE. */
+#define TSDFL_SUM_EXACT 0u    /* order-independent fixed-point likelihood sums (default) */
+#define TSDFL_SUM_SERIAL 1u   /* reference order float sums: raw weights bit-identical */
+int tsdfl_evaluate(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles, size_t P,
+                   const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6]);
+
+/* Per-particle diagnostics of one evaluation (host arrays, each optional):
+ * raw weights (evaluatePose sums), hit counts (points whose slot index is
+ * inside the map data), and for small cases the slot index of every
+ * particle*point (0xffffffff on a miss).  Also returns the weight sum. */
+typedef struct tsdfl_eval_debug {
+    float* raw_weights;       /* [P] */
+    uint32_t* hits;           /* [P] */
+    uint32_t* voxel_index;    /* [P*N] */
+    float* laser_pose;        /* [P*12] tf_laser of every particle */
+    double weight_sum;
+} tsdfl_eval_debug;
+int tsdfl_evaluate_debug(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles,
+                         size_t P, const float* points, size_t N, const float tf[16], uint32_t flags,
+                         float pose_out[6], tsdfl_eval_debug* dbg);
+
+/* Stream-ordered form on device buffers (no host synchronisation; errors that
+ * only the device sees are reported by tsdfl_ctx_sync).  d_particles: P x 7
+ * floats, updated in place with the normalised weights; d_points: N x 3;
+ * d_pose_out: 6 floats or NULL.  Allocates only when the workspace must grow
+ * (see tsdfl_ctx_reserve). */
+int tsdfl_evaluate_device(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* d_particles,
+                          size_t P, const float* d_points, size_t N, const float tf[16], uint32_t flags,
+                          float* d_pose_out);
+
+/* ---- systematic resampling ----
+ * SystematicResampler::resample (novel_resampling.h:41-72) with its uniform
+ * draw u0 in [0, 1/M) given.  Writes the source particle index of every
+ * emitted particle (up to cap) and the count the reference emits, which is not
+ * always M.  Bit-exact with the reference for the same weights and u0. */
+int tsdfl_resample_systematic(tsdfl_ctx* ctx, const float* weights, size_t M, float u0, uint32_t* idx_out,
+                              size_t cap, size_t* count_out);
+/* Device form: gathers the resampled particles (P x 7 floats) from d_particles
+ * into d_particles_out (capacity cap particles) and writes the count to
+ * *d_count (device).  Weights are the last field of every particle. */
+int tsdfl_resample_systematic_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
+                                     float* d_particles_out, size_t cap, uint32_t* d_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

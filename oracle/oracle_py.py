@@ -1,0 +1,296 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes binding of the oracle libraries.
+
+  oracle/_build/liboracle.so  CPU restatement of the reference sensor update
+  oracle/_ref/libref.so       the reference's own CPU sources (where built)
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+P = C.c_void_p
+SZ = C.c_size_t
+
+
+class Coef(C.Structure):
+    _fields_ = [
+        ("dim_x", C.c_uint64), ("dim_y", C.c_uint64), ("dim_z", C.c_uint64),
+        ("min_x", C.c_float), ("min_y", C.c_float), ("min_z", C.c_float),
+        ("max_x", C.c_float), ("max_y", C.c_float), ("max_z", C.c_float),
+        ("resolution", C.c_float), ("init_value", C.c_float),
+        ("up_dim_x", C.c_uint64), ("up_dim_y", C.c_uint64), ("up_dim_z", C.c_uint64), ("up_dim_2", C.c_uint64),
+        ("sub_dim", C.c_uint64), ("sub_dim_2", C.c_uint64),
+        ("grid_occ_size", C.c_uint64), ("data_size", C.c_uint64),
+    ]
+
+
+class Model(C.Structure):
+    _fields_ = [("a_hit", C.c_float), ("a_range", C.c_float), ("a_max", C.c_float), ("max_range", C.c_float)]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def coef_from(src) -> Coef:
+    """Copy of a MapCoef-like ctypes structure (same 120-byte layout)."""
+    c = Coef()
+    C.memmove(C.byref(c), C.byref(src), C.sizeof(Coef))
+    return c
+
+
+_orc = None
+_ref = None
+
+
+def oracle() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        path = HERE / "_build" / "liboracle.so"
+        if not path.exists():
+            raise ImportError("oracle/_build/liboracle.so is not built")
+        L = C.CDLL(str(path))
+        L.orc_f2u_x86.restype = C.c_uint64
+        L.orc_f2u_x86.argtypes = [C.c_float]
+        L.orc_map_coef_init.argtypes = [C.POINTER(Coef), P, P, C.c_float, C.c_float]
+        L.orc_map_set_data.argtypes = [C.POINTER(Coef), P, P, SZ, C.POINTER(P), C.POINTER(SZ)]
+        L.orc_get_index.restype = C.c_uint64
+        L.orc_get_index.argtypes = [C.POINTER(Coef), P, C.c_float, C.c_float, C.c_float]
+        L.orc_get_entry.restype = C.c_float
+        L.orc_get_entry.argtypes = [C.POINTER(Coef), P, P, C.c_float, C.c_float, C.c_float]
+        L.orc_particle_pose.argtypes = [P, P, P]
+        L.orc_evaluate.argtypes = [C.POINTER(Coef), P, P, C.POINTER(Model), P, SZ, P, SZ, P, P, P, P, P, P, C.c_int]
+        L.orc_likelihood_value.restype = C.c_float
+        L.orc_likelihood_value.argtypes = [C.c_int16, C.c_float]
+        L.orc_likelihood_init.restype = C.c_float
+        L.orc_likelihood_init.argtypes = [C.c_float]
+        L.orc_build_map_from_chunks.argtypes = [P, P, SZ, C.c_int, C.c_float, C.POINTER(Coef), C.POINTER(P),
+                                                C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
+        L.orc_resample_systematic.restype = SZ
+        L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
+        _orc = L
+    return _orc
+
+
+def reference_available() -> bool:
+    return (HERE / "_ref" / "libref.so").exists()
+
+
+def reference() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        path = HERE / "_ref" / "libref.so"
+        if not path.exists():
+            raise ImportError("oracle/_ref/libref.so is not built (the reference tree is not on this machine)")
+        L = C.CDLL(str(path))
+        L.ref_map_create.restype = P
+        L.ref_map_create.argtypes = [P, P, C.c_float, C.c_float, P, SZ]
+        L.ref_map_destroy.argtypes = [P]
+        L.ref_map_from_slots.restype = P
+        L.ref_map_from_slots.argtypes = [P, P, P]
+        L.ref_map_coef.argtypes = [P, P]
+        L.ref_map_grid_occ.restype = P
+        L.ref_map_grid_occ.argtypes = [P]
+        L.ref_map_data.restype = P
+        L.ref_map_data.argtypes = [P]
+        L.ref_map_get_entry.restype = C.c_float
+        L.ref_map_get_entry.argtypes = [P, C.c_float, C.c_float, C.c_float]
+        L.ref_evaluate.restype = C.c_int
+        L.ref_evaluate.argtypes = [P, P, P, SZ, P, SZ, P, P, P, P, C.c_int]
+        L.ref_draw_u0.restype = C.c_float
+        L.ref_draw_u0.argtypes = [C.c_uint32, SZ]
+        L.ref_resample_systematic.restype = SZ
+        L.ref_resample_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
+        L.ref_omp_threads.restype = C.c_int
+        _ref = L
+    return _ref
+
+
+# ------------------------------------------------------------------ restatement
+
+class OracleMap:
+    """A map in the reference's float-slot representation."""
+
+    def __init__(self, coef: Coef, grid_occ: np.ndarray, data: np.ndarray):
+        self.coef = coef
+        self.grid_occ = np.ascontiguousarray(grid_occ, np.int32)
+        self.data = np.ascontiguousarray(data, np.float32)
+
+    @staticmethod
+    def from_tuples(mn, mx, res: float, init: float, xyzv: np.ndarray) -> "OracleMap":
+        L = oracle()
+        c = Coef()
+        L.orc_map_coef_init(C.byref(c), _ptr(np.asarray(mn, np.float32)), _ptr(np.asarray(mx, np.float32)), res,
+                            init)
+        go = np.zeros(max(c.grid_occ_size, 1), np.int32)
+        t = np.ascontiguousarray(xyzv, np.float32)
+        dp = P()
+        skipped = SZ()
+        rc = L.orc_map_set_data(C.byref(c), _ptr(go), _ptr(t), t.shape[0], C.byref(dp), C.byref(skipped))
+        if rc != 0:
+            raise RuntimeError("Upper voxel index overflow!")
+        data = np.zeros(0, np.float32)
+        if dp.value:
+            data = np.ctypeslib.as_array(C.cast(dp, C.POINTER(C.c_float)), (max(c.data_size, 1),))[
+                : c.data_size].copy()
+            C.CDLL(None).free(dp)
+        m = OracleMap(c, go[: c.grid_occ_size], data)
+        m.skipped = skipped.value
+        return m
+
+    @staticmethod
+    def from_chunks(chunk_pos: np.ndarray, chunks: np.ndarray, voxel_mm: int = 64, sigma: float = 0.1):
+        L = oracle()
+        c = Coef()
+        go, dp, fp = P(), P(), P()
+        nf = SZ()
+        pos = np.ascontiguousarray(chunk_pos, np.int32)
+        raw = np.ascontiguousarray(chunks, np.uint32)
+        rc = L.orc_build_map_from_chunks(_ptr(pos), _ptr(raw), pos.shape[0], voxel_mm, sigma, C.byref(c),
+                                         C.byref(go), C.byref(dp), C.byref(fp), C.byref(nf))
+        if rc != 0:
+            raise RuntimeError("Upper voxel index overflow!")
+        libc = C.CDLL(None)
+        g = np.ctypeslib.as_array(C.cast(go, C.POINTER(C.c_int32)), (max(c.grid_occ_size, 1),))[
+            : c.grid_occ_size].copy()
+        d = np.zeros(0, np.float32)
+        if dp.value:
+            d = np.ctypeslib.as_array(C.cast(dp, C.POINTER(C.c_float)), (max(c.data_size, 1),))[: c.data_size].copy()
+        f = np.ctypeslib.as_array(C.cast(fp, C.POINTER(C.c_float)), (max(nf.value, 1) * 3,))[
+            : 3 * nf.value].reshape(-1, 3).copy()
+        for p in (go, dp, fp):
+            if p.value:
+                libc.free(p)
+        return OracleMap(c, g, d), f
+
+    def get_index(self, x, y, z) -> int:
+        return oracle().orc_get_index(C.byref(self.coef), _ptr(self.grid_occ), x, y, z)
+
+    def get_entry(self, x, y, z) -> float:
+        d = self.data if self.data.size else None
+        return oracle().orc_get_entry(C.byref(self.coef), _ptr(self.grid_occ), _ptr(d), x, y, z)
+
+
+def evaluate(m: OracleMap, particles: np.ndarray, points: np.ndarray, tf, model=(0.9, 0.1, 0.0, 100.0),
+             want_idx: bool = False, threads: int = 0) -> dict:
+    """TSDFEvaluator::evaluate CPU path; particles (P,7) float32 updated in place."""
+    L = oracle()
+    Pn, Nn = particles.shape[0], points.shape[0]
+    pts = np.ascontiguousarray(points, np.float32)
+    tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(16))
+    raw = np.zeros(Pn, np.float32)
+    hits = np.zeros(Pn, np.uint32)
+    s64 = np.zeros(Pn, np.float64)
+    idx = np.zeros((Pn, Nn), np.uint64) if want_idx else None
+    pose = np.zeros(6, np.float32)
+    mdl = Model(*model)
+    d = m.data if m.data.size else None
+    rc = L.orc_evaluate(C.byref(m.coef), _ptr(m.grid_occ), _ptr(d), C.byref(mdl), _ptr(particles), Pn, _ptr(pts),
+                        Nn, _ptr(tfa), _ptr(raw), _ptr(hits), _ptr(idx), _ptr(s64), _ptr(pose), threads)
+    return {"rc": rc, "raw": raw, "hits": hits, "sum64": s64, "voxel_index": idx, "pose": pose}
+
+
+def particle_pose(particle7, tf) -> np.ndarray:
+    out = np.zeros(12, np.float32)
+    oracle().orc_particle_pose(_ptr(np.ascontiguousarray(particle7, np.float32)),
+                               _ptr(np.ascontiguousarray(np.asarray(tf, np.float32).reshape(16))), _ptr(out))
+    return out
+
+
+def resample_systematic(weights: np.ndarray, u0: float, cap: int | None = None) -> np.ndarray:
+    w = np.ascontiguousarray(weights, np.float32)
+    cap = cap if cap is not None else 2 * w.shape[0] + 16
+    out = np.zeros(max(cap, 1), np.uint32)
+    n = oracle().orc_resample_systematic(_ptr(w), w.shape[0], np.float32(u0), _ptr(out), cap)
+    if n == (1 << 64) - 1:
+        raise RuntimeError("U stopped advancing")
+    return out[:n]
+
+
+def likelihood_value(mm: int, sigma: float = 0.1) -> float:
+    return oracle().orc_likelihood_value(mm, sigma)
+
+
+def likelihood_init(sigma: float = 0.1) -> float:
+    return oracle().orc_likelihood_init(sigma)
+
+
+# ------------------------------------------------------------------ reference
+
+class RefMap:
+    """CudaSubVoxelMap<float,float> built by the reference's own ctor + setData."""
+
+    @staticmethod
+    def from_slots(coef, grid_occ: np.ndarray, data: np.ndarray) -> "RefMap":
+        L = reference()
+        self = RefMap.__new__(RefMap)
+        c = coef_from(coef)
+        go = np.ascontiguousarray(grid_occ, np.int32)
+        d = np.ascontiguousarray(data, np.float32)
+        self.h = L.ref_map_from_slots(C.byref(c), _ptr(go), _ptr(d))
+        if not self.h:
+            raise RuntimeError("reference map construction failed")
+        self.coef = Coef()
+        L.ref_map_coef(self.h, C.byref(self.coef))
+        return self
+
+    def __init__(self, mn, mx, res: float, init: float, xyzv: np.ndarray):
+        L = reference()
+        t = np.ascontiguousarray(xyzv, np.float32)
+        self.h = L.ref_map_create(_ptr(np.asarray(mn, np.float32)), _ptr(np.asarray(mx, np.float32)), res, init,
+                                  _ptr(t), t.shape[0])
+        if not self.h:
+            raise RuntimeError("Upper voxel index overflow!")
+        self.coef = Coef()
+        L.ref_map_coef(self.h, C.byref(self.coef))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            reference().ref_map_destroy(self.h)
+            self.h = None
+
+    def grid_occ(self) -> np.ndarray:
+        p = reference().ref_map_grid_occ(self.h)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_int32)), (max(self.coef.grid_occ_size, 1),))[
+            : self.coef.grid_occ_size].copy()
+
+    def data(self) -> np.ndarray:
+        p = reference().ref_map_data(self.h)
+        if not p:
+            return np.zeros(0, np.float32)
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_float)), (max(self.coef.data_size, 1),))[
+            : self.coef.data_size].copy()
+
+    def get_entry(self, x, y, z) -> float:
+        return reference().ref_map_get_entry(self.h, x, y, z)
+
+    def evaluate(self, particles: np.ndarray, points: np.ndarray, tf, model=(0.9, 0.1, 0.0, 100.0),
+                 serial: bool = True) -> dict:
+        L = reference()
+        Pn = particles.shape[0]
+        raw = np.zeros(Pn, np.float32)
+        poses = np.zeros((Pn, 12), np.float32)
+        pose = np.zeros(6, np.float32)
+        mdl = np.asarray(model, np.float32)
+        pts = np.ascontiguousarray(points, np.float32)
+        tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(16))
+        rc = L.ref_evaluate(self.h, _ptr(mdl), _ptr(particles), Pn, _ptr(pts), pts.shape[0], _ptr(tfa), _ptr(raw),
+                            _ptr(poses), _ptr(pose), 1 if serial else 0)
+        return {"rc": rc, "raw": raw, "laser_pose": poses, "pose": pose}
+
+
+def ref_draw_u0(seed: int, m: int) -> float:
+    return reference().ref_draw_u0(seed, m)
+
+
+def ref_resample_systematic(weights: np.ndarray, seed: int, cap: int | None = None) -> np.ndarray:
+    w = np.ascontiguousarray(weights, np.float32)
+    cap = cap if cap is not None else 2 * w.shape[0] + 16
+    out = np.zeros(max(cap, 1), np.uint32)
+    n = reference().ref_resample_systematic(_ptr(w), w.shape[0], seed, _ptr(out), cap)
+    return out[:n]

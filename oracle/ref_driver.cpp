@@ -1,0 +1,219 @@
+// TEST INFRASTRUCTURE ONLY -- NOT PART OF THE PRODUCT.
+//
+// C entry points around the reference's own sources, compiled verbatim from
+// the reference tree by oracle/Makefile (tier-A oracle):
+//   include/tsdf_localization/cuda/cuda_sub_voxel_map.{h,tcc}  (map, getEntry)
+//   src/evaluation/tsdf_evaluator.cpp                          (CPU sensor update)
+//   src/evaluation/model/likelihood_evaluation.cpp             (linked by evaluate)
+//   include/tsdf_localization/resampling/novel_resampling.h    (SystematicResampler)
+// Used by the CPU tests to pin oracle/tsdf_oracle.c bit for bit, and as the
+// timed CPU baseline where it can be built.
+#include <tsdf_localization/evaluation/tsdf_evaluator.h>
+#include <tsdf_localization/resampling/novel_resampling.h>
+#include <tsdf_localization/util/constant.h>
+
+#include <omp.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+namespace tsdf_localization {
+
+// TSDFEvaluator's ctor always builds a CudaEvaluator (tsdf_evaluator.h:78); its
+// definitions live in CUDA sources (cuda_evaluator.cu) that the CPU path never
+// calls, so inert definitions stand in for them here.
+CudaEvaluator::CudaEvaluator(CudaSubVoxelMap<FLOAT_T, FLOAT_T>&, bool, FLOAT_T, FLOAT_T, FLOAT_T, FLOAT_T)
+    : d_map_(nullptr), per_point_(false), d_grid_occ_(nullptr), d_data_(nullptr), d_particles_(nullptr),
+      d_particles_ordered_(nullptr), particles_reserved_(0), d_points_(nullptr), d_points_ordered_(nullptr),
+      points_reserved_(0), d_transform_(nullptr), d_new_weights_(nullptr), d_point_weights_(nullptr),
+      point_weights_size_(0) {}
+geometry_msgs::PoseWithCovariance CudaEvaluator::evaluate(std::vector<Particle>&, const sensor_msgs::PointCloud2&, FLOAT_T*)
+{
+    throw std::runtime_error("CUDA evaluator is not part of the oracle build");
+}
+geometry_msgs::PoseWithCovariance CudaEvaluator::evaluate(std::vector<Particle>&, const std::vector<CudaPoint>&, FLOAT_T*)
+{
+    throw std::runtime_error("CUDA evaluator is not part of the oracle build");
+}
+CudaEvaluator::~CudaEvaluator() {}
+
+// The three ParticleCloud members SystematicResampler::resample uses
+// (particle_cloud.h:82,186,191); the rest of particle_cloud.cpp needs ROS.
+ParticleCloud::ParticleCloud() {}
+Particle& ParticleCloud::operator[](unsigned int index)
+{
+    if (index >= size()) throw std::out_of_range("Index exceeds number of particles");
+    return m_particles[index];
+}
+std::size_t ParticleCloud::size() const { return m_particles.size(); }
+
+}  // namespace tsdf_localization
+
+using namespace tsdf_localization;
+using Map = CudaSubVoxelMap<FLOAT_T, FLOAT_T>;
+
+namespace {
+
+// Records what the reference's evaluatePose receives and returns, per particle,
+// when the evaluation runs on one thread.
+struct ProbeEvaluator : TSDFEvaluator {
+    using TSDFEvaluator::TSDFEvaluator;
+    mutable bool record = false;
+    mutable std::vector<float> raw, poses;
+    FLOAT_T evaluatePose(FLOAT_T* pose, const std::vector<CudaPoint> cloud, EvaluationModel& model) const override
+    {
+        FLOAT_T w = TSDFEvaluator::evaluatePose(pose, cloud, model);
+        if (record) {
+            raw.push_back(w);
+            poses.insert(poses.end(), pose, pose + 12);
+        }
+        return w;
+    }
+};
+
+struct SeededSystematic : SystematicResampler {
+    explicit SeededSystematic(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
+};
+
+struct MapHandle {
+    std::shared_ptr<Map> map;
+};
+
+}  // namespace
+
+extern "C" {
+
+void* ref_map_create(const float mn[3], const float mx[3], float res, float init, const float* xyzv, size_t n)
+{
+    auto h = new MapHandle;
+    h->map = std::make_shared<Map>(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2], res, init);
+    std::vector<std::tuple<FLOAT_T, FLOAT_T, FLOAT_T, FLOAT_T>> data;
+    data.reserve(n);
+    for (size_t i = 0; i < n; ++i) data.emplace_back(xyzv[4 * i], xyzv[4 * i + 1], xyzv[4 * i + 2], xyzv[4 * i + 3]);
+    try {
+        h->map->setData(data);
+    } catch (const std::exception&) {
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+// A reference map holding the given slots: built by the reference ctor from the
+// coefficients' bounds, then its arrays replaced through the public raw-pointer
+// accessors (cuda_sub_voxel_map.h:131-159, 309-312).
+void* ref_map_from_slots(const void* coef_in, const int32_t* grid_occ, const float* data)
+{
+    Map::MapCoef c;
+    std::memcpy(&c, coef_in, sizeof(c));
+    auto h = new MapHandle;
+    h->map = std::make_shared<Map>(c.min_x_, c.min_y_, c.min_z_, c.max_x_, c.max_y_, c.max_z_, c.resolution_,
+                                   c.init_value_);
+    if (h->map->coef().grid_occ_size_ != c.grid_occ_size_) {
+        delete h;
+        return nullptr;
+    }
+    std::memcpy(h->map->rawGridOcc(), grid_occ, sizeof(OCC_T) * c.grid_occ_size_);
+    float* d = new float[c.data_size_ ? c.data_size_ : 1];
+    std::memcpy(d, data, sizeof(float) * c.data_size_);
+    *h->map->rawDataPtr() = d;
+    h->map->coef().data_size_ = c.data_size_;
+    return h;
+}
+
+void ref_map_destroy(void* h) { delete static_cast<MapHandle*>(h); }
+
+void ref_map_coef(void* h, void* out)
+{
+    static_assert(sizeof(Map::MapCoef) == 120, "MapCoef layout");
+    std::memcpy(out, &static_cast<MapHandle*>(h)->map->coef(), sizeof(Map::MapCoef));
+}
+
+const int32_t* ref_map_grid_occ(void* h) { return static_cast<MapHandle*>(h)->map->rawGridOcc(); }
+const float* ref_map_data(void* h) { return static_cast<MapHandle*>(h)->map->rawData(); }
+
+float ref_map_get_entry(void* h, float x, float y, float z)
+{
+    return static_cast<MapHandle*>(h)->map->getEntry(x, y, z);
+}
+
+// One TSDFEvaluator::evaluate(..., use_cuda=false).  particles: AoS 7 floats,
+// weights overwritten with the normalised weight.  serial != 0 runs the OpenMP
+// loops on one thread (deterministic weight sum) and records, per particle, the
+// laser pose (12 floats) and the un-normalised weight.  Returns 0, or 1 on
+// "No particle is valid!".
+int ref_evaluate(void* h, const float model[4], float* particles, size_t P, const float* points, size_t N,
+                 const float tf[16], float* raw_out, float* pose12_out, float pose_out[6], int serial)
+{
+    auto* mh = static_cast<MapHandle*>(h);
+    ProbeEvaluator ev(mh->map, false, model[0], model[1], model[2], model[3]);
+    std::vector<Particle> ps(P);
+    for (size_t i = 0; i < P; ++i) {
+        for (int k = 0; k < 6; ++k) ps[i].first[k] = particles[7 * i + k];
+        ps[i].second = particles[7 * i + 6];
+    }
+    std::vector<CudaPoint> pts(N);
+    for (size_t j = 0; j < N; ++j) pts[j] = CudaPoint(points[3 * j], points[3 * j + 1], points[3 * j + 2]);
+    FLOAT_T tfm[16];
+    std::memcpy(tfm, tf, sizeof(tfm));
+    int old_levels = omp_get_max_active_levels();
+    if (serial) {
+        omp_set_max_active_levels(0);
+        ev.record = true;
+    }
+    int rc = 0;
+    geometry_msgs::PoseWithCovariance pose;
+    try {
+        pose = ev.evaluate(ps, pts, tfm, false);
+    } catch (const std::runtime_error&) {
+        rc = 1;
+    }
+    omp_set_max_active_levels(old_levels);
+    if (rc) return rc;
+    for (size_t i = 0; i < P; ++i) particles[7 * i + 6] = ps[i].second;
+    if (serial) {
+        if (raw_out) std::memcpy(raw_out, ev.raw.data(), sizeof(float) * ev.raw.size());
+        if (pose12_out) std::memcpy(pose12_out, ev.poses.data(), sizeof(float) * ev.poses.size());
+    }
+    if (pose_out) {
+        pose_out[0] = (float)pose.pose.position.x;
+        pose_out[1] = (float)pose.pose.position.y;
+        pose_out[2] = (float)pose.pose.position.z;
+        for (int k = 0; k < 3; ++k) pose_out[3 + k] = (float)tf2::rpy_hook()[k];
+    }
+    return 0;
+}
+
+// The draw SystematicResampler makes first (novel_resampling.h:44-49).
+float ref_draw_u0(uint32_t seed, size_t M)
+{
+    std::mt19937 g(seed);
+    auto inverse_M = 1.0 / M;
+    std::uniform_real_distribution<FLOAT_T> d(0.0, inverse_M);
+    return d(g);
+}
+
+// SystematicResampler::resample on weights w with its generator seeded by seed;
+// writes the source index of every emitted particle.  Returns the count.
+size_t ref_resample_systematic(const float* w, size_t M, uint32_t seed, uint32_t* idx_out, size_t cap)
+{
+    ParticleCloud cloud;
+    cloud.particles().resize(M);
+    for (size_t i = 0; i < M; ++i) {
+        for (int k = 0; k < 6; ++k) cloud.particles()[i].first[k] = 0;
+        cloud.particles()[i].first[0] = (float)i;
+        cloud.particles()[i].second = w[i];
+    }
+    SeededSystematic r(seed);
+    r.resample(cloud);
+    size_t n = cloud.particles().size();
+    for (size_t i = 0; i < n && i < cap; ++i) idx_out[i] = (uint32_t)cloud.particles()[i].first[0];
+    return n;
+}
+
+int ref_omp_threads(void) { return (int)OMP_THREADS; }
+
+}  // extern "C"

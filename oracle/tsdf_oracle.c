@@ -1,0 +1,359 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- NOT PART OF THE PRODUCT.
+ *
+ * CPU restatement of the uos/tsdf_localization sensor update (the oracle).
+ * Every function cites the reference lines it restates.  Build flags (see
+ * oracle/Makefile): -O2 -ffp-contract=off -fopenmp, no -march, no fast-math,
+ * so float expressions round exactly as written on both x86-64 and aarch64.
+ *
+ * Two platform-dependent points of the reference are pinned here:
+ *  - float -> size_t conversions are out of range for negative or huge map
+ *    offsets; the reference's Release build on x86-64 gives the cvttss2si
+ *    results, which orc_f2u_x86 reproduces with integer code.
+ *  - sin/cos/atan2 of float arguments bind to the double-precision libm
+ *    functions (the result rounded to float), i.e. the correctly rounded value.
+ */
+#include "tsdf_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#define TWO63F 9223372036854775808.0f
+#define SIGN64 0x8000000000000000ull
+
+uint64_t orc_f2u_x86(float v)
+{
+    if (v != v) return SIGN64;                        /* cvttss2si of NaN: integer indefinite */
+    if (v < TWO63F) {
+        if (v >= -TWO63F) return (uint64_t)(int64_t)v; /* truncation, two's complement wrap */
+        return SIGN64;
+    }
+    float w = v - TWO63F;                             /* exact: both multiples of 2^40 */
+    if (w < TWO63F) return ((uint64_t)(int64_t)w) ^ SIGN64;
+    return 0;                                         /* indefinite ^ sign bit */
+}
+
+/* cuda_sub_voxel_map.tcc:4-48 */
+void orc_map_coef_init(orc_map_coef* c, const float mn[3], const float mx[3],
+                       float resolution, float init_value)
+{
+    memset(c, 0, sizeof(*c));
+    c->dim_x = (uint64_t)ceilf(fabsf(mx[0] - mn[0]) / resolution);
+    c->dim_y = (uint64_t)ceilf(fabsf(mx[1] - mn[1]) / resolution);
+    c->dim_z = (uint64_t)ceilf(fabsf(mx[2] - mn[2]) / resolution);
+    c->min_x = mn[0]; c->min_y = mn[1]; c->min_z = mn[2];
+    c->max_x = mx[0]; c->max_y = mx[1]; c->max_z = mx[2];
+    c->resolution = resolution;
+    c->init_value = init_value;
+    c->up_dim_x = (uint64_t)ceilf(fabsf(mx[0] - mn[0]) / 1.0f);
+    c->up_dim_y = (uint64_t)ceilf(fabsf(mx[1] - mn[1]) / 1.0f);
+    c->up_dim_z = (uint64_t)ceilf(fabsf(mx[2] - mn[2]) / 1.0f);
+    c->up_dim_2 = c->up_dim_x * c->up_dim_y;
+    c->sub_dim = (uint64_t)ceilf(1.0f / resolution);
+    c->sub_dim_2 = c->sub_dim * c->sub_dim;
+    c->grid_occ_size = c->up_dim_x * c->up_dim_y * c->up_dim_z;
+    c->data_size = 0;
+}
+
+/* cuda_sub_voxel_map.tcc:50-137 (track_reuse_ off, as on the evaluation path) */
+uint64_t orc_get_index(const orc_map_coef* c, const int32_t* grid_occ, float x, float y, float z)
+{
+    uint64_t gx = orc_f2u_x86(x - c->min_x);
+    uint64_t gy = orc_f2u_x86(y - c->min_y);
+    uint64_t gz = orc_f2u_x86(z - c->min_z);
+    gx = orc_f2u_x86((float)gx / c->resolution);
+    gy = orc_f2u_x86((float)gy / c->resolution);
+    gz = orc_f2u_x86((float)gz / c->resolution);
+    if (gx >= c->dim_x || gy >= c->dim_y || gz >= c->dim_z) return c->data_size;
+
+    float ox = x - c->min_x, oy = y - c->min_y, oz = z - c->min_z;
+    uint64_t ux = orc_f2u_x86(ox / 1.0f);
+    uint64_t uy = orc_f2u_x86(oy / 1.0f);
+    uint64_t uz = orc_f2u_x86(oz / 1.0f);
+    float sx = ox - (float)ux * 1.0f;
+    float sy = oy - (float)uy * 1.0f;
+    float sz = oz - (float)uz * 1.0f;
+    uint64_t up = ux + uy * c->up_dim_x + uz * c->up_dim_2;
+    if (up >= c->grid_occ_size) return c->data_size;
+    int32_t base = grid_occ[up];
+    if (base < 0) return c->data_size;
+    uint64_t qx = orc_f2u_x86(sx / c->resolution);
+    uint64_t qy = orc_f2u_x86(sy / c->resolution);
+    uint64_t qz = orc_f2u_x86(sz / c->resolution);
+    return (uint64_t)(int64_t)base + qx + qy * c->sub_dim + qz * c->sub_dim_2;
+}
+
+/* cuda_sub_voxel_map.tcc:139-157 */
+float orc_get_entry(const orc_map_coef* c, const int32_t* grid_occ, const float* data,
+                    float x, float y, float z)
+{
+    if (data == NULL || grid_occ == NULL) return c->init_value;
+    uint64_t i = orc_get_index(c, grid_occ, x, y, z);
+    return i < c->data_size ? data[i] : c->init_value;
+}
+
+/* cuda_sub_voxel_map.tcc:170-230 */
+int orc_map_set_data(orc_map_coef* c, int32_t* grid_occ, const float* xyzv, size_t n,
+                     float** data_out, size_t* skipped)
+{
+    *data_out = NULL;
+    if (skipped) *skipped = 0;
+    for (uint64_t i = 0; i < c->grid_occ_size; ++i) grid_occ[i] = -1;
+    if (n == 0) return 0;
+    for (size_t t = 0; t < n; ++t) {
+        const float* cell = xyzv + 4 * t;
+        uint64_t ux = orc_f2u_x86((cell[0] - c->min_x) / 1.0f);
+        uint64_t uy = orc_f2u_x86((cell[1] - c->min_y) / 1.0f);
+        uint64_t uz = orc_f2u_x86((cell[2] - c->min_z) / 1.0f);
+        uint64_t up = ux + uy * c->up_dim_x + uz * c->up_dim_x * c->up_dim_y;
+        if (up >= c->grid_occ_size) return -1; /* "Upper voxel index overflow!" */
+        grid_occ[up] = 0;
+    }
+    int32_t offset = 0;
+    int32_t sub_size = (int32_t)(c->sub_dim * c->sub_dim * c->sub_dim);
+    for (uint64_t i = 0; i < c->grid_occ_size; ++i) {
+        if (grid_occ[i] >= 0) { grid_occ[i] = offset; offset += sub_size; }
+    }
+    c->data_size = (uint64_t)offset;
+    float* data = (float*)malloc(sizeof(float) * (c->data_size ? c->data_size : 1));
+    for (uint64_t i = 0; i < c->data_size; ++i) data[i] = c->init_value;
+    for (size_t t = 0; t < n; ++t) {
+        const float* cell = xyzv + 4 * t;
+        uint64_t i = orc_get_index(c, grid_occ, cell[0], cell[1], cell[2]);
+        if (i < c->data_size) data[i] = cell[3];
+        else if (skipped) ++*skipped;   /* the reference writes data_[data_size]: not reproduced */
+    }
+    *data_out = data;
+    return 0;
+}
+
+static inline float trig_sin(float a) { return (float)sin((double)a); }
+static inline float trig_cos(float a) { return (float)cos((double)a); }
+
+/* tsdf_evaluator.cpp:102-147 */
+void orc_particle_pose(const float p[7], const float tf[16], float tl[12])
+{
+    float alpha = p[3], beta = p[4], gamma = p[5];
+    float sin_alpha = trig_sin(alpha), cos_alpha = trig_cos(alpha);
+    float sin_beta = trig_sin(beta), cos_beta = trig_cos(beta);
+    float sin_gamma = trig_sin(gamma), cos_gamma = trig_cos(gamma);
+    float t[12];
+    t[0] = cos_beta * cos_gamma;
+    t[4] = cos_beta * sin_gamma;
+    t[8] = -sin_beta;
+    t[3] = p[0];
+    t[1] = sin_alpha * sin_beta * cos_gamma - cos_alpha * sin_gamma;
+    t[5] = sin_alpha * sin_beta * sin_gamma + cos_alpha * cos_gamma;
+    t[9] = sin_alpha * cos_beta;
+    t[7] = p[1];
+    t[2] = cos_alpha * sin_beta * cos_gamma + sin_alpha * sin_gamma;
+    t[6] = cos_alpha * sin_beta * sin_gamma - sin_alpha * cos_gamma;
+    t[10] = cos_alpha * cos_beta;
+    t[11] = p[2];
+    for (int r = 0; r < 3; ++r) {
+        const float* a = t + 4 * r;
+        tl[4 * r + 0] = a[0] * tf[0] + a[1] * tf[4] + a[2] * tf[8];
+        tl[4 * r + 1] = a[0] * tf[1] + a[1] * tf[5] + a[2] * tf[9];
+        tl[4 * r + 2] = a[0] * tf[2] + a[1] * tf[6] + a[2] * tf[10];
+        tl[4 * r + 3] = a[0] * tf[3] + a[1] * tf[7] + a[2] * tf[11] + a[3];
+    }
+}
+
+/* tsdf_evaluator.cpp:78-245; the point loop is evaluatePose, :27-76 */
+int orc_evaluate(const orc_map_coef* c, const int32_t* grid_occ, const float* data,
+                 const orc_model* m, float* particles, size_t P,
+                 const float* points, size_t N, const float tf[16],
+                 float* raw_out, uint32_t* hits_out, uint64_t* idx_out,
+                 double* sum64_out, float pose_out[6], int n_threads)
+{
+    const float a_hit = m->a_hit, a_range = m->a_range, a_max = m->a_max;
+    const float inv_max_range = (float)(1.0 / (double)m->max_range);
+    const float max_range_squared = m->max_range * m->max_range;
+    const int have_map = (data != NULL && grid_occ != NULL);
+    float* raw = (float*)malloc(sizeof(float) * (P ? P : 1));
+
+    const int nt = n_threads > 0 ? n_threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic) num_threads(nt)
+    for (size_t i = 0; i < P; ++i) {
+        float tl[12];
+        orc_particle_pose(particles + 7 * i, tf, tl);
+        float eval_sum = 0.0f;
+        double sum64 = 0.0;
+        uint32_t hits = 0;
+        for (size_t j = 0; j < N; ++j) {
+            float x = points[3 * j], y = points[3 * j + 1], z = points[3 * j + 2];
+            float tx = tl[0] * x + tl[1] * y + tl[2] * z + tl[3];
+            float ty = tl[4] * x + tl[5] * y + tl[6] * z + tl[7];
+            float tz = tl[8] * x + tl[9] * y + tl[10] * z + tl[11];
+            uint64_t idx = have_map ? orc_get_index(c, grid_occ, tx, ty, tz) : c->data_size;
+            float value = c->init_value;
+            if (idx < c->data_size) { value = data[idx]; ++hits; }
+            if (idx_out) idx_out[i * N + j] = idx;
+            float square_dist = x * x + y * y + z * z;
+            if (square_dist < max_range_squared) value = a_hit * value + a_range * inv_max_range;
+            else value = a_hit * value + a_max;
+            eval_sum += value;
+            sum64 += (double)value;
+        }
+        raw[i] = eval_sum;
+        if (raw_out) raw_out[i] = eval_sum;
+        if (hits_out) hits_out[i] = hits;
+        if (sum64_out) sum64_out[i] = sum64;
+    }
+
+    float weight_sum = 0.0f;
+    for (size_t i = 0; i < P; ++i) weight_sum += raw[i];
+    if (weight_sum == 0.0f) { free(raw); return 1; }   /* "No particle is valid!" */
+
+    float avg_x = 0, avg_y = 0, avg_z = 0;
+    float sum_sin_roll = 0, sum_cos_roll = 0, sum_sin_pitch = 0, sum_cos_pitch = 0;
+    float sum_sin_yaw = 0, sum_cos_yaw = 0;
+    for (size_t i = 0; i < P; ++i) {
+        float* p = particles + 7 * i;
+        p[6] = raw[i] / weight_sum;
+        avg_x += p[0] * p[6];
+        avg_y += p[1] * p[6];
+        avg_z += p[2] * p[6];
+        sum_sin_roll = (float)((double)sum_sin_roll + sin((double)p[3]) * (double)p[6]);
+        sum_cos_roll = (float)((double)sum_cos_roll + cos((double)p[3]) * (double)p[6]);
+        sum_sin_pitch = (float)((double)sum_sin_pitch + sin((double)p[4]) * (double)p[6]);
+        sum_cos_pitch = (float)((double)sum_cos_pitch + cos((double)p[4]) * (double)p[6]);
+        sum_sin_yaw = (float)((double)sum_sin_yaw + sin((double)p[5]) * (double)p[6]);
+        sum_cos_yaw = (float)((double)sum_cos_yaw + cos((double)p[5]) * (double)p[6]);
+    }
+    if (pose_out) {
+        pose_out[0] = avg_x; pose_out[1] = avg_y; pose_out[2] = avg_z;
+        pose_out[3] = (float)atan2((double)sum_sin_roll, (double)sum_cos_roll);
+        pose_out[4] = (float)atan2((double)sum_sin_pitch, (double)sum_cos_pitch);
+        pose_out[5] = (float)atan2((double)sum_sin_yaw, (double)sum_cos_yaw);
+    }
+    free(raw);
+    return 0;
+}
+
+/* map_util.h:124-127 */
+float orc_likelihood_value(int16_t tsdf_mm, float sigma)
+{
+    float sigma_quad = sigma * sigma;
+    float tsdf_value = (float)tsdf_mm;
+    double value = (double)tsdf_value * 0.001;
+    value = (double)(expf((float)(-(value * value) / (double)sigma_quad / 2))
+                     / sqrtf((float)((double)(2 * sigma_quad) * M_PI)));
+    value = value * value * value;
+    return (float)value;
+}
+
+/* map_util.h:68-71 */
+float orc_likelihood_init(float sigma)
+{
+    float sigma_quad = sigma * sigma;
+    float init = expf((float)(-(10.0 * 10.0) / (double)sigma_quad / 2))
+                 / sqrtf((float)((double)(2 * sigma_quad) * M_PI));
+    init = init * init * init;
+    return init;
+}
+
+typedef struct { char name[48]; size_t index; } chunk_tag;
+
+static int cmp_tag(const void* a, const void* b)
+{
+    return strcmp(((const chunk_tag*)a)->name, ((const chunk_tag*)b)->name);
+}
+
+/* map_util.h:17-154 (HighFive lists "/map" members in increasing name order) */
+int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks,
+                              int voxel_mm, float sigma, orc_map_coef* c, int32_t** grid_occ_out,
+                              float** data_out, float** free_xyz_out, size_t* n_free_out)
+{
+    const int CH = 64;
+    float mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    for (size_t k = 0; k < n_chunks; ++k)
+        for (int a = 0; a < 3; ++a) {
+            int coord = chunk_pos[3 * k + a];
+            if ((float)coord < mn[a]) mn[a] = (float)coord;
+            if ((float)coord > mx[a]) mx[a] = (float)coord;
+        }
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = (float)((double)(mn[a] * (float)CH * (float)voxel_mm) * 0.001);
+        mx[a] = (float)((double)((mx[a] * (float)CH + (float)CH) * (float)voxel_mm) * 0.001);
+    }
+    float init = orc_likelihood_init(sigma);
+    orc_map_coef_init(c, mn, mx, (float)(voxel_mm * 0.001), init);
+
+    float lut[600];
+    for (int v = 0; v < 600; ++v) lut[v] = orc_likelihood_value((int16_t)v, sigma);
+
+    chunk_tag* tags = (chunk_tag*)malloc(sizeof(chunk_tag) * (n_chunks ? n_chunks : 1));
+    for (size_t k = 0; k < n_chunks; ++k) {
+        snprintf(tags[k].name, sizeof(tags[k].name), "%d_%d_%d",
+                 chunk_pos[3 * k], chunk_pos[3 * k + 1], chunk_pos[3 * k + 2]);
+        tags[k].index = k;
+    }
+    qsort(tags, n_chunks, sizeof(chunk_tag), cmp_tag);
+
+    size_t cap = 1 << 16, n = 0, fcap = 1 << 16, nf = 0;
+    float* tuples = (float*)malloc(sizeof(float) * 4 * cap);
+    float* freep = (float*)malloc(sizeof(float) * 3 * fcap);
+    for (size_t t = 0; t < n_chunks; ++t) {
+        size_t k = tags[t].index;
+        const uint32_t* raw = chunks + (size_t)k * CH * CH * CH;
+        const int32_t* cp = chunk_pos + 3 * k;
+        for (int i = 0; i < CH; i++)
+            for (int j = 0; j < CH; j++)
+                for (int l = 0; l < CH; l++) {
+                    uint32_t e = raw[CH * CH * i + CH * j + l];
+                    int16_t val = (int16_t)(uint16_t)(e & 0xffffu);
+                    int16_t wgt = (int16_t)(uint16_t)(e >> 16);
+                    float tsdf_value = (float)val;
+                    if (wgt == 0) continue;
+                    int x = CH * cp[0] + i, y = CH * cp[1] + j, z = CH * cp[2] + l;
+                    float px = (float)((double)((float)x * (float)voxel_mm) * 0.001);
+                    float py = (float)((double)((float)y * (float)voxel_mm) * 0.001);
+                    float pz = (float)((double)((float)z * (float)voxel_mm) * 0.001);
+                    if (fabsf(tsdf_value) < 600.0f) {
+                        if (n == cap) { cap *= 2; tuples = (float*)realloc(tuples, sizeof(float) * 4 * cap); }
+                        int av = val < 0 ? -val : val;
+                        tuples[4 * n] = px; tuples[4 * n + 1] = py; tuples[4 * n + 2] = pz;
+                        tuples[4 * n + 3] = lut[av];
+                        ++n;
+                    } else {
+                        if (nf == fcap) { fcap *= 2; freep = (float*)realloc(freep, sizeof(float) * 3 * fcap); }
+                        freep[3 * nf] = px; freep[3 * nf + 1] = py; freep[3 * nf + 2] = pz;
+                        ++nf;
+                    }
+                }
+    }
+    free(tags);
+    int32_t* grid_occ = (int32_t*)malloc(sizeof(int32_t) * (c->grid_occ_size ? c->grid_occ_size : 1));
+    float* data = NULL;
+    int rc = orc_map_set_data(c, grid_occ, tuples, n, &data, NULL);
+    free(tuples);
+    *grid_occ_out = grid_occ;
+    *data_out = data;
+    *free_xyz_out = freep;
+    *n_free_out = nf;
+    return rc;
+}
+
+/* novel_resampling.h:41-72 */
+size_t orc_resample_systematic(const float* w, size_t M, float U0, uint32_t* idx_out, size_t cap)
+{
+    double inverse_M = 1.0 / (double)M;
+    float U = U0;
+    double s = 0.0;
+    size_t n = 0;
+    for (size_t m = 0; m < M; ++m) {
+        s += (double)w[m];
+        while (s > (double)U) {
+            if (n < cap) idx_out[n] = (uint32_t)m;
+            ++n;
+            float next = (float)((double)U + inverse_M);
+            if (next == U) return (size_t)-1;   /* the reference would loop forever */
+            U = next;
+        }
+    }
+    return n;
+}

@@ -1,0 +1,107 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- NOT PART OF THE PRODUCT.
+ *
+ * CPU restatement ("the oracle") of the uos/tsdf_localization MCL sensor update
+ * and systematic resampler.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py may load it; the CUDA library never
+ * links or calls it.
+ *
+ * Parity pin: on x86-64 every function here is checked bit-for-bit against the
+ * reference's own sources compiled verbatim (oracle/ref_driver.cpp built by
+ * oracle/Makefile into oracle/_ref/).  The restatement is written so that it
+ * gives the same bits on x86-64 and aarch64 (explicit x86 float->size_t
+ * conversion semantics, no FP contraction, double-precision libm trig).
+ */
+#ifndef TSDF_ORACLE_H
+#define TSDF_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same field order and types as CudaSubVoxelMap<float,float>::MapCoef
+ * (include/tsdf_localization/cuda/cuda_sub_voxel_map.h:22-50). */
+typedef struct orc_map_coef {
+    uint64_t dim_x, dim_y, dim_z;
+    float min_x, min_y, min_z;
+    float max_x, max_y, max_z;
+    float resolution;
+    float init_value;
+    uint64_t up_dim_x, up_dim_y, up_dim_z, up_dim_2;
+    uint64_t sub_dim, sub_dim_2;
+    uint64_t grid_occ_size, data_size;
+} orc_map_coef;
+
+/* Sensor-model parameters (TSDFEvaluator ctor, tsdf_evaluator.h:72-80). */
+typedef struct orc_model {
+    float a_hit, a_range, a_max, max_range;
+} orc_model;
+
+/* float -> size_t exactly as gcc emits it on x86-64 (cvttss2si based). */
+uint64_t orc_f2u_x86(float v);
+
+/* CudaSubVoxelMap ctor (cuda_sub_voxel_map.tcc:4-48). */
+void orc_map_coef_init(orc_map_coef* c, const float mn[3], const float mx[3],
+                       float resolution, float init_value);
+
+/* CudaSubVoxelMap::setData (cuda_sub_voxel_map.tcc:170-230).  grid_occ must
+ * hold grid_occ_size ints; *data_out is malloc'd (NULL when n == 0, as in the
+ * reference where data_ stays nullptr).  Returns 0, or -1 on "Upper voxel index
+ * overflow!".  Writes that the reference makes out of bounds (getIndex miss
+ * inside setEntry) are skipped and counted in *skipped. */
+int orc_map_set_data(orc_map_coef* c, int32_t* grid_occ, const float* xyzv, size_t n,
+                     float** data_out, size_t* skipped);
+
+/* CudaSubVoxelMap::getIndex / getEntry (cuda_sub_voxel_map.tcc:50-157). */
+uint64_t orc_get_index(const orc_map_coef* c, const int32_t* grid_occ, float x, float y, float z);
+float orc_get_entry(const orc_map_coef* c, const int32_t* grid_occ, const float* data,
+                    float x, float y, float z);
+
+/* Per-particle laser pose tf_laser[0..11] (tsdf_evaluator.cpp:102-147). */
+void orc_particle_pose(const float particle7[7], const float tf[16], float out12[12]);
+
+/* TSDFEvaluator::evaluate CPU path (tsdf_evaluator.cpp:78-245) with serial
+ * per-particle sums (exactly as evaluatePose, :27-76) and a serial weight sum.
+ * particles: AoS of 7 floats (x,y,z,roll,pitch,yaw,weight); weights are
+ * overwritten with the normalised weight.  Optional outputs may be NULL:
+ *   raw_out[P]     un-normalised weight (eval_sum of evaluatePose)
+ *   hits_out[P]    number of points whose index < data_size
+ *   idx_out[P*N]   voxel index per particle·point (data_size on a miss)
+ *   sum64_out[P]   the same per-point scores accumulated in double
+ *   pose_out[6]    x,y,z,roll,pitch,yaw of the weighted mean
+ * n_threads <= 0 uses all OpenMP threads.  Returns 0, 1 when the weight sum is
+ * zero ("No particle is valid!"). */
+int orc_evaluate(const orc_map_coef* c, const int32_t* grid_occ, const float* data,
+                 const orc_model* m, float* particles, size_t P,
+                 const float* points, size_t N, const float tf[16],
+                 float* raw_out, uint32_t* hits_out, uint64_t* idx_out,
+                 double* sum64_out, float pose_out[6], int n_threads);
+
+/* Likelihood value of one TSDF cell (map_util.h:124-127): |tsdf| in mm. */
+float orc_likelihood_value(int16_t tsdf_mm, float sigma);
+/* Value of untouched cells (map_util.h:68-71). */
+float orc_likelihood_init(float sigma);
+
+/* createTSDFMap (map_util.h:17-154) without HDF5.  chunk_pos: 3 ints per chunk
+ * (chunk coordinates), chunks: n_chunks blocks of 64^3 uint32 raw TSDF values
+ * (low int16 = value in mm, high int16 = weight, tsdf.h:11-33) in the order the
+ * file lists them.  voxel_mm generalises the fixed 64 mm MAP_RESOLUTION.
+ * Outputs the map coef, a malloc'd grid_occ, a malloc'd data array and the
+ * free-space point list (malloc'd xyz triples). */
+int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks,
+                              int voxel_mm, float sigma, orc_map_coef* c, int32_t** grid_occ_out,
+                              float** data_out, float** free_xyz_out, size_t* n_free_out);
+
+/* SystematicResampler::resample (novel_resampling.h:41-72) with the uniform
+ * draw U0 supplied.  Writes up to cap source indices, returns the number of
+ * particles the reference would emit, or (size_t)-1 if U stops advancing. */
+size_t orc_resample_systematic(const float* w, size_t M, float U0, uint32_t* idx_out, size_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

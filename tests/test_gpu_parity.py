@@ -1,0 +1,204 @@
+"""GPU parity: the CUDA sensor update and resampler against the oracle.
+
+Bit-exact: laser poses, voxel (slot) indices, hit counts, serial-mode raw
+weights, resampled indices and counts.  Exact-mode weights (fixed-point
+likelihood sums): |gpu - fp64| <= 1e-5 |fp64| and never farther from the fp64
+sum than the reference-order float sum by more than that bound.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle_py as O
+from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator, TsdflError, synth
+
+pytestmark = pytest.mark.gpu
+
+MISS = 0xFFFFFFFF
+WEIGHT_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def room():
+    return synth.room_workload(seed=11, n_particles=600, n_points=2048)
+
+
+@pytest.fixture(scope="module")
+def room_oracle(room):
+    return O.OracleMap(O.coef_from(room.coef), room.grid_occ, room.float_data())
+
+
+def _oracle_eval(om, wl, particles=None, points=None, tf=None, model=(0.9, 0.1, 0.0, 100.0), want_idx=True):
+    p = (wl.particles if particles is None else particles).copy()
+    r = O.evaluate(om, p, wl.points if points is None else points, wl.tf if tf is None else tf, model,
+                   want_idx=want_idx)
+    r["particles"] = p
+    return r
+
+
+def _as_u32_index(idx, data_size):
+    return np.where(idx < data_size, idx, MISS).astype(np.uint32)
+
+
+@pytest.mark.parametrize("layout", ["brick", "dense"])
+def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout):
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"))
+    ev = TSDFEvaluator(dmap)
+    ref = _oracle_eval(room_oracle, room)
+    p = room.particles.copy()
+    d = ev.evaluate_debug(p, room.points, room.tf, voxel_index=True)
+    assert np.array_equal(d["hits"], ref["hits"])
+    if layout == "brick":
+        assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
+    else:  # the dense kernel reports slot codes
+        codes_ref = np.where(ref["voxel_index"] < room.coef.data_size,
+                             room.codes[np.minimum(ref["voxel_index"], room.coef.data_size - 1)], 601)
+        assert np.array_equal(d["voxel_index"], codes_ref.astype(np.uint32))
+    f64 = ref["sum64"]
+    err_gpu = np.abs(d["raw"].astype(np.float64) - f64)
+    err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
+    assert np.all(err_gpu <= WEIGHT_RTOL * np.abs(f64))
+    assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * np.abs(f64))
+    assert np.allclose(p[:, 6], ref["particles"][:, 6], rtol=WEIGHT_RTOL, atol=0)
+    assert np.allclose(d["pose"], ref["pose"], rtol=1e-5, atol=1e-5)
+    # inputs other than the weights untouched
+    assert np.array_equal(p[:, :6], room.particles[:, :6])
+
+
+def test_serial_mode_bit_exact(ctx, room, room_oracle):
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
+    ev = TSDFEvaluator(dmap, serial_sums=True)
+    ref = _oracle_eval(room_oracle, room)
+    p = room.particles.copy()
+    d = ev.evaluate_debug(p, room.points, room.tf, voxel_index=True)
+    assert np.array_equal(d["raw"], ref["raw"])
+    assert np.array_equal(d["hits"], ref["hits"])
+    assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
+    lp = np.stack([O.particle_pose(room.particles[i], room.tf) for i in range(room.particles.shape[0])])
+    assert np.array_equal(d["laser_pose"], lp)
+    assert np.allclose(p[:, 6], ref["particles"][:, 6], rtol=WEIGHT_RTOL, atol=0)
+
+
+def test_float_slot_map(ctx, room, room_oracle):
+    """A map uploaded as float slots (the CudaSubVoxelMap contents) converts to
+    codes losslessly; forced float storage gives the same results."""
+    for force in (False, True):
+        dmap = DeviceMap(ctx, room.coef, room.grid_occ, data=room.float_data(), force_f32=force)
+        assert dmap.info()["storage"] == (1 if force else 0)
+        ev = TSDFEvaluator(dmap, serial_sums=True)
+        ref = _oracle_eval(room_oracle, room, want_idx=False)
+        d = ev.evaluate_debug(room.particles.copy(), room.points, room.tf)
+        assert np.array_equal(d["raw"], ref["raw"])
+        ev2 = TSDFEvaluator(dmap)
+        d2 = ev2.evaluate_debug(room.particles.copy(), room.points, room.tf)
+        assert np.array_equal(d2["hits"], ref["hits"])
+        assert np.allclose(d2["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+
+
+def test_points_outside_map_and_negative_offsets(ctx, room, room_oracle):
+    """Points far outside the map, at negative offsets and in the (-1, 0) m band
+    where the reference's float->size_t conversions wrap."""
+    rng = np.random.default_rng(5)
+    pts = np.concatenate([
+        rng.uniform(-40, 40, size=(700, 3)),
+        rng.uniform(-1.0, 0.2, size=(300, 3)) + np.array([11.0, 11.0, -1.2]),
+        np.array([[1e20, 0, 0], [-1e20, 0, 0], [0, 0, -3e19], [np.inf, 0, 0], [5, 5, 1e10]]),
+    ]).astype(np.float32)
+    parts = synth.particles_gaussian([0.3, 0.4, 0.2, 0, 0, 0], 0.6, 0.2, 64, 9)
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=True)
+    for serial in (True, False):
+        ev = TSDFEvaluator(dmap, serial_sums=serial)
+        ref = _oracle_eval(room_oracle, room, particles=parts, points=pts)
+        d = ev.evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)
+        assert np.array_equal(d["hits"], ref["hits"])
+        if serial:
+            assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
+            assert np.array_equal(d["raw"], ref["raw"])
+
+
+def test_multi_pass_long_scan(ctx, room, room_oracle):
+    """Scans longer than one shared-memory pass (16384 exact, 8192 serial)."""
+    w = synth.World(synth.ROOM, 11)
+    xyz, ring = w.scan(room.true_pose, 32, 1024, seed=3)
+    pts = xyz[:20000]
+    parts = room.particles[:40].copy()
+    ref = _oracle_eval(room_oracle, room, particles=parts, points=pts, want_idx=False)
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
+    d = TSDFEvaluator(dmap, serial_sums=True).evaluate_debug(parts.copy(), pts, room.tf)
+    assert np.array_equal(d["raw"], ref["raw"])
+    d2 = TSDFEvaluator(dmap).evaluate_debug(parts.copy(), pts, room.tf)
+    assert np.array_equal(d2["hits"], ref["hits"])
+    assert np.allclose(d2["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+
+
+def test_empty_scan_leaves_particles(ctx, room):
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
+    p = room.particles.copy()
+    assert TSDFEvaluator(dmap).evaluate(p, np.zeros((0, 3), np.float32), room.tf) is None
+    assert np.array_equal(p, room.particles)
+
+
+def test_degenerate_weights_raise(ctx, room):
+    """All scores zero -> "No particle is valid!" and particles untouched."""
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
+    ev = TSDFEvaluator(dmap, a_hit=0.0, a_range=0.0, a_max=0.0)
+    p = room.particles.copy()
+    with pytest.raises(TsdflError, match="No particle is valid!"):
+        ev.evaluate(p, room.points, room.tf)
+    assert np.array_equal(p, room.particles)
+    # the context stays usable
+    p2 = room.particles.copy()
+    TSDFEvaluator(dmap).evaluate(p2, room.points, room.tf)
+    assert abs(float(p2[:, 6].astype(np.float64).sum()) - 1.0) < 1e-4
+
+
+def test_out_of_range_points_and_model(ctx, room, room_oracle):
+    """Points beyond max_range take a_max instead of a_range/max_range."""
+    model = (0.7, 0.2, 0.05, 6.0)
+    ref = _oracle_eval(room_oracle, room, model=model, want_idx=False)
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
+    d = TSDFEvaluator(dmap, a_hit=0.7, a_range=0.2, a_max=0.05, max_range=6.0, serial_sums=True).evaluate_debug(
+        room.particles.copy(), room.points, room.tf)
+    assert np.array_equal(d["raw"], ref["raw"])
+    d2 = TSDFEvaluator(dmap, a_hit=0.7, a_range=0.2, a_max=0.05, max_range=6.0).evaluate_debug(
+        room.particles.copy(), room.points, room.tf)
+    assert np.allclose(d2["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+
+
+def _random_weights(rng, m, kind):
+    if kind == "uniform":
+        w = np.full(m, 1.0 / m)
+    elif kind == "random":
+        w = rng.random(m)
+    elif kind == "peaked":
+        w = rng.random(m) ** 8
+    elif kind == "one":
+        w = np.zeros(m)
+        w[rng.integers(m)] = 1.0
+    elif kind == "tiny":   # weights below 2^-29: serial fallback on the device
+        w = rng.random(m)
+        w[: m // 3] = 1e-12
+    else:
+        raise ValueError(kind)
+    w = w / w.sum()
+    return w.astype(np.float32)
+
+
+@pytest.mark.parametrize("m", [1, 2, 7, 1000, 4096, 65537, 250000])
+@pytest.mark.parametrize("kind", ["uniform", "random", "peaked", "one", "tiny"])
+def test_resample_bit_exact(ctx, m, kind):
+    rng = np.random.default_rng(m * 31 + len(kind))
+    w = _random_weights(rng, m, kind)
+    rs = SystematicResampler(ctx, seed=m)
+    for u0 in (0.0, float(np.float32(0.5 / m)), float(np.nextafter(np.float32(1.0 / m), np.float32(0))),
+               rs.draw(m)):
+        got = rs.resample_indices(w, u0)
+        exp = O.resample_systematic(w, u0)
+        assert got.shape == exp.shape
+        assert np.array_equal(got, exp)

@@ -1,0 +1,706 @@
+// C ABI of the GB300 sensor update: contexts, maps, evaluation, resampling.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <atomic>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "map_host.h"
+#include "tsdfl.h"
+#include "tsdfl_internal.h"
+
+namespace tsdfl {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+}  // namespace tsdfl
+
+using namespace tsdfl;
+
+#define CUDA_TRY(expr)                                                                          \
+    do {                                                                                        \
+        cudaError_t _e = (expr);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            set_error("%s: %s (%s)", __func__, cudaGetErrorString(_e), #expr);                  \
+            return _e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE; \
+        }                                                                                       \
+    } while (0)
+
+namespace {
+
+constexpr int kSerialPassPoints = 8192;
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+namespace tsdfl {
+extern std::atomic<unsigned long long> g_launches;
+}
+
+struct tsdfl_ctx {
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t cap_P = 0, cap_N = 0;
+    void* ws = nullptr;          // per-evaluation workspace
+    size_t ws_bytes = 0;
+    void* rs_ws = nullptr;       // resampling workspace
+    size_t rs_bytes = 0;
+    void* io = nullptr;          // device copies of host inputs (host API)
+    size_t io_bytes = 0;
+    int32_t* status = nullptr;   // [0] sticky status, [1] per-evaluation status
+    int32_t* h_status = nullptr; // pinned
+    float* h_pose = nullptr;     // pinned, 8 floats
+    uint32_t* h_count = nullptr; // pinned
+    EvalBuffers buf{};
+    double* sum_f64 = nullptr;
+};
+
+struct tsdfl_map {
+    int device = 0;
+    tsdfl_map_coef coef{};
+    MapView view{};
+    int32_t* grid_occ = nullptr;
+    uint16_t* codes = nullptr;
+    float* data = nullptr;
+    uint16_t* dense = nullptr;
+    float* values = nullptr;      // kNumCodes likelihood values (device)
+    float max_value = 0;
+    uint64_t bricks = 0;
+    uint64_t bytes = 0;
+};
+
+namespace {
+
+int set_device(int dev)
+{
+    CUDA_TRY(cudaSetDevice(dev));
+    return TSDFL_OK;
+}
+
+// Carves the per-evaluation workspace for P particles and N points.
+int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
+{
+    if (P <= c->cap_P && N <= c->cap_N && c->ws) return TSDFL_OK;
+    size_t nP = P > c->cap_P ? P : c->cap_P;
+    size_t nN = N > c->cap_N ? N : c->cap_N;
+    if (nP < 1) nP = 1;
+    if (nN < 4) nN = 4;
+    size_t npad = align_up(nN, 4);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    size_t o_pose = take(sizeof(float) * 12 * nP);
+    size_t o_trig = take(sizeof(float) * 6 * nP);
+    size_t o_fx = take(sizeof(long long) * nP);
+    size_t o_f64 = take(sizeof(double) * nP);
+    size_t o_raw = take(sizeof(float) * nP);
+    size_t o_hits = take(sizeof(uint32_t) * nP);
+    size_t o_xs = take(sizeof(float) * npad);
+    size_t o_ys = take(sizeof(float) * npad);
+    size_t o_zs = take(sizeof(float) * npad);
+    size_t o_cs = take(sizeof(float) * npad);
+    size_t o_lfx = take(sizeof(long long) * kNumCodes);
+    size_t o_lf = take(sizeof(float) * kNumCodes);
+    size_t o_cnt = take(sizeof(int32_t) * 16);
+    size_t o_part = take(sizeof(double) * 256 * 10);
+    size_t o_sums = take(sizeof(double) * 16);
+    size_t o_wsf = take(sizeof(float) * 4);
+    size_t total = off;
+    void* ws = nullptr;
+    CUDA_TRY(cudaMalloc(&ws, total));
+    if (c->ws) cudaFree(c->ws);
+    c->ws = ws;
+    c->ws_bytes = total;
+    char* b = static_cast<char*>(ws);
+    EvalBuffers& e = c->buf;
+    e.pose12 = reinterpret_cast<float*>(b + o_pose);
+    e.trig6 = reinterpret_cast<float*>(b + o_trig);
+    e.sum_fx = reinterpret_cast<long long*>(b + o_fx);
+    c->sum_f64 = reinterpret_cast<double*>(b + o_f64);
+    e.raw = reinterpret_cast<float*>(b + o_raw);
+    e.hits = reinterpret_cast<uint32_t*>(b + o_hits);
+    e.xs = reinterpret_cast<float*>(b + o_xs);
+    e.ys = reinterpret_cast<float*>(b + o_ys);
+    e.zs = reinterpret_cast<float*>(b + o_zs);
+    e.cs = reinterpret_cast<float*>(b + o_cs);
+    e.lut_fx = reinterpret_cast<long long*>(b + o_lfx);
+    e.lut_f = reinterpret_cast<float*>(b + o_lf);
+    e.counts = reinterpret_cast<int32_t*>(b + o_cnt);
+    e.partials = reinterpret_cast<double*>(b + o_part);
+    e.sums = reinterpret_cast<double*>(b + o_sums);
+    e.weight_sum_f = reinterpret_cast<float*>(b + o_wsf);
+    e.status = c->status + 1;
+    c->cap_P = nP;
+    c->cap_N = nN;
+    return TSDFL_OK;
+}
+
+int ensure_resample_ws(tsdfl_ctx* c, size_t M)
+{
+    size_t need = resample_workspace_bytes(M);
+    if (need <= c->rs_bytes) return TSDFL_OK;
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, need));
+    if (c->rs_ws) cudaFree(c->rs_ws);
+    c->rs_ws = p;
+    c->rs_bytes = need;
+    return TSDFL_OK;
+}
+
+int ensure_io(tsdfl_ctx* c, size_t bytes)
+{
+    if (bytes <= c->io_bytes) return TSDFL_OK;
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, bytes));
+    if (c->io) cudaFree(c->io);
+    c->io = p;
+    c->io_bytes = bytes;
+    return TSDFL_OK;
+}
+
+int validate_coef(const tsdfl_map_coef* c)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    if (!(c->resolution > 0.0f) || !std::isfinite(c->resolution)) {
+        set_error("map: resolution must be positive");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (c->grid_occ_size != c->up_dim_x * c->up_dim_y * c->up_dim_z || c->up_dim_2 != c->up_dim_x * c->up_dim_y ||
+        c->sub_dim_2 != c->sub_dim * c->sub_dim) {
+        set_error("map: inconsistent coefficients");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    const uint64_t sub3 = c->sub_dim * c->sub_dim * c->sub_dim;
+    if (c->grid_occ_size >= (1ull << 31) || c->data_size + 4 * sub3 >= (1ull << 31) || c->sub_dim > 1024 ||
+        c->up_dim_x >= (1u << 22) || c->up_dim_y >= (1u << 22) || c->up_dim_z >= (1u << 22)) {
+        set_error("map: too large for 32-bit slot indices");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    return TSDFL_OK;
+}
+
+void fill_view(tsdfl_map* m)
+{
+    const tsdfl_map_coef& c = m->coef;
+    MapView& v = m->view;
+    v.min_x = c.min_x; v.min_y = c.min_y; v.min_z = c.min_z;
+    v.res = c.resolution;
+    v.init_value = c.init_value;
+    v.mmax_x = coarse_mmax(c.dim_x, c.resolution);
+    v.mmax_y = coarse_mmax(c.dim_y, c.resolution);
+    v.mmax_z = coarse_mmax(c.dim_z, c.resolution);
+    v.up_dim_x = (uint32_t)c.up_dim_x;
+    v.up_dim_2 = (uint32_t)c.up_dim_2;
+    v.grid_occ_size = (uint32_t)c.grid_occ_size;
+    v.sub_dim = (uint32_t)c.sub_dim;
+    v.sub_dim_2 = (uint32_t)c.sub_dim_2;
+    v.sub_dim_3 = (uint32_t)(c.sub_dim * c.sub_dim_2);
+    v.data_size = (uint32_t)c.data_size;
+    v.dim_x = c.dim_x; v.dim_y = c.dim_y; v.dim_z = c.dim_z;
+    v.up_dim_x64 = c.up_dim_x;
+    v.up_dim_2_64 = c.up_dim_2;
+    v.grid_occ_size64 = c.grid_occ_size;
+    v.sub_dim64 = c.sub_dim;
+    v.sub_dim_2_64 = c.sub_dim_2;
+    v.data_size64 = c.data_size;
+    v.grid_occ = m->grid_occ;
+    v.codes = m->codes;
+    v.data = m->data;
+    v.dense = m->dense;
+    v.storage = m->codes ? 0 : 1;
+}
+
+int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
+{
+    if ((flags & TSDFL_MAP_DENSE) && m->codes) {
+        uint64_t sub3 = m->coef.sub_dim * m->coef.sub_dim_2;
+        uint64_t n = m->coef.grid_occ_size * sub3;
+        if (n < (1ull << 32)) {
+            CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (n ? n : 1)));
+            m->bytes += sizeof(uint16_t) * n;
+            int rc = launch_dense_from_codes(m->grid_occ, m->codes, m->coef.grid_occ_size, (uint32_t)sub3, m->dense,
+                                             ctx->stream);
+            if (rc) return rc;
+        }
+    }
+    fill_view(m);
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return TSDFL_OK;
+}
+
+void destroy_map(tsdfl_map* m)
+{
+    if (!m) return;
+    cudaSetDevice(m->device);
+    cudaFree(m->grid_occ);
+    cudaFree(m->codes);
+    cudaFree(m->data);
+    cudaFree(m->dense);
+    cudaFree(m->values);
+    delete m;
+}
+
+// Map allocations shared by both create entry points.
+int map_common(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, float sigma, tsdfl_map* m)
+{
+    m->device = ctx->device;
+    m->coef = *coef;
+    float vals[kNumCodes];
+    code_values(sigma, coef->init_value, vals);
+    m->max_value = 0;
+    for (int k = 0; k < kNumCodes; ++k) m->max_value = std::fmax(m->max_value, std::fabs(vals[k]));
+    CUDA_TRY(cudaMalloc(&m->values, sizeof(vals)));
+    CUDA_TRY(cudaMemcpyAsync(m->values, vals, sizeof(vals), cudaMemcpyHostToDevice, ctx->stream));
+    size_t go = sizeof(int32_t) * (coef->grid_occ_size ? coef->grid_occ_size : 1);
+    CUDA_TRY(cudaMalloc(&m->grid_occ, go));
+    if (coef->grid_occ_size)
+        CUDA_TRY(cudaMemcpyAsync(m->grid_occ, grid_occ, sizeof(int32_t) * coef->grid_occ_size,
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    m->bytes = sizeof(vals) + go;
+    m->bricks = 0;
+    for (uint64_t i = 0; i < coef->grid_occ_size; ++i) m->bricks += grid_occ[i] >= 0;
+    return TSDFL_OK;
+}
+
+int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* d_particles, size_t P,
+             const float* d_points, size_t N, const float tf[16], uint32_t flags, float* d_pose, uint32_t* d_dbg)
+{
+    int rc = ensure_workspace(c, P, N);
+    if (rc) return rc;
+    EvalBuffers b = c->buf;
+    b.particles = d_particles;
+    b.dbg_index = d_dbg;
+    const bool serial = (flags & TSDFL_SUM_SERIAL) != 0;
+    const float inv_max_range = (float)(1.0 / (double)mdl->max_range);
+    const float max_range_sq = mdl->max_range * mdl->max_range;
+    const float c_in = mdl->a_range * inv_max_range;
+    const float c_out = mdl->a_max;
+    // fixed-point scale: sums of N values below max_value stay below 2^62
+    int shift = 40;
+    {
+        double bound = std::fmax((double)map->max_value, 1e-30) * (double)(N + 1);
+        int need = (int)std::ceil(std::log2(bound));
+        if (62 - need < shift) shift = 62 - need;
+    }
+    const int npad = (int)align_up(N, 4);
+    cudaStream_t s = c->stream;
+    rc = launch_prepare(d_points, (int)N, npad, max_range_sq, c_in, c_out, map->values, shift, b, s);
+    if (rc) return rc;
+    rc = launch_pose_kernel(tf, (int)P, b, s);
+    if (rc) return rc;
+    const int pass = serial ? kSerialPassPoints : kMaxPassPoints;
+    const bool dense = map->dense != nullptr;
+    if (c->timing) CUDA_TRY(cudaEventRecord(c->ev0, s));
+    for (size_t n0 = 0; n0 < N; n0 += pass) {
+        size_t n1 = n0 + pass < N ? n0 + pass : N;
+        rc = launch_eval_pass(map->view, mdl->a_hit, (int)P, (int)n0, (int)n1, (int)N, n0 == 0, serial,
+                              dense && !serial, b, c->sum_f64, c->sm_count, s);
+        if (rc) return rc;
+    }
+    if (c->timing) {
+        CUDA_TRY(cudaEventRecord(c->ev1, s));
+        c->timed = true;
+    }
+    const int mode = serial ? 2 : (map->view.storage == 1 ? 1 : 0);
+    rc = launch_norm((int)P, mode, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)N, c->sum_f64,
+                     d_particles, d_pose, b, s);
+    if (rc) return rc;
+    return launch_fold_status(c->status + 1, c->status, s);
+}
+
+int check_model(const tsdfl_model* mdl)
+{
+    if (!mdl || !(mdl->max_range > 0.0f)) {
+        set_error("model: max_range must be positive");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    return TSDFL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tsdfl_last_error(void) { return g_err; }
+const char* tsdfl_version(void) { return "tsdfl 0.1 (sm_103a)"; }
+
+int tsdfl_ctx_create(int device, tsdfl_ctx** out)
+{
+    if (!out) return TSDFL_ERR_INVALID_ARG;
+    *out = nullptr;
+    int rc = set_device(device);
+    if (rc) return rc;
+    auto* c = new (std::nothrow) tsdfl_ctx;
+    if (!c) return TSDFL_ERR_OUT_OF_MEMORY;
+    c->device = device;
+    cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->status, sizeof(int32_t) * 4);
+    if (e == cudaSuccess) e = cudaMemset(c->status, 0, sizeof(int32_t) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, sizeof(int32_t) * 4);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_pose, sizeof(float) * 8);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_count, sizeof(uint32_t) * 4);
+    if (e != cudaSuccess) {
+        set_error("tsdfl_ctx_create: %s", cudaGetErrorString(e));
+        tsdfl_ctx_destroy(c);
+        return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
+    }
+    c->stream = c->own;
+    *out = c;
+    return TSDFL_OK;
+}
+
+int tsdfl_ctx_destroy(tsdfl_ctx* c)
+{
+    if (!c) return TSDFL_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->ws);
+    cudaFree(c->rs_ws);
+    cudaFree(c->io);
+    cudaFree(c->status);
+    cudaFreeHost(c->h_status);
+    cudaFreeHost(c->h_pose);
+    cudaFreeHost(c->h_count);
+    if (c->own) cudaStreamDestroy(c->own);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    delete c;
+    return TSDFL_OK;
+}
+
+int tsdfl_ctx_set_stream(tsdfl_ctx* c, void* stream)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own;
+    return TSDFL_OK;
+}
+
+void* tsdfl_ctx_stream(tsdfl_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int tsdfl_ctx_set_timing(tsdfl_ctx* c, int enable)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    if (enable && !c->ev0) {
+        CUDA_TRY(cudaEventCreate(&c->ev0));
+        CUDA_TRY(cudaEventCreate(&c->ev1));
+    }
+    c->timing = enable != 0;
+    c->timed = false;
+    return TSDFL_OK;
+}
+
+int tsdfl_ctx_last_timing(tsdfl_ctx* c, float* eval_kernel_ms)
+{
+    if (!c || !eval_kernel_ms) return TSDFL_ERR_INVALID_ARG;
+    if (!c->timed) {
+        set_error("tsdfl_ctx_last_timing: no timed evaluation");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    CUDA_TRY(cudaEventSynchronize(c->ev1));
+    CUDA_TRY(cudaEventElapsedTime(eval_kernel_ms, c->ev0, c->ev1));
+    return TSDFL_OK;
+}
+
+uint64_t tsdfl_launch_count(void) { return (uint64_t)g_launches.load(); }
+
+int tsdfl_ctx_sync(tsdfl_ctx* c)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->h_status, c->status, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    int st = c->h_status[0];
+    if (st == TSDFL_ERR_DEGENERATE) set_error("No particle is valid!");
+    else if (st == TSDFL_ERR_TIMEOUT) set_error("a device wait timed out");
+    else if (st == TSDFL_ERR_CAPACITY) set_error("output capacity exceeded");
+    else if (st) set_error("device status %d", st);
+    return st;
+}
+
+int tsdfl_ctx_reserve(tsdfl_ctx* c, size_t P, size_t N)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_workspace(c, P, N);
+    if (rc) return rc;
+    return ensure_resample_ws(c, P);
+}
+
+int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
+                     float sigma, uint32_t flags, tsdfl_map** out)
+{
+    if (!ctx || !out || !coef || (coef->grid_occ_size && !grid_occ) || (coef->data_size && !data)) {
+        set_error("tsdfl_map_create: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int rc = validate_coef(coef);
+    if (rc) return rc;
+    rc = set_device(ctx->device);
+    if (rc) return rc;
+    auto* m = new tsdfl_map;
+    rc = map_common(ctx, coef, grid_occ, sigma, m);
+    if (rc) { destroy_map(m); return rc; }
+    size_t n = coef->data_size;
+    cudaError_t e = cudaMalloc(&m->data, sizeof(float) * (n ? n : 1));
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(m->data, data, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        set_error("tsdfl_map_create: %s", cudaGetErrorString(e));
+        destroy_map(m);
+        return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
+    }
+    bool use_codes = !(flags & TSDFL_MAP_FORCE_F32);
+    if (use_codes) {
+        int32_t* fail = ctx->status + 2;
+        e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n ? n : 1));
+        if (e == cudaSuccess) e = cudaMemsetAsync(fail, 0, sizeof(int32_t), ctx->stream);
+        if (e == cudaSuccess) {
+            rc = launch_codes_from_floats(m->data, n, m->values, coef->init_value, m->codes, fail, ctx->stream);
+            if (rc) { destroy_map(m); return rc; }
+            e = cudaMemcpyAsync(ctx->h_status + 2, fail, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {
+            set_error("tsdfl_map_create: %s", cudaGetErrorString(e));
+            destroy_map(m);
+            return TSDFL_ERR_DEVICE;
+        }
+        if (ctx->h_status[2]) {   // some slot is not a likelihood value of this sigma: keep floats
+            cudaFree(m->codes);
+            m->codes = nullptr;
+        }
+    }
+    if (m->codes) {
+        cudaFree(m->data);
+        m->data = nullptr;
+        m->bytes += sizeof(uint16_t) * n;
+    } else {
+        m->bytes += sizeof(float) * n;
+    }
+    rc = finish_map(ctx, m, flags);
+    if (rc) { destroy_map(m); return rc; }
+    *out = m;
+    return TSDFL_OK;
+}
+
+int tsdfl_map_create_codes(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ,
+                           const uint16_t* codes, float sigma, uint32_t flags, tsdfl_map** out)
+{
+    if (!ctx || !out || !coef || (coef->grid_occ_size && !grid_occ) || (coef->data_size && !codes)) {
+        set_error("tsdfl_map_create_codes: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int rc = validate_coef(coef);
+    if (rc) return rc;
+    rc = set_device(ctx->device);
+    if (rc) return rc;
+    auto* m = new tsdfl_map;
+    rc = map_common(ctx, coef, grid_occ, sigma, m);
+    if (rc) { destroy_map(m); return rc; }
+    size_t n = coef->data_size;
+    cudaError_t e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n ? n : 1));
+    if (e == cudaSuccess && n)
+        e = cudaMemcpyAsync(m->codes, codes, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        set_error("tsdfl_map_create_codes: %s", cudaGetErrorString(e));
+        destroy_map(m);
+        return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
+    }
+    m->bytes += sizeof(uint16_t) * n;
+    rc = finish_map(ctx, m, flags);
+    if (rc) { destroy_map(m); return rc; }
+    *out = m;
+    return TSDFL_OK;
+}
+
+int tsdfl_map_destroy(tsdfl_map* m)
+{
+    destroy_map(m);
+    return TSDFL_OK;
+}
+
+int tsdfl_map_get_info(const tsdfl_map* m, tsdfl_map_info* info)
+{
+    if (!m || !info) return TSDFL_ERR_INVALID_ARG;
+    info->grid_occ_size = m->coef.grid_occ_size;
+    info->data_size = m->coef.data_size;
+    info->bricks = m->bricks;
+    info->device_bytes = m->bytes;
+    info->storage = m->codes ? 0 : 1;
+    info->dense = m->dense ? 1 : 0;
+    return TSDFL_OK;
+}
+
+int tsdfl_evaluate_device(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* d_particles, size_t P,
+                          const float* d_points, size_t N, const float tf[16], uint32_t flags, float* d_pose_out)
+{
+    if (!c || !map || !tf || (P && !d_particles) || (N && !d_points)) {
+        set_error("tsdfl_evaluate_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(mdl);
+    if (rc) return rc;
+    if (N == 0) return TSDFL_OK;
+    if (P == 0) {
+        set_error("No particle is valid!");
+        return TSDFL_ERR_DEGENERATE;
+    }
+    if (P >= (1ull << 31) || N >= (1ull << 31)) {
+        set_error("tsdfl_evaluate_device: too many particles or points");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    rc = set_device(c->device);
+    if (rc) return rc;
+    return run_eval(c, map, mdl, d_particles, P, d_points, N, tf, flags, d_pose_out, nullptr);
+}
+
+int tsdfl_evaluate_debug(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* particles, size_t P,
+                         const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6],
+                         tsdfl_eval_debug* dbg)
+{
+    if (!c || !map || !tf || (P && !particles) || (N && !points)) {
+        set_error("tsdfl_evaluate: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(mdl);
+    if (rc) return rc;
+    if (N == 0) return TSDFL_OK;
+    if (P == 0) {
+        set_error("No particle is valid!");
+        return TSDFL_ERR_DEGENERATE;
+    }
+    if (P >= (1ull << 31) || N >= (1ull << 31)) {
+        set_error("tsdfl_evaluate: too many particles or points");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    rc = set_device(c->device);
+    if (rc) return rc;
+    const bool want_idx = dbg && dbg->voxel_index;
+    size_t part_b = align_up(sizeof(float) * 7 * P, 256);
+    size_t pts_b = align_up(sizeof(float) * 3 * N, 256);
+    size_t pose_b = 256;
+    size_t idx_b = want_idx ? align_up(sizeof(uint32_t) * P * N, 256) : 0;
+    rc = ensure_io(c, part_b + pts_b + pose_b + idx_b);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_part = reinterpret_cast<float*>(io);
+    float* d_pts = reinterpret_cast<float*>(io + part_b);
+    float* d_pose = reinterpret_cast<float*>(io + part_b + pts_b);
+    uint32_t* d_idx = want_idx ? reinterpret_cast<uint32_t*>(io + part_b + pts_b + pose_b) : nullptr;
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_part, particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d_pts, points, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, s));
+    rc = run_eval(c, map, mdl, d_part, P, d_pts, N, tf, flags, d_pose, d_idx);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(particles, d_part, sizeof(float) * 7 * P, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(c->h_pose, d_pose, sizeof(float) * 6, cudaMemcpyDeviceToHost, s));
+    if (dbg) {
+        if (dbg->raw_weights)
+            CUDA_TRY(cudaMemcpyAsync(dbg->raw_weights, c->buf.raw, sizeof(float) * P, cudaMemcpyDeviceToHost, s));
+        if (dbg->hits)
+            CUDA_TRY(cudaMemcpyAsync(dbg->hits, c->buf.hits, sizeof(uint32_t) * P, cudaMemcpyDeviceToHost, s));
+        if (dbg->laser_pose)
+            CUDA_TRY(cudaMemcpyAsync(dbg->laser_pose, c->buf.pose12, sizeof(float) * 12 * P, cudaMemcpyDeviceToHost, s));
+        if (want_idx)
+            CUDA_TRY(cudaMemcpyAsync(dbg->voxel_index, d_idx, sizeof(uint32_t) * P * N, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaMemcpyAsync(&dbg->weight_sum, c->buf.sums, sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    int st = tsdfl_ctx_sync(c);
+    if (st) return st;
+    if (pose_out) std::memcpy(pose_out, c->h_pose, sizeof(float) * 6);
+    return TSDFL_OK;
+}
+
+int tsdfl_evaluate(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* particles, size_t P,
+                   const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6])
+{
+    return tsdfl_evaluate_debug(c, map, mdl, particles, P, points, N, tf, flags, pose_out, nullptr);
+}
+
+int tsdfl_resample_systematic(tsdfl_ctx* c, const float* weights, size_t M, float u0, uint32_t* idx_out, size_t cap,
+                              size_t* count_out)
+{
+    if (!c || (M && !weights) || (cap && !idx_out) || !count_out) {
+        set_error("tsdfl_resample_systematic: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *count_out = 0;
+    if (M == 0) return TSDFL_OK;
+    if (M >= (1ull << 24)) {
+        set_error("tsdfl_resample_systematic: at most 2^24-1 particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_resample_ws(c, M);
+    if (rc) return rc;
+    size_t w_b = align_up(sizeof(float) * M, 256);
+    size_t i_b = align_up(sizeof(uint32_t) * (cap ? cap : 1), 256);
+    rc = ensure_io(c, w_b + i_b + 256);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_w = reinterpret_cast<float*>(io);
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(io + w_b);
+    uint32_t* d_cnt = reinterpret_cast<uint32_t*>(io + w_b + i_b);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_w, weights, sizeof(float) * M, cudaMemcpyHostToDevice, s));
+    rc = launch_resample_impl(nullptr, d_w, 1, M, u0, nullptr, d_idx, cap, d_cnt, c->rs_ws, c->status, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->h_count, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (cap) CUDA_TRY(cudaMemcpyAsync(idx_out, d_idx, sizeof(uint32_t) * cap, cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    *count_out = c->h_count[0];
+    return st;
+}
+
+int tsdfl_resample_systematic_device(tsdfl_ctx* c, const float* d_particles, size_t M, float u0,
+                                     float* d_particles_out, size_t cap, uint32_t* d_count)
+{
+    if (!c || (M && !d_particles) || !d_particles_out || !d_count) {
+        set_error("tsdfl_resample_systematic_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (M == 0) return TSDFL_OK;
+    if (M >= (1ull << 24)) {
+        set_error("tsdfl_resample_systematic_device: at most 2^24-1 particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_resample_ws(c, M);
+    if (rc) return rc;
+    return launch_resample_impl(d_particles, d_particles + 6, 7, M, u0, d_particles_out, nullptr, cap, d_count,
+                                c->rs_ws, c->status, c->stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,879 @@
+// Sensor-update kernels for sm_103a: pose build, scan staging, per-particle
+// scoring, normalisation / mean pose, systematic resampling, map re-layout.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "tsdfl_internal.h"
+
+namespace tsdfl {
+
+std::atomic<unsigned long long> g_launches{0};
+
+namespace {
+
+constexpr int kLutBytes = ((kNumCodes * 8 + 15) / 16) * 16;
+constexpr int kLutFBytes = ((kNumCodes * 4 + 15) / 16) * 16;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// 1-D bulk copy global -> this CTA's shared memory, completing on bar
+// (cp.async.bulk; src, dst 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: gives up after ~2^22 polls (try_wait itself suspends for a
+// while each time), so a copy that never lands cannot hang the GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase)
+{
+    for (uint32_t i = 0; i < (1u << 22); ++i)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+// Stages n floats of three arrays into shared memory with bulk copies; every
+// thread of the block must call it.  Returns false (and raises status) when
+// the copies did not complete in time.
+__device__ bool stage_xyz(float* xs, float* ys, float* zs, const float* gx, const float* gy, const float* gz,
+                          int npad, uint64_t* bar, int32_t* status)
+{
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t bytes = (uint32_t)npad * 4u;
+        mbar_expect_tx(bar, 3u * bytes);
+        bulk_g2s(xs, gx, bytes, bar);
+        bulk_g2s(ys, gy, bytes, bar);
+        bulk_g2s(zs, gz, bytes, bar);
+    }
+    bool ok = mbar_wait_bounded(bar, 0);
+    if (!ok && threadIdx.x == 0) atomicExch(status, TSDFL_ERR_TIMEOUT);
+    return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Code of the slot a point falls in through the dense layout: one gather
+// instead of brick table + slot.  Falls back to the brick path where the dense
+// address is not the reference's slot (offsets outside the fast range, or a
+// sub-voxel index that runs past the end of its brick).
+__device__ __forceinline__ uint32_t dense_code(const MapView& m, float x, float y, float z)
+{
+    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
+    bool fast = ox >= 0.0f && oy >= 0.0f && oz >= 0.0f && ox < kFastOffsetLimit && oy < kFastOffsetLimit &&
+                oz < kFastOffsetLimit;
+    if (fast) {
+        int32_t mx = __float2int_rz(ox), my = __float2int_rz(oy), mz = __float2int_rz(oz);
+        if (mx > m.mmax_x || my > m.mmax_y || mz > m.mmax_z) return kCodeMiss;
+        uint32_t up = (uint32_t)mx + (uint32_t)my * m.up_dim_x + (uint32_t)mz * m.up_dim_2;
+        if (up >= m.grid_occ_size) return kCodeMiss;
+        float sx = __fsub_rn(ox, (float)mx), sy = __fsub_rn(oy, (float)my), sz = __fsub_rn(oz, (float)mz);
+        uint32_t qx = (uint32_t)__float2int_rz(__fdiv_rn(sx, m.res));
+        uint32_t qy = (uint32_t)__float2int_rz(__fdiv_rn(sy, m.res));
+        uint32_t qz = (uint32_t)__float2int_rz(__fdiv_rn(sz, m.res));
+        uint32_t s = qx + qy * m.sub_dim + qz * m.sub_dim_2;
+        if (s < m.sub_dim_3) return __ldg(m.dense + (size_t)up * m.sub_dim_3 + s);
+    }
+    uint32_t idx = slot_index(m, x, y, z);
+    return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
+}
+
+struct PointParams {
+    const float* points;  // N x 3
+    int N, npad;
+    float max_range_sq, c_in, c_out;
+    const float* code_values;  // kNumCodes floats (device)
+    int shift;                 // fixed-point scale 2^shift
+};
+
+// Scan staging: AoS points -> SoA (padded with zeros to npad), the per-point
+// score constant of tsdf_evaluator.cpp:56-65 and the number of points inside
+// max_range; also the likelihood tables for this scan.  One block.
+__global__ void prepare_points_kernel(PointParams p, EvalBuffers b)
+{
+    __shared__ int warp_counts[32];
+    if (threadIdx.x == 0) *b.status = 0;
+    int in = 0;
+    for (int j = threadIdx.x; j < p.npad; j += blockDim.x) {
+        float x = 0, y = 0, z = 0, c = 0;
+        if (j < p.N) {
+            x = p.points[3 * j];
+            y = p.points[3 * j + 1];
+            z = p.points[3 * j + 2];
+            float sq = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+            bool inr = sq < p.max_range_sq;
+            c = inr ? p.c_in : p.c_out;
+            in += inr ? 1 : 0;
+        }
+        ((float*)b.xs)[j] = x;
+        ((float*)b.ys)[j] = y;
+        ((float*)b.zs)[j] = z;
+        ((float*)b.cs)[j] = c;
+    }
+    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) {
+        float v = p.code_values[c];
+        b.lut_f[c] = v;
+        b.lut_fx[c] = __double2ll_rn(ldexp((double)v, p.shift));
+    }
+    in = (int)warp_sum_u32((uint32_t)in);
+    if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = in;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_counts[w];
+        b.counts[0] = t;
+    }
+}
+
+struct Tf16 {
+    float v[16];
+};
+
+// Laser pose of every particle (tsdf_evaluator.cpp:102-147): trig in double,
+// rounded to float (the correctly rounded sin/cos), products and sums in the
+// reference's order without contraction.
+__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const float* p = particles + 7 * (size_t)i;
+    float px = p[0], py = p[1], pz = p[2];
+    double s, c;
+    sincos((double)p[3], &s, &c);
+    float sin_alpha = (float)s, cos_alpha = (float)c;
+    sincos((double)p[4], &s, &c);
+    float sin_beta = (float)s, cos_beta = (float)c;
+    sincos((double)p[5], &s, &c);
+    float sin_gamma = (float)s, cos_gamma = (float)c;
+    float t[12];
+    t[0] = __fmul_rn(cos_beta, cos_gamma);
+    t[4] = __fmul_rn(cos_beta, sin_gamma);
+    t[8] = -sin_beta;
+    t[3] = px;
+    t[1] = __fsub_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), cos_gamma), __fmul_rn(cos_alpha, sin_gamma));
+    t[5] = __fadd_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), sin_gamma), __fmul_rn(cos_alpha, cos_gamma));
+    t[9] = __fmul_rn(sin_alpha, cos_beta);
+    t[7] = py;
+    t[2] = __fadd_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), cos_gamma), __fmul_rn(sin_alpha, sin_gamma));
+    t[6] = __fsub_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), sin_gamma), __fmul_rn(sin_alpha, cos_gamma));
+    t[10] = __fmul_rn(cos_alpha, cos_beta);
+    t[11] = pz;
+    const float* f = tf.v;
+    float o[12];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float* a = t + 4 * r;
+        o[4 * r + 0] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[0]), __fmul_rn(a[1], f[4])), __fmul_rn(a[2], f[8]));
+        o[4 * r + 1] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[1]), __fmul_rn(a[1], f[5])), __fmul_rn(a[2], f[9]));
+        o[4 * r + 2] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[2]), __fmul_rn(a[1], f[6])), __fmul_rn(a[2], f[10]));
+        o[4 * r + 3] = __fadd_rn(
+            __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[3]), __fmul_rn(a[1], f[7])), __fmul_rn(a[2], f[11])), a[3]);
+    }
+    float4* dst = reinterpret_cast<float4*>(pose12 + 12 * (size_t)i);
+    dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+    dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+    dst[2] = make_float4(o[8], o[9], o[10], o[11]);
+    float* tg = trig6 + 6 * (size_t)i;
+    tg[0] = sin_alpha; tg[1] = cos_alpha; tg[2] = sin_beta; tg[3] = cos_beta; tg[4] = sin_gamma; tg[5] = cos_gamma;
+}
+
+struct EvalParams {
+    MapView m;
+    const float* pose12;
+    const float* xs;
+    const float* ys;
+    const float* zs;
+    const float* cs;
+    const long long* lut_fx;
+    const float* lut_f;
+    long long* sum_fx;   // exact mode, code storage
+    double* sum_f64;     // exact mode, float storage
+    float* raw;          // serial mode
+    uint32_t* hits;
+    uint32_t* dbg;       // optional: P x N_total slot index (brick) / code (dense)
+    int32_t* status;
+    int P;
+    int n0, n1;          // point range of this pass
+    int n_total;
+    int first_pass;
+    float a_hit;
+};
+
+// Exact mode: one warp per particle, lanes stride over the scan (neighbouring
+// lanes take neighbouring scan points, so their map gathers fall close
+// together).  Likelihood values are summed in 64-bit fixed point, which is
+// exact and independent of order; the weight is formed from the sum afterwards.
+template <bool DENSE, bool F32>
+__global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint64_t bar;
+    long long* lut = reinterpret_cast<long long*>(smem);
+    const int n = p.n1 - p.n0;
+    const int npad = (n + 3) & ~3;
+    float* xs = reinterpret_cast<float*>(smem + kLutBytes);
+    float* ys = xs + npad;
+    float* zs = ys + npad;
+    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
+    if (!stage_xyz(xs, ys, zs, p.xs + p.n0, p.ys + p.n0, p.zs + p.n0, npad, &bar, p.status)) return;
+
+    const int lane = threadIdx.x & 31;
+    const int warps = (blockDim.x >> 5) * gridDim.x;
+    const MapView& m = p.m;
+    for (int pi = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); pi < p.P; pi += warps) {
+        float t[12];
+        const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
+        float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
+        t[0] = a.x; t[1] = a.y; t[2] = a.z; t[3] = a.w;
+        t[4] = b4.x; t[5] = b4.y; t[6] = b4.z; t[7] = b4.w;
+        t[8] = c4.x; t[9] = c4.y; t[10] = c4.z; t[11] = c4.w;
+        long long acc = 0;
+        double accd = 0.0;
+        uint32_t h = 0;
+        for (int j = lane; j < n; j += 32) {
+            float tx, ty, tz;
+            transform_point(t, xs[j], ys[j], zs[j], tx, ty, tz);
+            if (DENSE) {
+                uint32_t code = dense_code(m, tx, ty, tz);
+                h += code != (uint32_t)kCodeMiss ? 1u : 0u;
+                acc += lut[code];
+                if (p.dbg) p.dbg[(size_t)pi * p.n_total + p.n0 + j] = code;
+            } else {
+                uint32_t idx = slot_index(m, tx, ty, tz);
+                if (F32) {
+                    float v = idx != kMissIndex ? __ldg(m.data + idx) : m.init_value;
+                    accd += (double)v;
+                } else {
+                    uint32_t code = idx != kMissIndex ? (uint32_t)__ldg(m.codes + idx) : (uint32_t)kCodeInit;
+                    acc += lut[code];
+                }
+                h += idx != kMissIndex ? 1u : 0u;
+                if (p.dbg) p.dbg[(size_t)pi * p.n_total + p.n0 + j] = idx;
+            }
+        }
+        h = warp_sum_u32(h);
+        if (F32) accd = warp_sum_d(accd);
+        else acc = warp_sum_ll(acc);
+        if (lane == 0) {
+            if (F32) p.sum_f64[pi] = p.first_pass ? accd : p.sum_f64[pi] + accd;
+            else p.sum_fx[pi] = p.first_pass ? acc : p.sum_fx[pi] + acc;
+            p.hits[pi] = p.first_pass ? h : p.hits[pi] + h;
+        }
+    }
+}
+
+// Serial mode: one thread per particle runs evaluatePose's loop
+// (tsdf_evaluator.cpp:38-68) in scan order with float sums, reproducing the
+// reference's un-normalised weight bit for bit.
+template <bool F32>
+__global__ void __launch_bounds__(256) eval_serial_kernel(EvalParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint64_t bar;
+    float* lut = reinterpret_cast<float*>(smem);
+    const int n = p.n1 - p.n0;
+    const int npad = (n + 3) & ~3;
+    float* xs = reinterpret_cast<float*>(smem + kLutFBytes);
+    float* ys = xs + npad;
+    float* zs = ys + npad;
+    float* cs = zs + npad;
+    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_f[c];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) cs[j] = p.cs[p.n0 + j];
+    if (!stage_xyz(xs, ys, zs, p.xs + p.n0, p.ys + p.n0, p.zs + p.n0, npad, &bar, p.status)) return;
+    int pi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pi >= p.P) return;
+    float t[12];
+    for (int k = 0; k < 12; ++k) t[k] = p.pose12[12 * (size_t)pi + k];
+    const MapView& m = p.m;
+    float sum = p.first_pass ? 0.0f : p.raw[pi];
+    uint32_t h = p.first_pass ? 0u : p.hits[pi];
+    for (int j = 0; j < n; ++j) {
+        float tx, ty, tz;
+        transform_point(t, xs[j], ys[j], zs[j], tx, ty, tz);
+        uint32_t idx = slot_index(m, tx, ty, tz);
+        float v;
+        if (F32) v = idx != kMissIndex ? m.data[idx] : m.init_value;
+        else v = lut[idx != kMissIndex ? (uint32_t)m.codes[idx] : (uint32_t)kCodeInit];
+        h += idx != kMissIndex ? 1u : 0u;
+        if (p.dbg) p.dbg[(size_t)pi * p.n_total + p.n0 + j] = idx;
+        v = __fadd_rn(__fmul_rn(p.a_hit, v), cs[j]);
+        sum = __fadd_rn(sum, v);
+    }
+    p.raw[pi] = sum;
+    p.hits[pi] = h;
+}
+
+constexpr int kNormBlocks = 256;
+constexpr int kNormThreads = 256;
+constexpr int kNormSums = 10;
+
+struct NormParams {
+    int P;
+    int mode;            // 0 fixed point, 1 double sums, 2 serial raw
+    int shift;
+    double a_hit, c_in, c_out;
+    int n_points;
+};
+
+// Forms each particle's un-normalised weight from its likelihood sum and
+// accumulates, in double and in a fixed order, the weight sum and the
+// weighted pose sums of tsdf_evaluator.cpp:198-217.
+__global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* sum_f64)
+{
+    double acc[kNormSums];
+    for (int k = 0; k < kNormSums; ++k) acc[k] = 0.0;
+    const double n_in = (double)b.counts[0];
+    const double n_out = (double)q.n_points - n_in;
+    const double scale = ldexp(1.0, -q.shift);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < q.P; i += gridDim.x * blockDim.x) {
+        float raw;
+        if (q.mode == 2) {
+            raw = b.raw[i];
+        } else {
+            double sl = q.mode == 0 ? (double)b.sum_fx[i] * scale : sum_f64[i];
+            raw = (float)(q.a_hit * sl + n_in * q.c_in + n_out * q.c_out);
+            b.raw[i] = raw;
+        }
+        double w = (double)raw;
+        const float* pp = b.particles + 7 * (size_t)i;
+        const float* tg = b.trig6 + 6 * (size_t)i;
+        acc[0] += w;
+        acc[1] += (double)pp[0] * w;
+        acc[2] += (double)pp[1] * w;
+        acc[3] += (double)pp[2] * w;
+        acc[4] += (double)tg[0] * w;
+        acc[5] += (double)tg[1] * w;
+        acc[6] += (double)tg[2] * w;
+        acc[7] += (double)tg[3] * w;
+        acc[8] += (double)tg[4] * w;
+        acc[9] += (double)tg[5] * w;
+    }
+    __shared__ double red[kNormSums][kNormThreads / 32];
+    for (int k = 0; k < kNormSums; ++k) {
+        double v = warp_sum_d(acc[k]);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNormSums) {
+        double v = 0.0;
+        for (int w = 0; w < kNormThreads / 32; ++w) v += red[threadIdx.x][w];
+        b.partials[blockIdx.x * kNormSums + threadIdx.x] = v;
+    }
+}
+
+// Final weight sum, the "No particle is valid!" check (tsdf_evaluator.cpp:159)
+// and the mean pose with circular means of the angles (:219-221).
+__global__ void norm_final_kernel(EvalBuffers b, float* pose_out)
+{
+    if (threadIdx.x != 0) return;
+    double s[kNormSums];
+    for (int k = 0; k < kNormSums; ++k) s[k] = 0.0;
+    for (int blk = 0; blk < kNormBlocks; ++blk)
+        for (int k = 0; k < kNormSums; ++k) s[k] += b.partials[blk * kNormSums + k];
+    for (int k = 0; k < kNormSums; ++k) b.sums[k] = s[k];
+    float wsum = (float)s[0];
+    b.weight_sum_f[0] = wsum;
+    if (!(wsum != 0.0f) || !isfinite(s[0])) {
+        atomicExch(b.status, TSDFL_ERR_DEGENERATE);
+        return;
+    }
+    if (pose_out) {
+        double inv = 1.0 / s[0];
+        pose_out[0] = (float)(s[1] * inv);
+        pose_out[1] = (float)(s[2] * inv);
+        pose_out[2] = (float)(s[3] * inv);
+        pose_out[3] = (float)atan2(s[4] * inv, s[5] * inv);
+        pose_out[4] = (float)atan2(s[6] * inv, s[7] * inv);
+        pose_out[5] = (float)atan2(s[8] * inv, s[9] * inv);
+    }
+}
+
+// particles[i].second = raw / weight_sum (tsdf_evaluator.cpp:203), skipped when
+// the sum was degenerate so the caller's particles stay untouched.
+__global__ void normalize_kernel(int P, EvalBuffers b, float* particles_out)
+{
+    if (*b.status == TSDFL_ERR_DEGENERATE) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    particles_out[7 * (size_t)i + 6] = __fdiv_rn(b.raw[i], b.weight_sum_f[0]);
+}
+
+// ---------------------------------------------------------------- resampling
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kMaxSegments = 1024;
+
+struct Segment {
+    double u_start;   // exact float value
+    double delta;     // exact float step
+    long long j0;     // index of the first value
+    long long n;      // number of values
+};
+
+struct ResampleWs {
+    long long* cdf;         // M: inclusive fixed-point prefix within the tile
+    long long* tile_sums;   // tiles
+    long long* tile_off;    // tiles (exclusive)
+    Segment* segs;          // kMaxSegments
+    int* nseg;
+    int* exact_ok;          // 1 when the parallel path reproduces the serial one
+    long long* total;
+};
+
+// Weight as an exact multiple of 2^-52 (its value in those units), or -1 when
+// it is negative, not finite, not a multiple, or too large.
+__device__ __forceinline__ long long weight_fx52(float w)
+{
+    uint32_t bits = __float_as_uint(w);
+    if (bits == 0u || bits == 0x80000000u) return 0;
+    if (bits >> 31) return -1;
+    uint32_t e = (bits >> 23) & 0xffu;
+    if (e == 0xffu) return -1;
+    long long mant = e ? (long long)((bits & 0x7fffffu) | 0x800000u) : (long long)(bits & 0x7fffffu);
+    int E = e ? (int)e - 150 : -149;
+    int sh = E + 52;
+    if (sh >= 0) {
+        if (sh > 36) return -1;
+        return mant << sh;
+    }
+    if (sh <= -63) return -1;
+    if (mant & ((1ll << -sh) - 1)) return -1;
+    return mant >> -sh;
+}
+
+// Tile-local inclusive scan of the fixed-point weights (exact integers).
+__global__ void resample_scan_kernel(const float* w, int stride, int M, ResampleWs ws)
+{
+    __shared__ long long warp_tot[kScanThreads / 32];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    long long v[kScanItems];
+    long long run = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        int i = base + k;
+        long long f = 0;
+        if (i < M) {
+            f = weight_fx52(w[(size_t)i * stride]);
+            if (f < 0) { bad = 1; f = 0; }
+        }
+        run += f;
+        v[k] = run;
+    }
+    // inclusive scan of per-thread totals across the block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    long long x = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    long long woff = 0;
+    for (int k = 0; k < warp; ++k) woff += warp_tot[k];
+    long long excl = woff + x - run;
+    for (int k = 0; k < kScanItems; ++k) {
+        int i = base + k;
+        if (i < M) ws.cdf[i] = excl + v[k];
+    }
+    if (threadIdx.x == kScanThreads - 1) ws.tile_sums[blockIdx.x] = excl + run;
+    __syncthreads();
+    if (threadIdx.x == 0 && bad) atomicExch(ws.exact_ok, 0);
+}
+
+// Builds the piecewise-arithmetic description of the reference's float draw
+// sequence U_{k+1} = (float)((double)U_k + 1.0/M) (novel_resampling.h:59-63):
+// inside one binade of float the step is constant except near its top, where
+// single steps are taken literally.  One thread.
+__global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs ws)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long acc = 0;
+    for (int t = 0; t < tiles; ++t) {
+        ws.tile_off[t] = acc;
+        acc += ws.tile_sums[t];
+    }
+    *ws.total = acc;
+    if (acc >= (1ll << 53)) *ws.exact_ok = 0;   // partial sums >= 2 may round in the serial double sum
+    if (!*ws.exact_ok) { *ws.nseg = 0; return; }
+    const double s_total = ldexp((double)acc, -52);
+    const double inv_m = 1.0 / (double)M;
+    double U = (double)u0;
+    long long j = 0;
+    int ns = 0;
+    while (U < s_total) {
+        if (ns == kMaxSegments) { *ws.exact_ok = 0; break; }
+        float uf = (float)U;
+        int e;
+        bool regular = false;
+        long long cnt = 0;
+        double delta = 0.0;
+        if (uf >= 1.17549435e-38f) {     // normal float: binade [2^e, 2^(e+1))
+            frexp(U, &e);
+            e -= 1;                       // U = m * 2^e, m in [1, 2)
+            double u = ldexp(1.0, e - 23);     // float ulp in the binade
+            double g = ldexp(1.0, e - 52);     // double ulp in the binade
+            double y = rint(inv_m / g) * g;    // (double)U + inv_m - U, while inside the binade
+            double r = y / u;
+            double frac = r - floor(r);
+            if (frac == 0.5) { *ws.exact_ok = 0; break; }   // step would depend on the parity of U
+            delta = rint(r) * u;
+            if (delta <= 0.0) { *ws.exact_ok = 0; break; }  // U would stop advancing
+            // values U + i*delta with U + i*delta + y < 2^(e+1) take the regular step
+            double top = ldexp(1.0, e + 1) - y;
+            if (U < top) {
+                long long Ui = (long long)(U / g), Di = (long long)(delta / g), Ti = (long long)(top / g);
+                cnt = (Ti - Ui + Di - 1) / Di;
+                regular = cnt > 0;
+            }
+        }
+        if (regular) {
+            ws.segs[ns].u_start = U;
+            ws.segs[ns].delta = delta;
+            ws.segs[ns].j0 = j;
+            ws.segs[ns].n = cnt;
+            ++ns;
+            j += cnt;
+            U = U + (double)cnt * delta;   // exact: a float value of this binade or 2^(e+1)
+        } else {
+            ws.segs[ns].u_start = U;
+            ws.segs[ns].delta = 0.0;
+            ws.segs[ns].j0 = j;
+            ws.segs[ns].n = 1;
+            ++ns;
+            j += 1;
+            U = (double)(float)(U + inv_m);
+        }
+    }
+    *ws.nseg = ns;
+}
+
+// Number of draws U_j below s (the count the serial loop has emitted once its
+// running sum reaches s).
+__device__ long long count_below(const Segment* seg, int ns, double s)
+{
+    int lo = 0, hi = ns;   // first segment with u_start >= s
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (seg[mid].u_start < s) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo == 0) return 0;
+    const Segment& g = seg[lo - 1];
+    if (g.delta == 0.0) return g.j0 + 1;
+    long long i = (long long)((s - g.u_start) / g.delta);
+    if (i < 0) i = 0;
+    while (i > 0 && g.u_start + (double)(i - 1) * g.delta >= s) --i;
+    while (i < g.n && g.u_start + (double)i * g.delta < s) ++i;
+    if (i > g.n) i = g.n;
+    return g.j0 + i;
+}
+
+// Particle m receives the draws in [cdf_{m-1}, cdf_m) (novel_resampling.h:52-68):
+// writes their indices and, when asked, copies of the particle.
+__global__ void resample_assign_kernel(const float* particles, int M, float* out, uint32_t* idx_out, long long cap,
+                                       uint32_t* count_out, ResampleWs ws, int32_t* status)
+{
+    __shared__ Segment seg[kMaxSegments];
+    if (!*ws.exact_ok) return;
+    const int ns = *ws.nseg;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) seg[k] = ws.segs[k];
+    __syncthreads();
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const long long c_hi_fx = ws.cdf[m] + ws.tile_off[m / kScanTile];
+    long long c_lo_fx = 0;
+    if (m > 0) c_lo_fx = ws.cdf[m - 1] + ws.tile_off[(m - 1) / kScanTile];
+    long long lo = count_below(seg, ns, ldexp((double)c_lo_fx, -52));
+    long long hi = count_below(seg, ns, ldexp((double)c_hi_fx, -52));
+    if (m == M - 1) {
+        *count_out = (uint32_t)hi;
+        if (hi > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
+    }
+    for (long long j = lo; j < hi && j < cap; ++j) {
+        if (idx_out) idx_out[j] = (uint32_t)m;
+        if (out) {
+            const float* src = particles + 7 * (size_t)m;
+            float* dst = out + 7 * (size_t)j;
+            for (int k = 0; k < 7; ++k) dst[k] = src[k];
+        }
+    }
+}
+
+// The reference loop literally, on one thread, for weights where the parallel
+// path would not be exact (negative, tiny or huge weights).
+__global__ void resample_serial_kernel(const float* particles, const float* w, int stride, int M, float u0,
+                                       float* out, uint32_t* idx_out, long long cap, uint32_t* count_out,
+                                       ResampleWs ws, int32_t* status)
+{
+    if (*ws.exact_ok) return;
+    const double inv_m = 1.0 / (double)M;
+    float U = u0;
+    double s = 0.0;
+    long long n = 0;
+    for (int m = 0; m < M; ++m) {
+        s += (double)w[(size_t)m * stride];
+        while (s > (double)U) {
+            if (n < cap) {
+                if (idx_out) idx_out[n] = (uint32_t)m;
+                if (out)
+                    for (int k = 0; k < 7; ++k) out[7 * (size_t)n + k] = particles[7 * (size_t)m + k];
+            }
+            ++n;
+            float next = (float)((double)U + inv_m);
+            if (next == U || n > 4ll * M + 16) {   // the reference would not terminate
+                atomicExch(status, TSDFL_ERR_UNSUPPORTED);
+                *count_out = (uint32_t)n;
+                return;
+            }
+            U = next;
+        }
+    }
+    *count_out = (uint32_t)n;
+    if (n > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
+}
+
+__global__ void set_int_kernel(int* p, int v) { *p = v; }
+
+// Carries a per-evaluation error into the context's sticky status word.
+__global__ void fold_status_kernel(int32_t* ev, int32_t* sticky)
+{
+    int v = *ev;
+    if (v && *sticky == 0) *sticky = v;
+}
+
+// ------------------------------------------------------------- map layouts
+
+__global__ void codes_from_floats_kernel(const float* data, size_t n, const float* values, float init_value,
+                                         uint16_t* codes, int32_t* fail)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float v = data[i];
+        uint32_t vb = __float_as_uint(v);
+        int code = -1;
+        if (vb == __float_as_uint(init_value)) {
+            code = kCodeInit;
+        } else {
+            // likelihood values decrease with |tsdf|: binary search, then exact match
+            int lo = 0, hi = kCodeInit - 1;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (values[mid] > v) lo = mid + 1;
+                else hi = mid;
+            }
+            for (int c = max(0, lo - 2); c <= min(kCodeInit - 1, lo + 2); ++c)
+                if (__float_as_uint(values[c]) == vb) { code = c; break; }
+        }
+        if (code < 0) {
+            atomicExch(fail, 1);
+            code = kCodeInit;
+        }
+        codes[i] = (uint16_t)code;
+    }
+}
+
+__global__ void dense_from_codes_kernel(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size,
+                                        uint32_t sub3, uint16_t* dense)
+{
+    size_t total = grid_occ_size * sub3;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t up = i / sub3, s = i - up * sub3;
+        int32_t base = grid_occ[up];
+        dense[i] = base < 0 ? (uint16_t)kCodeMiss : codes[(size_t)base + s];
+    }
+}
+
+int check(cudaError_t e)
+{
+    return e == cudaSuccess ? TSDFL_OK : TSDFL_ERR_DEVICE;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+
+int launch_prepare(const float* points, int N, int npad, float max_range_sq, float c_in, float c_out,
+                   const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
+{
+    PointParams p{points, N, npad, max_range_sq, c_in, c_out, code_values, shift};
+    prepare_points_kernel<<<1, 1024, 0, s>>>(p, b);
+    g_launches += 1;
+    return check(cudaGetLastError());
+}
+
+int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s)
+{
+    Tf16 t;
+    for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
+    if (P > 0) {
+        pose_kernel<<<(P + 255) / 256, 256, 0, s>>>(b.particles, P, t, b.pose12, b.trig6);
+        g_launches += 1;
+    }
+    return check(cudaGetLastError());
+}
+
+size_t eval_smem_bytes(bool serial, int n)
+{
+    int npad = (n + 3) & ~3;
+    return serial ? (size_t)kLutFBytes + 4ull * npad * 4 : (size_t)kLutBytes + 3ull * npad * 4;
+}
+
+int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
+                     bool dense, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s)
+{
+    EvalParams p;
+    p.m = m;
+    p.pose12 = b.pose12;
+    p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
+    p.lut_fx = b.lut_fx;
+    p.lut_f = b.lut_f;
+    p.sum_fx = b.sum_fx;
+    p.sum_f64 = sum_f64;
+    p.raw = b.raw;
+    p.hits = b.hits;
+    p.dbg = b.dbg_index;
+    p.status = b.status;
+    p.P = P; p.n0 = n0; p.n1 = n1; p.n_total = n_total; p.first_pass = first ? 1 : 0;
+    p.a_hit = a_hit;
+    size_t smem = eval_smem_bytes(serial, n1 - n0);
+    const bool f32 = m.storage == 1;
+    if (serial) {
+        auto k = f32 ? eval_serial_kernel<true> : eval_serial_kernel<false>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<(P + 255) / 256, 256, smem, s>>>(p);
+        g_launches += 1;
+    } else {
+        auto k = dense && !f32 ? eval_exact_kernel<true, false>
+                               : (f32 ? eval_exact_kernel<false, true> : eval_exact_kernel<false, false>);
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int blocks = sm_count;
+        int need = (P + 31) / 32;
+        if (need < blocks) blocks = need > 0 ? need : 1;
+        k<<<blocks, 1024, smem, s>>>(p);
+        g_launches += 1;
+    }
+    return check(cudaGetLastError());
+}
+
+int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
+                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s)
+{
+    NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points};
+    norm_partial_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(q, b, sum_f64);
+    norm_final_kernel<<<1, 32, 0, s>>>(b, pose_out);
+    g_launches += 2;
+    if (P > 0) {
+        normalize_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
+        g_launches += 1;
+    }
+    return check(cudaGetLastError());
+}
+
+int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s)
+{
+    fold_status_kernel<<<1, 1, 0, s>>>(eval_status, sticky);
+    g_launches += 1;
+    return check(cudaGetLastError());
+}
+
+size_t resample_workspace_bytes(size_t M)
+{
+    size_t tiles = (M + kScanTile - 1) / kScanTile + 1;
+    return 8 * (M + 2 * tiles) + sizeof(Segment) * kMaxSegments + 64;
+}
+
+int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
+                         uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
+                         cudaStream_t s)
+{
+    size_t tiles = (M + kScanTile - 1) / kScanTile;
+    char* p = static_cast<char*>(workspace);
+    ResampleWs ws;
+    ws.cdf = reinterpret_cast<long long*>(p); p += 8 * M;
+    ws.tile_sums = reinterpret_cast<long long*>(p); p += 8 * (tiles + 1);
+    ws.tile_off = reinterpret_cast<long long*>(p); p += 8 * (tiles + 1);
+    ws.segs = reinterpret_cast<Segment*>(p); p += sizeof(Segment) * kMaxSegments;
+    ws.nseg = reinterpret_cast<int*>(p); p += 16;
+    ws.exact_ok = reinterpret_cast<int*>(p); p += 16;
+    ws.total = reinterpret_cast<long long*>(p);
+    set_int_kernel<<<1, 1, 0, s>>>(ws.exact_ok, 1);
+    resample_scan_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(w, stride, (int)M, ws);
+    resample_segments_kernel<<<1, 32, 0, s>>>((int)M, u0, (int)tiles, ws);
+    resample_assign_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(particles, (int)M, out, idx_out,
+                                                                        (long long)cap, count_out, ws, status);
+    resample_serial_kernel<<<1, 1, 0, s>>>(particles, w, stride, (int)M, u0, out, idx_out, (long long)cap,
+                                          count_out, ws, status);
+    g_launches += 5;
+    return check(cudaGetLastError());
+}
+
+int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
+                             uint16_t* codes, int32_t* fail, cudaStream_t s)
+{
+    if (n) codes_from_floats_kernel<<<1024, 256, 0, s>>>(data, n, code_values, init_value, codes, fail);
+    return check(cudaGetLastError());
+}
+
+int launch_dense_from_codes(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size, uint32_t sub3,
+                            uint16_t* dense, cudaStream_t s)
+{
+    if (grid_occ_size) dense_from_codes_kernel<<<2048, 256, 0, s>>>(grid_occ, codes, grid_occ_size, sub3, dense);
+    return check(cudaGetLastError());
+}
+
+}  // namespace tsdfl

@@ -1,0 +1,172 @@
+// Internal declarations shared by the host API and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tsdfl.h"
+
+namespace tsdfl {
+
+// Slot codes: 0..599 = likelihood of |tsdf| in mm (map_util.h:124-127),
+// 600 = init value (allocated slot never written), 601 = unallocated brick in
+// the dense layout (a miss).
+constexpr int kCodeInit = 600;
+constexpr int kCodeMiss = 601;
+constexpr int kNumCodes = 602;
+constexpr uint32_t kMissIndex = 0xffffffffu;
+
+// Largest scan a single evaluation pass stages in shared memory (3 floats per
+// point); longer scans are evaluated in several passes over point ranges.
+constexpr int kMaxPassPoints = 16384;
+
+// Fast-path bound on a map offset (metres): below it float->integer conversions
+// are exact and cannot wrap.
+constexpr float kFastOffsetLimit = 4194304.0f;
+
+// Everything a kernel needs to look a point up in one map, passed by value
+// (kernel parameters live in the constant bank).
+struct MapView {
+    float min_x, min_y, min_z;
+    float res;
+    float init_value;
+    // fast path (non-negative offsets below kFastOffsetLimit)
+    int32_t mmax_x, mmax_y, mmax_z;   // trunc(offset) passes the coarse bound check iff <= mmax
+    uint32_t up_dim_x, up_dim_2, grid_occ_size;
+    uint32_t sub_dim, sub_dim_2, sub_dim_3;
+    uint32_t data_size;
+    // full semantics (slow path)
+    uint64_t dim_x, dim_y, dim_z;
+    uint64_t up_dim_x64, up_dim_2_64, grid_occ_size64;
+    uint64_t sub_dim64, sub_dim_2_64, data_size64;
+    const int32_t* grid_occ;
+    const uint16_t* codes;    // 16-bit slot codes (storage 0)
+    const float* data;        // float slots (storage 1)
+    const uint16_t* dense;    // dense brick layout (may be null)
+    int32_t storage;          // 0 = codes, 1 = float
+};
+
+#ifdef __CUDACC__
+
+// float -> size_t as the reference's x86-64 build converts it (cvttss2si):
+// in-range values truncate, negatives wrap modulo 2^64, out-of-range values give
+// 2^63 (below 2^63) or 0 (at or above 2^64).
+static __device__ __forceinline__ uint64_t f2u_x86(float v)
+{
+    const float two63 = 9223372036854775808.0f;
+    if (v != v) return 0x8000000000000000ull;
+    if (v < two63) {
+        if (v >= -two63) return (uint64_t)__float2ll_rz(v);
+        return 0x8000000000000000ull;
+    }
+    float w = __fsub_rn(v, two63);
+    if (w < two63) return ((uint64_t)__float2ll_rz(w)) ^ 0x8000000000000000ull;
+    return 0;
+}
+
+// CudaSubVoxelMap::getIndex (cuda_sub_voxel_map.tcc:50-137) with every
+// conversion of the reference's x86-64 build: used for offsets the fast path
+// does not cover.  Returns the slot index, or kMissIndex when it is not below
+// data_size (getEntry then returns the init value, :139-157).
+static __device__ __noinline__ uint32_t slot_index_slow(const MapView& m, float x, float y, float z)
+{
+    uint64_t gx = f2u_x86(__fsub_rn(x, m.min_x));
+    uint64_t gy = f2u_x86(__fsub_rn(y, m.min_y));
+    uint64_t gz = f2u_x86(__fsub_rn(z, m.min_z));
+    gx = f2u_x86(__fdiv_rn(__ull2float_rn(gx), m.res));
+    gy = f2u_x86(__fdiv_rn(__ull2float_rn(gy), m.res));
+    gz = f2u_x86(__fdiv_rn(__ull2float_rn(gz), m.res));
+    if (gx >= m.dim_x || gy >= m.dim_y || gz >= m.dim_z) return kMissIndex;
+    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
+    uint64_t ux = f2u_x86(ox), uy = f2u_x86(oy), uz = f2u_x86(oz);
+    float sx = __fsub_rn(ox, __ull2float_rn(ux));
+    float sy = __fsub_rn(oy, __ull2float_rn(uy));
+    float sz = __fsub_rn(oz, __ull2float_rn(uz));
+    uint64_t up = ux + uy * m.up_dim_x64 + uz * m.up_dim_2_64;
+    if (up >= m.grid_occ_size64) return kMissIndex;
+    int32_t base = m.grid_occ[up];
+    if (base < 0) return kMissIndex;
+    uint64_t qx = f2u_x86(__fdiv_rn(sx, m.res));
+    uint64_t qy = f2u_x86(__fdiv_rn(sy, m.res));
+    uint64_t qz = f2u_x86(__fdiv_rn(sz, m.res));
+    uint64_t idx = (uint64_t)(int64_t)base + qx + qy * m.sub_dim64 + qz * m.sub_dim_2_64;
+    return idx < m.data_size64 ? (uint32_t)idx : kMissIndex;
+}
+
+// Slot index of a map-frame point (exact reference semantics), kMissIndex on a
+// miss.  Fast path: all three offsets in [0, kFastOffsetLimit), where
+// trunc(offset) is the reference's brick coordinate and the coarse bound check
+// (:54-66) reduces to trunc(offset) <= mmax.
+static __device__ __forceinline__ uint32_t slot_index(const MapView& m, float x, float y, float z)
+{
+    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
+    bool fast = ox >= 0.0f && oy >= 0.0f && oz >= 0.0f && ox < kFastOffsetLimit && oy < kFastOffsetLimit &&
+                oz < kFastOffsetLimit;
+    if (!fast) return slot_index_slow(m, x, y, z);
+    int32_t mx = __float2int_rz(ox), my = __float2int_rz(oy), mz = __float2int_rz(oz);
+    if (mx > m.mmax_x || my > m.mmax_y || mz > m.mmax_z) return kMissIndex;
+    uint32_t up = (uint32_t)mx + (uint32_t)my * m.up_dim_x + (uint32_t)mz * m.up_dim_2;
+    if (up >= m.grid_occ_size) return kMissIndex;
+    int32_t base = __ldg(m.grid_occ + up);
+    if (base < 0) return kMissIndex;
+    float sx = __fsub_rn(ox, (float)mx), sy = __fsub_rn(oy, (float)my), sz = __fsub_rn(oz, (float)mz);
+    uint32_t qx = (uint32_t)__float2int_rz(__fdiv_rn(sx, m.res));
+    uint32_t qy = (uint32_t)__float2int_rz(__fdiv_rn(sy, m.res));
+    uint32_t qz = (uint32_t)__float2int_rz(__fdiv_rn(sz, m.res));
+    uint32_t idx = (uint32_t)base + qx + qy * m.sub_dim + qz * m.sub_dim_2;
+    return idx < m.data_size ? idx : kMissIndex;
+}
+
+// Transform of one scan point by a laser pose (tsdf_evaluator.cpp:44-46) with
+// the reference's rounding order and no contraction into FMA.
+static __device__ __forceinline__ void transform_point(const float* t, float x, float y, float z, float& tx, float& ty,
+                                                float& tz)
+{
+    tx = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[0], x), __fmul_rn(t[1], y)), __fmul_rn(t[2], z)), t[3]);
+    ty = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[4], x), __fmul_rn(t[5], y)), __fmul_rn(t[6], z)), t[7]);
+    tz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(t[8], x), __fmul_rn(t[9], y)), __fmul_rn(t[10], z)), t[11]);
+}
+
+#endif  // __CUDACC__
+
+// Kernel launchers (kernels.cu)
+struct EvalBuffers {
+    const float* particles;  // P x 7
+    const float* xs;         // N (padded to 4)
+    const float* ys;
+    const float* zs;
+    const float* cs;         // per-point score constant (a_range*inv_max_range or a_max)
+    float* pose12;           // P x 12 laser poses
+    float* trig6;            // P x 6: sin/cos of roll, pitch, yaw
+    long long* sum_fx;       // P: fixed-point likelihood sums
+    float* raw;              // P: un-normalised weights
+    uint32_t* hits;          // P
+    long long* lut_fx;       // kNumCodes fixed-point likelihoods
+    float* lut_f;            // kNumCodes float likelihoods
+    int32_t* counts;         // [0] = points in range
+    double* partials;        // reduction partials
+    double* sums;            // [0] weight sum, [1..9] pose sums
+    float* weight_sum_f;     // [1]
+    int32_t* status;         // per-evaluation device status word
+    uint32_t* dbg_index;     // optional P x N
+};
+
+int launch_prepare(const float* points, int N, int npad, float max_range_sq, float c_in, float c_out,
+                   const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s);
+int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
+size_t eval_smem_bytes(bool serial, int n);
+int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
+                     bool dense, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
+int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
+                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s);
+int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s);
+size_t resample_workspace_bytes(size_t M);
+int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
+                         uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
+                         cudaStream_t s);
+int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
+                             uint16_t* codes, int32_t* fail, cudaStream_t s);
+int launch_dense_from_codes(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size, uint32_t sub3,
+                            uint16_t* dense, cudaStream_t s);
+
+}  // namespace tsdfl

@@ -1,0 +1,233 @@
+"""Host-side mirror of the reference's sensor-update interface over libtsdfl.
+
+    TSDFEvaluator(map, per_point, a_hit, a_range, a_max, max_range)
+        .evaluate(particles, points, tf_matrix) -> mean pose
+    SystematicResampler(seed).resample(particles) -> resampled particles
+
+follow include/tsdf_localization/evaluation/tsdf_evaluator.h:72-114 and
+include/tsdf_localization/resampling/novel_resampling.h:38-74: particles are a
+(P, 7) float32 array (x, y, z, roll, pitch, yaw, weight) whose weights are
+overwritten with the normalised weights; errors raise RuntimeError with the
+reference's messages ("No particle is valid!").
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+
+
+def _f32(a, shape_tail=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape_tail is not None and (a.ndim != 2 or a.shape[1] != shape_tail):
+        raise ValueError(f"expected an (n, {shape_tail}) array, got {a.shape}")
+    return a
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One device and stream with the evaluation workspace (tsdfl_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = N.lib()
+        h = C.c_void_p()
+        N.check(self._lib.tsdfl_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self._lib.tsdfl_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        N.check(self._lib.tsdfl_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def sync(self) -> None:
+        N.check(self._lib.tsdfl_ctx_sync(self.handle))
+
+    def reserve(self, particles: int, points: int) -> None:
+        N.check(self._lib.tsdfl_ctx_reserve(self.handle, particles, points))
+
+
+class DeviceMap:
+    """A likelihood map resident on the device (tsdfl_map)."""
+
+    def __init__(self, ctx: Context, coef: N.MapCoef, grid_occ: np.ndarray, data: np.ndarray | None = None,
+                 codes: np.ndarray | None = None, sigma: float = 0.1, dense: bool = False, force_f32: bool = False):
+        self.ctx = ctx
+        self.coef = coef
+        lib = N.lib()
+        go = np.ascontiguousarray(grid_occ, dtype=np.int32)
+        flags = (N.TSDFL_MAP_DENSE if dense else 0) | (N.TSDFL_MAP_FORCE_F32 if force_f32 else 0)
+        h = C.c_void_p()
+        if codes is not None:
+            cd = np.ascontiguousarray(codes, dtype=np.uint16)
+            N.check(lib.tsdfl_map_create_codes(ctx.handle, C.byref(coef), _ptr(go), _ptr(cd), sigma, flags,
+                                               C.byref(h)))
+        else:
+            d = np.ascontiguousarray(data, dtype=np.float32)
+            N.check(lib.tsdfl_map_create(ctx.handle, C.byref(coef), _ptr(go), _ptr(d), sigma, flags, C.byref(h)))
+        self.handle = h
+
+    def info(self) -> dict:
+        inf = N.MapInfo()
+        N.check(N.lib().tsdfl_map_get_info(self.handle, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in N.MapInfo._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            N.lib().tsdfl_map_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Pose:
+    """Mean pose: position and roll/pitch/yaw (geometry_msgs::PoseWithCovariance
+    carries the same as a quaternion, tsdf_evaluator.cpp:223-229)."""
+
+    x: float
+    y: float
+    z: float
+    roll: float
+    pitch: float
+    yaw: float
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.x, self.y, self.z, self.roll, self.pitch, self.yaw], dtype=np.float32)
+
+
+class TSDFEvaluator:
+    """GPU sensor update with the reference evaluator's constructor and call.
+
+    per_point is accepted for signature compatibility; both reference modes
+    give the same weights here (the per-point kernel's range test on the
+    particle position, cuda_eval_particles.h:499, is not reproduced).
+    """
+
+    def __init__(self, device_map: DeviceMap, per_point: bool = False, a_hit: float = 0.9, a_range: float = 0.1,
+                 a_max: float = 0.0, max_range: float = 100.0, serial_sums: bool = False):
+        self.map = device_map
+        self.ctx = device_map.ctx
+        self.per_point = per_point
+        self.model = N.Model(a_hit, a_range, a_max, max_range)
+        self.flags = N.TSDFL_SUM_SERIAL if serial_sums else N.TSDFL_SUM_EXACT
+
+    def evaluate(self, particles: np.ndarray, points: np.ndarray, tf_matrix) -> Pose | None:
+        """Writes normalised weights into particles[:, 6]; returns the mean pose,
+        or None for an empty scan (the reference returns a default pose)."""
+        if not (isinstance(particles, np.ndarray) and particles.dtype == np.float32 and particles.flags.c_contiguous
+                and particles.ndim == 2 and particles.shape[1] == 7):
+            raise ValueError("particles must be a C-contiguous (P, 7) float32 array")
+        pts = _f32(points, 3)
+        tf = np.ascontiguousarray(np.asarray(tf_matrix, dtype=np.float32).reshape(16))
+        if pts.shape[0] == 0:
+            return None
+        pose = np.zeros(6, dtype=np.float32)
+        rc = N.lib().tsdfl_evaluate(self.ctx.handle, self.map.handle, C.byref(self.model), _ptr(particles),
+                                    particles.shape[0], _ptr(pts), pts.shape[0], _ptr(tf), self.flags, _ptr(pose))
+        N.check(rc)
+        return Pose(*[float(v) for v in pose])
+
+    def evaluate_debug(self, particles: np.ndarray, points: np.ndarray, tf_matrix, voxel_index: bool = False):
+        """evaluate() plus per-particle raw weights, hit counts, laser poses and
+        (small cases) the slot index of every particle*point."""
+        pts = _f32(points, 3)
+        tf = np.ascontiguousarray(np.asarray(tf_matrix, dtype=np.float32).reshape(16))
+        P, Nn = particles.shape[0], pts.shape[0]
+        raw = np.zeros(P, np.float32)
+        hits = np.zeros(P, np.uint32)
+        lp = np.zeros((P, 12), np.float32)
+        idx = np.zeros((P, Nn), np.uint32) if voxel_index else None
+        dbg = N.EvalDebug(raw.ctypes.data, hits.ctypes.data, idx.ctypes.data if idx is not None else None,
+                          lp.ctypes.data, 0.0)
+        pose = np.zeros(6, dtype=np.float32)
+        N.check(N.lib().tsdfl_evaluate_debug(self.ctx.handle, self.map.handle, C.byref(self.model), _ptr(particles),
+                                             P, _ptr(pts), Nn, _ptr(tf), self.flags, _ptr(pose), C.byref(dbg)))
+        return {"pose": pose, "raw": raw, "hits": hits, "laser_pose": lp, "voxel_index": idx,
+                "weight_sum": dbg.weight_sum}
+
+
+class SystematicResampler:
+    """SystematicResampler (novel_resampling.h:38-74) on the GPU.  The uniform
+    draw U0 ~ U[0, 1/M) comes from a seeded numpy generator unless given."""
+
+    def __init__(self, ctx: Context, seed: int | None = None):
+        self.ctx = ctx
+        self.rng = np.random.default_rng(seed)
+
+    def draw(self, m: int) -> float:
+        return float(np.float32(self.rng.random() * (1.0 / m)))
+
+    def resample_indices(self, weights: np.ndarray, u0: float | None = None, cap: int | None = None) -> np.ndarray:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        m = w.shape[0]
+        if u0 is None:
+            u0 = self.draw(m)
+        cap = cap if cap is not None else 2 * m + 16
+        out = np.zeros(max(cap, 1), np.uint32)
+        cnt = C.c_size_t()
+        N.check(N.lib().tsdfl_resample_systematic(self.ctx.handle, _ptr(w), m, np.float32(u0), _ptr(out), cap,
+                                                  C.byref(cnt)))
+        return out[: cnt.value]
+
+    def resample(self, particles: np.ndarray, u0: float | None = None) -> np.ndarray:
+        idx = self.resample_indices(particles[:, 6], u0)
+        return particles[idx].copy()
+
+
+def code_values(sigma: float = 0.1, init_value: float = 0.0) -> np.ndarray:
+    out = np.zeros(601, np.float32)
+    N.check(N.lib().tsdfl_code_values(sigma, init_value, _ptr(out)))
+    return out
+
+
+def build_map_codes(chunk_pos: np.ndarray, chunks: np.ndarray, edge: int, voxel_mm: int, sigma: float = 0.1,
+                    want_free: bool = True):
+    """createTSDFMap's likelihood map from TSDF chunks (map_util.h:17-154):
+    returns (coef, grid_occ, codes, free_xyz)."""
+    lib = N.lib()
+    pos = np.ascontiguousarray(chunk_pos, dtype=np.int32)
+    raw = np.ascontiguousarray(chunks, dtype=np.uint32)
+    n = pos.shape[0]
+    coef = N.MapCoef()
+    go = C.c_void_p()
+    cd = C.c_void_p()
+    fr = C.c_void_p()
+    nf = C.c_size_t()
+    N.check(lib.tsdfl_build_map_codes(_ptr(pos), _ptr(raw), n, edge, voxel_mm, sigma, C.byref(coef), C.byref(go),
+                                      C.byref(cd), C.byref(fr) if want_free else None,
+                                      C.byref(nf) if want_free else None))
+    try:
+        g = np.ctypeslib.as_array(C.cast(go, C.POINTER(C.c_int32)), (max(coef.grid_occ_size, 1),))
+        grid_occ = g[: coef.grid_occ_size].copy()
+        c = np.ctypeslib.as_array(C.cast(cd, C.POINTER(C.c_uint16)), (max(coef.data_size, 1),))
+        codes = c[: coef.data_size].copy()
+        free_xyz = np.zeros((0, 3), np.float32)
+        if want_free and nf.value:
+            f = np.ctypeslib.as_array(C.cast(fr, C.POINTER(C.c_float)), (nf.value * 3,))
+            free_xyz = f.reshape(-1, 3).copy()
+    finally:
+        lib.tsdfl_free(go)
+        lib.tsdfl_free(cd)
+        if want_free:
+            lib.tsdfl_free(fr)
+    return coef, grid_occ, codes, free_xyz
