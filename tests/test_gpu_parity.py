@@ -46,6 +46,27 @@ def _as_u32_index(idx, data_size):
     return np.where(idx < data_size, idx, MISS).astype(np.uint32)
 
 
+def _fp64_normalised(sum64):
+    return sum64 / sum64.sum()
+
+
+def _fp64_pose(particles, sum64):
+    """Weighted mean pose of tsdf_evaluator.cpp:198-221 in double precision."""
+    w = _fp64_normalised(sum64)
+    p = particles.astype(np.float64)
+    xyz = (p[:, :3] * w[:, None]).sum(0)
+    ang = [np.arctan2((np.sin(p[:, k]) * w).sum(), (np.cos(p[:, k]) * w).sum()) for k in (3, 4, 5)]
+    return np.concatenate([xyz, ang])
+
+
+def _check_normalised(gpu_w, ref_w, sum64):
+    f64 = _fp64_normalised(sum64)
+    err_gpu = np.abs(gpu_w.astype(np.float64) - f64)
+    err_ref = np.abs(ref_w.astype(np.float64) - f64)
+    assert np.all(err_gpu <= WEIGHT_RTOL * f64)
+    assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
+
+
 @pytest.mark.parametrize("layout", ["brick", "dense"])
 def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout):
     dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"))
@@ -65,8 +86,8 @@ def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout):
     err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
     assert np.all(err_gpu <= WEIGHT_RTOL * np.abs(f64))
     assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * np.abs(f64))
-    assert np.allclose(p[:, 6], ref["particles"][:, 6], rtol=WEIGHT_RTOL, atol=0)
-    assert np.allclose(d["pose"], ref["pose"], rtol=1e-5, atol=1e-5)
+    _check_normalised(p[:, 6], ref["particles"][:, 6], f64)
+    assert np.allclose(d["pose"], _fp64_pose(room.particles, f64), rtol=0, atol=2e-5)
     # inputs other than the weights untouched
     assert np.array_equal(p[:, :6], room.particles[:, :6])
 
@@ -82,7 +103,7 @@ def test_serial_mode_bit_exact(ctx, room, room_oracle):
     assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
     lp = np.stack([O.particle_pose(room.particles[i], room.tf) for i in range(room.particles.shape[0])])
     assert np.array_equal(d["laser_pose"], lp)
-    assert np.allclose(p[:, 6], ref["particles"][:, 6], rtol=WEIGHT_RTOL, atol=0)
+    _check_normalised(p[:, 6], ref["particles"][:, 6], ref["sum64"])
 
 
 def test_float_slot_map(ctx, room, room_oracle):

@@ -556,8 +556,8 @@ __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs 
     double U = (double)u0;
     long long j = 0;
     int ns = 0;
-    while (U < s_total) {
-        if (ns == kMaxSegments) { *ws.exact_ok = 0; break; }
+    for (int iter = 0; U < s_total; ++iter) {
+        if (ns == kMaxSegments || iter > 4 * kMaxSegments) { *ws.exact_ok = 0; break; }
         float uf = (float)U;
         int e;
         bool regular = false;
@@ -597,7 +597,9 @@ __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs 
             ws.segs[ns].n = 1;
             ++ns;
             j += 1;
-            U = (double)(float)(U + inv_m);
+            double next = (double)(float)(U + inv_m);
+            if (!(next > U)) { *ws.exact_ok = 0; break; }   // U stopped advancing
+            U = next;
         }
     }
     *ws.nseg = ns;
