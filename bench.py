@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
     ap.add_argument("--layout", default="dense", choices=["dense", "brick"])
+    ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -245,11 +246,11 @@ def main():
     ctx.reserve(P, Npts)
     rng = np.random.default_rng(1234 + rank)
     vp = C.c_void_p
+    eflags = N.TSDFL_SUM_EXACT | (N.TSDFL_EVAL_GENERIC if args.kernel == "generic" else 0)
 
     def step():
         N.check(lib.tsdfl_evaluate_device(ctx.handle, dmap.handle, C.byref(model), vp(d_part.data_ptr()), P,
-                                          vp(d_pts.data_ptr()), Npts, tfp, N.TSDFL_SUM_EXACT,
-                                          vp(d_pose.data_ptr())))
+                                          vp(d_pts.data_ptr()), Npts, tfp, eflags, vp(d_pose.data_ptr())))
         u0 = float(np.float32(rng.random() / P))
         N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(d_part.data_ptr()), P, u0,
                                                      vp(d_out.data_ptr()), cap, vp(d_cnt.data_ptr())))
@@ -296,7 +297,8 @@ def main():
     peak, peak_src = measured_peaks()
     achieved = alg / (kmed / 1000.0) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "eval_exact_kernel", "kernel_ms": kmed, "peak_source": peak_src,
+            "traffic": None, "kernel": "eval_fast_kernel" if (args.kernel == "fast" and info["fast_index"])
+            else "eval_exact_kernel", "kernel_ms": kmed, "peak_source": peak_src,
             "algorithmic_bytes": alg}
 
     # end to end through the host C ABI, pinned host buffers
@@ -313,8 +315,7 @@ def main():
         def e2e_step(i):
             h_part[:] = wl.particles
             N.check(lib.tsdfl_evaluate(ctx.handle, dmap.handle, C.byref(model), h_part.ctypes.data_as(vp), P,
-                                       h_pts.ctypes.data_as(vp), Npts, tfp, N.TSDFL_SUM_EXACT,
-                                       pose.ctypes.data_as(vp)))
+                                       h_pts.ctypes.data_as(vp), Npts, tfp, eflags, pose.ctypes.data_as(vp)))
             h_w[:] = h_part[:, 6]
             N.check(lib.tsdfl_resample_systematic(ctx.handle, h_w.ctypes.data_as(vp), P,
                                                   np.float32(rng.random() / P), h_idx.ctypes.data_as(vp), cap,
@@ -347,7 +348,7 @@ def main():
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": {"workload": wl.name, "particles": P, "points": Npts, "voxel_m": wl.voxel_mm / 1000.0,
-                          "layout": args.layout, "map_bricks": int(info["bricks"]),
+                          "layout": args.layout, "kernel": args.kernel, "map_bricks": int(info["bricks"]),
                           "map_device_bytes": int(info["device_bytes"]), "sums": "exact fixed point",
                           "l2": "flushed (512 MB write) before every timed step",
                           "step": "sensor update + normalise + mean pose + systematic resample",

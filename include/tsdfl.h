@@ -100,6 +100,8 @@ typedef struct tsdfl_map_info {
     uint64_t device_bytes;     /* all device memory the map holds */
     int32_t storage;           /* 0 = 16-bit codes, 1 = float */
     int32_t dense;             /* dense layout present */
+    int32_t fast_index;        /* division-free slot indexing verified for this resolution */
+    int32_t reserved;
 } tsdfl_map_info;
 int tsdfl_map_get_info(const tsdfl_map* map, tsdfl_map_info* info);
 
@@ -131,6 +133,7 @@ void tsdfl_free(void* p);
  * (cuda_evaluator.cu:122-125).  Weight sum 0 -> TSDFL_ERR_DEGENERATE. */
 #define TSDFL_SUM_EXACT 0u    /* order-independent fixed-point likelihood sums (default) */
 #define TSDFL_SUM_SERIAL 1u   /* reference order float sums: raw weights bit-identical */
+#define TSDFL_EVAL_GENERIC 4u /* exact sums with the generic (division-based) scoring kernel */
 int tsdfl_evaluate(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles, size_t P,
                    const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6]);
 

@@ -67,20 +67,25 @@ def _check_normalised(gpu_w, ref_w, sum64):
     assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
 
 
+def _codes_of(ref_idx, codes, data_size):
+    hit = ref_idx < data_size
+    return np.where(hit, codes[np.minimum(ref_idx, data_size - 1)], 601).astype(np.uint32)
+
+
+@pytest.mark.parametrize("kernel", ["fast", "generic"])
 @pytest.mark.parametrize("layout", ["brick", "dense"])
-def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout):
+def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
     dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"))
-    ev = TSDFEvaluator(dmap)
+    assert dmap.info()["fast_index"] == 1
+    ev = TSDFEvaluator(dmap, generic=(kernel == "generic"))
     ref = _oracle_eval(room_oracle, room)
     p = room.particles.copy()
     d = ev.evaluate_debug(p, room.points, room.tf, voxel_index=True)
     assert np.array_equal(d["hits"], ref["hits"])
-    if layout == "brick":
+    if layout == "brick" and kernel == "generic":
         assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
-    else:  # the dense kernel reports slot codes
-        codes_ref = np.where(ref["voxel_index"] < room.coef.data_size,
-                             room.codes[np.minimum(ref["voxel_index"], room.coef.data_size - 1)], 601)
-        assert np.array_equal(d["voxel_index"], codes_ref.astype(np.uint32))
+    else:  # these kernels report slot codes
+        assert np.array_equal(d["voxel_index"], _codes_of(ref["voxel_index"], room.codes, room.coef.data_size))
     f64 = ref["sum64"]
     err_gpu = np.abs(d["raw"].astype(np.float64) - f64)
     err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
@@ -90,6 +95,15 @@ def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout):
     assert np.allclose(d["pose"], _fp64_pose(room.particles, f64), rtol=0, atol=2e-5)
     # inputs other than the weights untouched
     assert np.array_equal(p[:, :6], room.particles[:, :6])
+
+
+def test_fast_and_generic_kernels_identical(ctx, room):
+    """Both exact-mode kernels give identical fixed-point sums, so identical weights."""
+    for dense in (False, True):
+        dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=dense)
+        a = TSDFEvaluator(dmap).evaluate_debug(room.particles.copy(), room.points, room.tf)
+        b = TSDFEvaluator(dmap, generic=True).evaluate_debug(room.particles.copy(), room.points, room.tf)
+        assert np.array_equal(a["raw"], b["raw"]) and np.array_equal(a["hits"], b["hits"])
 
 
 def test_serial_mode_bit_exact(ctx, room, room_oracle):
@@ -103,7 +117,8 @@ def test_serial_mode_bit_exact(ctx, room, room_oracle):
     assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
     lp = np.stack([O.particle_pose(room.particles[i], room.tf) for i in range(room.particles.shape[0])])
     assert np.array_equal(d["laser_pose"], lp)
-    _check_normalised(p[:, 6], ref["particles"][:, 6], ref["sum64"])
+    f64 = _fp64_normalised(ref["sum64"])
+    assert np.all(np.abs(p[:, 6] - f64) <= np.abs(ref["particles"][:, 6] - f64) + WEIGHT_RTOL * f64)
 
 
 def test_float_slot_map(ctx, room, room_oracle):
@@ -132,15 +147,20 @@ def test_points_outside_map_and_negative_offsets(ctx, room, room_oracle):
         np.array([[1e20, 0, 0], [-1e20, 0, 0], [0, 0, -3e19], [np.inf, 0, 0], [5, 5, 1e10]]),
     ]).astype(np.float32)
     parts = synth.particles_gaussian([0.3, 0.4, 0.2, 0, 0, 0], 0.6, 0.2, 64, 9)
-    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=True)
-    for serial in (True, False):
-        ev = TSDFEvaluator(dmap, serial_sums=serial)
-        ref = _oracle_eval(room_oracle, room, particles=parts, points=pts)
-        d = ev.evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)
-        assert np.array_equal(d["hits"], ref["hits"])
-        if serial:
-            assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
-            assert np.array_equal(d["raw"], ref["raw"])
+    ref = _oracle_eval(room_oracle, room, particles=parts, points=pts)
+    for dense in (False, True):
+        dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=dense)
+        for serial, generic in ((True, False), (False, False), (False, True)):
+            ev = TSDFEvaluator(dmap, serial_sums=serial, generic=generic)
+            d = ev.evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)
+            assert np.array_equal(d["hits"], ref["hits"])
+            if serial or (generic and not dense):
+                assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
+            else:
+                assert np.array_equal(d["voxel_index"], _codes_of(ref["voxel_index"], room.codes,
+                                                                  room.coef.data_size))
+            if serial:
+                assert np.array_equal(d["raw"], ref["raw"])
 
 
 def test_multi_pass_long_scan(ctx, room, room_oracle):

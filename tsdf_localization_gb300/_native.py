@@ -23,6 +23,7 @@ TSDFL_MAP_DENSE = 1
 TSDFL_MAP_FORCE_F32 = 2
 TSDFL_SUM_EXACT = 0
 TSDFL_SUM_SERIAL = 1
+TSDFL_EVAL_GENERIC = 4
 
 
 class MapCoef(C.Structure):
@@ -51,7 +52,8 @@ class Model(C.Structure):
 
 class MapInfo(C.Structure):
     _fields_ = [("grid_occ_size", C.c_uint64), ("data_size", C.c_uint64), ("bricks", C.c_uint64),
-                ("device_bytes", C.c_uint64), ("storage", C.c_int32), ("dense", C.c_int32)]
+                ("device_bytes", C.c_uint64), ("storage", C.c_int32), ("dense", C.c_int32),
+                ("fast_index", C.c_int32), ("reserved", C.c_int32)]
 
 
 class EvalDebug(C.Structure):

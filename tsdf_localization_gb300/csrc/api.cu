@@ -9,6 +9,7 @@
 #include <atomic>
 #include <mutex>
 #include <new>
+#include <algorithm>
 #include <vector>
 
 #include "map_host.h"
@@ -122,6 +123,9 @@ int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
     size_t o_ys = take(sizeof(float) * npad);
     size_t o_zs = take(sizeof(float) * npad);
     size_t o_cs = take(sizeof(float) * npad);
+    size_t npairs = 32 * ((nN + 63) / 64);
+    size_t o_pxy = take(sizeof(float) * 4 * npairs);
+    size_t o_pz = take(sizeof(float) * 2 * npairs);
     size_t o_lfx = take(sizeof(long long) * kNumCodes);
     size_t o_lf = take(sizeof(float) * kNumCodes);
     size_t o_cnt = take(sizeof(int32_t) * 16);
@@ -146,6 +150,8 @@ int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
     e.ys = reinterpret_cast<float*>(b + o_ys);
     e.zs = reinterpret_cast<float*>(b + o_zs);
     e.cs = reinterpret_cast<float*>(b + o_cs);
+    e.pxy = reinterpret_cast<float4*>(b + o_pxy);
+    e.pz = reinterpret_cast<float2*>(b + o_pz);
     e.lut_fx = reinterpret_cast<long long*>(b + o_lfx);
     e.lut_f = reinterpret_cast<float*>(b + o_lf);
     e.counts = reinterpret_cast<int32_t*>(b + o_cnt);
@@ -231,6 +237,17 @@ void fill_view(tsdfl_map* m)
     v.data = m->data;
     v.dense = m->dense;
     v.storage = m->codes ? 0 : 1;
+    v.sub_fast = sub_index_table(c.resolution, c.sub_dim, &v.sub_inv, v.sub_thr, kSubThr);
+    auto lim = [](int32_t mmax) {
+        float f = (float)std::min<int64_t>((int64_t)mmax + 1, 4194304);
+        if (mmax < 0) f = 0.0f;
+        uint32_t b;
+        std::memcpy(&b, &f, 4);
+        return b;
+    };
+    v.lim_x = lim(v.mmax_x);
+    v.lim_y = lim(v.mmax_y);
+    v.lim_z = lim(v.mmax_z);
 }
 
 int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
@@ -317,7 +334,7 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     for (size_t n0 = 0; n0 < N; n0 += pass) {
         size_t n1 = n0 + pass < N ? n0 + pass : N;
         rc = launch_eval_pass(map->view, mdl->a_hit, (int)P, (int)n0, (int)n1, (int)N, n0 == 0, serial,
-                              dense && !serial, b, c->sum_f64, c->sm_count, s);
+                              dense && !serial, (flags & TSDFL_EVAL_GENERIC) != 0, b, c->sum_f64, c->sm_count, s);
         if (rc) return rc;
     }
     if (c->timing) {
@@ -558,6 +575,8 @@ int tsdfl_map_get_info(const tsdfl_map* m, tsdfl_map_info* info)
     info->device_bytes = m->bytes;
     info->storage = m->codes ? 0 : 1;
     info->dense = m->dense ? 1 : 0;
+    info->fast_index = m->view.sub_fast;
+    info->reserved = 0;
     return TSDFL_OK;
 }
 

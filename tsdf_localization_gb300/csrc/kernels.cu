@@ -132,7 +132,7 @@ __device__ __forceinline__ uint32_t dense_code(const MapView& m, float x, float 
 
 struct PointParams {
     const float* points;  // N x 3
-    int N, npad;
+    int N, npad, npairs;
     float max_range_sq, c_in, c_out;
     const float* code_values;  // kNumCodes floats (device)
     int shift;                 // fixed-point scale 2^shift
@@ -161,6 +161,17 @@ __global__ void prepare_points_kernel(PointParams p, EvalBuffers b)
         ((float*)b.ys)[j] = y;
         ((float*)b.zs)[j] = z;
         ((float*)b.cs)[j] = c;
+    }
+    // pair layout of the fast kernel: in every block of 64 points, lane l of a
+    // warp takes points 64*blk + l and 64*blk + 32 + l
+    for (int q = threadIdx.x; q < p.npairs; q += blockDim.x) {
+        int blk = q >> 5, l = q & 31;
+        int ja = 64 * blk + l, jb = ja + 32;
+        float xa = 0, ya = 0, za = 0, xb = 0, yb = 0, zb = 0;
+        if (ja < p.N) { xa = p.points[3 * ja]; ya = p.points[3 * ja + 1]; za = p.points[3 * ja + 2]; }
+        if (jb < p.N) { xb = p.points[3 * jb]; yb = p.points[3 * jb + 1]; zb = p.points[3 * jb + 2]; }
+        b.pxy[q] = make_float4(xa, xb, ya, yb);
+        b.pz[q] = make_float2(za, zb);
     }
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) {
         float v = p.code_values[c];
@@ -231,6 +242,8 @@ __global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose1
 
 struct EvalParams {
     MapView m;
+    const float4* pxy;
+    const float2* pz;
     const float* pose12;
     const float* xs;
     const float* ys;
@@ -310,6 +323,192 @@ __global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
             if (F32) p.sum_f64[pi] = p.first_pass ? accd : p.sum_f64[pi] + accd;
             else p.sum_fx[pi] = p.first_pass ? acc : p.sum_fx[pi] + acc;
             p.hits[pi] = p.first_pass ? h : p.hits[pi] + h;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- fast kernel
+
+typedef unsigned long long f2_t;   // two floats in one 64-bit register pair
+
+__device__ __forceinline__ f2_t pk(float a, float b)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2_t v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2_t add2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t add2_rz(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("add.rz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t sub2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t fma2_rz(f2_t a, f2_t b, f2_t c)
+{
+    f2_t r;
+    asm("fma.rz.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+constexpr uint32_t kMagic = 0x4B000000u;   // bits of 2^23
+constexpr uint32_t kFastLimitBits = 0x4A800000u;   // bits of 2^22
+
+// Code of a point the fast path does not cover: a coarse-bound miss is decided
+// directly, everything else goes through the full reference semantics.
+template <bool DENSE>
+__device__ __noinline__ uint32_t slow_code(const MapView& m, float x, float y, float z)
+{
+    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
+    uint32_t bx = __float_as_uint(ox), by = __float_as_uint(oy), bz = __float_as_uint(oz);
+    bool beyond = (bx >= m.lim_x && bx < kFastLimitBits && m.lim_x < kFastLimitBits) ||
+                  (by >= m.lim_y && by < kFastLimitBits && m.lim_y < kFastLimitBits) ||
+                  (bz >= m.lim_z && bz < kFastLimitBits && m.lim_z < kFastLimitBits);
+    if (beyond) return kCodeMiss;   // trunc(offset) > mmax: the coarse bound check fails
+    uint32_t idx = slot_index_slow(m, x, y, z);
+    return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
+}
+
+// Fast path of one point: o* are the map offsets, t* = 2^23 + trunc(offset),
+// c* = 2^23 + floor(sub * sub_inv), s* the sub-voxel positions (all floats).
+template <bool DENSE>
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const float* thr, float tx, float ty, float tz,
+                                              float ox, float oy, float oz, float mx, float my, float mz, float sx,
+                                              float sy, float sz, float cx, float cy, float cz)
+{
+    uint32_t bx = __float_as_uint(ox), by = __float_as_uint(oy), bz = __float_as_uint(oz);
+    bool fast = bx < m.lim_x && by < m.lim_y && bz < m.lim_z;
+    if (fast) {
+        uint32_t ix = __float_as_uint(cx) - kMagic, iy = __float_as_uint(cy) - kMagic,
+                 iz = __float_as_uint(cz) - kMagic;
+        uint32_t qx = ix + (sx >= thr[ix + 1] ? 1u : 0u);
+        uint32_t qy = iy + (sy >= thr[iy + 1] ? 1u : 0u);
+        uint32_t qz = iz + (sz >= thr[iz + 1] ? 1u : 0u);
+        uint32_t up = (__float_as_uint(mx) - kMagic) + (__float_as_uint(my) - kMagic) * m.up_dim_x +
+                      (__float_as_uint(mz) - kMagic) * m.up_dim_2;
+        if (up >= m.grid_occ_size) return kCodeMiss;
+        uint32_t sl = qx + qy * m.sub_dim + qz * m.sub_dim_2;
+        if (DENSE) {
+            if (sl < m.sub_dim_3) return __ldg(m.dense + (size_t)up * m.sub_dim_3 + sl);
+        } else {
+            int32_t base = __ldg(m.grid_occ + up);
+            if (base < 0) return kCodeMiss;
+            uint32_t idx = (uint32_t)base + sl;
+            return idx < m.data_size ? (uint32_t)__ldg(m.codes + idx) : (uint32_t)kCodeMiss;
+        }
+    }
+    return slow_code<DENSE>(m, tx, ty, tz);
+}
+
+constexpr int kFastThreads = 768;
+
+// Fast exact mode: one warp per particle, every lane scores two scan points
+// per step with packed f32x2 arithmetic; no divisions or float<->int
+// conversions on the fast path (truncation by round-toward-zero adds of 2^23,
+// the sub-voxel index from a verified threshold table).  Results are identical
+// to eval_exact_kernel.
+template <bool DENSE>
+__global__ void __launch_bounds__(kFastThreads, 1) eval_fast_kernel(EvalParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ float thr[kSubThr];
+    long long* lut = reinterpret_cast<long long*>(smem);
+    const int n = p.n1 - p.n0;
+    const int nblk = (n + 63) >> 6;
+    const int npairs = nblk * 32;
+    float4* sxy = reinterpret_cast<float4*>(smem + kLutBytes);
+    float2* sz = reinterpret_cast<float2*>(sxy + npairs);
+    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
+    if (threadIdx.x < kSubThr) thr[threadIdx.x] = p.m.sub_thr[threadIdx.x];
+    // bulk copies of the point pairs of this pass
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t bxy = (uint32_t)npairs * 16u, bz = (uint32_t)npairs * 8u;
+        mbar_expect_tx(&bar, bxy + bz);
+        bulk_g2s(sxy, p.pxy + p.n0 / 2, bxy, &bar);
+        bulk_g2s(sz, p.pz + p.n0 / 2, bz, &bar);
+    }
+    bool ok = mbar_wait_bounded(&bar, 0);
+    if (!ok && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
+    if (__syncthreads_and(ok ? 1 : 0) == 0) return;
+
+    const MapView& m = p.m;
+    const int lane = threadIdx.x & 31;
+    const int warps = (blockDim.x >> 5) * gridDim.x;
+    const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
+    const f2_t MAG = pk(8388608.0f, 8388608.0f);
+    const f2_t INV = pk(m.sub_inv, m.sub_inv);
+    const int nfull = n >> 6;
+    for (int pi = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); pi < p.P; pi += warps) {
+        const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
+        float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
+        const f2_t R0 = pk(a.x, a.x), R1 = pk(a.y, a.y), R2 = pk(a.z, a.z), R3 = pk(a.w, a.w);
+        const f2_t R4 = pk(b4.x, b4.x), R5 = pk(b4.y, b4.y), R6 = pk(b4.z, b4.z), R7 = pk(b4.w, b4.w);
+        const f2_t R8 = pk(c4.x, c4.x), R9 = pk(c4.y, c4.y), R10 = pk(c4.z, c4.z), R11 = pk(c4.w, c4.w);
+        long long acc = 0;
+        uint32_t hits = 0;
+        for (int blk = 0; blk < nblk; ++blk) {
+            float4 xy = sxy[blk * 32 + lane];
+            float2 zz = sz[blk * 32 + lane];
+            f2_t X = pk(xy.x, xy.y), Y = pk(xy.z, xy.w), Z = pk(zz.x, zz.y);
+            // tsdf_evaluator.cpp:44-46, two points at a time
+            f2_t TX = add2(add2(add2(mul2(R0, X), mul2(R1, Y)), mul2(R2, Z)), R3);
+            f2_t TY = add2(add2(add2(mul2(R4, X), mul2(R5, Y)), mul2(R6, Z)), R7);
+            f2_t TZ = add2(add2(add2(mul2(R8, X), mul2(R9, Y)), mul2(R10, Z)), R11);
+            f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
+            f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);   // 2^23 + trunc
+            f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
+            f2_t CX = fma2_rz(SX, INV, MAG), CY = fma2_rz(SY, INV, MAG), CZ = fma2_rz(SZ, INV, MAG);
+            float tx0, tx1, ty0, ty1, tz0, tz1, ox0, ox1, oy0, oy1, oz0, oz1, mx0, mx1, my0, my1, mz0, mz1;
+            float sx0, sx1, sy0, sy1, sz0, sz1, cx0, cx1, cy0, cy1, cz0, cz1;
+            upk(TX, tx0, tx1); upk(TY, ty0, ty1); upk(TZ, tz0, tz1);
+            upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1);
+            upk(MX, mx0, mx1); upk(MY, my0, my1); upk(MZ, mz0, mz1);
+            upk(SX, sx0, sx1); upk(SY, sy0, sy1); upk(SZ, sz0, sz1);
+            upk(CX, cx0, cx1); upk(CY, cy0, cy1); upk(CZ, cz0, cz1);
+            uint32_t c0 = fast_code<DENSE>(m, thr, tx0, ty0, tz0, ox0, oy0, oz0, mx0, my0, mz0, sx0, sy0, sz0, cx0,
+                                           cy0, cz0);
+            uint32_t c1 = fast_code<DENSE>(m, thr, tx1, ty1, tz1, ox1, oy1, oz1, mx1, my1, mz1, sx1, sy1, sz1, cx1,
+                                           cy1, cz1);
+            if (blk >= nfull) {   // the last, partial block
+                if (64 * blk + lane >= n) c0 = kCodeNone;
+                if (64 * blk + 32 + lane >= n) c1 = kCodeNone;
+            }
+            if (p.dbg) {
+                if (64 * blk + lane < n) p.dbg[(size_t)pi * p.n_total + p.n0 + 64 * blk + lane] = c0;
+                if (64 * blk + 32 + lane < n) p.dbg[(size_t)pi * p.n_total + p.n0 + 64 * blk + 32 + lane] = c1;
+            }
+            acc += lut[c0] + lut[c1];
+            hits += __popc(__ballot_sync(0xffffffffu, c0 <= (uint32_t)kCodeInit)) +
+                    __popc(__ballot_sync(0xffffffffu, c1 <= (uint32_t)kCodeInit));
+        }
+        acc = warp_sum_ll(acc);
+        if (lane == 0) {
+            p.sum_fx[pi] = p.first_pass ? acc : p.sum_fx[pi] + acc;
+            p.hits[pi] = p.first_pass ? hits : p.hits[pi] + hits;
         }
     }
 }
@@ -752,7 +951,7 @@ int check(cudaError_t e)
 int launch_prepare(const float* points, int N, int npad, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
 {
-    PointParams p{points, N, npad, max_range_sq, c_in, c_out, code_values, shift};
+    PointParams p{points, N, npad, 32 * ((N + 63) / 64), max_range_sq, c_in, c_out, code_values, shift};
     prepare_points_kernel<<<1, 1024, 0, s>>>(p, b);
     g_launches += 1;
     return check(cudaGetLastError());
@@ -776,12 +975,13 @@ size_t eval_smem_bytes(bool serial, int n)
 }
 
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
-                     bool dense, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s)
+                     bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s)
 {
     EvalParams p;
     p.m = m;
     p.pose12 = b.pose12;
     p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
+    p.pxy = b.pxy; p.pz = b.pz;
     p.lut_fx = b.lut_fx;
     p.lut_f = b.lut_f;
     p.sum_fx = b.sum_fx;
@@ -798,6 +998,15 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         auto k = f32 ? eval_serial_kernel<true> : eval_serial_kernel<false>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k<<<(P + 255) / 256, 256, smem, s>>>(p);
+        g_launches += 1;
+    } else if (!f32 && m.sub_fast && !generic) {
+        auto k = dense ? eval_fast_kernel<true> : eval_fast_kernel<false>;
+        size_t fsmem = (size_t)kLutBytes + (size_t)(32 * (((n1 - n0) + 63) / 64)) * 24;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
+        int blocks = sm_count;
+        int need = (P + kFastThreads / 32 - 1) / (kFastThreads / 32);
+        if (need < blocks) blocks = need > 0 ? need : 1;
+        k<<<blocks, kFastThreads, fsmem, s>>>(p);
         g_launches += 1;
     } else {
         auto k = dense && !f32 ? eval_exact_kernel<true, false>

@@ -50,11 +50,12 @@ float likelihood_init(float sigma)
     return init * init * init;
 }
 
-void code_values(float sigma, float init_value, float out[602])
+void code_values(float sigma, float init_value, float out[603])
 {
     for (int c = 0; c < 600; ++c) out[c] = likelihood_value(c, sigma);
     out[600] = init_value;
     out[601] = init_value;
+    out[602] = 0.0f;
 }
 
 // CudaSubVoxelMap ctor (cuda_sub_voxel_map.tcc:4-48)
@@ -115,6 +116,55 @@ int32_t coarse_mmax(uint64_t dim, float res)
     return 4194304;
 }
 
+// Smallest non-negative float s (searched up to 2.0) for which pred(s) holds;
+// pred must be monotone in s.  2.0 when it never holds below 2.
+template <class Pred>
+static float min_float_where(Pred pred)
+{
+    uint32_t lo = 0, hi;
+    float two = 2.0f;
+    std::memcpy(&hi, &two, 4);
+    if (!pred(two)) return two;
+    while (lo < hi) {   // float order == bit order for non-negative floats
+        uint32_t mid = lo + (hi - lo) / 2;
+        float f;
+        std::memcpy(&f, &mid, 4);
+        if (pred(f)) hi = mid;
+        else lo = mid + 1;
+    }
+    float f;
+    std::memcpy(&f, &lo, 4);
+    return f;
+}
+
+int sub_index_table(float res, uint64_t sub_dim, float* inv_out, float* thr, int n)
+{
+    if (!(res > 0.0f) || sub_dim + 2 > (uint64_t)n) return 0;
+    const int K = (int)sub_dim + 1;
+    for (int k = 0; k < n; ++k) thr[k] = 2.0f;
+    thr[0] = 0.0f;
+    for (int k = 1; k <= K; ++k)
+        thr[k] = min_float_where([&](float s) { return f2u_x86_host(s / res) >= (uint64_t)k; });
+    float inv = 1.0f / res;
+    auto approx_thr = [&](int k, float m) {
+        return min_float_where([&](float s) { return std::floor((double)s * (double)m) >= (double)k; });
+    };
+    for (int tries = 0; tries < 64; ++tries) {
+        bool low_ok = true;   // floor(s*inv) <= q  <=>  approx threshold k is not below the exact one
+        for (int k = 1; k <= K && low_ok; ++k) low_ok = approx_thr(k, inv) >= thr[k];
+        if (low_ok) break;
+        inv = std::nextafter(inv, 0.0f);
+    }
+    for (int k = 1; k <= K; ++k) {
+        float a = approx_thr(k, inv);
+        if (a < thr[k]) return 0;                   // could overshoot q
+        if (k + 1 <= K && a > thr[k + 1]) return 0;  // could undershoot q by two
+    }
+    if (std::floor(1.0 * (double)inv) > (double)K - 1) return 0;   // c + 1 must stay inside the table
+    *inv_out = inv;
+    return 1;
+}
+
 }  // namespace tsdfl
 
 using namespace tsdfl;
@@ -140,7 +190,7 @@ void tsdfl_free(void* p) { std::free(p); }
 
 int tsdfl_code_values(float sigma, float init_value, float* out601)
 {
-    float v[602];
+    float v[603];
     code_values(sigma, init_value, v);
     std::memcpy(out601, v, sizeof(float) * 601);
     return TSDFL_OK;

@@ -13,7 +13,8 @@ namespace tsdfl {
 // the dense layout (a miss).
 constexpr int kCodeInit = 600;
 constexpr int kCodeMiss = 601;
-constexpr int kNumCodes = 602;
+constexpr int kCodeNone = 602;   // no point (padding): no hit, contributes 0
+constexpr int kNumCodes = 603;
 constexpr uint32_t kMissIndex = 0xffffffffu;
 
 // Largest scan a single evaluation pass stages in shared memory (3 floats per
@@ -23,6 +24,8 @@ constexpr int kMaxPassPoints = 16384;
 // Fast-path bound on a map offset (metres): below it float->integer conversions
 // are exact and cannot wrap.
 constexpr float kFastOffsetLimit = 4194304.0f;
+
+constexpr int kSubThr = 32;
 
 // Everything a kernel needs to look a point up in one map, passed by value
 // (kernel parameters live in the constant bank).
@@ -44,6 +47,13 @@ struct MapView {
     const float* data;        // float slots (storage 1)
     const uint16_t* dense;    // dense brick layout (may be null)
     int32_t storage;          // 0 = codes, 1 = float
+    // Division-free sub-voxel index for s in [0, 1):
+    //   trunc(s / res) == c + (s >= sub_thr[c + 1]),  c = floor(s * sub_inv)
+    // (exact for every float s; verified on the host, sub_fast = 1 when it holds).
+    int32_t sub_fast;
+    float sub_inv;
+    float sub_thr[kSubThr];
+    uint32_t lim_x, lim_y, lim_z;  // float bits of min(mmax + 1, 2^22) per axis
 };
 
 #ifdef __CUDACC__
@@ -136,6 +146,8 @@ struct EvalBuffers {
     const float* ys;
     const float* zs;
     const float* cs;         // per-point score constant (a_range*inv_max_range or a_max)
+    float4* pxy;             // point pairs (x_a, x_b, y_a, y_b) per 64-point block
+    float2* pz;              // point pairs (z_a, z_b)
     float* pose12;           // P x 12 laser poses
     float* trig6;            // P x 6: sin/cos of roll, pitch, yaw
     long long* sum_fx;       // P: fixed-point likelihood sums
@@ -156,7 +168,7 @@ int launch_prepare(const float* points, int N, int npad, float max_range_sq, flo
 int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
 size_t eval_smem_bytes(bool serial, int n);
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
-                     bool dense, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
+                     bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s);
 int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s);

@@ -124,12 +124,13 @@ class TSDFEvaluator:
     """
 
     def __init__(self, device_map: DeviceMap, per_point: bool = False, a_hit: float = 0.9, a_range: float = 0.1,
-                 a_max: float = 0.0, max_range: float = 100.0, serial_sums: bool = False):
+                 a_max: float = 0.0, max_range: float = 100.0, serial_sums: bool = False, generic: bool = False):
         self.map = device_map
         self.ctx = device_map.ctx
         self.per_point = per_point
         self.model = N.Model(a_hit, a_range, a_max, max_range)
-        self.flags = N.TSDFL_SUM_SERIAL if serial_sums else N.TSDFL_SUM_EXACT
+        self.flags = (N.TSDFL_SUM_SERIAL if serial_sums else N.TSDFL_SUM_EXACT) | (N.TSDFL_EVAL_GENERIC if generic
+                                                                                    else 0)
 
     def evaluate(self, particles: np.ndarray, points: np.ndarray, tf_matrix) -> Pose | None:
         """Writes normalised weights into particles[:, 6]; returns the mean pose,
@@ -148,8 +149,10 @@ class TSDFEvaluator:
         return Pose(*[float(v) for v in pose])
 
     def evaluate_debug(self, particles: np.ndarray, points: np.ndarray, tf_matrix, voxel_index: bool = False):
-        """evaluate() plus per-particle raw weights, hit counts, laser poses and
-        (small cases) the slot index of every particle*point."""
+        """evaluate() plus per-particle raw weights, hit counts, laser poses and,
+        for small cases, per particle*point: the slot index (serial sums, and
+        the generic kernel on the brick layout) or the slot code (0..599 |tsdf|
+        mm, 600 init, 601 miss) otherwise."""
         pts = _f32(points, 3)
         tf = np.ascontiguousarray(np.asarray(tf_matrix, dtype=np.float32).reshape(16))
         P, Nn = particles.shape[0], pts.shape[0]
