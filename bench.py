@@ -297,7 +297,7 @@ def main():
     peak, peak_src = measured_peaks()
     achieved = alg / (kmed / 1000.0) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "eval_fast_kernel" if (args.kernel == "fast" and info["fast_index"])
+            "traffic": None, "kernel": "eval_tiled_kernel" if (args.kernel == "fast" and info["fast_index"])
             else "eval_exact_kernel", "kernel_ms": kmed, "peak_source": peak_src,
             "algorithmic_bytes": alg}
 

@@ -1,0 +1,110 @@
+// Compares the library's slot-index arithmetic (index_math.h: the signed
+// second tier, and a host emulation of the division-free fast path) with the
+// oracle's getIndex (oracle/tsdf_oracle.c) on random maps and points,
+// including negative, out-of-bounds and special offsets.  Exit status 0 when
+// every handled lookup matches; prints counts.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "index_math.h"
+#include "map_host.h"
+
+extern "C" {
+#include "tsdf_oracle.h"
+}
+
+namespace tsdfl {
+void set_error(const char*, ...) {}
+}
+using namespace tsdfl;
+
+static uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+int main(int argc, char** argv)
+{
+    long n_points = argc > 1 ? atol(argv[1]) : 2000000;
+    const float ress[] = {0.064f, 0.05f, 0.1f, 0.08f, 0.04f};
+    const float mins[][3] = {{0, 0, 0}, {-4.096f, -8.192f, -4.096f}, {-10.0f, 3.2f, -0.3f}};
+    std::mt19937_64 rng(12345);
+    long bad = 0, handled = 0, slow = 0, fast_n = 0, fast_bad = 0;
+    for (float res : ress)
+        for (auto& mn0 : mins) {
+            float mn[3] = {mn0[0], mn0[1], mn0[2]};
+            float mx[3] = {mn[0] + 21.3f, mn[1] + 17.7f, mn[2] + 6.1f};
+            orc_map_coef c;
+            orc_map_coef_init(&c, mn, mx, res, 0.0f);
+            std::vector<int32_t> go(c.grid_occ_size);
+            int32_t off = 0;
+            int32_t S3 = (int32_t)(c.sub_dim * c.sub_dim_2);
+            for (auto& g : go) {
+                g = (rng() % 3 == 0) ? -1 : off;
+                if (g >= 0) off += S3;
+            }
+            c.data_size = (uint64_t)off;
+            MapView v{};
+            v.min_x = c.min_x; v.min_y = c.min_y; v.min_z = c.min_z;
+            v.res = c.resolution;
+            v.mmax_x = coarse_mmax(c.dim_x, res); v.mmax_y = coarse_mmax(c.dim_y, res); v.mmax_z = coarse_mmax(c.dim_z, res);
+            auto lim = [](int32_t mm) { return mm < 0 ? 0u : fbits((float)std::min<int64_t>((int64_t)mm + 1, 4194304)); };
+            v.lim_x = lim(v.mmax_x); v.lim_y = lim(v.mmax_y); v.lim_z = lim(v.mmax_z);
+            v.up_dim_x = (uint32_t)c.up_dim_x; v.up_dim_2 = (uint32_t)c.up_dim_2; v.grid_occ_size = (uint32_t)c.grid_occ_size;
+            v.sub_dim = (uint32_t)c.sub_dim; v.sub_dim_2 = (uint32_t)c.sub_dim_2; v.sub_dim_3 = (uint32_t)S3;
+            v.data_size = (uint32_t)c.data_size;
+            v.dim_x = c.dim_x; v.dim_y = c.dim_y; v.dim_z = c.dim_z;
+            v.up_dim_x64 = c.up_dim_x; v.up_dim_2_64 = c.up_dim_2; v.grid_occ_size64 = c.grid_occ_size;
+            v.sub_dim64 = c.sub_dim; v.sub_dim_2_64 = c.sub_dim_2; v.data_size64 = c.data_size;
+            v.sub_fast = sub_index_table(res, c.sub_dim, &v.sub_inv, v.sub_thr, kSubThr);
+            std::uniform_real_distribution<float> U(-3.5f, 25.0f);
+            const float special[] = {-1.0f, -0.99999994f, -0.5f, -0.0f, 0.0f, 1e-30f, 0.99999994f, 1.0f, -2.0f, -1e-7f};
+            for (long i = 0; i < n_points; ++i) {
+                float o[3];
+                for (int a = 0; a < 3; ++a) {
+                    uint64_t r = rng();
+                    if (r % 17 == 0) o[a] = special[(r >> 8) % 10];
+                    else if (r % 17 == 1) o[a] = (float)((int)((r >> 8) % 30)) + ((r >> 40) % 2 ? -1e-6f : 1e-6f);
+                    else o[a] = U(rng);
+                }
+                if (i % 1000 == 0) o[i / 1000 % 3] = (i / 3000) % 2 ? NAN : 1e20f;
+                float x = mn[0] + o[0], y = mn[1] + o[1], z = mn[2] + o[2];
+                // the offsets the device computes: point - min, rounded once
+                float ox = x - mn[0], oy = y - mn[1], oz = z - mn[2];
+                uint64_t ref = orc_get_index(&c, go.data(), x, y, z);
+                uint32_t want = ref < c.data_size ? (uint32_t)ref : kIdxMiss;
+                uint32_t t2 = slot_index_tier2(v, go.data(), ox, oy, oz);
+                if (t2 == kIdxSlow) { ++slow; continue; }
+                ++handled;
+                if (t2 != want) {
+                    if (bad < 10) printf("tier2 mismatch res=%g o=(%.9g %.9g %.9g) got %u want %u\n", res, ox, oy, oz, t2, want);
+                    ++bad;
+                }
+                // fast path emulation (only for offsets inside [0, mmax + 1) on every axis)
+                if (v.sub_fast && fbits(ox) < v.lim_x && fbits(oy) < v.lim_y && fbits(oz) < v.lim_z) {
+                    ++fast_n;
+                    float oo[3] = {ox, oy, oz};
+                    int64_t mm[3], qq[3];
+                    for (int a = 0; a < 3; ++a) {
+                        mm[a] = (int64_t)oo[a];
+                        float s = oo[a] - (float)mm[a];
+                        int64_t cc = (int64_t)std::floor((double)s * (double)v.sub_inv);
+                        qq[a] = v.sub_fast == 2 ? cc : cc + (s >= v.sub_thr[cc + 1] ? 1 : 0);
+                    }
+                    uint64_t up = (uint64_t)(mm[0] + mm[1] * (int64_t)c.up_dim_x + mm[2] * (int64_t)c.up_dim_2);
+                    uint32_t got = kIdxMiss;
+                    if (up < c.grid_occ_size && go[up] >= 0) {
+                        uint64_t idx = (uint64_t)go[up] + qq[0] + qq[1] * c.sub_dim + qq[2] * c.sub_dim_2;
+                        if (idx < c.data_size) got = (uint32_t)idx;
+                    }
+                    if (got != want) {
+                        if (fast_bad < 10) printf("fast mismatch res=%g o=(%.9g %.9g %.9g) got %u want %u\n", res, ox, oy, oz, got, want);
+                        ++fast_bad;
+                    }
+                }
+            }
+        }
+    printf("handled %ld slow %ld tier2_bad %ld fast %ld fast_bad %ld\n", handled, slow, bad, fast_n, fast_bad);
+    return (bad || fast_bad) ? 1 : 0;
+}

@@ -76,11 +76,13 @@ def _codes_of(ref_idx, codes, data_size):
 @pytest.mark.parametrize("layout", ["brick", "dense"])
 def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
     dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"))
-    assert dmap.info()["fast_index"] == 1
+    assert dmap.info()["fast_index"] in (1, 2)
     ev = TSDFEvaluator(dmap, generic=(kernel == "generic"))
     ref = _oracle_eval(room_oracle, room)
     p = room.particles.copy()
     d = ev.evaluate_debug(p, room.points, room.tf, voxel_index=True)
+    if kernel == "fast":
+        d["voxel_index"] &= 0xFFFF   # drop the slow-path flag of the tiled kernel
     assert np.array_equal(d["hits"], ref["hits"])
     if layout == "brick" and kernel == "generic":
         assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
@@ -153,6 +155,8 @@ def test_points_outside_map_and_negative_offsets(ctx, room, room_oracle):
         for serial, generic in ((True, False), (False, False), (False, True)):
             ev = TSDFEvaluator(dmap, serial_sums=serial, generic=generic)
             d = ev.evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)
+            if not serial and not generic:
+                d["voxel_index"] &= 0xFFFF
             assert np.array_equal(d["hits"], ref["hits"])
             if serial or (generic and not dense):
                 assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))

@@ -1,0 +1,26 @@
+"""CPU check of the slot-index arithmetic the kernels use (signed second tier
+and the division-free fast path) against the oracle's getIndex, on random maps
+with negative, out-of-bounds and special offsets."""
+import shutil
+import subprocess
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_index_math_matches_oracle(tmp_path):
+    exe = tmp_path / "index_check"
+    csrc = ROOT / "tsdf_localization_gb300" / "csrc"
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda_inc = Path(nvcc).resolve().parent.parent / "include"
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp",
+           "-I", str(csrc), "-I", str(ROOT / "include"), "-I", str(ROOT / "oracle"), "-I", str(cuda_inc),
+           str(ROOT / "tests" / "native" / "index_check.cpp"), str(csrc / "map_build.cpp"),
+           "-x", "c", str(ROOT / "oracle" / "tsdf_oracle.c"), "-o", str(exe), "-lm"]
+    subprocess.run(cmd, check=True)
+    res = subprocess.run([str(exe), "400000"], capture_output=True, text=True)
+    print(res.stdout)
+    assert res.returncode == 0, res.stdout
+    handled = int(res.stdout.split("handled ")[1].split()[0])
+    fast = int(res.stdout.split("fast ")[1].split()[0])
+    assert handled > 1_000_000 and fast > 100_000

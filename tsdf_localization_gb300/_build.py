@@ -63,7 +63,9 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         o = OBJ / (src.stem + ".o")
         objs.append(o)
         if force or _stale(o, [src] + headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            # -fmad=false: no multiply-add contraction anywhere (the scan transform
+            # must round after every product and sum, as the reference does)
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                          "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(src), "-o", str(o)])
     for src in cpp_lib:
         o = OBJ / (src.stem + ".o")

@@ -125,9 +125,11 @@ _synth = None
 
 
 def lib() -> C.CDLL:
+    """libtsdfl.so of this package, or the build named by TSDFL_LIBRARY."""
     global _lib
     if _lib is None:
-        _lib = _load(_LIB_DIR / "libtsdfl.so", SIGNATURES)
+        import os
+        _lib = _load(Path(os.environ.get("TSDFL_LIBRARY", _LIB_DIR / "libtsdfl.so")), SIGNATURES)
     return _lib
 
 

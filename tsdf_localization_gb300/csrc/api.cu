@@ -328,7 +328,7 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     if (rc) return rc;
     rc = launch_pose_kernel(tf, (int)P, b, s);
     if (rc) return rc;
-    const int pass = serial ? kSerialPassPoints : kMaxPassPoints;
+    const size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
     const bool dense = map->dense != nullptr;
     if (c->timing) CUDA_TRY(cudaEventRecord(c->ev0, s));
     for (size_t n0 = 0; n0 < N; n0 += pass) {

@@ -5,6 +5,7 @@
 
 #include <atomic>
 
+#include "index_math.h"
 #include "tsdfl_internal.h"
 
 namespace tsdfl {
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
     }
 }
 
-// ---------------------------------------------------------------- fast kernel
+// ---------------------------------------------------------------- tiled kernel
 
 typedef unsigned long long f2_t;   // two floats in one 64-bit register pair
 
@@ -341,6 +342,8 @@ __device__ __forceinline__ void upk(f2_t v, float& a, float& b)
 {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
+// Packed additions only: ptxas fuses packed multiply/add pairs into FMA even
+// with explicit .rn, so products stay scalar (__fmul_rn is never contracted).
 __device__ __forceinline__ f2_t add2(f2_t a, f2_t b)
 {
     f2_t r;
@@ -359,12 +362,6 @@ __device__ __forceinline__ f2_t sub2(f2_t a, f2_t b)
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
-__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b)
-{
-    f2_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
 __device__ __forceinline__ f2_t fma2_rz(f2_t a, f2_t b, f2_t c)
 {
     f2_t r;
@@ -372,143 +369,246 @@ __device__ __forceinline__ f2_t fma2_rz(f2_t a, f2_t b, f2_t c)
     return r;
 }
 
-constexpr uint32_t kMagic = 0x4B000000u;   // bits of 2^23
-constexpr uint32_t kFastLimitBits = 0x4A800000u;   // bits of 2^22
+constexpr uint32_t kMagic = 0x4B000000u;          // bits of 2^23
+constexpr uint32_t kFastLimitBits = 0x4A800000u;  // bits of 2^22
+constexpr uint32_t kCodeSlow = (uint32_t)kCodeLater;   // fast path does not apply
 
-// Code of a point the fast path does not cover: a coarse-bound miss is decided
-// directly, everything else goes through the full reference semantics.
-template <bool DENSE>
-__device__ __noinline__ uint32_t slow_code(const MapView& m, float x, float y, float z)
+// Code of a point the fast path does not cover: finite offsets go through the
+// signed second tier, NaN / infinite / huge ones through the 64-bit emulation.
+__device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y, float z)
 {
-    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
-    uint32_t bx = __float_as_uint(ox), by = __float_as_uint(oy), bz = __float_as_uint(oz);
-    bool beyond = (bx >= m.lim_x && bx < kFastLimitBits && m.lim_x < kFastLimitBits) ||
-                  (by >= m.lim_y && by < kFastLimitBits && m.lim_y < kFastLimitBits) ||
-                  (bz >= m.lim_z && bz < kFastLimitBits && m.lim_z < kFastLimitBits);
-    if (beyond) return kCodeMiss;   // trunc(offset) > mmax: the coarse bound check fails
-    uint32_t idx = slot_index_slow(m, x, y, z);
+    const float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
+    uint32_t idx = slot_index_tier2(m, m.grid_occ, ox, oy, oz);
+    if (idx == kIdxSlow) idx = slot_index_slow(m, x, y, z);
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
 
-// Fast path of one point: o* are the map offsets, t* = 2^23 + trunc(offset),
-// c* = 2^23 + floor(sub * sub_inv), s* the sub-voxel positions (all floats).
-template <bool DENSE>
-__device__ __forceinline__ uint32_t fast_code(const MapView& m, const float* thr, float tx, float ty, float tz,
-                                              float ox, float oy, float oz, float mx, float my, float mz, float sx,
-                                              float sy, float sz, float cx, float cy, float cz)
+// Sub-voxel index trunc(s / res) from c = 2^23 + floor(s * sub_inv) (a float):
+// exact by one multiplier (SUB_SINGLE) or with the threshold correction.
+template <int SUBMODE>
+__device__ __forceinline__ uint32_t sub_q(const float* thr, float s, float c, bool fast)
 {
-    uint32_t bx = __float_as_uint(ox), by = __float_as_uint(oy), bz = __float_as_uint(oz);
-    bool fast = bx < m.lim_x && by < m.lim_y && bz < m.lim_z;
-    if (fast) {
-        uint32_t ix = __float_as_uint(cx) - kMagic, iy = __float_as_uint(cy) - kMagic,
-                 iz = __float_as_uint(cz) - kMagic;
-        uint32_t qx = ix + (sx >= thr[ix + 1] ? 1u : 0u);
-        uint32_t qy = iy + (sy >= thr[iy + 1] ? 1u : 0u);
-        uint32_t qz = iz + (sz >= thr[iz + 1] ? 1u : 0u);
-        uint32_t up = (__float_as_uint(mx) - kMagic) + (__float_as_uint(my) - kMagic) * m.up_dim_x +
-                      (__float_as_uint(mz) - kMagic) * m.up_dim_2;
-        if (up >= m.grid_occ_size) return kCodeMiss;
-        uint32_t sl = qx + qy * m.sub_dim + qz * m.sub_dim_2;
-        if (DENSE) {
-            if (sl < m.sub_dim_3) return __ldg(m.dense + (size_t)up * m.sub_dim_3 + sl);
-        } else {
-            int32_t base = __ldg(m.grid_occ + up);
-            if (base < 0) return kCodeMiss;
-            uint32_t idx = (uint32_t)base + sl;
-            return idx < m.data_size ? (uint32_t)__ldg(m.codes + idx) : (uint32_t)kCodeMiss;
-        }
-    }
-    return slow_code<DENSE>(m, tx, ty, tz);
+    uint32_t i = __float_as_uint(c) - kMagic;
+    if (SUBMODE == 1) return i;
+    i = fast ? i : 0u;
+    return i + (s >= thr[i + 1] ? 1u : 0u);
 }
 
-constexpr int kFastThreads = 768;
+// Fast path of one point: o* the map offsets, m* = 2^23 + trunc(offset),
+// s* the sub-voxel positions, c* = 2^23 + floor(s * sub_inv).  Branch-free:
+// loads use clamped addresses and the result is selected afterwards.
+template <bool DENSE, int SUBMODE>
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const float* thr, float ox, float oy, float oz,
+                                              float mx, float my, float mz, float sx, float sy, float sz, float cx,
+                                              float cy, float cz)
+{
+    const bool fast = __float_as_uint(ox) < m.lim_x && __float_as_uint(oy) < m.lim_y && __float_as_uint(oz) < m.lim_z;
+    const uint32_t qx = sub_q<SUBMODE>(thr, sx, cx, fast), qy = sub_q<SUBMODE>(thr, sy, cy, fast),
+                   qz = sub_q<SUBMODE>(thr, sz, cz, fast);
+    const uint32_t up = (__float_as_uint(mx) - kMagic) + (__float_as_uint(my) - kMagic) * m.up_dim_x +
+                        (__float_as_uint(mz) - kMagic) * m.up_dim_2;
+    const uint32_t sl = qx + qy * m.sub_dim + qz * m.sub_dim_2;
+    const bool inside = fast && up < m.grid_occ_size;
+    if (DENSE) {
+        const bool ok = inside && sl < m.sub_dim_3;
+        const uint32_t code = __ldg(m.dense + (ok ? (size_t)up * m.sub_dim_3 + sl : (size_t)0));
+        return ok ? code : (fast && !inside ? (uint32_t)kCodeMiss : kCodeSlow);
+    } else {
+        const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
+        const uint32_t idx = (uint32_t)base + sl;
+        const bool ok = inside && base >= 0 && idx < m.data_size;
+        const uint32_t code = __ldg(m.codes + (ok ? idx : 0u));
+        return ok ? code : (fast ? (uint32_t)kCodeMiss : kCodeSlow);
+    }
+}
 
-// Fast exact mode: one warp per particle, every lane scores two scan points
-// per step with packed f32x2 arithmetic; no divisions or float<->int
-// conversions on the fast path (truncation by round-toward-zero adds of 2^23,
-// the sub-voxel index from a verified threshold table).  Results are identical
-// to eval_exact_kernel.
-template <bool DENSE>
-__global__ void __launch_bounds__(kFastThreads, 1) eval_fast_kernel(EvalParams p)
+constexpr int kTiledThreads = 768;
+constexpr int kTiledWarps = kTiledThreads / 32;
+constexpr int kRing = 64;   // deferred lookups per warp (transformed point + scan index)
+constexpr uint32_t kDbgSlow = 0x10000u;   // debug code flag: decided by the exact slow tiers
+
+// Appends the lanes with `slow` set to the warp's ring of deferred lookups.
+__device__ __forceinline__ void defer(float4* ring, uint32_t head, uint32_t& tail, bool slow, float tx, float ty,
+                                      float tz, int j, int lane)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, slow);
+    if (mask == 0u) return;
+    const uint32_t pos = tail + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    if (slow) ring[pos & (kRing - 1)] = make_float4(tx, ty, tz, __int_as_float(j));
+    tail += (uint32_t)__popc(mask);
+    __syncwarp();
+}
+
+struct Partial {
+    long long acc;
+    uint32_t hits;
+};
+
+// Scores `count` (<= 32) deferred lookups from the ring, one per lane, through
+// the exact second tier / 64-bit emulation.  The map view is read from a
+// shared-memory copy so that no kernel parameter's address escapes.
+__device__ __noinline__ Partial drain(const MapView* m, const long long* lut, const float4* ring, uint32_t head,
+                                      int count, int lane, uint32_t* dbg_row)
+{
+    Partial r{0, 0u};
+    if (lane < count) {
+        const float4 e = ring[(head + (uint32_t)lane) & (kRing - 1)];
+        const uint32_t code = slow_code(*m, e.x, e.y, e.z);
+        r.acc = lut[code];
+        r.hits = code <= (uint32_t)kCodeInit ? 1u : 0u;
+        if (dbg_row) dbg_row[__float_as_int(e.w)] = code | kDbgSlow;
+    }
+    __syncwarp();
+    return r;
+}
+
+constexpr int kTiledChunk = 1024;     // scan points per work item
+constexpr int kTiledGroup = 4;        // particles per work item
+
+struct TiledParams {
+    EvalParams e;
+    int chunk;          // points per work item (multiple of 64)
+    int group;          // particles per work item
+    int groups;         // particle groups
+    int items;          // chunks * groups
+};
+
+// Exact mode, tiled.  The pass's scan points are staged once per CTA (bulk
+// copies into shared memory, pair layout); then every warp walks its share of
+// the (point chunk, particle group) work items in chunk-major order -- item k
+// belongs to warp k mod W of the W warps of the grid -- so all SMs score the
+// same part of the scan at a time and its map footprint stays in L2, with no
+// block-wide barrier after staging.  Each lane scores two points per step
+// (packed f32x2 additions).  Likelihood codes are summed in 64-bit fixed point
+// and added to the particle's total with an integer atomic: exact and
+// independent of order, so results equal eval_exact_kernel's bit for bit.
+template <bool DENSE, int SUBMODE>
+__global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ float thr[kSubThr];
+    __shared__ MapView s_map;   // the map view the slow tiers read
+    const EvalParams& p = tp.e;
+    const MapView& m = p.m;
     long long* lut = reinterpret_cast<long long*>(smem);
     const int n = p.n1 - p.n0;
-    const int nblk = (n + 63) >> 6;
-    const int npairs = nblk * 32;
+    const int npairs = ((n + 63) >> 6) * 32;
+    if (threadIdx.x == 0) s_map = m;
     float4* sxy = reinterpret_cast<float4*>(smem + kLutBytes);
-    float2* sz = reinterpret_cast<float2*>(sxy + npairs);
+    float2* spz = reinterpret_cast<float2*>(sxy + npairs);
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
-    if (threadIdx.x < kSubThr) thr[threadIdx.x] = p.m.sub_thr[threadIdx.x];
-    // bulk copies of the point pairs of this pass
+    if (threadIdx.x < kSubThr) thr[threadIdx.x] = m.sub_thr[threadIdx.x];
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t bxy = (uint32_t)npairs * 16u, bz = (uint32_t)npairs * 8u;
-        mbar_expect_tx(&bar, bxy + bz);
-        bulk_g2s(sxy, p.pxy + p.n0 / 2, bxy, &bar);
-        bulk_g2s(sz, p.pz + p.n0 / 2, bz, &bar);
+        mbar_expect_tx(&bar, (uint32_t)npairs * 24u);
+        bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
+        bulk_g2s(spz, p.pz + p.n0 / 2, (uint32_t)npairs * 8u, &bar);
     }
-    bool ok = mbar_wait_bounded(&bar, 0);
-    if (!ok && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
-    if (__syncthreads_and(ok ? 1 : 0) == 0) return;
+    bool staged = mbar_wait_bounded(&bar, 0);
+    if (!staged && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
+    if (__syncthreads_and(staged ? 1 : 0) == 0) return;
 
-    const MapView& m = p.m;
     const int lane = threadIdx.x & 31;
-    const int warps = (blockDim.x >> 5) * gridDim.x;
+    float4* ring = reinterpret_cast<float4*>(spz + npairs) + (threadIdx.x >> 5) * kRing;
+    uint32_t head = 0, tail = 0;
+    const int gwarp = blockIdx.x * kTiledWarps + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * kTiledWarps;
     const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
     const f2_t MAG = pk(8388608.0f, 8388608.0f);
     const f2_t INV = pk(m.sub_inv, m.sub_inv);
-    const int nfull = n >> 6;
-    for (int pi = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); pi < p.P; pi += warps) {
-        const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
-        float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
-        const f2_t R0 = pk(a.x, a.x), R1 = pk(a.y, a.y), R2 = pk(a.z, a.z), R3 = pk(a.w, a.w);
-        const f2_t R4 = pk(b4.x, b4.x), R5 = pk(b4.y, b4.y), R6 = pk(b4.z, b4.z), R7 = pk(b4.w, b4.w);
-        const f2_t R8 = pk(c4.x, c4.x), R9 = pk(c4.y, c4.y), R10 = pk(c4.z, c4.z), R11 = pk(c4.w, c4.w);
-        long long acc = 0;
-        uint32_t hits = 0;
-        for (int blk = 0; blk < nblk; ++blk) {
-            float4 xy = sxy[blk * 32 + lane];
-            float2 zz = sz[blk * 32 + lane];
-            f2_t X = pk(xy.x, xy.y), Y = pk(xy.z, xy.w), Z = pk(zz.x, zz.y);
-            // tsdf_evaluator.cpp:44-46, two points at a time
-            f2_t TX = add2(add2(add2(mul2(R0, X), mul2(R1, Y)), mul2(R2, Z)), R3);
-            f2_t TY = add2(add2(add2(mul2(R4, X), mul2(R5, Y)), mul2(R6, Z)), R7);
-            f2_t TZ = add2(add2(add2(mul2(R8, X), mul2(R9, Y)), mul2(R10, Z)), R11);
-            f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
-            f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);   // 2^23 + trunc
-            f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
-            f2_t CX = fma2_rz(SX, INV, MAG), CY = fma2_rz(SY, INV, MAG), CZ = fma2_rz(SZ, INV, MAG);
-            float tx0, tx1, ty0, ty1, tz0, tz1, ox0, ox1, oy0, oy1, oz0, oz1, mx0, mx1, my0, my1, mz0, mz1;
-            float sx0, sx1, sy0, sy1, sz0, sz1, cx0, cx1, cy0, cy1, cz0, cz1;
-            upk(TX, tx0, tx1); upk(TY, ty0, ty1); upk(TZ, tz0, tz1);
-            upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1);
-            upk(MX, mx0, mx1); upk(MY, my0, my1); upk(MZ, mz0, mz1);
-            upk(SX, sx0, sx1); upk(SY, sy0, sy1); upk(SZ, sz0, sz1);
-            upk(CX, cx0, cx1); upk(CY, cy0, cy1); upk(CZ, cz0, cz1);
-            uint32_t c0 = fast_code<DENSE>(m, thr, tx0, ty0, tz0, ox0, oy0, oz0, mx0, my0, mz0, sx0, sy0, sz0, cx0,
-                                           cy0, cz0);
-            uint32_t c1 = fast_code<DENSE>(m, thr, tx1, ty1, tz1, ox1, oy1, oz1, mx1, my1, mz1, sx1, sy1, sz1, cx1,
-                                           cy1, cz1);
-            if (blk >= nfull) {   // the last, partial block
-                if (64 * blk + lane >= n) c0 = kCodeNone;
-                if (64 * blk + 32 + lane >= n) c1 = kCodeNone;
+    for (int item = gwarp; item < tp.items; item += nwarps) {
+        const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
+        const int c0 = chunk * tp.chunk;
+        const int cn = min(tp.chunk, n - c0);
+        const int b0 = c0 >> 6, nblk = (cn + 63) >> 6, nfull = cn >> 6;
+        for (int k = 0; k < tp.group; ++k) {
+            const int pi = grp * tp.group + k;
+            if (pi >= p.P) break;
+            const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
+            const float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
+            const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
+            long long acc = 0;
+            uint32_t hits = 0;
+            uint32_t* dbg_row = p.dbg ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
+            for (int blk = 0; blk < nblk; ++blk) {
+                const float4 xy = sxy[(b0 + blk) * 32 + lane];
+                const float2 zz = spz[(b0 + blk) * 32 + lane];
+                // tsdf_evaluator.cpp:44-46 for two points: ((r0 x + r1 y) + r2 z) + r3
+                const f2_t TX = add2(add2(add2(pk(__fmul_rn(a.x, xy.x), __fmul_rn(a.x, xy.y)),
+                                               pk(__fmul_rn(a.y, xy.z), __fmul_rn(a.y, xy.w))),
+                                          pk(__fmul_rn(a.z, zz.x), __fmul_rn(a.z, zz.y))),
+                                     R3);
+                const f2_t TY = add2(add2(add2(pk(__fmul_rn(b4.x, xy.x), __fmul_rn(b4.x, xy.y)),
+                                               pk(__fmul_rn(b4.y, xy.z), __fmul_rn(b4.y, xy.w))),
+                                          pk(__fmul_rn(b4.z, zz.x), __fmul_rn(b4.z, zz.y))),
+                                     R7);
+                const f2_t TZ = add2(add2(add2(pk(__fmul_rn(c4.x, xy.x), __fmul_rn(c4.x, xy.y)),
+                                               pk(__fmul_rn(c4.y, xy.z), __fmul_rn(c4.y, xy.w))),
+                                          pk(__fmul_rn(c4.z, zz.x), __fmul_rn(c4.z, zz.y))),
+                                     R11);
+                const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
+                const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);  // 2^23 + trunc
+                const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
+                const f2_t CX = fma2_rz(SX, INV, MAG), CY = fma2_rz(SY, INV, MAG), CZ = fma2_rz(SZ, INV, MAG);
+                float ox0, ox1, oy0, oy1, oz0, oz1, mx0, mx1, my0, my1, mz0, mz1;
+                float sx0, sx1, sy0, sy1, sz0, sz1, cx0, cx1, cy0, cy1, cz0, cz1;
+                upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1);
+                upk(MX, mx0, mx1); upk(MY, my0, my1); upk(MZ, mz0, mz1);
+                upk(SX, sx0, sx1); upk(SY, sy0, sy1); upk(SZ, sz0, sz1);
+                upk(CX, cx0, cx1); upk(CY, cy0, cy1); upk(CZ, cz0, cz1);
+                uint32_t k0 = fast_code<DENSE, SUBMODE>(m, thr, ox0, oy0, oz0, mx0, my0, mz0, sx0, sy0, sz0, cx0,
+                                                         cy0, cz0);
+                uint32_t k1 = fast_code<DENSE, SUBMODE>(m, thr, ox1, oy1, oz1, mx1, my1, mz1, sx1, sy1, sz1, cx1,
+                                                         cy1, cz1);
+                if (blk >= nfull) {   // the chunk's last, partial block: padding points count for nothing
+                    if (64 * blk + lane >= cn) k0 = kCodeNone;
+                    if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
+                }
+                // lanes the fast path cannot decide are deferred to the warp's ring and
+                // scored 32 at a time (kCodeLater contributes nothing here), so no warp
+                // diverges into the slow tiers; at most 31 entries wait between steps,
+                // so each append of <= 32 fits the ring
+                if (__any_sync(0xffffffffu, k0 == kCodeSlow || k1 == kCodeSlow)) {
+                    float tx, ty, tz, u;
+                    upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
+                    defer(ring, head, tail, k0 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + lane, lane);
+                    if (tail - head >= 32) {
+                        const Partial d = drain(&s_map, lut, ring, head, 32, lane, dbg_row);
+                        acc += d.acc;
+                        hits += d.hits;
+                        head += 32;
+                    }
+                    upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
+                    defer(ring, head, tail, k1 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
+                    if (tail - head >= 32) {
+                        const Partial d = drain(&s_map, lut, ring, head, 32, lane, dbg_row);
+                        acc += d.acc;
+                        hits += d.hits;
+                        head += 32;
+                    }
+                }
+                if (dbg_row) {
+                    const int j = c0 + 64 * blk + lane;
+                    if (k0 < (uint32_t)kCodeNone) dbg_row[j] = k0;
+                    if (k1 < (uint32_t)kCodeNone) dbg_row[j + 32] = k1;
+                }
+                acc += lut[k0] + lut[k1];
+                hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
             }
-            if (p.dbg) {
-                if (64 * blk + lane < n) p.dbg[(size_t)pi * p.n_total + p.n0 + 64 * blk + lane] = c0;
-                if (64 * blk + 32 + lane < n) p.dbg[(size_t)pi * p.n_total + p.n0 + 64 * blk + 32 + lane] = c1;
+            if (tail != head) {
+                const Partial d = drain(&s_map, lut, ring, head, (int)(tail - head), lane, dbg_row);
+                acc += d.acc;
+                hits += d.hits;
+                head = tail;
             }
-            acc += lut[c0] + lut[c1];
-            hits += __popc(__ballot_sync(0xffffffffu, c0 <= (uint32_t)kCodeInit)) +
-                    __popc(__ballot_sync(0xffffffffu, c1 <= (uint32_t)kCodeInit));
-        }
-        acc = warp_sum_ll(acc);
-        if (lane == 0) {
-            p.sum_fx[pi] = p.first_pass ? acc : p.sum_fx[pi] + acc;
-            p.hits[pi] = p.first_pass ? hits : p.hits[pi] + hits;
+            acc = warp_sum_ll(acc);
+            hits = warp_sum_u32(hits);
+            if (lane == 0) {
+                atomicAdd(reinterpret_cast<unsigned long long*>(p.sum_fx + pi), (unsigned long long)acc);
+                atomicAdd(p.hits + pi, hits);
+            }
         }
     }
 }
@@ -1000,13 +1100,26 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         k<<<(P + 255) / 256, 256, smem, s>>>(p);
         g_launches += 1;
     } else if (!f32 && m.sub_fast && !generic) {
-        auto k = dense ? eval_fast_kernel<true> : eval_fast_kernel<false>;
-        size_t fsmem = (size_t)kLutBytes + (size_t)(32 * (((n1 - n0) + 63) / 64)) * 24;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
+        // one launch covers the whole scan; sums are accumulated with atomics
+        TiledParams tp;
+        tp.e = p;
+        tp.chunk = kTiledChunk;
+        tp.group = kTiledGroup;
+        tp.groups = (P + tp.group - 1) / tp.group;
+        tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
+        auto k = dense ? (m.sub_fast == 2 ? eval_tiled_kernel<true, 1> : eval_tiled_kernel<true, 0>)
+                       : (m.sub_fast == 2 ? eval_tiled_kernel<false, 1> : eval_tiled_kernel<false, 0>);
+        size_t tsmem = (size_t)kLutBytes + (size_t)(32 * (((n1 - n0) + 63) / 64)) * 24 +
+                       sizeof(float4) * kRing * kTiledWarps;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
+        if (first) {
+            cudaMemsetAsync(b.sum_fx, 0, sizeof(long long) * (size_t)P, s);
+            cudaMemsetAsync(b.hits, 0, sizeof(uint32_t) * (size_t)P, s);
+        }
         int blocks = sm_count;
-        int need = (P + kFastThreads / 32 - 1) / (kFastThreads / 32);
+        int need = (tp.items + kTiledWarps - 1) / kTiledWarps;
         if (need < blocks) blocks = need > 0 ? need : 1;
-        k<<<blocks, kFastThreads, fsmem, s>>>(p);
+        k<<<blocks, kTiledThreads, tsmem, s>>>(tp);
         g_launches += 1;
     } else {
         auto k = dense && !f32 ? eval_exact_kernel<true, false>

@@ -50,12 +50,13 @@ float likelihood_init(float sigma)
     return init * init * init;
 }
 
-void code_values(float sigma, float init_value, float out[603])
+void code_values(float sigma, float init_value, float out[604])
 {
     for (int c = 0; c < 600; ++c) out[c] = likelihood_value(c, sigma);
     out[600] = init_value;
     out[601] = init_value;
     out[602] = 0.0f;
+    out[603] = 0.0f;
 }
 
 // CudaSubVoxelMap ctor (cuda_sub_voxel_map.tcc:4-48)
@@ -162,6 +163,31 @@ int sub_index_table(float res, uint64_t sub_dim, float* inv_out, float* thr, int
     }
     if (std::floor(1.0 * (double)inv) > (double)K - 1) return 0;   // c + 1 must stay inside the table
     *inv_out = inv;
+    // A multiplier m with floor(s * m) == trunc(s / res) for every float s in
+    // [0, 1) makes the correction unnecessary: look for one near 1 / res.
+    auto bits_of = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
+    auto float_of = [](uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; };
+    const float below_one = float_of(bits_of(1.0f) - 1);
+    const float base = 1.0f / res;
+    for (int d = 0; d <= 8192; ++d) {
+        for (int sgn = -1; sgn <= 1; sgn += 2) {
+            if (d == 0 && sgn > 0) continue;
+            float m = float_of(bits_of(base) + (uint32_t)(sgn * d));
+            bool good = true;
+            for (int k = 1; k <= K && good; ++k) {
+                if (thr[k] < 1.0f) {
+                    double hi = (double)thr[k] * m, lo = (double)float_of(bits_of(thr[k]) - 1) * m;
+                    good = hi >= k && lo < k;
+                } else {
+                    good = (double)below_one * m < k;
+                }
+            }
+            if (good) {
+                *inv_out = m;
+                return 2;
+            }
+        }
+    }
     return 1;
 }
 
@@ -190,7 +216,7 @@ void tsdfl_free(void* p) { std::free(p); }
 
 int tsdfl_code_values(float sigma, float init_value, float* out601)
 {
-    float v[603];
+    float v[604];
     code_values(sigma, init_value, v);
     std::memcpy(out601, v, sizeof(float) * 601);
     return TSDFL_OK;

@@ -14,7 +14,8 @@ namespace tsdfl {
 constexpr int kCodeInit = 600;
 constexpr int kCodeMiss = 601;
 constexpr int kCodeNone = 602;   // no point (padding): no hit, contributes 0
-constexpr int kNumCodes = 603;
+constexpr int kCodeLater = 603;  // scored later by the exact slow tiers: no hit, contributes 0 here
+constexpr int kNumCodes = 604;
 constexpr uint32_t kMissIndex = 0xffffffffu;
 
 // Largest scan a single evaluation pass stages in shared memory (3 floats per
@@ -47,9 +48,10 @@ struct MapView {
     const float* data;        // float slots (storage 1)
     const uint16_t* dense;    // dense brick layout (may be null)
     int32_t storage;          // 0 = codes, 1 = float
-    // Division-free sub-voxel index for s in [0, 1):
-    //   trunc(s / res) == c + (s >= sub_thr[c + 1]),  c = floor(s * sub_inv)
-    // (exact for every float s; verified on the host, sub_fast = 1 when it holds).
+    // Division-free sub-voxel index for s in [0, 1), verified on the host for
+    // every float s: sub_fast = 1: trunc(s / res) == c + (s >= sub_thr[c + 1]),
+    // c = floor(s * sub_inv); sub_fast = 2: trunc(s / res) == floor(s * sub_inv);
+    // 0: neither (generic kernel).
     int32_t sub_fast;
     float sub_inv;
     float sub_thr[kSubThr];
@@ -101,30 +103,6 @@ static __device__ __noinline__ uint32_t slot_index_slow(const MapView& m, float 
     uint64_t qz = f2u_x86(__fdiv_rn(sz, m.res));
     uint64_t idx = (uint64_t)(int64_t)base + qx + qy * m.sub_dim64 + qz * m.sub_dim_2_64;
     return idx < m.data_size64 ? (uint32_t)idx : kMissIndex;
-}
-
-// Slot index of a map-frame point (exact reference semantics), kMissIndex on a
-// miss.  Fast path: all three offsets in [0, kFastOffsetLimit), where
-// trunc(offset) is the reference's brick coordinate and the coarse bound check
-// (:54-66) reduces to trunc(offset) <= mmax.
-static __device__ __forceinline__ uint32_t slot_index(const MapView& m, float x, float y, float z)
-{
-    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
-    bool fast = ox >= 0.0f && oy >= 0.0f && oz >= 0.0f && ox < kFastOffsetLimit && oy < kFastOffsetLimit &&
-                oz < kFastOffsetLimit;
-    if (!fast) return slot_index_slow(m, x, y, z);
-    int32_t mx = __float2int_rz(ox), my = __float2int_rz(oy), mz = __float2int_rz(oz);
-    if (mx > m.mmax_x || my > m.mmax_y || mz > m.mmax_z) return kMissIndex;
-    uint32_t up = (uint32_t)mx + (uint32_t)my * m.up_dim_x + (uint32_t)mz * m.up_dim_2;
-    if (up >= m.grid_occ_size) return kMissIndex;
-    int32_t base = __ldg(m.grid_occ + up);
-    if (base < 0) return kMissIndex;
-    float sx = __fsub_rn(ox, (float)mx), sy = __fsub_rn(oy, (float)my), sz = __fsub_rn(oz, (float)mz);
-    uint32_t qx = (uint32_t)__float2int_rz(__fdiv_rn(sx, m.res));
-    uint32_t qy = (uint32_t)__float2int_rz(__fdiv_rn(sy, m.res));
-    uint32_t qz = (uint32_t)__float2int_rz(__fdiv_rn(sz, m.res));
-    uint32_t idx = (uint32_t)base + qx + qy * m.sub_dim + qz * m.sub_dim_2;
-    return idx < m.data_size ? idx : kMissIndex;
 }
 
 // Transform of one scan point by a laser pose (tsdf_evaluator.cpp:44-46) with
