@@ -3,6 +3,9 @@
 // oracle's getIndex (oracle/tsdf_oracle.c) on random maps and points,
 // including negative, out-of-bounds and special offsets.  Exit status 0 when
 // every handled lookup matches; prints counts.
+//
+// "index_check exhaustive RES..." instead checks the division-free sub-voxel
+// index against trunc(s / res) for every float s in [0, 1).
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -23,9 +26,44 @@ void set_error(const char*, ...) {}
 using namespace tsdfl;
 
 static uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+static float fof(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+
+// Division-free sub-voxel index as the tiled kernel computes it: c from an
+// exact product, then (mode 1) one threshold compare decides c or c + 1.
+static int64_t fast_sub_index(int mode, float s, float inv, const float* next)
+{
+    const int64_t c = (int64_t)std::floor((double)s * (double)inv);
+    if (mode == 2) return c;
+    return c + (s >= next[c & (kSubTable - 1)] ? 1 : 0);
+}
+
+static int exhaustive(int argc, char** argv)
+{
+    int fails = 0;
+    for (int a = 2; a < argc; ++a) {
+        const float res = (float)atof(argv[a]);
+        const uint64_t sub_dim = (uint64_t)std::ceil(1.0f / res);
+        float inv = 0.0f, next[kSubTable];
+        const int mode = sub_index_mult(res, sub_dim, &inv, next);
+        long bad = 0;
+        if (mode) {
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+            for (long u = 0; u < (long)fbits(1.0f); ++u) {
+                const float s = fof((uint32_t)u);
+                const int64_t want = (int64_t)f2u_x86_host(s / res);
+                if (fast_sub_index(mode, s, inv, next) != want) ++bad;
+            }
+        }
+        printf("exhaustive res=%g sub_dim=%llu mode=%d inv=%.9g bad=%ld\n", res, (unsigned long long)sub_dim, mode,
+               inv, bad);
+        if (bad || !mode) ++fails;
+    }
+    return fails ? 1 : 0;
+}
 
 int main(int argc, char** argv)
 {
+    if (argc > 1 && std::strcmp(argv[1], "exhaustive") == 0) return exhaustive(argc, argv);
     long n_points = argc > 1 ? atol(argv[1]) : 2000000;
     const float ress[] = {0.064f, 0.05f, 0.1f, 0.08f, 0.04f};
     const float mins[][3] = {{0, 0, 0}, {-4.096f, -8.192f, -4.096f}, {-10.0f, 3.2f, -0.3f}};
@@ -57,7 +95,7 @@ int main(int argc, char** argv)
             v.dim_x = c.dim_x; v.dim_y = c.dim_y; v.dim_z = c.dim_z;
             v.up_dim_x64 = c.up_dim_x; v.up_dim_2_64 = c.up_dim_2; v.grid_occ_size64 = c.grid_occ_size;
             v.sub_dim64 = c.sub_dim; v.sub_dim_2_64 = c.sub_dim_2; v.data_size64 = c.data_size;
-            v.sub_fast = sub_index_table(res, c.sub_dim, &v.sub_inv, v.sub_thr, kSubThr);
+            v.sub_fast = sub_index_mult(res, c.sub_dim, &v.sub_inv, v.sub_next);
             std::uniform_real_distribution<float> U(-3.5f, 25.0f);
             const float special[] = {-1.0f, -0.99999994f, -0.5f, -0.0f, 0.0f, 1e-30f, 0.99999994f, 1.0f, -2.0f, -1e-7f};
             for (long i = 0; i < n_points; ++i) {
@@ -89,8 +127,7 @@ int main(int argc, char** argv)
                     for (int a = 0; a < 3; ++a) {
                         mm[a] = (int64_t)oo[a];
                         float s = oo[a] - (float)mm[a];
-                        int64_t cc = (int64_t)std::floor((double)s * (double)v.sub_inv);
-                        qq[a] = v.sub_fast == 2 ? cc : cc + (s >= v.sub_thr[cc + 1] ? 1 : 0);
+                        qq[a] = fast_sub_index(v.sub_fast, s, v.sub_inv, v.sub_next);
                     }
                     uint64_t up = (uint64_t)(mm[0] + mm[1] * (int64_t)c.up_dim_x + mm[2] * (int64_t)c.up_dim_2);
                     uint32_t got = kIdxMiss;

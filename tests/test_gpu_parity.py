@@ -99,6 +99,26 @@ def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
     assert np.array_equal(p[:, :6], room.particles[:, :6])
 
 
+@pytest.mark.parametrize("voxel_mm", [50, 32])
+def test_fast_index_with_residual_correction(ctx, voxel_mm):
+    """Resolutions whose sub-voxel multiplier can be one short (0.05 m, 0.032 m):
+    the tiled kernel's FMA residual test, both layouts, against the oracle's
+    getIndex, including points in the (-1, 0) m band and outside the map."""
+    wl = synth.make_workload(synth.ROOM, 13, voxel_mm, 1500, 96, 16, 512, edge=64, name="room@res")
+    om = O.OracleMap(O.coef_from(wl.coef), wl.grid_occ, wl.float_data())
+    rng = np.random.default_rng(voxel_mm)
+    pts = np.concatenate([wl.points, rng.uniform(-1.0, 0.3, size=(200, 3)).astype(np.float32),
+                          rng.uniform(-30, 30, size=(200, 3)).astype(np.float32)])
+    ref = _oracle_eval(om, wl, points=pts)
+    for dense in (False, True):
+        dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=dense)
+        assert dmap.info()["fast_index"] == 1
+        d = TSDFEvaluator(dmap).evaluate_debug(wl.particles.copy(), pts, wl.tf, voxel_index=True)
+        assert np.array_equal(d["hits"], ref["hits"])
+        assert np.array_equal(d["voxel_index"] & 0xFFFF, _codes_of(ref["voxel_index"], wl.codes, wl.coef.data_size))
+        assert np.allclose(d["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+
+
 def test_fast_and_generic_kernels_identical(ctx, room):
     """Both exact-mode kernels give identical fixed-point sums, so identical weights."""
     for dense in (False, True):

@@ -8,7 +8,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def test_index_math_matches_oracle(tmp_path):
+def _build(tmp_path):
     exe = tmp_path / "index_check"
     csrc = ROOT / "tsdf_localization_gb300" / "csrc"
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
@@ -18,9 +18,29 @@ def test_index_math_matches_oracle(tmp_path):
            str(ROOT / "tests" / "native" / "index_check.cpp"), str(csrc / "map_build.cpp"),
            "-x", "c", str(ROOT / "oracle" / "tsdf_oracle.c"), "-o", str(exe), "-lm"]
     subprocess.run(cmd, check=True)
+    return exe
+
+
+def test_index_math_matches_oracle(tmp_path):
+    exe = _build(tmp_path)
     res = subprocess.run([str(exe), "400000"], capture_output=True, text=True)
     print(res.stdout)
     assert res.returncode == 0, res.stdout
     handled = int(res.stdout.split("handled ")[1].split()[0])
     fast = int(res.stdout.split("fast ")[1].split()[0])
     assert handled > 1_000_000 and fast > 100_000
+
+
+def test_sub_index_exhaustive(tmp_path):
+    """Every float s in [0, 1): the multiplier (and, where needed, the
+    threshold table) gives trunc(s / res)."""
+    exe = _build(tmp_path)
+    ress = ["0.05", "0.064", "0.032", "0.1", "0.03"]
+    res = subprocess.run([str(exe), "exhaustive", *ress], capture_output=True, text=True)
+    print(res.stdout)
+    assert res.returncode == 0, res.stdout
+    lines = [ln for ln in res.stdout.splitlines() if ln.startswith("exhaustive")]
+    assert len(lines) == len(ress)
+    for ln in lines:
+        f = dict(kv.split("=") for kv in ln.split()[1:])
+        assert f["bad"] == "0" and f["mode"] in ("1", "2")

@@ -84,6 +84,8 @@ struct tsdfl_map {
     uint16_t* codes = nullptr;
     float* data = nullptr;
     uint16_t* dense = nullptr;
+    uint32_t* occ = nullptr;      // brick occupancy bits (with the dense layout)
+    uint32_t occ_words = 0;
     float* values = nullptr;      // kNumCodes likelihood values (device)
     float max_value = 0;
     uint64_t bricks = 0;
@@ -237,7 +239,7 @@ void fill_view(tsdfl_map* m)
     v.data = m->data;
     v.dense = m->dense;
     v.storage = m->codes ? 0 : 1;
-    v.sub_fast = sub_index_table(c.resolution, c.sub_dim, &v.sub_inv, v.sub_thr, kSubThr);
+    v.sub_fast = sub_index_mult(c.resolution, c.sub_dim, &v.sub_inv, v.sub_next);
     auto lim = [](int32_t mmax) {
         float f = (float)std::min<int64_t>((int64_t)mmax + 1, 4194304);
         if (mmax < 0) f = 0.0f;
@@ -248,6 +250,11 @@ void fill_view(tsdfl_map* m)
     v.lim_x = lim(v.mmax_x);
     v.lim_y = lim(v.mmax_y);
     v.lim_z = lim(v.mmax_z);
+    const uint32_t K = 0x4B000000u;
+    v.up_bias = K * (1u + v.up_dim_x + v.up_dim_2);
+    v.sl_bias = K * (1u + v.sub_dim + v.sub_dim_2);
+    v.occ = m->occ;
+    v.occ_words = m->occ_words;
 }
 
 int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
@@ -260,6 +267,11 @@ int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
             m->bytes += sizeof(uint16_t) * n;
             int rc = launch_dense_from_codes(m->grid_occ, m->codes, m->coef.grid_occ_size, (uint32_t)sub3, m->dense,
                                              ctx->stream);
+            if (rc) return rc;
+            m->occ_words = (uint32_t)(((m->coef.grid_occ_size + 31) / 32 + 3) / 4 * 4);
+            CUDA_TRY(cudaMalloc(&m->occ, sizeof(uint32_t) * m->occ_words));
+            m->bytes += sizeof(uint32_t) * m->occ_words;
+            rc = launch_occupancy_bits(m->grid_occ, m->coef.grid_occ_size, m->occ, m->occ_words, ctx->stream);
             if (rc) return rc;
         }
     }
@@ -276,6 +288,7 @@ void destroy_map(tsdfl_map* m)
     cudaFree(m->codes);
     cudaFree(m->data);
     cudaFree(m->dense);
+    cudaFree(m->occ);
     cudaFree(m->values);
     delete m;
 }
@@ -328,8 +341,17 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     if (rc) return rc;
     rc = launch_pose_kernel(tf, (int)P, b, s);
     if (rc) return rc;
-    const size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
-    const bool dense = map->dense != nullptr;
+    bool dense = map->dense != nullptr;
+    const bool tiled = !serial && map->view.storage == 0 && map->view.sub_fast && !(flags & TSDFL_EVAL_GENERIC);
+    size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
+    if (tiled) {
+        int tp = tiled_pass_points(map->view, dense);
+        if (tp < 1024 && dense) {   // the bitmap crowds out the scan: use the brick table instead
+            dense = false;
+            tp = tiled_pass_points(map->view, false);
+        }
+        pass = (size_t)tp;
+    }
     if (c->timing) CUDA_TRY(cudaEventRecord(c->ev0, s));
     for (size_t n0 = 0; n0 < N; n0 += pass) {
         size_t n1 = n0 + pass < N ? n0 + pass : N;

@@ -383,42 +383,48 @@ __device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
 
-// Sub-voxel index trunc(s / res) from c = 2^23 + floor(s * sub_inv) (a float):
-// exact by one multiplier (SUB_SINGLE) or with the threshold correction.
-template <int SUBMODE>
-__device__ __forceinline__ uint32_t sub_q(const float* thr, float s, float c, bool fast)
-{
-    uint32_t i = __float_as_uint(c) - kMagic;
-    if (SUBMODE == 1) return i;
-    i = fast ? i : 0u;
-    return i + (s >= thr[i + 1] ? 1u : 0u);
-}
+// Per-lookup inputs of the fast path, all from the packed pipeline: map
+// offsets o, bm = bits(2^23 + trunc(o)), bc = bits(2^23 + floor(s * sub_inv))
+// and the in-brick remainders s = o - trunc(o).
+struct FastIn {
+    float ox, oy, oz;
+    uint32_t bmx, bmy, bmz;
+    uint32_t bcx, bcy, bcz;
+    float sx, sy, sz;
+};
 
-// Fast path of one point: o* the map offsets, m* = 2^23 + trunc(offset),
-// s* the sub-voxel positions, c* = 2^23 + floor(s * sub_inv).  Branch-free:
-// loads use clamped addresses and the result is selected afterwards.
-template <bool DENSE, int SUBMODE>
-__device__ __forceinline__ uint32_t fast_code(const MapView& m, const float* thr, float ox, float oy, float oz,
-                                              float mx, float my, float mz, float sx, float sy, float sz, float cx,
-                                              float cy, float cz)
+// Branch-free fast path: the slot code, kCodeMiss, or kCodeSlow when the exact
+// slow tiers must decide (offset outside [0, mmax + 1), or -- dense layout -- a
+// sub-voxel index past the brick's end).  CORR: floor(s * sub_inv) may be one
+// short; the shared-memory threshold table `next` decides (bc's low bits are c).
+// DENSE: one gather from the dense layout, the brick's occupancy bit from the
+// shared-memory bitmap `occ`; otherwise the brick table and the slot array.
+template <bool DENSE, bool CORR>
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const float* next,
+                                              const FastIn& in)
 {
-    const bool fast = __float_as_uint(ox) < m.lim_x && __float_as_uint(oy) < m.lim_y && __float_as_uint(oz) < m.lim_z;
-    const uint32_t qx = sub_q<SUBMODE>(thr, sx, cx, fast), qy = sub_q<SUBMODE>(thr, sy, cy, fast),
-                   qz = sub_q<SUBMODE>(thr, sz, cz, fast);
-    const uint32_t up = (__float_as_uint(mx) - kMagic) + (__float_as_uint(my) - kMagic) * m.up_dim_x +
-                        (__float_as_uint(mz) - kMagic) * m.up_dim_2;
-    const uint32_t sl = qx + qy * m.sub_dim + qz * m.sub_dim_2;
+    const bool fast = __float_as_uint(in.ox) < m.lim_x && __float_as_uint(in.oy) < m.lim_y &&
+                      __float_as_uint(in.oz) < m.lim_z;
+    const uint32_t up = in.bmx + in.bmy * m.up_dim_x + in.bmz * m.up_dim_2 - m.up_bias;
+    uint32_t sl = in.bcx + in.bcy * m.sub_dim + in.bcz * m.sub_dim_2 - m.sl_bias;
+    if (CORR) {
+        constexpr uint32_t mask = kSubTable - 1;
+        sl += (in.sx >= next[in.bcx & mask] ? 1u : 0u) + (in.sy >= next[in.bcy & mask] ? m.sub_dim : 0u) +
+              (in.sz >= next[in.bcz & mask] ? m.sub_dim_2 : 0u);
+    }
     const bool inside = fast && up < m.grid_occ_size;
     if (DENSE) {
-        const bool ok = inside && sl < m.sub_dim_3;
+        const uint32_t word = occ[inside ? (up >> 5) : 0u];
+        const bool alloc = (word >> (up & 31u)) & 1u;
+        const bool ok = inside && alloc && sl < m.sub_dim_3;
         const uint32_t code = __ldg(m.dense + (ok ? (size_t)up * m.sub_dim_3 + sl : (size_t)0));
-        return ok ? code : (fast && !inside ? (uint32_t)kCodeMiss : kCodeSlow);
+        return ok ? code : (inside && !alloc) || (fast && !inside) ? (uint32_t)kCodeMiss : kCodeSlow;
     } else {
         const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
         const uint32_t idx = (uint32_t)base + sl;
         const bool ok = inside && base >= 0 && idx < m.data_size;
         const uint32_t code = __ldg(m.codes + (ok ? idx : 0u));
-        return ok ? code : (fast ? (uint32_t)kCodeMiss : kCodeSlow);
+        return ok ? code : fast ? (uint32_t)kCodeMiss : kCodeSlow;
     }
 }
 
@@ -482,29 +488,32 @@ struct TiledParams {
 // (packed f32x2 additions).  Likelihood codes are summed in 64-bit fixed point
 // and added to the particle's total with an integer atomic: exact and
 // independent of order, so results equal eval_exact_kernel's bit for bit.
-template <bool DENSE, int SUBMODE>
+template <bool DENSE, bool CORR>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint64_t bar;
-    __shared__ float thr[kSubThr];
     __shared__ MapView s_map;   // the map view the slow tiers read
+    __shared__ float s_next[kSubTable];
     const EvalParams& p = tp.e;
     const MapView& m = p.m;
     long long* lut = reinterpret_cast<long long*>(smem);
     const int n = p.n1 - p.n0;
     const int npairs = ((n + 63) >> 6) * 32;
     if (threadIdx.x == 0) s_map = m;
-    float4* sxy = reinterpret_cast<float4*>(smem + kLutBytes);
+    const uint32_t occ_words = DENSE ? m.occ_words : 0u;
+    uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
+    float4* sxy = reinterpret_cast<float4*>(occ + occ_words);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
-    if (threadIdx.x < kSubThr) thr[threadIdx.x] = m.sub_thr[threadIdx.x];
+    if (threadIdx.x < kSubTable) s_next[threadIdx.x] = m.sub_next[threadIdx.x];
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, (uint32_t)npairs * 24u);
+        mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_words * 4u);
         bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
         bulk_g2s(spz, p.pz + p.n0 / 2, (uint32_t)npairs * 8u, &bar);
+        if (occ_words) bulk_g2s(occ, m.occ, occ_words * 4u, &bar);
     }
     bool staged = mbar_wait_bounded(&bar, 0);
     if (!staged && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
@@ -552,16 +561,22 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
                 const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);  // 2^23 + trunc
                 const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
                 const f2_t CX = fma2_rz(SX, INV, MAG), CY = fma2_rz(SY, INV, MAG), CZ = fma2_rz(SZ, INV, MAG);
-                float ox0, ox1, oy0, oy1, oz0, oz1, mx0, mx1, my0, my1, mz0, mz1;
-                float sx0, sx1, sy0, sy1, sz0, sz1, cx0, cx1, cy0, cy1, cz0, cz1;
-                upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1);
-                upk(MX, mx0, mx1); upk(MY, my0, my1); upk(MZ, mz0, mz1);
-                upk(SX, sx0, sx1); upk(SY, sy0, sy1); upk(SZ, sz0, sz1);
-                upk(CX, cx0, cx1); upk(CY, cy0, cy1); upk(CZ, cz0, cz1);
-                uint32_t k0 = fast_code<DENSE, SUBMODE>(m, thr, ox0, oy0, oz0, mx0, my0, mz0, sx0, sy0, sz0, cx0,
-                                                         cy0, cz0);
-                uint32_t k1 = fast_code<DENSE, SUBMODE>(m, thr, ox1, oy1, oz1, mx1, my1, mz1, sx1, sy1, sz1, cx1,
-                                                         cy1, cz1);
+                FastIn i0, i1;
+                upk(OX, i0.ox, i1.ox); upk(OY, i0.oy, i1.oy); upk(OZ, i0.oz, i1.oz);
+                {
+                    float a0, a1;
+                    upk(MX, a0, a1); i0.bmx = __float_as_uint(a0); i1.bmx = __float_as_uint(a1);
+                    upk(MY, a0, a1); i0.bmy = __float_as_uint(a0); i1.bmy = __float_as_uint(a1);
+                    upk(MZ, a0, a1); i0.bmz = __float_as_uint(a0); i1.bmz = __float_as_uint(a1);
+                    upk(CX, a0, a1); i0.bcx = __float_as_uint(a0); i1.bcx = __float_as_uint(a1);
+                    upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
+                    upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
+                }
+                if (CORR) {
+                    upk(SX, i0.sx, i1.sx); upk(SY, i0.sy, i1.sy); upk(SZ, i0.sz, i1.sz);
+                }
+                uint32_t k0 = fast_code<DENSE, CORR>(m, occ, s_next, i0);
+                uint32_t k1 = fast_code<DENSE, CORR>(m, occ, s_next, i1);
                 if (blk >= nfull) {   // the chunk's last, partial block: padding points count for nothing
                     if (64 * blk + lane >= cn) k0 = kCodeNone;
                     if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
@@ -1028,6 +1043,18 @@ __global__ void codes_from_floats_kernel(const float* data, size_t n, const floa
     }
 }
 
+__global__ void occupancy_bits_kernel(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words)
+{
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
+        uint32_t bits = 0;
+        for (uint32_t b = 0; b < 32; ++b) {
+            size_t up = (size_t)w * 32 + b;
+            if (up < grid_occ_size && grid_occ[up] >= 0) bits |= 1u << b;
+        }
+        occ[w] = bits;
+    }
+}
+
 __global__ void dense_from_codes_kernel(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size,
                                         uint32_t sub3, uint16_t* dense)
 {
@@ -1074,6 +1101,21 @@ size_t eval_smem_bytes(bool serial, int n)
     return serial ? (size_t)kLutFBytes + 4ull * npad * 4 : (size_t)kLutBytes + 3ull * npad * 4;
 }
 
+size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
+{
+    return (size_t)kLutBytes + (dense ? (size_t)m.occ_words * 4 : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
+           sizeof(float4) * kRing * kTiledWarps;
+}
+
+int tiled_pass_points(const MapView& m, bool dense)
+{
+    const size_t budget = 227 * 1024 - 1024;   // dynamic shared memory left beside the static part
+    size_t fixed = tiled_smem_bytes(m, dense, 0);
+    if (fixed >= budget) return 0;
+    size_t pts = (budget - fixed) / 12 / 64 * 64;
+    return (int)(pts < (size_t)kMaxPassPoints ? pts : (size_t)kMaxPassPoints);
+}
+
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
                      bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s)
 {
@@ -1107,10 +1149,10 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.group = kTiledGroup;
         tp.groups = (P + tp.group - 1) / tp.group;
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
-        auto k = dense ? (m.sub_fast == 2 ? eval_tiled_kernel<true, 1> : eval_tiled_kernel<true, 0>)
-                       : (m.sub_fast == 2 ? eval_tiled_kernel<false, 1> : eval_tiled_kernel<false, 0>);
-        size_t tsmem = (size_t)kLutBytes + (size_t)(32 * (((n1 - n0) + 63) / 64)) * 24 +
-                       sizeof(float4) * kRing * kTiledWarps;
+        // sub_fast 2: floor(s * sub_inv) is the sub-voxel index itself; 1: it may be one short
+        auto k = dense ? (m.sub_fast == 1 ? eval_tiled_kernel<true, true> : eval_tiled_kernel<true, false>)
+                       : (m.sub_fast == 1 ? eval_tiled_kernel<false, true> : eval_tiled_kernel<false, false>);
+        size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (first) {
             cudaMemsetAsync(b.sum_fx, 0, sizeof(long long) * (size_t)P, s);
@@ -1190,6 +1232,13 @@ int launch_codes_from_floats(const float* data, size_t n, const float* code_valu
                              uint16_t* codes, int32_t* fail, cudaStream_t s)
 {
     if (n) codes_from_floats_kernel<<<1024, 256, 0, s>>>(data, n, code_values, init_value, codes, fail);
+    return check(cudaGetLastError());
+}
+
+int launch_occupancy_bits(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words,
+                          cudaStream_t s)
+{
+    if (words) occupancy_bits_kernel<<<(words + 255) / 256, 256, 0, s>>>(grid_occ, grid_occ_size, occ, words);
     return check(cudaGetLastError());
 }
 

@@ -138,11 +138,12 @@ static float min_float_where(Pred pred)
     return f;
 }
 
-int sub_index_table(float res, uint64_t sub_dim, float* inv_out, float* thr, int n)
+int sub_index_mult(float res, uint64_t sub_dim, float* inv_out, float* next_thr)
 {
-    if (!(res > 0.0f) || sub_dim + 2 > (uint64_t)n) return 0;
+    if (!(res > 0.0f) || !(res <= 1.0f) || sub_dim + 1 > (uint64_t)kSubTable) return 0;
     const int K = (int)sub_dim + 1;
-    for (int k = 0; k < n; ++k) thr[k] = 2.0f;
+    // thr[k] = smallest float s >= 0 with trunc(s / res) >= k (2.0 when none below 2)
+    std::vector<float> thr(K + 2, 2.0f);
     thr[0] = 0.0f;
     for (int k = 1; k <= K; ++k)
         thr[k] = min_float_where([&](float s) { return f2u_x86_host(s / res) >= (uint64_t)k; });
@@ -161,8 +162,9 @@ int sub_index_table(float res, uint64_t sub_dim, float* inv_out, float* thr, int
         if (a < thr[k]) return 0;                   // could overshoot q
         if (k + 1 <= K && a > thr[k + 1]) return 0;  // could undershoot q by two
     }
-    if (std::floor(1.0 * (double)inv) > (double)K - 1) return 0;   // c + 1 must stay inside the table
+    if (std::floor(1.0 * (double)inv) > (double)K - 1) return 0;   // c <= sub_dim: inside the table
     *inv_out = inv;
+    for (int c = 0; c < kSubTable; ++c) next_thr[c] = c + 1 <= K ? thr[c + 1] : 2.0f;
     // A multiplier m with floor(s * m) == trunc(s / res) for every float s in
     // [0, 1) makes the correction unnecessary: look for one near 1 / res.
     auto bits_of = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };

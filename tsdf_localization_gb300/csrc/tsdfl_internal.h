@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "map_host.h"
 #include "tsdfl.h"
 
 namespace tsdfl {
@@ -26,7 +27,6 @@ constexpr int kMaxPassPoints = 16384;
 // are exact and cannot wrap.
 constexpr float kFastOffsetLimit = 4194304.0f;
 
-constexpr int kSubThr = 32;
 
 // Everything a kernel needs to look a point up in one map, passed by value
 // (kernel parameters live in the constant bank).
@@ -49,13 +49,20 @@ struct MapView {
     const uint16_t* dense;    // dense brick layout (may be null)
     int32_t storage;          // 0 = codes, 1 = float
     // Division-free sub-voxel index for s in [0, 1), verified on the host for
-    // every float s: sub_fast = 1: trunc(s / res) == c + (s >= sub_thr[c + 1]),
-    // c = floor(s * sub_inv); sub_fast = 2: trunc(s / res) == floor(s * sub_inv);
-    // 0: neither (generic kernel).
+    // every float s with c = floor(s * sub_inv): sub_fast = 2: trunc(s / res) == c;
+    // sub_fast = 1: trunc(s / res) == c + (s >= sub_next[c]); 0: neither
+    // (generic kernel).
     int32_t sub_fast;
     float sub_inv;
-    float sub_thr[kSubThr];
+    float sub_next[kSubTable];
     uint32_t lim_x, lim_y, lim_z;  // float bits of min(mmax + 1, 2^22) per axis
+    // Fast path on float bits: with bm = bits(2^23 + trunc(offset)) and
+    // bc = bits(2^23 + floor(s * sub_inv)) per axis,
+    //   brick = bm_x + bm_y * up_dim_x + bm_z * up_dim_2 - up_bias   (mod 2^32)
+    //   slot  = bc_x + bc_y * sub_dim + bc_z * sub_dim_2 - sl_bias    (mod 2^32)
+    uint32_t up_bias, sl_bias;
+    const uint32_t* occ;           // one bit per brick: allocated (dense layout only)
+    uint32_t occ_words;            // words in occ (a multiple of 4)
 };
 
 #ifdef __CUDACC__
@@ -145,6 +152,9 @@ int launch_prepare(const float* points, int N, int npad, float max_range_sq, flo
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s);
 int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
 size_t eval_smem_bytes(bool serial, int n);
+// Scan points one pass of the tiled kernel stages (0: the kernel cannot hold
+// this map's occupancy bitmap beside any points).
+int tiled_pass_points(const MapView& m, bool dense);
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
                      bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
@@ -156,6 +166,8 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
                          cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
+int launch_occupancy_bits(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words,
+                          cudaStream_t s);
 int launch_dense_from_codes(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size, uint32_t sub3,
                             uint16_t* dense, cudaStream_t s);
 
