@@ -174,6 +174,19 @@ int tsdfl_resample_systematic(tsdfl_ctx* ctx, const float* weights, size_t M, fl
 int tsdfl_resample_systematic_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
                                      float* d_particles_out, size_t cap, uint32_t* d_count);
 
+/* No counterpart in the reference.  tsdfl_resample_systematic_device for
+ * callers that must not allocate device memory while their filter runs: the
+ * scratch is a fixed area compiled into the library (one per device, about
+ * 2.2 MB) instead of the context's growable workspace, so M is limited to
+ * 262144 particles (larger M: TSDFL_ERR_UNSUPPORTED, nothing launched).
+ * Same arguments, results and error reporting as the device form.  The first
+ * call on a device looks the scratch up (cudaGetSymbolAddress): make it before
+ * any stream capture.  Nothing in the scratch has to start at zero.  Calls
+ * whose work overlaps on one device (different streams or host threads with
+ * no ordering between them) share the scratch and race: order them. */
+int tsdfl_resample_systematic_static(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
+                                     float* d_particles_out, size_t cap, uint32_t* d_count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -745,3 +745,80 @@ int tsdfl_resample_systematic_device(tsdfl_ctx* c, const float* d_particles, siz
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ resampling without allocation
+//
+// Some callers must not allocate device memory once their filter loop runs: a
+// real-time localisation node whose update deadline cannot absorb cudaMalloc's
+// device-wide synchronisation, or a host process whose device memory is owned
+// by a fixed pool it cannot grow.  tsdfl_resample_systematic_static serves them
+// with a scratch area compiled into this library (one per device, in the
+// module's static device memory) instead of the context's growable workspace.
+
+namespace {
+
+constexpr size_t kStaticResampleParticles = size_t(1) << 18;   // largest M the static scratch holds
+// Upper bound of resample_workspace_bytes(kStaticResampleParticles): the
+// fixed-point prefix sums (8 bytes a particle), two tile tables and the
+// segment table with headroom.  Checked against the launcher's own figure on
+// every call.
+constexpr size_t kStaticResampleBytes = 8 * (kStaticResampleParticles + 2 * (kStaticResampleParticles / 256 + 2)) +
+                                        64 * 1024;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_resample_scratch[kStaticResampleBytes];
+
+std::mutex g_static_mu;
+void* g_static_ptr[kStaticMaxDevices] = {};
+
+// Device address of this device's copy of g_resample_scratch, looked up once
+// per device with that device current (the caller has made it current).
+int static_scratch(int dev, void** out)
+{
+    if (dev < 0 || dev >= kStaticMaxDevices) {
+        set_error("tsdfl_resample_systematic_static: device %d beyond the %d devices supported", dev,
+                  kStaticMaxDevices);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_resample_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error("tsdfl_resample_systematic_static: cudaGetSymbolAddress failed on device %d: %s", dev,
+                      cudaGetErrorString(e));
+            return TSDFL_ERR_DEVICE;
+        }
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return TSDFL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tsdfl_resample_systematic_static(tsdfl_ctx* c, const float* d_particles, size_t M, float u0,
+                                     float* d_particles_out, size_t cap, uint32_t* d_count)
+{
+    if (!c || (M && !d_particles) || !d_particles_out || !d_count) {
+        set_error("tsdfl_resample_systematic_static: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (M == 0) return TSDFL_OK;
+    if (M > kStaticResampleParticles || resample_workspace_bytes(M) > kStaticResampleBytes) {
+        set_error("tsdfl_resample_systematic_static: %zu particles exceed the static scratch limit of %zu", M,
+                  kStaticResampleParticles);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    void* scratch = nullptr;
+    rc = static_scratch(c->device, &scratch);
+    if (rc) return rc;
+    return launch_resample_impl(d_particles, d_particles + 6, 7, M, u0, d_particles_out, nullptr, cap, d_count,
+                                scratch, c->status, c->stream);
+}
+
+}  // extern "C"
