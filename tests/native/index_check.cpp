@@ -28,13 +28,12 @@ using namespace tsdfl;
 static uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 static float fof(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
-// Division-free sub-voxel index as the tiled kernel computes it: c from an
-// exact product, then (mode 1) one threshold compare decides c or c + 1.
-static int64_t fast_sub_index(int mode, float s, float inv, const float* next)
+// Division-free sub-voxel index as the tiled kernel computes it: mode 2
+// floor of the exact product s * hi; mode 1 trunc(fl(fma(s, hi, fl(s * lo)))).
+static int64_t fast_sub_index(int mode, float s, float hi, float lo)
 {
-    const int64_t c = (int64_t)std::floor((double)s * (double)inv);
-    if (mode == 2) return c;
-    return c + (s >= next[c & (kSubTable - 1)] ? 1 : 0);
+    if (mode == 2) return (int64_t)std::floor((double)s * (double)hi);
+    return (int64_t)std::fmaf(s, hi, s * lo);
 }
 
 static int exhaustive(int argc, char** argv)
@@ -43,19 +42,19 @@ static int exhaustive(int argc, char** argv)
     for (int a = 2; a < argc; ++a) {
         const float res = (float)atof(argv[a]);
         const uint64_t sub_dim = (uint64_t)std::ceil(1.0f / res);
-        float inv = 0.0f, next[kSubTable];
-        const int mode = sub_index_mult(res, sub_dim, &inv, next);
+        float inv = 0.0f, lo = 0.0f;
+        const int mode = sub_index_mult(res, sub_dim, &inv, &lo);
         long bad = 0;
         if (mode) {
 #pragma omp parallel for reduction(+ : bad) schedule(static)
             for (long u = 0; u < (long)fbits(1.0f); ++u) {
                 const float s = fof((uint32_t)u);
                 const int64_t want = (int64_t)f2u_x86_host(s / res);
-                if (fast_sub_index(mode, s, inv, next) != want) ++bad;
+                if (fast_sub_index(mode, s, inv, lo) != want) ++bad;
             }
         }
-        printf("exhaustive res=%g sub_dim=%llu mode=%d inv=%.9g bad=%ld\n", res, (unsigned long long)sub_dim, mode,
-               inv, bad);
+        printf("exhaustive res=%g sub_dim=%llu mode=%d hi=%.9g lo=%.9g bad=%ld\n", res, (unsigned long long)sub_dim,
+               mode, inv, lo, bad);
         if (bad || !mode) ++fails;
     }
     return fails ? 1 : 0;
@@ -95,7 +94,7 @@ int main(int argc, char** argv)
             v.dim_x = c.dim_x; v.dim_y = c.dim_y; v.dim_z = c.dim_z;
             v.up_dim_x64 = c.up_dim_x; v.up_dim_2_64 = c.up_dim_2; v.grid_occ_size64 = c.grid_occ_size;
             v.sub_dim64 = c.sub_dim; v.sub_dim_2_64 = c.sub_dim_2; v.data_size64 = c.data_size;
-            v.sub_fast = sub_index_mult(res, c.sub_dim, &v.sub_inv, v.sub_next);
+            v.sub_fast = sub_index_mult(res, c.sub_dim, &v.sub_inv, &v.sub_inv_lo);
             std::uniform_real_distribution<float> U(-3.5f, 25.0f);
             const float special[] = {-1.0f, -0.99999994f, -0.5f, -0.0f, 0.0f, 1e-30f, 0.99999994f, 1.0f, -2.0f, -1e-7f};
             for (long i = 0; i < n_points; ++i) {
@@ -127,7 +126,7 @@ int main(int argc, char** argv)
                     for (int a = 0; a < 3; ++a) {
                         mm[a] = (int64_t)oo[a];
                         float s = oo[a] - (float)mm[a];
-                        qq[a] = fast_sub_index(v.sub_fast, s, v.sub_inv, v.sub_next);
+                        qq[a] = fast_sub_index(v.sub_fast, s, v.sub_inv, v.sub_inv_lo);
                     }
                     uint64_t up = (uint64_t)(mm[0] + mm[1] * (int64_t)c.up_dim_x + mm[2] * (int64_t)c.up_dim_2);
                     uint32_t got = kIdxMiss;

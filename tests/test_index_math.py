@@ -32,10 +32,10 @@ def test_index_math_matches_oracle(tmp_path):
 
 
 def test_sub_index_exhaustive(tmp_path):
-    """Every float s in [0, 1): the multiplier (and, where needed, the
-    threshold table) gives trunc(s / res)."""
+    """Every float s in [0, 1): the one- or two-term multiplier gives
+    trunc(s / res)."""
     exe = _build(tmp_path)
-    ress = ["0.05", "0.064", "0.032", "0.1", "0.03"]
+    ress = ["0.05", "0.064", "0.032", "0.02"]
     res = subprocess.run([str(exe), "exhaustive", *ress], capture_output=True, text=True)
     print(res.stdout)
     assert res.returncode == 0, res.stdout

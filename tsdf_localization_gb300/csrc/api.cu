@@ -239,7 +239,7 @@ void fill_view(tsdfl_map* m)
     v.data = m->data;
     v.dense = m->dense;
     v.storage = m->codes ? 0 : 1;
-    v.sub_fast = sub_index_mult(c.resolution, c.sub_dim, &v.sub_inv, v.sub_next);
+    v.sub_fast = sub_index_mult(c.resolution, c.sub_dim, &v.sub_inv, &v.sub_inv_lo);
     auto lim = [](int32_t mmax) {
         float f = (float)std::min<int64_t>((int64_t)mmax + 1, 4194304);
         if (mmax < 0) f = 0.0f;

@@ -342,8 +342,10 @@ __device__ __forceinline__ void upk(f2_t v, float& a, float& b)
 {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
-// Packed additions only: ptxas fuses packed multiply/add pairs into FMA even
-// with explicit .rn, so products stay scalar (__fmul_rn is never contracted).
+// Packed additions: ptxas fuses a packed multiply feeding a packed add into an
+// FMA even with explicit .rn, so products that feed additions stay scalar
+// (__fmul_rn is never contracted).  mul2 is used only where its product is the
+// addend of an FMA, which no contraction can absorb.
 __device__ __forceinline__ f2_t add2(f2_t a, f2_t b)
 {
     f2_t r;
@@ -360,6 +362,18 @@ __device__ __forceinline__ f2_t sub2(f2_t a, f2_t b)
 {
     f2_t r;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t mul2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2_t fma2_rn(f2_t a, f2_t b, f2_t c)
+{
+    f2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
     return r;
 }
 __device__ __forceinline__ f2_t fma2_rz(f2_t a, f2_t b, f2_t c)
@@ -384,38 +398,30 @@ __device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y
 }
 
 // Per-lookup inputs of the fast path, all from the packed pipeline: map
-// offsets o, bm = bits(2^23 + trunc(o)), bc = bits(2^23 + floor(s * sub_inv))
-// and the in-brick remainders s = o - trunc(o).
+// offsets o, bm = bits(2^23 + trunc(o)) and bc = bits(2^23 + q) with q the
+// sub-voxel index of the remainder s = o - trunc(o).
 struct FastIn {
     float ox, oy, oz;
     uint32_t bmx, bmy, bmz;
     uint32_t bcx, bcy, bcz;
-    float sx, sy, sz;
 };
 
 // Branch-free fast path: the slot code, kCodeMiss, or kCodeSlow when the exact
 // slow tiers must decide (offset outside [0, mmax + 1), or -- dense layout -- a
-// sub-voxel index past the brick's end).  CORR: floor(s * sub_inv) may be one
-// short; the shared-memory threshold table `next` decides (bc's low bits are c).
-// DENSE: one gather from the dense layout, the brick's occupancy bit from the
-// shared-memory bitmap `occ`; otherwise the brick table and the slot array.
-template <bool DENSE, bool CORR>
-__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const float* next,
-                                              const FastIn& in)
+// sub-voxel index past the brick's end).  DENSE: one gather from the dense
+// layout, the brick's occupancy bit from the shared-memory bitmap `occ`;
+// otherwise the brick table and the slot array.
+template <bool DENSE>
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const FastIn& in)
 {
     const bool fast = __float_as_uint(in.ox) < m.lim_x && __float_as_uint(in.oy) < m.lim_y &&
                       __float_as_uint(in.oz) < m.lim_z;
     const uint32_t up = in.bmx + in.bmy * m.up_dim_x + in.bmz * m.up_dim_2 - m.up_bias;
-    uint32_t sl = in.bcx + in.bcy * m.sub_dim + in.bcz * m.sub_dim_2 - m.sl_bias;
-    if (CORR) {
-        constexpr uint32_t mask = kSubTable - 1;
-        sl += (in.sx >= next[in.bcx & mask] ? 1u : 0u) + (in.sy >= next[in.bcy & mask] ? m.sub_dim : 0u) +
-              (in.sz >= next[in.bcz & mask] ? m.sub_dim_2 : 0u);
-    }
+    const uint32_t sl = in.bcx + in.bcy * m.sub_dim + in.bcz * m.sub_dim_2 - m.sl_bias;
     const bool inside = fast && up < m.grid_occ_size;
     if (DENSE) {
         const uint32_t word = occ[inside ? (up >> 5) : 0u];
-        const bool alloc = (word >> (up & 31u)) & 1u;
+        const bool alloc = (__funnelshift_r(word, word, up) & 1u) != 0u;   // bit up mod 32
         const bool ok = inside && alloc && sl < m.sub_dim_3;
         const uint32_t code = __ldg(m.dense + (ok ? (size_t)up * m.sub_dim_3 + sl : (size_t)0));
         return ok ? code : (inside && !alloc) || (fast && !inside) ? (uint32_t)kCodeMiss : kCodeSlow;
@@ -485,16 +491,17 @@ struct TiledParams {
 // belongs to warp k mod W of the W warps of the grid -- so all SMs score the
 // same part of the scan at a time and its map footprint stays in L2, with no
 // block-wide barrier after staging.  Each lane scores two points per step
-// (packed f32x2 additions).  Likelihood codes are summed in 64-bit fixed point
+// (packed f32x2 arithmetic).  Likelihood codes are summed in 64-bit fixed point
 // and added to the particle's total with an integer atomic: exact and
 // independent of order, so results equal eval_exact_kernel's bit for bit.
-template <bool DENSE, bool CORR>
+// TWO: the sub-voxel index needs the two-term multiplier (sub_fast 1);
+// DBG: per-point codes are written to the debug buffer.
+template <bool DENSE, bool TWO, bool DBG>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ MapView s_map;   // the map view the slow tiers read
-    __shared__ float s_next[kSubTable];
     const EvalParams& p = tp.e;
     const MapView& m = p.m;
     long long* lut = reinterpret_cast<long long*>(smem);
@@ -506,7 +513,6 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     float4* sxy = reinterpret_cast<float4*>(occ + occ_words);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
-    if (threadIdx.x < kSubTable) s_next[threadIdx.x] = m.sub_next[threadIdx.x];
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -527,6 +533,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
     const f2_t MAG = pk(8388608.0f, 8388608.0f);
     const f2_t INV = pk(m.sub_inv, m.sub_inv);
+    const f2_t INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
         const int c0 = chunk * tp.chunk;
@@ -540,8 +547,10 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
             const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
             long long acc = 0;
             uint32_t hits = 0;
-            uint32_t* dbg_row = p.dbg ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
-            for (int blk = 0; blk < nblk; ++blk) {
+            uint32_t* dbg_row = DBG ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
+            // one step: the two points of block blk held by this lane (the
+            // chunk's partial last block masks its padding points)
+            auto step = [&](int blk, bool partial) {
                 const float4 xy = sxy[(b0 + blk) * 32 + lane];
                 const float2 zz = spz[(b0 + blk) * 32 + lane];
                 // tsdf_evaluator.cpp:44-46 for two points: ((r0 x + r1 y) + r2 z) + r3
@@ -560,7 +569,16 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
                 const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
                 const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);  // 2^23 + trunc
                 const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
-                const f2_t CX = fma2_rz(SX, INV, MAG), CY = fma2_rz(SY, INV, MAG), CZ = fma2_rz(SZ, INV, MAG);
+                f2_t CX, CY, CZ;   // 2^23 + sub-voxel index
+                if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
+                    CX = add2_rz(fma2_rn(SX, INV, mul2(SX, INVLO)), MAG);
+                    CY = add2_rz(fma2_rn(SY, INV, mul2(SY, INVLO)), MAG);
+                    CZ = add2_rz(fma2_rn(SZ, INV, mul2(SZ, INVLO)), MAG);
+                } else {           // floor(s * inv), the product unrounded
+                    CX = fma2_rz(SX, INV, MAG);
+                    CY = fma2_rz(SY, INV, MAG);
+                    CZ = fma2_rz(SZ, INV, MAG);
+                }
                 FastIn i0, i1;
                 upk(OX, i0.ox, i1.ox); upk(OY, i0.oy, i1.oy); upk(OZ, i0.oz, i1.oz);
                 {
@@ -572,12 +590,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
                     upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
                     upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
                 }
-                if (CORR) {
-                    upk(SX, i0.sx, i1.sx); upk(SY, i0.sy, i1.sy); upk(SZ, i0.sz, i1.sz);
-                }
-                uint32_t k0 = fast_code<DENSE, CORR>(m, occ, s_next, i0);
-                uint32_t k1 = fast_code<DENSE, CORR>(m, occ, s_next, i1);
-                if (blk >= nfull) {   // the chunk's last, partial block: padding points count for nothing
+                uint32_t k0 = fast_code<DENSE>(m, occ, i0);
+                uint32_t k1 = fast_code<DENSE>(m, occ, i1);
+                if (partial) {
                     if (64 * blk + lane >= cn) k0 = kCodeNone;
                     if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
                 }
@@ -604,14 +619,16 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
                         head += 32;
                     }
                 }
-                if (dbg_row) {
+                if (DBG) {
                     const int j = c0 + 64 * blk + lane;
                     if (k0 < (uint32_t)kCodeNone) dbg_row[j] = k0;
                     if (k1 < (uint32_t)kCodeNone) dbg_row[j + 32] = k1;
                 }
                 acc += lut[k0] + lut[k1];
                 hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
-            }
+            };
+            for (int blk = 0; blk < nfull; ++blk) step(blk, false);
+            if (nfull < nblk) step(nfull, true);
             if (tail != head) {
                 const Partial d = drain(&s_map, lut, ring, head, (int)(tail - head), lane, dbg_row);
                 acc += d.acc;
@@ -1149,9 +1166,12 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.group = kTiledGroup;
         tp.groups = (P + tp.group - 1) / tp.group;
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
-        // sub_fast 2: floor(s * sub_inv) is the sub-voxel index itself; 1: it may be one short
-        auto k = dense ? (m.sub_fast == 1 ? eval_tiled_kernel<true, true> : eval_tiled_kernel<true, false>)
-                       : (m.sub_fast == 1 ? eval_tiled_kernel<false, true> : eval_tiled_kernel<false, false>);
+        // sub_fast 2: floor(s * sub_inv) is the sub-voxel index; 1: the two-term multiplier
+        const bool two = m.sub_fast == 1, dbg = p.dbg != nullptr;
+        auto k = dense ? (two ? (dbg ? eval_tiled_kernel<true, true, true> : eval_tiled_kernel<true, true, false>)
+                              : (dbg ? eval_tiled_kernel<true, false, true> : eval_tiled_kernel<true, false, false>))
+                       : (two ? (dbg ? eval_tiled_kernel<false, true, true> : eval_tiled_kernel<false, true, false>)
+                              : (dbg ? eval_tiled_kernel<false, false, true> : eval_tiled_kernel<false, false, false>));
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (first) {

@@ -138,59 +138,66 @@ static float min_float_where(Pred pred)
     return f;
 }
 
-int sub_index_mult(float res, uint64_t sub_dim, float* inv_out, float* next_thr)
+int sub_index_mult(float res, uint64_t sub_dim, float* hi_out, float* lo_out)
 {
-    if (!(res > 0.0f) || !(res <= 1.0f) || sub_dim + 1 > (uint64_t)kSubTable) return 0;
+    if (!(res > 0.0f) || !(res <= 1.0f) || sub_dim + 2 > 4096) return 0;
     const int K = (int)sub_dim + 1;
     // thr[k] = smallest float s >= 0 with trunc(s / res) >= k (2.0 when none below 2)
-    std::vector<float> thr(K + 2, 2.0f);
-    thr[0] = 0.0f;
+    std::vector<float> thr(K + 1, 2.0f);
     for (int k = 1; k <= K; ++k)
         thr[k] = min_float_where([&](float s) { return f2u_x86_host(s / res) >= (uint64_t)k; });
-    float inv = 1.0f / res;
-    auto approx_thr = [&](int k, float m) {
-        return min_float_where([&](float s) { return std::floor((double)s * (double)m) >= (double)k; });
-    };
-    for (int tries = 0; tries < 64; ++tries) {
-        bool low_ok = true;   // floor(s*inv) <= q  <=>  approx threshold k is not below the exact one
-        for (int k = 1; k <= K && low_ok; ++k) low_ok = approx_thr(k, inv) >= thr[k];
-        if (low_ok) break;
-        inv = std::nextafter(inv, 0.0f);
-    }
-    for (int k = 1; k <= K; ++k) {
-        float a = approx_thr(k, inv);
-        if (a < thr[k]) return 0;                   // could overshoot q
-        if (k + 1 <= K && a > thr[k + 1]) return 0;  // could undershoot q by two
-    }
-    if (std::floor(1.0 * (double)inv) > (double)K - 1) return 0;   // c <= sub_dim: inside the table
-    *inv_out = inv;
-    for (int c = 0; c < kSubTable; ++c) next_thr[c] = c + 1 <= K ? thr[c + 1] : 2.0f;
-    // A multiplier m with floor(s * m) == trunc(s / res) for every float s in
-    // [0, 1) makes the correction unnecessary: look for one near 1 / res.
     auto bits_of = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
     auto float_of = [](uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; };
     const float below_one = float_of(bits_of(1.0f) - 1);
+    // q(s) and both candidate forms are non-decreasing in s, so they agree on
+    // every float in [0, 1) iff they agree on both sides of every threshold.
+    auto agrees = [&](auto idx) {
+        for (int k = 1; k <= K; ++k) {
+            if (thr[k] < 1.0f) {
+                if (idx(thr[k]) < (uint64_t)k || idx(float_of(bits_of(thr[k]) - 1)) >= (uint64_t)k) return false;
+            } else if (idx(below_one) >= (uint64_t)k) {
+                return false;
+            }
+        }
+        return true;
+    };
+    // one multiplier m: q == floor(s * m), the product taken exactly
     const float base = 1.0f / res;
     for (int d = 0; d <= 8192; ++d) {
         for (int sgn = -1; sgn <= 1; sgn += 2) {
             if (d == 0 && sgn > 0) continue;
-            float m = float_of(bits_of(base) + (uint32_t)(sgn * d));
-            bool good = true;
-            for (int k = 1; k <= K && good; ++k) {
-                if (thr[k] < 1.0f) {
-                    double hi = (double)thr[k] * m, lo = (double)float_of(bits_of(thr[k]) - 1) * m;
-                    good = hi >= k && lo < k;
-                } else {
-                    good = (double)below_one * m < k;
-                }
-            }
-            if (good) {
-                *inv_out = m;
+            const float m = float_of(bits_of(base) + (uint32_t)(sgn * d));
+            if (agrees([&](float s) { return (uint64_t)std::floor((double)s * (double)m); })) {
+                *hi_out = m;
+                *lo_out = 0.0f;
                 return 2;
             }
         }
     }
-    return 1;
+    // two terms hi + lo ~ 1 / res to about 48 bits: q == trunc(fl(s * hi + fl(s * lo)));
+    // |lo| << hi keeps the form monotone in s
+    const double inv = 1.0 / (double)res;
+    const float h0 = (float)inv;
+    for (int da = 0; da <= 16; ++da) {
+        for (int sa = -1; sa <= 1; sa += 2) {
+            if (da == 0 && sa > 0) continue;
+            const float hi = float_of(bits_of(h0) + (uint32_t)(sa * da));
+            const float l0 = (float)(inv - (double)hi);
+            for (int db = 0; db <= 16; ++db) {
+                for (int sb = -1; sb <= 1; sb += 2) {
+                    if (db == 0 && sb > 0) continue;
+                    const float lo = l0 == 0.0f ? 0.0f : float_of(bits_of(l0) + (uint32_t)(sb * db));
+                    if (!(std::fabs(lo) * 4.0f < hi)) continue;
+                    if (agrees([&](float s) { return (uint64_t)std::fmaf(s, hi, s * lo); })) {
+                        *hi_out = hi;
+                        *lo_out = lo;
+                        return 1;
+                    }
+                }
+            }
+        }
+    }
+    return 0;
 }
 
 }  // namespace tsdfl

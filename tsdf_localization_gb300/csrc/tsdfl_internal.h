@@ -48,13 +48,13 @@ struct MapView {
     const float* data;        // float slots (storage 1)
     const uint16_t* dense;    // dense brick layout (may be null)
     int32_t storage;          // 0 = codes, 1 = float
-    // Division-free sub-voxel index for s in [0, 1), verified on the host for
-    // every float s with c = floor(s * sub_inv): sub_fast = 2: trunc(s / res) == c;
-    // sub_fast = 1: trunc(s / res) == c + (s >= sub_next[c]); 0: neither
-    // (generic kernel).
+    // Division-free sub-voxel index q = trunc(fl(s / res)) for s in [0, 1),
+    // verified on the host (every threshold of q; monotone in s):
+    // sub_fast = 2: q == floor(s * sub_inv) (exact product);
+    // sub_fast = 1: q == trunc(fl(s * sub_inv + fl(s * sub_inv_lo))) (one FMA);
+    // 0: neither (generic kernel).
     int32_t sub_fast;
-    float sub_inv;
-    float sub_next[kSubTable];
+    float sub_inv, sub_inv_lo;
     uint32_t lim_x, lim_y, lim_z;  // float bits of min(mmax + 1, 2^22) per axis
     // Fast path on float bits: with bm = bits(2^23 + trunc(offset)) and
     // bc = bits(2^23 + floor(s * sub_inv)) per axis,
