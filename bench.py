@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--workload", default="building", choices=["building", "room"])
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
-    ap.add_argument("--layout", default="dense", choices=["dense", "brick"])
+    ap.add_argument("--layout", default="brick", choices=["dense", "brick"])
     ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -118,16 +118,19 @@ int main(int argc, char** argv)
                     if (bad < 10) printf("tier2 mismatch res=%g o=(%.9g %.9g %.9g) got %u want %u\n", res, ox, oy, oz, t2, want);
                     ++bad;
                 }
-                // fast path emulation (only for offsets inside [0, mmax + 1) on every axis)
-                if (v.sub_fast && fbits(ox) < v.lim_x && fbits(oy) < v.lim_y && fbits(oz) < v.lim_z) {
+                // fast path emulation: offsets inside [0, mmax + 1) on x and y, and on
+                // z also (-1, 0) when lim_z > 0 (brick 0, negative sub-voxel index)
+                const bool zneg = std::signbit(oz) && std::fabs(oz) < 1.0f && v.lim_z != 0;
+                if (v.sub_fast && fbits(ox) < v.lim_x && fbits(oy) < v.lim_y && (fbits(oz) < v.lim_z || zneg)) {
                     ++fast_n;
-                    float oo[3] = {ox, oy, oz};
+                    float oo[3] = {ox, oy, std::fabs(oz)};
                     int64_t mm[3], qq[3];
                     for (int a = 0; a < 3; ++a) {
                         mm[a] = (int64_t)oo[a];
                         float s = oo[a] - (float)mm[a];
                         qq[a] = fast_sub_index(v.sub_fast, s, v.sub_inv, v.sub_inv_lo);
                     }
+                    if (std::signbit(oz)) qq[2] = -qq[2];
                     uint64_t up = (uint64_t)(mm[0] + mm[1] * (int64_t)c.up_dim_x + mm[2] * (int64_t)c.up_dim_2);
                     uint32_t got = kIdxMiss;
                     if (up < c.grid_occ_size && go[up] >= 0) {

@@ -253,6 +253,8 @@ void fill_view(tsdfl_map* m)
     const uint32_t K = 0x4B000000u;
     v.up_bias = K * (1u + v.up_dim_x + v.up_dim_2);
     v.sl_bias = K * (1u + v.sub_dim + v.sub_dim_2);
+    v.lim_zn = v.lim_z ? 0x3F800000u : 0u;
+    v.sl_bias_xy = K * (1u + v.sub_dim);
     v.occ = m->occ;
     v.occ_words = m->occ_words;
 }

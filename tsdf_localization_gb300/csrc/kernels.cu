@@ -364,6 +364,12 @@ __device__ __forceinline__ f2_t sub2(f2_t a, f2_t b)
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ f2_t and2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("and.b64 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ f2_t mul2(f2_t a, f2_t b)
 {
     f2_t r;
@@ -398,8 +404,8 @@ __device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y
 }
 
 // Per-lookup inputs of the fast path, all from the packed pipeline: map
-// offsets o, bm = bits(2^23 + trunc(o)) and bc = bits(2^23 + q) with q the
-// sub-voxel index of the remainder s = o - trunc(o).
+// offsets o, bm = bits(2^23 + trunc(|o|)) and bc = bits(2^23 + q(s)) with q the
+// sub-voxel index of s = |o| - trunc(|o|) (x and y are fast only when o >= 0).
 struct FastIn {
     float ox, oy, oz;
     uint32_t bmx, bmy, bmz;
@@ -407,17 +413,20 @@ struct FastIn {
 };
 
 // Branch-free fast path: the slot code, kCodeMiss, or kCodeSlow when the exact
-// slow tiers must decide (offset outside [0, mmax + 1), or -- dense layout -- a
-// sub-voxel index past the brick's end).  DENSE: one gather from the dense
-// layout, the brick's occupancy bit from the shared-memory bitmap `occ`;
-// otherwise the brick table and the slot array.
+// slow tiers must decide (offset outside [0, mmax + 1) -- on z outside
+// (-1, mmax + 1) -- or, dense layout, a sub-voxel index outside the brick).
+// DENSE: one gather from the dense layout, the brick's occupancy bit from the
+// shared-memory bitmap `occ`; otherwise the brick table and the slot array.
 template <bool DENSE>
 __device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const FastIn& in)
 {
+    const uint32_t zb = __float_as_uint(in.oz);
+    const uint32_t sgn = (uint32_t)((int32_t)zb >> 31);   // all ones when oz < 0
     const bool fast = __float_as_uint(in.ox) < m.lim_x && __float_as_uint(in.oy) < m.lim_y &&
-                      __float_as_uint(in.oz) < m.lim_z;
+                      (zb & 0x7fffffffu) < (sgn ? m.lim_zn : m.lim_z);
     const uint32_t up = in.bmx + in.bmy * m.up_dim_x + in.bmz * m.up_dim_2 - m.up_bias;
-    const uint32_t sl = in.bcx + in.bcy * m.sub_dim + in.bcz * m.sub_dim_2 - m.sl_bias;
+    const uint32_t qz = ((in.bcz - kMagic) ^ sgn) - sgn;   // -q(|oz|) below the map
+    const uint32_t sl = in.bcx + in.bcy * m.sub_dim - m.sl_bias_xy + qz * m.sub_dim_2;
     const bool inside = fast && up < m.grid_occ_size;
     if (DENSE) {
         const uint32_t word = occ[inside ? (up >> 5) : 0u];
@@ -426,6 +435,7 @@ __device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* 
         const uint32_t code = __ldg(m.dense + (ok ? (size_t)up * m.sub_dim_3 + sl : (size_t)0));
         return ok ? code : (inside && !alloc) || (fast && !inside) ? (uint32_t)kCodeMiss : kCodeSlow;
     } else {
+        // slot indices below 0 wrap past 2^31 > data_size: a miss, as in getIndex's 64-bit sum
         const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
         const uint32_t idx = (uint32_t)base + sl;
         const bool ok = inside && base >= 0 && idx < m.data_size;
@@ -534,6 +544,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const f2_t MAG = pk(8388608.0f, 8388608.0f);
     const f2_t INV = pk(m.sub_inv, m.sub_inv);
     const f2_t INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
+    const f2_t ABS = 0x7fffffff7fffffffull;
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
         const int c0 = chunk * tp.chunk;
@@ -567,8 +578,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
                                           pk(__fmul_rn(c4.z, zz.x), __fmul_rn(c4.z, zz.y))),
                                      R11);
                 const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
-                const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(OZ, MAG);  // 2^23 + trunc
-                const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(OZ, sub2(MZ, MAG));
+                const f2_t AZ = and2(OZ, ABS);   // |oz|
+                const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(AZ, MAG);  // 2^23 + trunc
+                const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(AZ, sub2(MZ, MAG));
                 f2_t CX, CY, CZ;   // 2^23 + sub-voxel index
                 if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
                     CX = add2_rz(fma2_rn(SX, INV, mul2(SX, INVLO)), MAG);

@@ -61,6 +61,11 @@ struct MapView {
     //   brick = bm_x + bm_y * up_dim_x + bm_z * up_dim_2 - up_bias   (mod 2^32)
     //   slot  = bc_x + bc_y * sub_dim + bc_z * sub_dim_2 - sl_bias    (mod 2^32)
     uint32_t up_bias, sl_bias;
+    // Negative z offsets in (-1, 0) (points just below the map) also take the
+    // fast path: brick z 0 and sub-voxel index -q(|oz|), as getIndex gives them.
+    // lim_zn: float bits bounding |oz| there (1.0, or 0 when lim_z is 0);
+    // sl_bias_xy = bits(2^23) * (1 + sub_dim).
+    uint32_t lim_zn, sl_bias_xy;
     const uint32_t* occ;           // one bit per brick: allocated (dense layout only)
     uint32_t occ_words;            // words in occ (a multiple of 4)
 };
