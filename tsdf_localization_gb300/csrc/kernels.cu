@@ -757,15 +757,27 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
 }
 
 // Final weight sum, the "No particle is valid!" check (tsdf_evaluator.cpp:159)
-// and the mean pose with circular means of the angles (:219-221).
-__global__ void norm_final_kernel(EvalBuffers b, float* pose_out)
+// and the mean pose with circular means of the angles (:219-221).  One block
+// of kNormBlocks threads: thread t takes block t's partial sums, then a fixed
+// reduction tree (so the result does not depend on timing).
+__global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, float* pose_out)
 {
-    if (threadIdx.x != 0) return;
-    double s[kNormSums];
-    for (int k = 0; k < kNormSums; ++k) s[k] = 0.0;
-    for (int blk = 0; blk < kNormBlocks; ++blk)
-        for (int k = 0; k < kNormSums; ++k) s[k] += b.partials[blk * kNormSums + k];
-    for (int k = 0; k < kNormSums; ++k) b.sums[k] = s[k];
+    __shared__ double red[kNormSums][kNormBlocks / 32];
+    __shared__ double s[kNormSums];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int k = 0; k < kNormSums; ++k) {
+        const double v = warp_sum_d(b.partials[t * kNormSums + k]);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (t < kNormSums) {
+        double v = 0.0;
+        for (int w = 0; w < kNormBlocks / 32; ++w) v += red[t][w];
+        s[t] = v;
+        b.sums[t] = v;
+    }
+    __syncthreads();
+    if (t != 0) return;
     float wsum = (float)s[0];
     b.weight_sum_f[0] = wsum;
     if (!(wsum != 0.0f) || !isfinite(s[0])) {
@@ -879,18 +891,36 @@ __global__ void resample_scan_kernel(const float* w, int stride, int M, Resample
     if (threadIdx.x == 0 && bad) atomicExch(ws.exact_ok, 0);
 }
 
+// 2^k for -1022 <= k <= 1023, exactly.
+__device__ __forceinline__ double pow2(int k)
+{
+    return __longlong_as_double((long long)(k + 1023) << 52);
+}
+
 // Builds the piecewise-arithmetic description of the reference's float draw
 // sequence U_{k+1} = (float)((double)U_k + 1.0/M) (novel_resampling.h:59-63):
 // inside one binade of float the step is constant except near its top, where
-// single steps are taken literally.  One thread.
+// single steps are taken literally.  One warp: the lanes form the tiles'
+// prefix offsets, lane 0 walks the binades (scalings by powers of two only).
 __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs ws)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    long long acc = 0;
-    for (int t = 0; t < tiles; ++t) {
-        ws.tile_off[t] = acc;
-        acc += ws.tile_sums[t];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32 || blockIdx.x != 0) return;
+    const int per = (tiles + 31) / 32, t0 = min(tiles, lane * per), t1 = min(tiles, t0 + per);
+    long long loc = 0;
+    for (int t = t0; t < t1; ++t) loc += ws.tile_sums[t];
+    long long x = loc;   // inclusive scan over the lanes (exact integers)
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
+    long long off = x - loc;
+    for (int t = t0; t < t1; ++t) {
+        ws.tile_off[t] = off;
+        off += ws.tile_sums[t];
+    }
+    const long long acc = __shfl_sync(0xffffffffu, x, 31);
+    if (lane != 0) return;
     *ws.total = acc;
     if (acc >= (1ll << 53)) *ws.exact_ok = 0;   // partial sums >= 2 may round in the serial double sum
     if (!*ws.exact_ok) { *ws.nseg = 0; return; }
@@ -902,25 +932,24 @@ __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs 
     for (int iter = 0; U < s_total; ++iter) {
         if (ns == kMaxSegments || iter > 4 * kMaxSegments) { *ws.exact_ok = 0; break; }
         float uf = (float)U;
-        int e;
         bool regular = false;
         long long cnt = 0;
         double delta = 0.0;
         if (uf >= 1.17549435e-38f) {     // normal float: binade [2^e, 2^(e+1))
-            frexp(U, &e);
-            e -= 1;                       // U = m * 2^e, m in [1, 2)
-            double u = ldexp(1.0, e - 23);     // float ulp in the binade
-            double g = ldexp(1.0, e - 52);     // double ulp in the binade
-            double y = rint(inv_m / g) * g;    // (double)U + inv_m - U, while inside the binade
-            double r = y / u;
+            const int e = (int)((__double_as_longlong(U) >> 52) & 0x7ff) - 1023;
+            const double u = pow2(e - 23);     // float ulp in the binade
+            const double g = pow2(e - 52);     // double ulp in the binade
+            const double ginv = pow2(52 - e);
+            const double y = rint(inv_m * ginv) * g;   // (double)U + inv_m - U, while inside the binade
+            const double r = y * pow2(23 - e);          // y / u
             double frac = r - floor(r);
             if (frac == 0.5) { *ws.exact_ok = 0; break; }   // step would depend on the parity of U
             delta = rint(r) * u;
             if (delta <= 0.0) { *ws.exact_ok = 0; break; }  // U would stop advancing
             // values U + i*delta with U + i*delta + y < 2^(e+1) take the regular step
-            double top = ldexp(1.0, e + 1) - y;
+            double top = pow2(e + 1) - y;
             if (U < top) {
-                long long Ui = (long long)(U / g), Di = (long long)(delta / g), Ti = (long long)(top / g);
+                long long Ui = (long long)(U * ginv), Di = (long long)(delta * ginv), Ti = (long long)(top * ginv);
                 cnt = (Ti - Ui + Di - 1) / Di;
                 regular = cnt > 0;
             }
@@ -1213,7 +1242,7 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
 {
     NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points};
     norm_partial_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(q, b, sum_f64);
-    norm_final_kernel<<<1, 32, 0, s>>>(b, pose_out);
+    norm_final_kernel<<<1, kNormBlocks, 0, s>>>(b, pose_out);
     g_launches += 2;
     if (P > 0) {
         normalize_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
