@@ -30,14 +30,14 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "scored particle*points/s at 100k x 8k"
-UNIT = "particle*points/s"
+METRIC = "scored particle\u00b7points/s at 100k\u00d78k (vs plain); p50/p99 update latency served"
+UNIT = "particle\u00b7points/s"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="building", choices=["building", "room"])
@@ -171,6 +171,18 @@ def _reference_map(O, wl):
     return O.RefMap.from_slots(wl.coef, wl.grid_occ, wl.float_data())
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest of every rank's x (all ranks get it); x itself without a
+    process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference_arm(args, rank: int) -> None:
     if rank != 0:
         return
@@ -282,11 +294,10 @@ def main():
         launches = lib.tsdfl_launch_count() - l0
         clocks = clk.summary()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(np.sum(step_ms))
+    total_ms = max_over_ranks(float(np.sum(step_ms)), device=f"cuda:{local}")
+    latency = {"p50": max_over_ranks(float(np.percentile(step_ms, 50)), device=f"cuda:{local}"),
+               "p99": max_over_ranks(float(np.percentile(step_ms, 99)), device=f"cuda:{local}")}
     if world > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     value = P * Npts * args.steps * world / (total_ms / 1000.0)
     lib.tsdfl_ctx_set_timing(ctx.handle, 0)
@@ -352,9 +363,9 @@ def main():
                           "map_device_bytes": int(info["device_bytes"]), "sums": "exact fixed point",
                           "l2": "flushed (512 MB write) before every timed step",
                           "step": "sensor update + normalise + mean pose + systematic resample",
-                          "parallelism": f"replicas x{world}"},
+                          "form": "plain single filter", "parallelism": f"replicas x{world}"},
                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
-               "clocks": clocks}
+               "latency_ms": latency, "clocks": clocks}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -1,0 +1,256 @@
+/* C++ host side of libtsdfl: RAII handles, the sensor update and systematic
+ * resampling on the caller's particle containers, and -- when compiled inside
+ * tsdf_localization (define TSDFL_WITH_TSDF_LOCALIZATION after including its
+ * headers) -- the drop-in plug-ins for its Evaluator and Resampler interfaces:
+ *
+ *   tsdf_localization::GpuTsdfEvaluator      replaces CudaEvaluator
+ *       (include/tsdf_localization/cuda/cuda_evaluator.h:94-125)
+ *   tsdf_localization::GpuSystematicResampler replaces SystematicResampler
+ *       (include/tsdf_localization/resampling/novel_resampling.h:38-74)
+ *
+ * Errors surface as std::runtime_error carrying libtsdfl's message, as the
+ * reference's evaluators throw them ("No particle is valid!" for a zero
+ * weight sum). */
+#ifndef TSDFL_EVALUATOR_HPP
+#define TSDFL_EVALUATOR_HPP
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <utility>
+#include <vector>
+
+#include "tsdfl.h"
+
+namespace tsdfl {
+
+inline void check(int rc)
+{
+    if (rc != TSDFL_OK) throw std::runtime_error(tsdfl_last_error());
+}
+
+// One device with its stream and workspace.
+class Context {
+public:
+    explicit Context(int device = 0) { check(tsdfl_ctx_create(device, &h_)); }
+    ~Context() { tsdfl_ctx_destroy(h_); }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    tsdfl_ctx* get() const { return h_; }
+    void set_stream(void* cuda_stream) { check(tsdfl_ctx_set_stream(h_, cuda_stream)); }
+    void sync() { check(tsdfl_ctx_sync(h_)); }
+
+private:
+    tsdfl_ctx* h_ = nullptr;
+};
+
+// A likelihood map on the device, from the reference's map contents: its
+// MapCoef, brick table and float slots (CudaSubVoxelMap::coef(), rawGridOcc(),
+// rawData()).  sigma is the likelihood's standard deviation the slots were made
+// with (map_util.h:124-127); slots that are not likelihood values of it keep
+// float storage.
+class Map {
+public:
+    Map(Context& ctx, const tsdfl_map_coef& coef, const int32_t* grid_occ, const float* data, float sigma = 0.1f,
+        uint32_t flags = 0)
+    {
+        check(tsdfl_map_create(ctx.get(), &coef, grid_occ, data, sigma, flags, &h_));
+    }
+    ~Map() { tsdfl_map_destroy(h_); }
+    Map(const Map&) = delete;
+    Map& operator=(const Map&) = delete;
+    tsdfl_map* get() const { return h_; }
+
+private:
+    tsdfl_map* h_ = nullptr;
+};
+
+struct Pose6 {
+    float x = 0, y = 0, z = 0, roll = 0, pitch = 0, yaw = 0;
+};
+
+// The sensor update of TSDFEvaluator::evaluate (tsdf_evaluator.cpp:78-245) on
+// any particle type with `float first[6]` (x, y, z, roll, pitch, yaw) and
+// `float second` (the weight) -- tsdf_localization::Particle -- and any point
+// type with float members x, y, z.  Writes the normalised weights into the
+// particles and returns the weighted mean pose; an empty scan leaves the
+// particles untouched and returns false.
+class SensorUpdate {
+public:
+    SensorUpdate(Context& ctx, Map& map, float a_hit = 0.9f, float a_range = 0.1f, float a_max = 0.0f,
+                 float max_range = 100.0f, uint32_t flags = TSDFL_SUM_EXACT)
+        : ctx_(ctx), map_(map), flags_(flags)
+    {
+        model_.a_hit = a_hit;
+        model_.a_range = a_range;
+        model_.a_max = a_max;
+        model_.max_range = max_range;
+    }
+
+    template <class ParticleT, class PointT>
+    bool evaluate(std::vector<ParticleT>& particles, const std::vector<PointT>& points, const float tf[16],
+                  Pose6* pose)
+    {
+        if (points.empty()) return false;
+        parts_.resize(7 * particles.size());
+        for (size_t i = 0; i < particles.size(); ++i) {
+            for (int k = 0; k < 6; ++k) parts_[7 * i + k] = particles[i].first[k];
+            parts_[7 * i + 6] = particles[i].second;
+        }
+        pts_.resize(3 * points.size());
+        for (size_t j = 0; j < points.size(); ++j) {
+            pts_[3 * j] = points[j].x;
+            pts_[3 * j + 1] = points[j].y;
+            pts_[3 * j + 2] = points[j].z;
+        }
+        float out[6];
+        check(tsdfl_evaluate(ctx_.get(), map_.get(), &model_, parts_.data(), particles.size(), pts_.data(),
+                             points.size(), tf, flags_, out));
+        for (size_t i = 0; i < particles.size(); ++i) particles[i].second = parts_[7 * i + 6];
+        if (pose) *pose = Pose6{out[0], out[1], out[2], out[3], out[4], out[5]};
+        return true;
+    }
+
+private:
+    Context& ctx_;
+    Map& map_;
+    tsdfl_model model_{};
+    uint32_t flags_;
+    std::vector<float> parts_, pts_;
+};
+
+// SystematicResampler::resample (novel_resampling.h:41-72) for a given draw
+// u0 in [0, 1/M): replaces `particles` by the reference's output sequence
+// (bit-exact, including its particle count, which is not always M).
+template <class ParticleT>
+void resample_systematic(Context& ctx, std::vector<ParticleT>& particles, float u0)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    std::vector<float> w(M);
+    for (size_t i = 0; i < M; ++i) w[i] = particles[i].second;
+    std::vector<uint32_t> idx(2 * M + 16);
+    size_t count = 0;
+    check(tsdfl_resample_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+    if (count > idx.size()) {   // more draws than the first guess held: ask again with room for all
+        idx.resize(count);
+        check(tsdfl_resample_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+    }
+    std::vector<ParticleT> out;
+    out.reserve(count);
+    for (size_t k = 0; k < count; ++k) out.push_back(particles[idx[k]]);
+    particles = std::move(out);
+}
+
+// Cell-centre reduction of a scan as CudaEvaluator's point-cloud overload
+// performs it (cuda_evaluator.cu:77-115): every point maps to the centre of its
+// 0.064 m cell, each centre kept once.  Order does not matter downstream: the
+// exact-mode sums do not depend on it.
+template <class PointT>
+std::vector<PointT> reduce_to_cells(const std::vector<PointT>& points)
+{
+    std::vector<PointT> c;
+    c.reserve(points.size());
+    for (const auto& p : points) {
+        PointT q = p;
+        q.x = static_cast<float>(std::floor(p.x / 0.064) * 0.064 + 0.032);
+        q.y = static_cast<float>(std::floor(p.y / 0.064) * 0.064 + 0.032);
+        q.z = static_cast<float>(std::floor(p.z / 0.064) * 0.064 + 0.032);
+        c.push_back(q);
+    }
+    auto key = [](const PointT& a) {
+        uint32_t k[3];
+        std::memcpy(&k[0], &a.x, 4);
+        std::memcpy(&k[1], &a.y, 4);
+        std::memcpy(&k[2], &a.z, 4);
+        return std::make_tuple(k[0], k[1], k[2]);
+    };
+    std::sort(c.begin(), c.end(), [&](const PointT& a, const PointT& b) { return key(a) < key(b); });
+    c.erase(std::unique(c.begin(), c.end(),
+                        [](const PointT& a, const PointT& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }),
+            c.end());
+    return c;
+}
+
+}  // namespace tsdfl
+
+#ifdef TSDFL_WITH_TSDF_LOCALIZATION
+#include <memory>
+
+namespace tsdf_localization {
+
+// Drop-in for CudaEvaluator: same constructor arguments (per_point is accepted;
+// both reference modes give the same weights here) and the same two evaluate
+// overloads.  The map's slots are copied to the device once, here.
+class GpuTsdfEvaluator : public Evaluator {
+public:
+    GpuTsdfEvaluator(CudaSubVoxelMap<FLOAT_T, FLOAT_T>& map, bool per_point = false, FLOAT_T a_hit = 0.9,
+                     FLOAT_T a_range = 0.1, FLOAT_T a_max = 0.0, FLOAT_T max_range = 100.0, int device = 0,
+                     float sigma = 0.1f)
+        : ctx_(new tsdfl::Context(device)),
+          map_(new tsdfl::Map(*ctx_, *reinterpret_cast<const tsdfl_map_coef*>(&map.coef()), map.rawGridOcc(),
+                              map.rawData(), sigma)),
+          update_(new tsdfl::SensorUpdate(*ctx_, *map_, a_hit, a_range, a_max, max_range))
+    {
+        static_assert(sizeof(tsdfl_map_coef) == sizeof(typename CudaSubVoxelMap<FLOAT_T, FLOAT_T>::MapCoef),
+                      "MapCoef layout");
+        (void)per_point;
+    }
+
+    geometry_msgs::PoseWithCovariance evaluate(std::vector<Particle>& particles,
+                                               const sensor_msgs::PointCloud2& real_cloud,
+                                               FLOAT_T tf_matrix[16]) override
+    {
+        sensor_msgs::PointCloud2ConstIterator<float> iter_x(real_cloud, "x");
+        std::vector<CudaPoint> points;
+        for (; iter_x != iter_x.end(); ++iter_x) points.push_back(CudaPoint(iter_x[0], iter_x[1], iter_x[2]));
+        return evaluate(particles, tsdfl::reduce_to_cells(points), tf_matrix);
+    }
+
+    geometry_msgs::PoseWithCovariance evaluate(std::vector<Particle>& particles, const std::vector<CudaPoint>& points,
+                                               FLOAT_T tf_matrix[16]) override
+    {
+        geometry_msgs::PoseWithCovariance out;
+        tsdfl::Pose6 p;
+        if (!update_->evaluate(particles, points, tf_matrix, &p)) return out;
+        out.pose.position.x = p.x;
+        out.pose.position.y = p.y;
+        out.pose.position.z = p.z;
+        tf2::Quaternion q;   // as tsdf_evaluator.cpp:226-228 converts the mean pose
+        q.setRPY(p.roll, p.pitch, p.yaw);
+        tf2::convert(q, out.pose.orientation);
+        return out;
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+    std::unique_ptr<tsdfl::Map> map_;
+    std::unique_ptr<tsdfl::SensorUpdate> update_;
+};
+
+// Drop-in for SystematicResampler: draws U ~ U[0, 1/M) from the inherited
+// generator exactly as the reference does, then resamples on the device.
+class GpuSystematicResampler : public Resampler {
+public:
+    explicit GpuSystematicResampler(int device = 0) : ctx_(new tsdfl::Context(device)) {}
+
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        auto inverse_M = 1.0 / particle_cloud.size();
+        std::uniform_real_distribution<FLOAT_T> uniform_distribution(0.0, inverse_M);
+        const float u0 = uniform_distribution(*m_generator_ptr);
+        tsdfl::resample_systematic(*ctx_, particle_cloud.particles(), u0);
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+};
+
+}  // namespace tsdf_localization
+#endif
+
+#endif

@@ -1,0 +1,118 @@
+"""Generates the golden fixtures in this directory from the reference's own
+sources compiled here (oracle/_ref/libref.so, built by __graft_entry__.build()
+when the reference tree is present).
+
+Each case stores its inputs in full (map tuples, bounds, resolution, particles,
+points, sensor transform, query points, weight vectors, generator seeds) and
+what the reference computes from them: the map's coefficients and brick table
+and a digest of its slots (CudaSubVoxelMap ctor + setData), getEntry at the
+query points, TSDFEvaluator::evaluate's un-normalised and normalised weights,
+laser poses and mean pose (serial, in point order), and SystematicResampler's
+output indices for seeded draws.
+
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle_py as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def _pose_tf(rng):
+    a, b, c = rng.uniform(-0.3, 0.3, 3)
+    ca, sa, cb, sb, cc, sc = np.cos(a), np.sin(a), np.cos(b), np.sin(b), np.cos(c), np.sin(c)
+    R = np.array([[cc * cb, cc * sb * sa - sc * ca, cc * sb * ca + sc * sa],
+                  [sc * cb, sc * sb * sa + cc * ca, sc * sb * ca - cc * sa],
+                  [-sb, cb * sa, cb * ca]])
+    T = np.eye(4)
+    T[:3, :3] = R
+    T[:3, 3] = rng.uniform(-0.2, 0.2, 3)
+    return T.astype(np.float32).reshape(16)
+
+
+def map_case(name, res, mn, mx, n_tuples, seed):
+    rng = np.random.default_rng(seed)
+    mn = np.asarray(mn, np.float32)
+    mx = np.asarray(mx, np.float32)
+    xyz = rng.uniform(mn, mx, size=(n_tuples, 3)).astype(np.float32)
+    xyz[: n_tuples // 10] = xyz[n_tuples // 10: 2 * (n_tuples // 10)] + rng.normal(0, res / 4, (n_tuples // 10, 3))
+    vals = rng.uniform(0.001, 63.0, n_tuples).astype(np.float32)
+    tuples = np.concatenate([xyz, vals[:, None]], 1).astype(np.float32)
+    rm = O.RefMap(mn, mx, res, 0.0, tuples)
+    data = rm.data()
+    centre = (mn + mx) / 2
+    span = mx - mn
+    q = np.concatenate([
+        rng.uniform(mn - 1.5, mx + 1.5, size=(300, 3)),
+        xyz[rng.choice(n_tuples, 200, replace=False)],
+        mn + rng.uniform(-1.0, 0.3, size=(100, 3)),
+        np.array([[np.nan, 0, 0], [1e20, 0, 0], [-1e20, 0, 0], [0, 0, np.inf]]) + mn,
+    ]).astype(np.float32)
+    entries = np.array([rm.get_entry(*p) for p in q], np.float32)
+    P = 48
+    parts = np.zeros((P, 7), np.float32)
+    parts[:, :3] = centre + rng.normal(0, 0.3, (P, 3))
+    parts[:, 3:6] = rng.normal(0, 0.08, (P, 3))
+    parts[:, 5] += rng.uniform(-3.1, 3.1)
+    parts[:, 6] = 1.0 / P
+    dirs = rng.normal(size=(300, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    pts = (dirs * rng.uniform(0.3, 0.6 * span.min(), (300, 1))).astype(np.float32)
+    pts[::37] *= 500.0   # beyond max_range and outside the map
+    tf = _pose_tf(rng)
+    p_ref = parts.copy()
+    r = rm.evaluate(p_ref, pts, tf, serial=True)
+    assert r["rc"] == 0
+    return {
+        f"{name}/tuples": tuples, f"{name}/mn": mn, f"{name}/mx": mx, f"{name}/res": np.float32(res),
+        f"{name}/coef": np.frombuffer(bytes(rm.coef), np.uint8), f"{name}/grid_occ": rm.grid_occ(),
+        f"{name}/data_sha256": np.frombuffer(hashlib.sha256(data.tobytes()).digest(), np.uint8),
+        f"{name}/data_sample_idx": (idx := rng.choice(max(data.size, 1), 500)).astype(np.int64),
+        f"{name}/data_sample": data[idx] if data.size else np.zeros(500, np.float32),
+        f"{name}/query": q, f"{name}/entries": entries,
+        f"{name}/particles": parts, f"{name}/points": pts, f"{name}/tf": tf,
+        f"{name}/raw": r["raw"], f"{name}/weights": p_ref[:, 6].copy(), f"{name}/laser_pose": r["laser_pose"],
+        f"{name}/pose": r["pose"],
+    }
+
+
+def resample_case(seed):
+    rng = np.random.default_rng(seed)
+    out = {}
+    sets = {
+        "uniform": np.full(1000, 1.0 / 1000, np.float32),
+        "random": (lambda w: (w / w.sum()).astype(np.float32))(rng.random(2500) ** 3),
+        "sparse": (lambda w: (w / w.sum()).astype(np.float32))(np.where(rng.random(3000) < 0.05, rng.random(3000), 0.0)),
+        "tiny": (lambda w: (w / w.sum()).astype(np.float32))(np.exp(-rng.uniform(0, 40, 4000))),
+        "unnormalised": rng.uniform(0.0, 2.0 / 700, 700).astype(np.float32),
+    }
+    for k, w in sets.items():
+        s = int(rng.integers(1, 2 ** 31))
+        out[f"resample/{k}/weights"] = w
+        out[f"resample/{k}/seed"] = np.int64(s)
+        out[f"resample/{k}/u0"] = np.float32(O.ref_draw_u0(s, w.shape[0]))
+        out[f"resample/{k}/indices"] = O.ref_resample_systematic(w, s)
+    return out
+
+
+def main():
+    if not O.reference_available():
+        raise SystemExit("oracle/_ref/libref.so is not built: the reference tree is needed")
+    fx = {}
+    fx.update(map_case("map_0064", 0.064, (-1.3, -0.7, -0.45), (5.1, 4.3, 2.6), 6000, 11))
+    fx.update(map_case("map_005", 0.05, (0.0, 0.0, 0.0), (4.2, 3.6, 2.2), 6000, 12))
+    fx.update(resample_case(13))
+    np.savez_compressed(OUT / "reference_cases.npz", **fx)
+    print("wrote", OUT / "reference_cases.npz", (OUT / "reference_cases.npz").stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

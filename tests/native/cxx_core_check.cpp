@@ -1,0 +1,91 @@
+// Drives the C++ host layer (include/tsdfl_evaluator.hpp) on its own particle
+// and point types: reads a map (MapCoef bytes, brick table, float slots),
+// particles (P x 7), points (N x 3), tf[16] and a draw u0 from files in the
+// directory given as argv[1]; writes the normalised weights, the mean pose and
+// the resampled particles back there.
+#include "tsdfl_evaluator.hpp"
+
+#include <cstdio>
+#include <fstream>
+#include <iterator>
+#include <string>
+#include <vector>
+
+struct MyParticle {
+    float first[6];
+    float second;
+};
+struct MyPoint {
+    float x, y, z;
+};
+
+template <class T>
+static std::vector<T> load(const std::string& path)
+{
+    std::ifstream f(path, std::ios::binary);
+    std::vector<char> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<T> v(b.size() / sizeof(T));
+    std::memcpy(v.data(), b.data(), v.size() * sizeof(T));
+    return v;
+}
+
+template <class T>
+static void save(const std::string& path, const T* p, size_t n)
+{
+    std::ofstream f(path, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(p), (std::streamsize)(n * sizeof(*p)));
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 2) return 2;
+    const std::string d = argv[1];
+    auto coef_b = load<char>(d + "/coef.bin");
+    tsdfl_map_coef coef;
+    if (coef_b.size() != sizeof(coef)) return 3;
+    std::memcpy(&coef, coef_b.data(), sizeof(coef));
+    auto grid_occ = load<int32_t>(d + "/grid_occ.bin");
+    auto data = load<float>(d + "/data.bin");
+    auto pf = load<float>(d + "/particles.bin");
+    auto qf = load<float>(d + "/points.bin");
+    auto tf = load<float>(d + "/tf.bin");
+    auto u0 = load<float>(d + "/u0.bin");
+    std::vector<MyParticle> parts(pf.size() / 7);
+    for (size_t i = 0; i < parts.size(); ++i) {
+        for (int k = 0; k < 6; ++k) parts[i].first[k] = pf[7 * i + k];
+        parts[i].second = pf[7 * i + 6];
+    }
+    std::vector<MyPoint> pts(qf.size() / 3);
+    for (size_t j = 0; j < pts.size(); ++j) pts[j] = MyPoint{qf[3 * j], qf[3 * j + 1], qf[3 * j + 2]};
+    try {
+        tsdfl::Context ctx(0);
+        tsdfl::Map map(ctx, coef, grid_occ.data(), data.data(), 0.1f);
+        tsdfl::SensorUpdate upd(ctx, map);
+        tsdfl::Pose6 pose;
+        upd.evaluate(parts, pts, tf.data(), &pose);
+        std::vector<float> w(parts.size());
+        for (size_t i = 0; i < parts.size(); ++i) w[i] = parts[i].second;
+        save(d + "/weights_out.bin", w.data(), w.size());
+        save(d + "/pose_out.bin", &pose.x, 6);
+        tsdfl::resample_systematic(ctx, parts, u0.at(0));
+        std::vector<float> out(7 * parts.size());
+        for (size_t i = 0; i < parts.size(); ++i) {
+            for (int k = 0; k < 6; ++k) out[7 * i + k] = parts[i].first[k];
+            out[7 * i + 6] = parts[i].second;
+        }
+        save(d + "/resampled_out.bin", out.data(), out.size());
+        bool threw = false;
+        try {   // an empty cloud: the reference's "No particle is valid!"
+            std::vector<MyParticle> none;
+            upd.evaluate(none, pts, tf.data(), &pose);
+        } catch (const std::runtime_error& e) {
+            threw = std::string(e.what()).find("No particle is valid!") != std::string::npos;
+        }
+        std::printf("cxx core ok P=%zu N=%zu resampled=%zu empty_cloud_throws=%d\n", w.size(), pts.size(), parts.size(),
+                    threw ? 1 : 0);
+        return threw ? 0 : 4;
+    } catch (const std::runtime_error& e) {
+        std::printf("runtime_error: %s\n", e.what());
+        return 1;
+    }
+}

@@ -1,0 +1,53 @@
+// Builds the drop-in plug-ins of include/tsdfl_evaluator.hpp against the
+// reference's own headers (tsdf_localization's Evaluator, Resampler, Particle,
+// CudaSubVoxelMap, compiled with the test shims for ROS) and links them with
+// libtsdfl.  Run without a GPU, constructing them must raise std::runtime_error
+// with libtsdfl's message; with a GPU, one update and one resample run.
+#include <tsdf_localization/cuda/cuda_evaluator.h>
+#include <tsdf_localization/resampling/novel_resampling.h>
+
+#define TSDFL_WITH_TSDF_LOCALIZATION
+#include "tsdfl_evaluator.hpp"
+
+#include <cstdio>
+#include <tuple>
+#include <vector>
+
+namespace tsdf_localization {
+// The two ParticleCloud members the resampler touches (particle_cloud.cpp is
+// not part of this build).
+ParticleCloud::ParticleCloud() {}
+Particle& ParticleCloud::operator[](unsigned int index) { return m_particles.at(index); }
+std::size_t ParticleCloud::size() const { return m_particles.size(); }
+}  // namespace tsdf_localization
+
+int main()
+{
+    using namespace tsdf_localization;
+    CudaSubVoxelMap<FLOAT_T, FLOAT_T> map(0.0f, 0.0f, 0.0f, 4.0f, 4.0f, 2.0f, 0.064f, 0.0f);
+    std::vector<std::tuple<FLOAT_T, FLOAT_T, FLOAT_T, FLOAT_T>> slots{{1.0f, 1.0f, 1.0f, 2.0f}};
+    map.setData(slots);
+    int status = 0;
+    try {
+        GpuTsdfEvaluator ev(map, false, 0.9f, 0.1f, 0.0f, 100.0f, 0, 0.1f);
+        std::vector<Particle> parts(3);
+        for (int i = 0; i < 3; ++i) {
+            for (int k = 0; k < 6; ++k) parts[i].first[k] = 0.0f;
+            parts[i].second = 1.0f / 3.0f;
+        }
+        std::vector<CudaPoint> pts{CudaPoint(1.0f, 1.0f, 1.0f), CudaPoint(2.0f, 1.0f, 1.0f)};
+        FLOAT_T tf[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        geometry_msgs::PoseWithCovariance pose = ev.evaluate(parts, pts, tf);
+        std::printf("evaluated w0=%.9g x=%.9g\n", parts[0].second, pose.pose.position.x);
+        GpuSystematicResampler rs(0);
+        ParticleCloud cloud;
+        cloud.particles() = parts;
+        rs.resample(cloud);
+        std::printf("resampled %zu\n", cloud.size());
+    } catch (const std::runtime_error& e) {
+        std::printf("runtime_error: %s\n", e.what());
+        status = 0;
+    }
+    std::printf("dropin compiled\n");
+    return status;
+}

@@ -1,0 +1,63 @@
+"""The oracle (CPU restatement) against the reference's own outputs recorded in
+tests/golden/reference_cases.npz (made by tests/golden/make_golden.py from the
+reference sources compiled here): map construction, getEntry, the serial
+sensor update, laser poses and systematic resampling, bit for bit."""
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle_py as O
+
+GOLD = np.load(Path(__file__).resolve().parent / "golden" / "reference_cases.npz")
+MAPS = ["map_0064", "map_005"]
+SETS = sorted({k.split("/")[1] for k in GOLD.files if k.startswith("resample/")})
+
+
+def oracle_map(name):
+    return O.OracleMap.from_tuples(GOLD[f"{name}/mn"], GOLD[f"{name}/mx"], float(GOLD[f"{name}/res"]), 0.0,
+                                   GOLD[f"{name}/tuples"])
+
+
+@pytest.mark.parametrize("name", MAPS)
+def test_map_build_matches_reference(name):
+    om = oracle_map(name)
+    assert bytes(om.coef) == GOLD[f"{name}/coef"].tobytes()
+    assert np.array_equal(om.grid_occ, GOLD[f"{name}/grid_occ"])
+    assert hashlib.sha256(om.data.tobytes()).digest() == GOLD[f"{name}/data_sha256"].tobytes()
+    assert np.array_equal(om.data[GOLD[f"{name}/data_sample_idx"]], GOLD[f"{name}/data_sample"])
+
+
+@pytest.mark.parametrize("name", MAPS)
+def test_get_entry_matches_reference(name):
+    om = oracle_map(name)
+    got = np.array([om.get_entry(*p) for p in GOLD[f"{name}/query"]], np.float32)
+    assert np.array_equal(got, GOLD[f"{name}/entries"], equal_nan=True)
+
+
+@pytest.mark.parametrize("name", MAPS)
+def test_sensor_update_matches_reference(name):
+    om = oracle_map(name)
+    parts = GOLD[f"{name}/particles"].copy()
+    r = O.evaluate(om, parts, GOLD[f"{name}/points"], GOLD[f"{name}/tf"])
+    assert r["rc"] == 0
+    assert np.array_equal(r["raw"], GOLD[f"{name}/raw"])
+    assert np.array_equal(parts[:, 6], GOLD[f"{name}/weights"])
+    lp = np.stack([O.particle_pose(p, GOLD[f"{name}/tf"]) for p in GOLD[f"{name}/particles"]])
+    assert np.array_equal(lp, GOLD[f"{name}/laser_pose"])
+    assert np.allclose(r["pose"], GOLD[f"{name}/pose"], rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("wset", SETS)
+def test_resample_matches_reference(wset):
+    w = GOLD[f"resample/{wset}/weights"]
+    got = O.resample_systematic(w, float(GOLD[f"resample/{wset}/u0"]))
+    assert np.array_equal(got, GOLD[f"resample/{wset}/indices"])
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference not compiled on this machine")
+def test_fixture_draws_match_reference_generator():
+    for wset in SETS:
+        assert np.float32(O.ref_draw_u0(int(GOLD[f"resample/{wset}/seed"]), GOLD[f"resample/{wset}/weights"].shape[0])) \
+            == GOLD[f"resample/{wset}/u0"]
