@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--workload", default="building", choices=["building", "room"])
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
-    ap.add_argument("--layout", default="brick", choices=["dense", "brick"])
+    ap.add_argument("--layout", default="compact", choices=["compact", "brick"])
     ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -60,10 +60,11 @@ def make_workload(args):
 
 
 def roofline_bytes(P: int, N: int, layout: str) -> float:
-    """Algorithmic bytes of one scoring launch: per particle*point the slot
-    reads (brick reference 4 B + 2 B code, or 2 B in the dense layout), per
-    particle 56 B (pose in, weight, index, pose out), per point 12 B."""
-    bpp = 2 if layout == "dense" else 6
+    """Algorithmic bytes of one scoring launch: per particle*point the map
+    reads (brick layout: 4 B brick-table entry + 2 B slot code; compact layout:
+    the 2 B slot code, its brick rank coming from shared memory), per particle
+    56 B (pose in, weight, index, pose out), per point 12 B."""
+    bpp = 2 if layout == "compact" else 6
     return float(bpp) * P * N + 56.0 * P + 12.0 * N
 
 
@@ -243,7 +244,7 @@ def main():
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
-    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=(args.layout == "dense"))
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=(args.layout == "compact"))
     info = dmap.info()
     model = N.Model(0.9, 0.1, 0.0, 100.0)
     tf = np.ascontiguousarray(wl.tf, np.float32)

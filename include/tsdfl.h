@@ -69,7 +69,7 @@ void* tsdfl_ctx_stream(tsdfl_ctx* ctx);
  * last sync (e.g. TSDFL_ERR_DEGENERATE from tsdfl_evaluate_device). */
 int tsdfl_ctx_sync(tsdfl_ctx* ctx);
 /* Pre-sizes the workspace for P particles and N points so that later calls
- * allocate nothing (needed before capturing calls into a CUDA graph). */
+ * with at most as many allocate nothing. */
 int tsdfl_ctx_reserve(tsdfl_ctx* ctx, size_t P, size_t N);
 
 /* Device timing of the scoring kernels of the next evaluations (CUDA events
@@ -85,7 +85,12 @@ uint64_t tsdfl_launch_count(void);
  * cuda_evaluator.cu:21-59).  When every slot equals one of the likelihood
  * values of createTSDFMap for `sigma` (map_util.h:68-71,124-127), slots are
  * stored as 16-bit codes, losslessly; otherwise as float.  flags: TSDFL_MAP_*. */
-#define TSDFL_MAP_DENSE 1u        /* also build the one-gather dense brick layout */
+/* TSDFL_MAP_DENSE: also build the compact layout -- the allocated bricks in
+ * brick-index order, a skirt of slots below layer z = 0, brick ranks from a
+ * bitmap held in shared memory -- so the tiled kernel makes one map gather per
+ * lookup instead of two.  Skipped (brick layout only) when a sub-voxel index
+ * can reach sub_dim or the slots exceed 2^31. */
+#define TSDFL_MAP_DENSE 1u
 #define TSDFL_MAP_FORCE_F32 2u    /* keep float slots */
 int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
                      float sigma, uint32_t flags, tsdfl_map** out);

@@ -83,9 +83,10 @@ struct tsdfl_map {
     int32_t* grid_occ = nullptr;
     uint16_t* codes = nullptr;
     float* data = nullptr;
-    uint16_t* dense = nullptr;
-    uint32_t* occ = nullptr;      // brick occupancy bits (with the dense layout)
+    uint16_t* dense = nullptr;    // compact layout (TSDFL_MAP_DENSE)
+    uint32_t* occ = nullptr;      // its bitmap and prefix counts
     uint32_t occ_words = 0;
+    uint32_t n0 = 0;
     float* values = nullptr;      // kNumCodes likelihood values (device)
     float max_value = 0;
     uint64_t bricks = 0;
@@ -257,25 +258,91 @@ void fill_view(tsdfl_map* m)
     v.sl_bias_xy = K * (1u + v.sub_dim);
     v.occ = m->occ;
     v.occ_words = m->occ_words;
+    v.n0 = m->n0;
+}
+
+// Largest sub-voxel index trunc(fl(s / res)) over floats s in [0, 1).
+uint64_t max_sub_index(float res)
+{
+    float below_one;
+    const uint32_t b = 0x3F7FFFFFu;
+    std::memcpy(&below_one, &b, 4);
+    return f2u_x86_host(below_one / res);
+}
+
+// Compact layout (MapView::dense): needs every fast-path slot inside its brick
+// (sub-voxel indices below sub_dim) and 32-bit slot offsets.
+int build_compact(tsdfl_ctx* ctx, tsdfl_map* m)
+{
+    const tsdfl_map_coef& c = m->coef;
+    const uint64_t S3 = c.sub_dim * c.sub_dim_2, gos = c.grid_occ_size;
+    if (max_sub_index(c.resolution) >= c.sub_dim) return TSDFL_OK;   // keep the brick layout only
+    std::vector<int32_t> go(gos ? gos : 1);
+    if (gos) CUDA_TRY(cudaMemcpy(go.data(), m->grid_occ, sizeof(int32_t) * gos, cudaMemcpyDeviceToHost));
+    const uint32_t words = (uint32_t)(((gos + 31) / 32 + 3) / 4 * 4);
+    std::vector<uint32_t> occ(2 * (size_t)words, 0u);
+    uint64_t nb = 0, n0 = 0;
+    for (uint64_t up = 0; up < gos; ++up) {
+        if (go[up] < 0) continue;
+        occ[up / 32] |= 1u << (up % 32);
+        ++nb;
+        if (up < c.up_dim_2) ++n0;
+    }
+    uint32_t run = 0;
+    for (uint32_t w = 0; w < words; ++w) {
+        occ[words + w] = run;
+        run += (uint32_t)__builtin_popcount(occ[w]);
+    }
+    const uint64_t slots = (nb + n0) * S3;
+    if (slots >= (1ull << 31)) return TSDFL_OK;
+    std::vector<int64_t> src, dst;
+    std::vector<uint8_t> skirt;
+    src.reserve(nb);
+    dst.reserve(nb);
+    skirt.reserve(nb);
+    uint64_t r = 0;
+    for (uint64_t up = 0; up < gos; ++up) {
+        if (go[up] < 0) continue;
+        const bool layer0 = up < c.up_dim_2;
+        src.push_back(go[up]);
+        dst.push_back((int64_t)((layer0 ? 2 * r + 1 : r + n0) * S3));
+        skirt.push_back(layer0 ? 1 : 0);
+        ++r;
+    }
+    CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (slots ? slots : 1)));
+    CUDA_TRY(cudaMalloc(&m->occ, sizeof(uint32_t) * occ.size()));
+    m->bytes += sizeof(uint16_t) * slots + sizeof(uint32_t) * occ.size();
+    CUDA_TRY(cudaMemcpy(m->occ, occ.data(), sizeof(uint32_t) * occ.size(), cudaMemcpyHostToDevice));
+    m->occ_words = words;
+    m->n0 = (uint32_t)n0;
+    if (nb) {
+        void* tmp = nullptr;
+        const size_t nbytes = nb * (2 * sizeof(int64_t) + 1);
+        CUDA_TRY(cudaMalloc(&tmp, nbytes));
+        int64_t* d_src = static_cast<int64_t*>(tmp);
+        int64_t* d_dst = d_src + nb;
+        uint8_t* d_sk = reinterpret_cast<uint8_t*>(d_dst + nb);
+        cudaError_t e = cudaMemcpy(d_src, src.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_dst, dst.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_sk, skirt.data(), nb, cudaMemcpyHostToDevice);
+        int rc = e == cudaSuccess ? launch_compact_fill(m->codes, d_src, d_dst, d_sk, (uint32_t)nb, (uint32_t)S3,
+                                                        m->dense, ctx->stream)
+                                  : TSDFL_ERR_DEVICE;
+        if (rc == TSDFL_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = TSDFL_ERR_DEVICE;
+        cudaFree(tmp);
+        if (rc) {
+            set_error("map: building the compact layout failed");
+            return rc;
+        }
+    }
+    return TSDFL_OK;
 }
 
 int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
 {
     if ((flags & TSDFL_MAP_DENSE) && m->codes) {
-        uint64_t sub3 = m->coef.sub_dim * m->coef.sub_dim_2;
-        uint64_t n = m->coef.grid_occ_size * sub3;
-        if (n < (1ull << 32)) {
-            CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (n ? n : 1)));
-            m->bytes += sizeof(uint16_t) * n;
-            int rc = launch_dense_from_codes(m->grid_occ, m->codes, m->coef.grid_occ_size, (uint32_t)sub3, m->dense,
-                                             ctx->stream);
-            if (rc) return rc;
-            m->occ_words = (uint32_t)(((m->coef.grid_occ_size + 31) / 32 + 3) / 4 * 4);
-            CUDA_TRY(cudaMalloc(&m->occ, sizeof(uint32_t) * m->occ_words));
-            m->bytes += sizeof(uint32_t) * m->occ_words;
-            rc = launch_occupancy_bits(m->grid_occ, m->coef.grid_occ_size, m->occ, m->occ_words, ctx->stream);
-            if (rc) return rc;
-        }
+        int rc = build_compact(ctx, m);
+        if (rc) return rc;
     }
     fill_view(m);
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -348,7 +415,7 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
     if (tiled) {
         int tp = tiled_pass_points(map->view, dense);
-        if (tp < 1024 && dense) {   // the bitmap crowds out the scan: use the brick table instead
+        if (tp < 1024 && dense) {   // the rank tables crowd out the scan: use the brick table instead
             dense = false;
             tp = tiled_pass_points(map->view, false);
         }

@@ -106,27 +106,11 @@ __device__ __forceinline__ double warp_sum_d(double v)
     return v;
 }
 
-// Code of the slot a point falls in through the dense layout: one gather
-// instead of brick table + slot.  Falls back to the brick path where the dense
-// address is not the reference's slot (offsets outside the fast range, or a
-// sub-voxel index that runs past the end of its brick).
+// Code of the slot a point falls in (kCodeMiss when getIndex misses): the
+// generic kernel's view of a map with the compact layout, read through the
+// brick table.
 __device__ __forceinline__ uint32_t dense_code(const MapView& m, float x, float y, float z)
 {
-    float ox = __fsub_rn(x, m.min_x), oy = __fsub_rn(y, m.min_y), oz = __fsub_rn(z, m.min_z);
-    bool fast = ox >= 0.0f && oy >= 0.0f && oz >= 0.0f && ox < kFastOffsetLimit && oy < kFastOffsetLimit &&
-                oz < kFastOffsetLimit;
-    if (fast) {
-        int32_t mx = __float2int_rz(ox), my = __float2int_rz(oy), mz = __float2int_rz(oz);
-        if (mx > m.mmax_x || my > m.mmax_y || mz > m.mmax_z) return kCodeMiss;
-        uint32_t up = (uint32_t)mx + (uint32_t)my * m.up_dim_x + (uint32_t)mz * m.up_dim_2;
-        if (up >= m.grid_occ_size) return kCodeMiss;
-        float sx = __fsub_rn(ox, (float)mx), sy = __fsub_rn(oy, (float)my), sz = __fsub_rn(oz, (float)mz);
-        uint32_t qx = (uint32_t)__float2int_rz(__fdiv_rn(sx, m.res));
-        uint32_t qy = (uint32_t)__float2int_rz(__fdiv_rn(sy, m.res));
-        uint32_t qz = (uint32_t)__float2int_rz(__fdiv_rn(sz, m.res));
-        uint32_t s = qx + qy * m.sub_dim + qz * m.sub_dim_2;
-        if (s < m.sub_dim_3) return __ldg(m.dense + (size_t)up * m.sub_dim_3 + s);
-    }
     uint32_t idx = slot_index(m, x, y, z);
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
@@ -428,12 +412,16 @@ __device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* 
     const uint32_t qz = ((in.bcz - kMagic) ^ sgn) - sgn;   // -q(|oz|) below the map
     const uint32_t sl = in.bcx + in.bcy * m.sub_dim - m.sl_bias_xy + qz * m.sub_dim_2;
     const bool inside = fast && up < m.grid_occ_size;
-    if (DENSE) {
-        const uint32_t word = occ[inside ? (up >> 5) : 0u];
-        const bool alloc = (__funnelshift_r(word, word, up) & 1u) != 0u;   // bit up mod 32
-        const bool ok = inside && alloc && sl < m.sub_dim_3;
-        const uint32_t code = __ldg(m.dense + (ok ? (size_t)up * m.sub_dim_3 + sl : (size_t)0));
-        return ok ? code : (inside && !alloc) || (fast && !inside) ? (uint32_t)kCodeMiss : kCodeSlow;
+    if (DENSE) {   // the brick's rank from the shared-memory bitmap and prefix counts
+        const uint32_t w = inside ? (up >> 5) : 0u;
+        const uint32_t word = occ[w], below = occ[m.occ_words + w];
+        const uint32_t bit = 1u << (up & 31u);
+        const bool alloc = (word & bit) != 0u;
+        const uint32_t r = below + __popc(word & (bit - 1u));
+        const uint32_t k = r + (up < m.up_dim_2 ? r + 1u : m.n0);   // bricks (and skirts) before this one
+        const bool ok = inside && alloc;
+        const uint32_t code = __ldg(m.dense + (ok ? k * m.sub_dim_3 + sl : 0u));
+        return ok ? code : fast ? (uint32_t)kCodeMiss : kCodeSlow;
     } else {
         // slot indices below 0 wrap past 2^31 > data_size: a miss, as in getIndex's 64-bit sum
         const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
@@ -518,7 +506,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const int n = p.n1 - p.n0;
     const int npairs = ((n + 63) >> 6) * 32;
     if (threadIdx.x == 0) s_map = m;
-    const uint32_t occ_words = DENSE ? m.occ_words : 0u;
+    const uint32_t occ_words = DENSE ? 2u * m.occ_words : 0u;   // bitmap + prefix counts
     uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
     float4* sxy = reinterpret_cast<float4*>(occ + occ_words);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
@@ -1101,26 +1089,20 @@ __global__ void codes_from_floats_kernel(const float* data, size_t n, const floa
     }
 }
 
-__global__ void occupancy_bits_kernel(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words)
+// Compact layout: one CTA per allocated brick copies its sub3 slot codes (and,
+// for bricks of layer z = 0, the sub3 slots before it in the reference's data
+// order into the skirt in front of it).
+__global__ void compact_fill_kernel(const uint16_t* codes, const int64_t* src, const int64_t* dst,
+                                    const uint8_t* skirt, uint32_t n, uint32_t sub3, uint16_t* dense)
 {
-    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
-        uint32_t bits = 0;
-        for (uint32_t b = 0; b < 32; ++b) {
-            size_t up = (size_t)w * 32 + b;
-            if (up < grid_occ_size && grid_occ[up] >= 0) bits |= 1u << b;
-        }
-        occ[w] = bits;
-    }
-}
-
-__global__ void dense_from_codes_kernel(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size,
-                                        uint32_t sub3, uint16_t* dense)
-{
-    size_t total = grid_occ_size * sub3;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        size_t up = i / sub3, s = i - up * sub3;
-        int32_t base = grid_occ[up];
-        dense[i] = base < 0 ? (uint16_t)kCodeMiss : codes[(size_t)base + s];
+    for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
+        const int64_t s0 = src[b], d0 = dst[b];
+        for (uint32_t i = threadIdx.x; i < sub3; i += blockDim.x) dense[d0 + i] = codes[s0 + i];
+        if (skirt[b])
+            for (uint32_t i = threadIdx.x; i < sub3; i += blockDim.x) {
+                const int64_t from = s0 - (int64_t)sub3 + i;
+                dense[d0 - (int64_t)sub3 + i] = from >= 0 ? codes[from] : (uint16_t)kCodeMiss;
+            }
     }
 }
 
@@ -1161,7 +1143,7 @@ size_t eval_smem_bytes(bool serial, int n)
 
 size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
 {
-    return (size_t)kLutBytes + (dense ? (size_t)m.occ_words * 4 : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
+    return (size_t)kLutBytes + (dense ? (size_t)m.occ_words * 8 : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
            sizeof(float4) * kRing * kTiledWarps;
 }
 
@@ -1296,17 +1278,10 @@ int launch_codes_from_floats(const float* data, size_t n, const float* code_valu
     return check(cudaGetLastError());
 }
 
-int launch_occupancy_bits(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words,
-                          cudaStream_t s)
+int launch_compact_fill(const uint16_t* codes, const int64_t* src, const int64_t* dst, const uint8_t* skirt,
+                        uint32_t n, uint32_t sub3, uint16_t* dense, cudaStream_t s)
 {
-    if (words) occupancy_bits_kernel<<<(words + 255) / 256, 256, 0, s>>>(grid_occ, grid_occ_size, occ, words);
-    return check(cudaGetLastError());
-}
-
-int launch_dense_from_codes(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size, uint32_t sub3,
-                            uint16_t* dense, cudaStream_t s)
-{
-    if (grid_occ_size) dense_from_codes_kernel<<<2048, 256, 0, s>>>(grid_occ, codes, grid_occ_size, sub3, dense);
+    if (n) compact_fill_kernel<<<n < 65535u ? n : 65535u, 256, 0, s>>>(codes, src, dst, skirt, n, sub3, dense);
     return check(cudaGetLastError());
 }
 

@@ -46,7 +46,7 @@ struct MapView {
     const int32_t* grid_occ;
     const uint16_t* codes;    // 16-bit slot codes (storage 0)
     const float* data;        // float slots (storage 1)
-    const uint16_t* dense;    // dense brick layout (may be null)
+    const uint16_t* dense;    // compact rank-ordered layout (may be null; see occ)
     int32_t storage;          // 0 = codes, 1 = float
     // Division-free sub-voxel index q = trunc(fl(s / res)) for s in [0, 1),
     // verified on the host (every threshold of q; monotone in s):
@@ -66,8 +66,17 @@ struct MapView {
     // lim_zn: float bits bounding |oz| there (1.0, or 0 when lim_z is 0);
     // sl_bias_xy = bits(2^23) * (1 + sub_dim).
     uint32_t lim_zn, sl_bias_xy;
-    const uint32_t* occ;           // one bit per brick: allocated (dense layout only)
-    uint32_t occ_words;            // words in occ (a multiple of 4)
+    // Compact layout (TSDFL_MAP_DENSE): the allocated bricks' slots in brick
+    // index order, bricks of layer z = 0 each preceded by a "skirt" of sub_dim^3
+    // slots holding what getIndex reads below them (the sub_dim^3 slots before
+    // the brick in the reference's data order, kCodeMiss below slot 0).  occ is
+    // [occ_words bitmap words | occ_words prefix counts]: bit up of the bitmap
+    // is set when brick up is allocated, prefix[w] counts the set bits of words
+    // 0..w-1.  A brick of rank r starts at (2r + 1) S^3 in layer 0 (up < up_dim_2)
+    // and at (r + n0) S^3 above, n0 = allocated bricks in layer 0.
+    const uint32_t* occ;
+    uint32_t occ_words;            // a multiple of 4
+    uint32_t n0;
 };
 
 #ifdef __CUDACC__
@@ -171,9 +180,10 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
                          cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
-int launch_occupancy_bits(const int32_t* grid_occ, size_t grid_occ_size, uint32_t* occ, uint32_t words,
-                          cudaStream_t s);
-int launch_dense_from_codes(const int32_t* grid_occ, const uint16_t* codes, size_t grid_occ_size, uint32_t sub3,
-                            uint16_t* dense, cudaStream_t s);
+// Fills the compact layout: brick b (of n) copies sub3 codes from codes[src[b]]
+// to dense[dst[b]]; skirt[b] != 0 also fills the sub3 slots before dst[b] from
+// the sub3 before src[b] (kCodeMiss below 0).
+int launch_compact_fill(const uint16_t* codes, const int64_t* src, const int64_t* dst, const uint8_t* skirt,
+                        uint32_t n, uint32_t sub3, uint16_t* dense, cudaStream_t s);
 
 }  // namespace tsdfl

@@ -63,7 +63,8 @@ class Context:
 
 
 class DeviceMap:
-    """A likelihood map resident on the device (tsdfl_map)."""
+    """A likelihood map resident on the device (tsdfl_map).  dense=True also
+    builds the compact layout (TSDFL_MAP_DENSE): one map gather per lookup."""
 
     def __init__(self, ctx: Context, coef: N.MapCoef, grid_occ: np.ndarray, data: np.ndarray | None = None,
                  codes: np.ndarray | None = None, sigma: float = 0.1, dense: bool = False, force_f32: bool = False):
