@@ -179,6 +179,19 @@ int tsdfl_resample_systematic(tsdfl_ctx* ctx, const float* weights, size_t M, fl
 int tsdfl_resample_systematic_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
                                      float* d_particles_out, size_t cap, uint32_t* d_count);
 
+/* ---- residual systematic resampling ----
+ * ResidualSystematicResampler::resample (novel_resampling.h:76-104), mcl_3d's
+ * default resampler (mcl_3d.cpp:765), with its draw u0 in [0, 1) given:
+ * particle m is emitted (size_t)(temp + 1.0) times, temp = (float)M * w_m - u,
+ * u then becomes (float)count - temp.  Bit-exact with the reference for the
+ * same weights and u0 (the float chain is walked in particle order by one
+ * device thread; the copies are parallel).  Negative or non-finite weights, or
+ * a particle count of 2^24, give TSDFL_ERR_UNSUPPORTED. */
+int tsdfl_resample_residual_systematic(tsdfl_ctx* ctx, const float* weights, size_t M, float u0, uint32_t* idx_out,
+                                       size_t cap, size_t* count_out);
+int tsdfl_resample_residual_systematic_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
+                                              float* d_particles_out, size_t cap, uint32_t* d_count);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about

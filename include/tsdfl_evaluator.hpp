@@ -7,6 +7,8 @@
  *       (include/tsdf_localization/cuda/cuda_evaluator.h:94-125)
  *   tsdf_localization::GpuSystematicResampler replaces SystematicResampler
  *       (include/tsdf_localization/resampling/novel_resampling.h:38-74)
+ *   tsdf_localization::GpuResidualSystematicResampler replaces
+ *       ResidualSystematicResampler (novel_resampling.h:76-104)
  *
  * Errors surface as std::runtime_error carrying libtsdfl's message, as the
  * reference's evaluators throw them ("No particle is valid!" for a zero
@@ -146,6 +148,28 @@ void resample_systematic(Context& ctx, std::vector<ParticleT>& particles, float 
     particles = std::move(out);
 }
 
+// ResidualSystematicResampler::resample (novel_resampling.h:76-104) for a given
+// draw u0 in [0, 1): replaces `particles` by the reference's output sequence.
+template <class ParticleT>
+void resample_residual_systematic(Context& ctx, std::vector<ParticleT>& particles, float u0)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    std::vector<float> w(M);
+    for (size_t i = 0; i < M; ++i) w[i] = particles[i].second;
+    std::vector<uint32_t> idx(2 * M + 16);
+    size_t count = 0;
+    check(tsdfl_resample_residual_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+    if (count > idx.size()) {
+        idx.resize(count);
+        check(tsdfl_resample_residual_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+    }
+    std::vector<ParticleT> out;
+    out.reserve(count);
+    for (size_t k = 0; k < count; ++k) out.push_back(particles[idx[k]]);
+    particles = std::move(out);
+}
+
 // Cell-centre reduction of a scan as CudaEvaluator's point-cloud overload
 // performs it (cuda_evaluator.cu:77-115): every point maps to the centre of its
 // 0.064 m cell, each centre kept once.  Order does not matter downstream: the
@@ -244,6 +268,23 @@ public:
         std::uniform_real_distribution<FLOAT_T> uniform_distribution(0.0, inverse_M);
         const float u0 = uniform_distribution(*m_generator_ptr);
         tsdfl::resample_systematic(*ctx_, particle_cloud.particles(), u0);
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+};
+
+// Drop-in for ResidualSystematicResampler (mcl_3d's default, mcl_3d.cpp:765):
+// the same draw u ~ U[0, 1) from the inherited generator, then the device.
+class GpuResidualSystematicResampler : public Resampler {
+public:
+    explicit GpuResidualSystematicResampler(int device = 0) : ctx_(new tsdfl::Context(device)) {}
+
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        std::uniform_real_distribution<FLOAT_T> uniform_distribution(0.0, 1.0);
+        const float u = uniform_distribution(*m_generator_ptr);
+        tsdfl::resample_residual_systematic(*ctx_, particle_cloud.particles(), u);
     }
 
 private:

@@ -73,6 +73,8 @@ def oracle() -> C.CDLL:
                                                 C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
         L.orc_resample_systematic.restype = SZ
         L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
+        L.orc_resample_residual_systematic.restype = SZ
+        L.orc_resample_residual_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
         _orc = L
     return _orc
 
@@ -106,6 +108,10 @@ def reference() -> C.CDLL:
         L.ref_draw_u0.argtypes = [C.c_uint32, SZ]
         L.ref_resample_systematic.restype = SZ
         L.ref_resample_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
+        L.ref_draw_u01.restype = C.c_float
+        L.ref_draw_u01.argtypes = [C.c_uint32]
+        L.ref_resample_residual_systematic.restype = SZ
+        L.ref_resample_residual_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
         L.ref_omp_threads.restype = C.c_int
         _ref = L
     return _ref
@@ -212,6 +218,16 @@ def resample_systematic(weights: np.ndarray, u0: float, cap: int | None = None) 
     return out[:n]
 
 
+def resample_residual_systematic(weights: np.ndarray, u0: float, cap: int | None = None) -> np.ndarray:
+    w = np.ascontiguousarray(weights, np.float32)
+    cap = cap if cap is not None else 2 * w.shape[0] + 16
+    out = np.zeros(max(cap, 1), np.uint32)
+    n = oracle().orc_resample_residual_systematic(_ptr(w), w.shape[0], np.float32(u0), _ptr(out), cap)
+    if n == (1 << 64) - 1:
+        raise RuntimeError("a particle count reaches 2^32")
+    return out[: min(n, cap)] if n > cap else out[:n]
+
+
 def likelihood_value(mm: int, sigma: float = 0.1) -> float:
     return oracle().orc_likelihood_value(mm, sigma)
 
@@ -286,6 +302,18 @@ class RefMap:
 
 def ref_draw_u0(seed: int, m: int) -> float:
     return reference().ref_draw_u0(seed, m)
+
+
+def ref_draw_u01(seed: int) -> float:
+    return reference().ref_draw_u01(seed)
+
+
+def ref_resample_residual_systematic(weights: np.ndarray, seed: int, cap: int | None = None) -> np.ndarray:
+    w = np.ascontiguousarray(weights, np.float32)
+    cap = cap if cap is not None else 2 * w.shape[0] + 16
+    out = np.zeros(max(cap, 1), np.uint32)
+    n = reference().ref_resample_residual_systematic(_ptr(w), w.shape[0], seed, _ptr(out), cap)
+    return out[:n]
 
 
 def ref_resample_systematic(weights: np.ndarray, seed: int, cap: int | None = None) -> np.ndarray:

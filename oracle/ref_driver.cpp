@@ -78,6 +78,10 @@ struct SeededSystematic : SystematicResampler {
     explicit SeededSystematic(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
 };
 
+struct SeededResidualSystematic : ResidualSystematicResampler {
+    explicit SeededResidualSystematic(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
+};
+
 struct MapHandle {
     std::shared_ptr<Map> map;
 };
@@ -208,6 +212,31 @@ size_t ref_resample_systematic(const float* w, size_t M, uint32_t seed, uint32_t
         cloud.particles()[i].second = w[i];
     }
     SeededSystematic r(seed);
+    r.resample(cloud);
+    size_t n = cloud.particles().size();
+    for (size_t i = 0; i < n && i < cap; ++i) idx_out[i] = (uint32_t)cloud.particles()[i].first[0];
+    return n;
+}
+
+// ResidualSystematicResampler's draw u ~ U[0, 1) for a generator seeded by seed.
+float ref_draw_u01(uint32_t seed)
+{
+    std::mt19937 g(seed);
+    std::uniform_real_distribution<FLOAT_T> d(0.0, 1.0);
+    return d(g);
+}
+
+// ResidualSystematicResampler::resample on weights w, generator seeded by seed.
+size_t ref_resample_residual_systematic(const float* w, size_t M, uint32_t seed, uint32_t* idx_out, size_t cap)
+{
+    ParticleCloud cloud;
+    cloud.particles().resize(M);
+    for (size_t i = 0; i < M; ++i) {
+        for (int k = 0; k < 6; ++k) cloud.particles()[i].first[k] = 0;
+        cloud.particles()[i].first[0] = (float)i;
+        cloud.particles()[i].second = w[i];
+    }
+    SeededResidualSystematic r(seed);
     r.resample(cloud);
     size_t n = cloud.particles().size();
     for (size_t i = 0; i < n && i < cap; ++i) idx_out[i] = (uint32_t)cloud.particles()[i].first[0];

@@ -36,6 +36,19 @@ uint64_t orc_f2u_x86(float v)
     return 0;                                         /* indefinite ^ sign bit */
 }
 
+uint64_t orc_d2u_x86(double v)
+{
+    const double two63 = 9223372036854775808.0;
+    if (v != v) return SIGN64;                        /* cvttsd2si of NaN: integer indefinite */
+    if (v < two63) {
+        if (v >= -two63) return (uint64_t)(int64_t)v;  /* truncation, two's complement wrap */
+        return SIGN64;
+    }
+    double w = v - two63;                             /* exact for these magnitudes */
+    if (w < two63) return ((uint64_t)(int64_t)w) ^ SIGN64;
+    return 0;
+}
+
 /* cuda_sub_voxel_map.tcc:4-48 */
 void orc_map_coef_init(orc_map_coef* c, const float mn[3], const float mx[3],
                        float resolution, float init_value)
@@ -353,6 +366,25 @@ size_t orc_resample_systematic(const float* w, size_t M, float U0, uint32_t* idx
             float next = (float)((double)U + inverse_M);
             if (next == U) return (size_t)-1;   /* the reference would loop forever */
             U = next;
+        }
+    }
+    return n;
+}
+
+/* novel_resampling.h:76-104 */
+size_t orc_resample_residual_systematic(const float* w, size_t M, float u0, uint32_t* idx_out, size_t cap)
+{
+    const float Mf = (float)M;                        /* size_t * float converts M to float */
+    float u = u0;
+    size_t n = 0;
+    for (size_t m = 0; m < M; ++m) {
+        float temp = Mf * w[m] - u;                   /* float product and difference */
+        uint64_t o = orc_d2u_x86((double)temp + 1.0);
+        if (o >= (1ull << 32)) return (size_t)-1;
+        u = (float)o - temp;                          /* size_t - float: o converted to float */
+        for (uint64_t k = 0; k < o; ++k) {
+            if (n < cap) idx_out[n] = (uint32_t)m;
+            ++n;
         }
     }
     return n;

@@ -100,6 +100,18 @@ int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, 
  * particles the reference would emit, or (size_t)-1 if U stops advancing. */
 size_t orc_resample_systematic(const float* w, size_t M, float U0, uint32_t* idx_out, size_t cap);
 
+/* double -> size_t as the reference's x86-64 build converts it (cvttsd2si with
+ * the 2^63 split), like orc_f2u_x86 for float. */
+uint64_t orc_d2u_x86(double v);
+
+/* ResidualSystematicResampler::resample (novel_resampling.h:76-104) with the
+ * uniform draw u0 in [0, 1) supplied: particle m is emitted
+ * o_m = (size_t)(temp + 1.0) times, temp = (float)M * w_m - u (float), and u
+ * becomes (float)o_m - temp.  Writes up to cap source indices and returns the
+ * number of particles the reference would emit, or (size_t)-1 when a count
+ * reaches 2^32 (the reference would try to allocate it). */
+size_t orc_resample_residual_systematic(const float* w, size_t M, float u0, uint32_t* idx_out, size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,7 +8,7 @@ what the reference computes from them: the map's coefficients and brick table
 and a digest of its slots (CudaSubVoxelMap ctor + setData), getEntry at the
 query points, TSDFEvaluator::evaluate's un-normalised and normalised weights,
 laser poses and mean pose (serial, in point order), and SystematicResampler's
-output indices for seeded draws.
+and ResidualSystematicResampler's output indices for seeded draws.
 
     python tests/golden/make_golden.py
 """
@@ -100,6 +100,10 @@ def resample_case(seed):
         out[f"resample/{k}/seed"] = np.int64(s)
         out[f"resample/{k}/u0"] = np.float32(O.ref_draw_u0(s, w.shape[0]))
         out[f"resample/{k}/indices"] = O.ref_resample_systematic(w, s)
+        s2 = int(rng.integers(1, 2 ** 31))
+        out[f"residual/{k}/seed"] = np.int64(s2)
+        out[f"residual/{k}/u0"] = np.float32(O.ref_draw_u01(s2))
+        out[f"residual/{k}/indices"] = O.ref_resample_residual_systematic(w, s2)
     return out
 
 

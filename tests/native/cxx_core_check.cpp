@@ -67,6 +67,14 @@ int main(int argc, char** argv)
         for (size_t i = 0; i < parts.size(); ++i) w[i] = parts[i].second;
         save(d + "/weights_out.bin", w.data(), w.size());
         save(d + "/pose_out.bin", &pose.x, 6);
+        std::vector<MyParticle> parts_r = parts;
+        tsdfl::resample_residual_systematic(ctx, parts_r, u0.at(1));
+        std::vector<float> out_r(7 * parts_r.size());
+        for (size_t i = 0; i < parts_r.size(); ++i) {
+            for (int k = 0; k < 6; ++k) out_r[7 * i + k] = parts_r[i].first[k];
+            out_r[7 * i + 6] = parts_r[i].second;
+        }
+        save(d + "/residual_out.bin", out_r.data(), out_r.size());
         tsdfl::resample_systematic(ctx, parts, u0.at(0));
         std::vector<float> out(7 * parts.size());
         for (size_t i = 0; i < parts.size(); ++i) {

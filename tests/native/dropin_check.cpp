@@ -44,6 +44,9 @@ int main()
         cloud.particles() = parts;
         rs.resample(cloud);
         std::printf("resampled %zu\n", cloud.size());
+        GpuResidualSystematicResampler rr(0);
+        rr.resample(cloud);
+        std::printf("residual resampled %zu\n", cloud.size());
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         status = 0;

@@ -61,3 +61,22 @@ def test_fixture_draws_match_reference_generator():
     for wset in SETS:
         assert np.float32(O.ref_draw_u0(int(GOLD[f"resample/{wset}/seed"]), GOLD[f"resample/{wset}/weights"].shape[0])) \
             == GOLD[f"resample/{wset}/u0"]
+
+
+@pytest.mark.parametrize("wset", SETS)
+def test_residual_resample_matches_reference(wset):
+    w = GOLD[f"resample/{wset}/weights"]
+    got = O.resample_residual_systematic(w, float(GOLD[f"residual/{wset}/u0"]))
+    assert np.array_equal(got, GOLD[f"residual/{wset}/indices"])
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference not compiled on this machine")
+def test_residual_resample_random_weights_match_reference():
+    """Beyond the fixtures: 100 random weight vectors and seeds."""
+    rng = np.random.default_rng(5)
+    for _ in range(100):
+        m = int(rng.integers(1, 2000))
+        w = (lambda x: (x / x.sum()).astype(np.float32))(rng.random(m) ** 4 + 1e-9)
+        seed = int(rng.integers(1, 2 ** 31))
+        assert np.array_equal(O.resample_residual_systematic(w, O.ref_draw_u01(seed), cap=4 * m + 16),
+                              O.ref_resample_residual_systematic(w, seed, cap=4 * m + 16))

@@ -32,13 +32,15 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     wl.particles.astype(np.float32).tofile(tmp_path / "particles.bin")
     wl.points.astype(np.float32).tofile(tmp_path / "points.bin")
     np.asarray(wl.tf, np.float32).tofile(tmp_path / "tf.bin")
-    np.array([u0], np.float32).tofile(tmp_path / "u0.bin")
+    u1 = np.float32(0.618)
+    np.array([u0, u1], np.float32).tofile(tmp_path / "u0.bin")
     res = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     print(res.stdout, res.stderr)
     assert res.returncode == 0, res.stdout + res.stderr
     w_cxx = np.fromfile(tmp_path / "weights_out.bin", np.float32)
     pose_cxx = np.fromfile(tmp_path / "pose_out.bin", np.float32)
     rs_cxx = np.fromfile(tmp_path / "resampled_out.bin", np.float32).reshape(-1, 7)
+    rr_cxx = np.fromfile(tmp_path / "residual_out.bin", np.float32).reshape(-1, 7)
 
     ctx = Context(0)
     dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, data=data)
@@ -54,3 +56,5 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     f64 = ref["sum64"] / ref["sum64"].sum()
     assert np.all(np.abs(w_cxx.astype(np.float64) - f64) <= 1e-5 * f64)
     assert np.array_equal(idx, O.resample_systematic(p[:, 6], float(u0)))
+    ridx = O.resample_residual_systematic(p[:, 6], float(u1))
+    assert np.array_equal(rr_cxx, p[ridx])

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle_py as O
-from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator
+from tsdf_localization_gb300 import (Context, DeviceMap, ResidualSystematicResampler, SystematicResampler,
+                                     TSDFEvaluator)
 from tsdf_localization_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
@@ -49,3 +50,10 @@ def test_gpu_resample_matches_reference(ctx, wset):
     got = SystematicResampler(ctx).resample_indices(GOLD[f"resample/{wset}/weights"],
                                                     float(GOLD[f"resample/{wset}/u0"]))
     assert np.array_equal(got, GOLD[f"resample/{wset}/indices"])
+
+
+@pytest.mark.parametrize("wset", sorted({k.split("/")[1] for k in GOLD.files if k.startswith("residual/")}))
+def test_gpu_residual_resample_matches_reference(ctx, wset):
+    got = ResidualSystematicResampler(ctx).resample_indices(GOLD[f"resample/{wset}/weights"],
+                                                            float(GOLD[f"residual/{wset}/u0"]))
+    assert np.array_equal(got, GOLD[f"residual/{wset}/indices"])

@@ -246,9 +246,12 @@ def _random_weights(rng, m, kind):
     elif kind == "one":
         w = np.zeros(m)
         w[rng.integers(m)] = 1.0
-    elif kind == "tiny":   # weights below 2^-29: serial fallback on the device
+    elif kind == "tiny":   # weights below 2^-29: serial double sums on the device
         w = rng.random(m)
         w[: m // 3] = 1e-12
+    elif kind == "negative":   # negative weights: the literal loop on the device
+        w = rng.random(m)
+        w[:: max(1, m // 5)] *= -0.01
     else:
         raise ValueError(kind)
     w = w / w.sum()
@@ -256,7 +259,7 @@ def _random_weights(rng, m, kind):
 
 
 @pytest.mark.parametrize("m", [1, 2, 7, 1000, 4096, 65537, 250000])
-@pytest.mark.parametrize("kind", ["uniform", "random", "peaked", "one", "tiny"])
+@pytest.mark.parametrize("kind", ["uniform", "random", "peaked", "one", "tiny", "negative"])
 def test_resample_bit_exact(ctx, m, kind):
     rng = np.random.default_rng(m * 31 + len(kind))
     w = _random_weights(rng, m, kind)
@@ -267,3 +270,47 @@ def test_resample_bit_exact(ctx, m, kind):
         exp = O.resample_systematic(w, u0)
         assert got.shape == exp.shape
         assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("m", [1, 2, 7, 1000, 65537, 250000])
+@pytest.mark.parametrize("kind", ["uniform", "random", "peaked", "one", "tiny"])
+def test_residual_resample_bit_exact(ctx, m, kind):
+    """ResidualSystematicResampler: indices and count equal the oracle's (pinned
+    to the reference) for draws at both ends of [0, 1)."""
+    from tsdf_localization_gb300 import ResidualSystematicResampler
+    rng = np.random.default_rng(m * 17 + len(kind))
+    w = _random_weights(rng, m, kind)
+    rs = ResidualSystematicResampler(ctx, seed=m)
+    for u0 in (0.0, 0.5, float(np.nextafter(np.float32(1.0), np.float32(0))), rs.draw()):
+        got = rs.resample_indices(w, u0, cap=2 * m + 16)
+        exp = O.resample_residual_systematic(w, u0, cap=2 * m + 16)
+        assert np.array_equal(got, exp)
+
+
+def test_residual_resample_device_form_and_errors(ctx):
+    from tsdf_localization_gb300 import ResidualSystematicResampler
+    from tsdf_localization_gb300 import _native as N
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    m = 5000
+    parts = rng.normal(size=(m, 7)).astype(np.float32)
+    parts[:, 6] = _random_weights(rng, m, "random")
+    u0 = 0.3125
+    idx = ResidualSystematicResampler(ctx).resample_indices(parts[:, 6], u0)
+    d_in = torch.from_numpy(parts).cuda()
+    d_out = torch.zeros((2 * m + 16, 7), dtype=torch.float32, device="cuda")
+    d_cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(N.lib().tsdfl_resample_residual_systematic_device(ctx.handle, C.c_void_p(d_in.data_ptr()), m,
+                                                              np.float32(u0), C.c_void_p(d_out.data_ptr()),
+                                                              2 * m + 16, C.c_void_p(d_cnt.data_ptr())))
+    ctx.sync()
+    n = int(d_cnt.item())
+    assert n == idx.shape[0]
+    assert np.array_equal(d_out[:n].cpu().numpy(), parts[idx])
+    bad = parts[:, 6].copy()
+    bad[10] = -1.0
+    with pytest.raises(TsdflError):
+        ResidualSystematicResampler(ctx).resample_indices(bad, u0)
+    # the context stays usable
+    assert np.array_equal(ResidualSystematicResampler(ctx).resample_indices(parts[:, 6], u0), idx)

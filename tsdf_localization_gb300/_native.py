@@ -93,6 +93,8 @@ SIGNATURES = [
     ("tsdfl_resample_systematic", I, [P, P, SZ, F, P, SZ, C.POINTER(SZ)]),
     ("tsdfl_resample_systematic_device", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_systematic_static", I, [P, P, SZ, F, P, SZ, P]),
+    ("tsdfl_resample_residual_systematic", I, [P, P, SZ, F, P, SZ, P]),
+    ("tsdfl_resample_residual_systematic_device", I, [P, P, SZ, F, P, SZ, P]),
 ]
 
 SYNTH_SIGNATURES = [

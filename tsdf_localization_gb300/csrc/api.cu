@@ -813,6 +813,64 @@ int tsdfl_resample_systematic_device(tsdfl_ctx* c, const float* d_particles, siz
                                 c->rs_ws, c->status, c->stream);
 }
 
+int tsdfl_resample_residual_systematic(tsdfl_ctx* c, const float* weights, size_t M, float u0, uint32_t* idx_out,
+                                       size_t cap, size_t* count_out)
+{
+    if (!c || (M && !weights) || (cap && !idx_out) || !count_out) {
+        set_error("tsdfl_resample_residual_systematic: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *count_out = 0;
+    if (M == 0) return TSDFL_OK;
+    if (M >= (1ull << 24)) {
+        set_error("tsdfl_resample_residual_systematic: at most 2^24-1 particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_resample_ws(c, M);
+    if (rc) return rc;
+    size_t w_b = align_up(sizeof(float) * M, 256);
+    size_t i_b = align_up(sizeof(uint32_t) * (cap ? cap : 1), 256);
+    rc = ensure_io(c, w_b + i_b + 256);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_w = reinterpret_cast<float*>(io);
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(io + w_b);
+    uint32_t* d_cnt = reinterpret_cast<uint32_t*>(io + w_b + i_b);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_w, weights, sizeof(float) * M, cudaMemcpyHostToDevice, s));
+    rc = launch_resample_residual(nullptr, d_w, 1, M, u0, nullptr, d_idx, cap, d_cnt, c->rs_ws, c->status, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->h_count, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (cap) CUDA_TRY(cudaMemcpyAsync(idx_out, d_idx, sizeof(uint32_t) * cap, cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    *count_out = c->h_count[0];
+    if (st == TSDFL_ERR_UNSUPPORTED)
+        set_error("tsdfl_resample_residual_systematic: negative or non-finite weights, or a particle count of 2^24");
+    return st;
+}
+
+int tsdfl_resample_residual_systematic_device(tsdfl_ctx* c, const float* d_particles, size_t M, float u0,
+                                              float* d_particles_out, size_t cap, uint32_t* d_count)
+{
+    if (!c || (M && !d_particles) || !d_particles_out || !d_count) {
+        set_error("tsdfl_resample_residual_systematic_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (M == 0) return TSDFL_OK;
+    if (M >= (1ull << 24)) {
+        set_error("tsdfl_resample_residual_systematic_device: at most 2^24-1 particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_resample_ws(c, M);
+    if (rc) return rc;
+    return launch_resample_residual(d_particles, d_particles + 6, 7, M, u0, d_particles_out, nullptr, cap, d_count,
+                                    c->rs_ws, c->status, c->stream);
+}
+
 }  // extern "C"
 
 // ------------------------------------------------ resampling without allocation

@@ -815,6 +815,8 @@ struct ResampleWs {
     int* nseg;
     int* exact_ok;          // 1 when the parallel path reproduces the serial one
     long long* total;
+    int* serial;            // 1 when only the literal loop reproduces it
+    double* sums;           // M serial double prefix sums (aliases cdf; used when !exact_ok)
 };
 
 // Weight as an exact multiple of 2^-52 (its value in those units), or -1 when
@@ -886,6 +888,68 @@ __device__ __forceinline__ double pow2(int k)
 }
 
 // Builds the piecewise-arithmetic description of the reference's float draw
+// sequence U_{k+1} = (float)((double)U_k + 1.0/M) (novel_resampling.h:59-63)
+// for all draws below s_total: inside one binade of float the step is constant
+// except near its top, where single steps are taken literally.  False when it
+// cannot (a step that would depend on the parity of U, a draw that stops
+// advancing, more than kMaxSegments pieces).  Scalings by powers of two only.
+__device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
+{
+    bool ok = true;
+    const double inv_m = 1.0 / (double)M;
+    double U = (double)u0;
+    long long j = 0;
+    int ns = 0;
+    for (int iter = 0; U < s_total; ++iter) {
+        if (ns == kMaxSegments || iter > 4 * kMaxSegments) { ok = false; break; }
+        float uf = (float)U;
+        bool regular = false;
+        long long cnt = 0;
+        double delta = 0.0;
+        if (uf >= 1.17549435e-38f) {     // normal float: binade [2^e, 2^(e+1))
+            const int e = (int)((__double_as_longlong(U) >> 52) & 0x7ff) - 1023;
+            const double u = pow2(e - 23);     // float ulp in the binade
+            const double g = pow2(e - 52);     // double ulp in the binade
+            const double ginv = pow2(52 - e);
+            const double y = rint(inv_m * ginv) * g;   // (double)U + inv_m - U, while inside the binade
+            const double r = y * pow2(23 - e);          // y / u
+            double frac = r - floor(r);
+            if (frac == 0.5) { ok = false; break; }   // step would depend on the parity of U
+            delta = rint(r) * u;
+            if (delta <= 0.0) { ok = false; break; }  // U would stop advancing
+            // values U + i*delta with U + i*delta + y < 2^(e+1) take the regular step
+            double top = pow2(e + 1) - y;
+            if (U < top) {
+                long long Ui = (long long)(U * ginv), Di = (long long)(delta * ginv), Ti = (long long)(top * ginv);
+                cnt = (Ti - Ui + Di - 1) / Di;
+                regular = cnt > 0;
+            }
+        }
+        if (regular) {
+            ws.segs[ns].u_start = U;
+            ws.segs[ns].delta = delta;
+            ws.segs[ns].j0 = j;
+            ws.segs[ns].n = cnt;
+            ++ns;
+            j += cnt;
+            U = U + (double)cnt * delta;   // exact: a float value of this binade or 2^(e+1)
+        } else {
+            ws.segs[ns].u_start = U;
+            ws.segs[ns].delta = 0.0;
+            ws.segs[ns].j0 = j;
+            ws.segs[ns].n = 1;
+            ++ns;
+            j += 1;
+            double next = (double)(float)(U + inv_m);
+            if (!(next > U)) { ok = false; break; }   // U stopped advancing
+            U = next;
+        }
+    }
+    *ws.nseg = ns;
+    return ok;
+}
+
+// Builds the piecewise-arithmetic description of the reference's float draw
 // sequence U_{k+1} = (float)((double)U_k + 1.0/M) (novel_resampling.h:59-63):
 // inside one binade of float the step is constant except near its top, where
 // single steps are taken literally.  One warp: the lanes form the tiles'
@@ -912,57 +976,7 @@ __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs 
     *ws.total = acc;
     if (acc >= (1ll << 53)) *ws.exact_ok = 0;   // partial sums >= 2 may round in the serial double sum
     if (!*ws.exact_ok) { *ws.nseg = 0; return; }
-    const double s_total = ldexp((double)acc, -52);
-    const double inv_m = 1.0 / (double)M;
-    double U = (double)u0;
-    long long j = 0;
-    int ns = 0;
-    for (int iter = 0; U < s_total; ++iter) {
-        if (ns == kMaxSegments || iter > 4 * kMaxSegments) { *ws.exact_ok = 0; break; }
-        float uf = (float)U;
-        bool regular = false;
-        long long cnt = 0;
-        double delta = 0.0;
-        if (uf >= 1.17549435e-38f) {     // normal float: binade [2^e, 2^(e+1))
-            const int e = (int)((__double_as_longlong(U) >> 52) & 0x7ff) - 1023;
-            const double u = pow2(e - 23);     // float ulp in the binade
-            const double g = pow2(e - 52);     // double ulp in the binade
-            const double ginv = pow2(52 - e);
-            const double y = rint(inv_m * ginv) * g;   // (double)U + inv_m - U, while inside the binade
-            const double r = y * pow2(23 - e);          // y / u
-            double frac = r - floor(r);
-            if (frac == 0.5) { *ws.exact_ok = 0; break; }   // step would depend on the parity of U
-            delta = rint(r) * u;
-            if (delta <= 0.0) { *ws.exact_ok = 0; break; }  // U would stop advancing
-            // values U + i*delta with U + i*delta + y < 2^(e+1) take the regular step
-            double top = pow2(e + 1) - y;
-            if (U < top) {
-                long long Ui = (long long)(U * ginv), Di = (long long)(delta * ginv), Ti = (long long)(top * ginv);
-                cnt = (Ti - Ui + Di - 1) / Di;
-                regular = cnt > 0;
-            }
-        }
-        if (regular) {
-            ws.segs[ns].u_start = U;
-            ws.segs[ns].delta = delta;
-            ws.segs[ns].j0 = j;
-            ws.segs[ns].n = cnt;
-            ++ns;
-            j += cnt;
-            U = U + (double)cnt * delta;   // exact: a float value of this binade or 2^(e+1)
-        } else {
-            ws.segs[ns].u_start = U;
-            ws.segs[ns].delta = 0.0;
-            ws.segs[ns].j0 = j;
-            ws.segs[ns].n = 1;
-            ++ns;
-            j += 1;
-            double next = (double)(float)(U + inv_m);
-            if (!(next > U)) { *ws.exact_ok = 0; break; }   // U stopped advancing
-            U = next;
-        }
-    }
-    *ws.nseg = ns;
+    if (!build_segments(M, u0, ldexp((double)acc, -52), ws)) *ws.exact_ok = 0;
 }
 
 // Number of draws U_j below s (the count the serial loop has emitted once its
@@ -1017,37 +1031,273 @@ __global__ void resample_assign_kernel(const float* particles, int M, float* out
     }
 }
 
-// The reference loop literally, on one thread, for weights where the parallel
-// path would not be exact (negative, tiny or huge weights).
-__global__ void resample_serial_kernel(const float* particles, const float* w, int stride, int M, float u0,
-                                       float* out, uint32_t* idx_out, long long cap, uint32_t* count_out,
-                                       ResampleWs ws, int32_t* status)
+constexpr int kChainTile = 2048;
+constexpr int kChainThreads = 512;
+
+// Fallback of the parallel systematic path for weights that are not exact
+// multiples of 2^-52 (tiny or huge) but non-negative and finite: the serial
+// double sums s_m = s_{m-1} + w_m of the reference loop are formed by one
+// thread over tiles staged in shared memory (one dependent double addition a
+// particle); with s monotone, the draws each particle emits follow from the
+// draw segments in parallel (resample_assign_sums_kernel).  Negative or
+// non-finite weights set *ws.serial: only the literal loop reproduces them.
+__global__ void __launch_bounds__(kChainThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
+                                                                      ResampleWs ws)
 {
+    __shared__ float sw[kChainTile];
+    __shared__ double sd[kChainTile];
     if (*ws.exact_ok) return;
-    const double inv_m = 1.0 / (double)M;
-    float U = u0;
     double s = 0.0;
-    long long n = 0;
-    for (int m = 0; m < M; ++m) {
-        s += (double)w[(size_t)m * stride];
-        while (s > (double)U) {
-            if (n < cap) {
-                if (idx_out) idx_out[n] = (uint32_t)m;
-                if (out)
-                    for (int k = 0; k < 7; ++k) out[7 * (size_t)n + k] = particles[7 * (size_t)m + k];
+    for (int base = 0; base < M; base += kChainTile) {
+        const int t = min(kChainTile, M - base);
+        bool bad = false;
+        for (int i = threadIdx.x; i < t; i += blockDim.x) {
+            const float x = w[(size_t)(base + i) * stride];
+            bad |= !(x >= 0.0f) || !(fabsf(x) < INFINITY);
+            sw[i] = x;
+        }
+        if (__syncthreads_or(bad ? 1 : 0)) {
+            if (threadIdx.x == 0) *ws.serial = 1;
+            return;
+        }
+        if (threadIdx.x == 0) {
+#pragma unroll 8
+            for (int i = 0; i < t; ++i) {
+                s += (double)sw[i];
+                sd[i] = s;
             }
-            ++n;
-            float next = (float)((double)U + inv_m);
-            if (next == U || n > 4ll * M + 16) {   // the reference would not terminate
-                atomicExch(status, TSDFL_ERR_UNSUPPORTED);
-                *count_out = (uint32_t)n;
-                return;
-            }
-            U = next;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < t; i += blockDim.x) ws.sums[base + i] = sd[i];
+        __syncthreads();
+    }
+}
+
+// Draw segments up to the serial sum's total, for the fallback above.
+__global__ void resample_segments_sums_kernel(int M, float u0, ResampleWs ws)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || *ws.exact_ok || *ws.serial) return;
+    if (!build_segments(M, u0, ws.sums[M - 1], ws)) *ws.serial = 1;
+}
+
+// Particle m receives the draws in [s_{m-1}, s_m) of the serial double sums.
+__global__ void resample_assign_sums_kernel(const float* particles, int M, float* out, uint32_t* idx_out,
+                                            long long cap, uint32_t* count_out, ResampleWs ws, int32_t* status)
+{
+    __shared__ Segment seg[kMaxSegments];
+    if (*ws.exact_ok || *ws.serial) return;
+    const int ns = *ws.nseg;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) seg[k] = ws.segs[k];
+    __syncthreads();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const long long lo = m > 0 ? count_below(seg, ns, ws.sums[m - 1]) : 0;
+    const long long hi = count_below(seg, ns, ws.sums[m]);
+    if (m == M - 1) {
+        *count_out = (uint32_t)hi;
+        if (hi > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
+    }
+    for (long long j = lo; j < hi && j < cap; ++j) {
+        if (idx_out) idx_out[j] = (uint32_t)m;
+        if (out) {
+            const float* src = particles + 7 * (size_t)m;
+            float* dst = out + 7 * (size_t)j;
+            for (int k = 0; k < 7; ++k) dst[k] = src[k];
         }
     }
-    *count_out = (uint32_t)n;
-    if (n > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
+}
+
+__global__ void set_flags_kernel(int* exact_ok, int* serial, int* err)
+{
+    *exact_ok = 1;
+    *serial = 0;
+    *err = 0;
+}
+
+// SystematicResampler's loop (novel_resampling.h:41-72) literally, for the
+// weights the parallel path cannot reproduce exactly (negative, tiny or huge):
+// one thread walks it over tiles of weights the block stages in shared memory,
+// writing every particle's count and exclusive offset; the copies are made in
+// parallel afterwards.  A draw that stops advancing or a count beyond 4M + 16
+// (the reference would never finish) stops the walk and sets *err.  Runs only
+// when *run is set (neither parallel form applies).
+__global__ void __launch_bounds__(kChainThreads) systematic_chain_kernel(const float* __restrict__ w, int stride,
+                                                                         int M, float u0,
+                                                                         uint32_t* __restrict__ cnt,
+                                                                         uint32_t* __restrict__ off,
+                                                                         unsigned long long* total, int* err,
+                                                                         const int* run)
+{
+    __shared__ float sw[kChainTile];
+    __shared__ uint32_t sc[kChainTile], so[kChainTile];
+    __shared__ int s_stop;
+    if (!*run) return;
+    const double inv_m = 1.0 / (double)M;
+    float u = u0;
+    double s = 0.0;
+    unsigned long long n = 0;
+    if (threadIdx.x == 0) s_stop = 0;
+    for (int base = 0; base < M; base += kChainTile) {
+        const int t = min(kChainTile, M - base);
+        for (int i = threadIdx.x; i < t; i += blockDim.x) sw[i] = w[(size_t)(base + i) * stride];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            bool stop = false;   // kept in a register: the loop reads no shared flag
+#pragma unroll 4
+            for (int i = 0; i < t; ++i) {
+                uint32_t k = 0;
+                s += (double)sw[i];
+                while (s > (double)u) {
+                    ++k;
+                    const float next = (float)((double)u + inv_m);
+                    if (next == u || n + k > 4ull * (unsigned long long)M + 16ull) {   // would never finish
+                        stop = true;
+                        break;
+                    }
+                    u = next;
+                }
+                sc[i] = k;
+                so[i] = (uint32_t)n;
+                n += k;
+                if (n >= (1ull << 31)) stop = true;   // offsets stay 32-bit
+                if (stop) break;
+            }
+            *total = n;
+            s_stop = stop ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_stop) {
+            if (threadIdx.x == 0) *err = 1;
+            return;
+        }
+        for (int i = threadIdx.x; i < t; i += blockDim.x) {
+            cnt[base + i] = sc[i];
+            off[base + i] = so[i];
+        }
+        __syncthreads();
+    }
+}
+
+// ResidualSystematicResampler::resample (novel_resampling.h:76-104) for
+// weights w >= 0 with (float)M * w < 2^22 - 1 (others stop it with *err): one
+// thread walks the draw chain -- temp = (float)M w - u; o = floor(temp) + 1,
+// the reference's (size_t)(temp + 1.0); u = (float)o - temp -- over tiles of
+// (float)M w staged in shared memory, four dependent float additions a
+// particle and nothing else; the block then turns the counts into offsets with
+// a scan.
+__global__ void __launch_bounds__(kChainThreads) residual_chain_kernel(const float* __restrict__ w, int stride,
+                                                                       int M, float u0, uint32_t* __restrict__ cnt,
+                                                                       uint32_t* __restrict__ off,
+                                                                       unsigned long long* total, int* err)
+{
+    static_assert(kChainTile == 4 * kChainThreads, "four counts per thread in the scan");
+    __shared__ float sc[kChainTile];   // (float)M * w, then the counts
+    __shared__ uint32_t warp_tot[kChainThreads / 32];
+    __shared__ uint32_t s_base;
+    const float Mf = (float)M;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float u = u0;
+    if (threadIdx.x == 0) s_base = 0u;
+    for (int base = 0; base < M; base += kChainTile) {
+        const int t = min(kChainTile, M - base);
+        bool bad = false;
+        for (int i = threadIdx.x; i < t; i += blockDim.x) {
+            const float x = w[(size_t)(base + i) * stride];
+            const float c = __fmul_rn(Mf, x);
+            bad |= !(x >= 0.0f) || !(c < 4194303.0f);
+            sc[i] = c;
+        }
+        if (__syncthreads_or(bad ? 1 : 0)) {
+            if (threadIdx.x == 0) {
+                *err = 1;
+                *total = s_base;
+            }
+            return;
+        }
+        if (threadIdx.x == 0) {
+#pragma unroll 8
+            for (int i = 0; i < t; ++i) {
+                const float temp = __fsub_rn(sc[i], u);
+                // floor(temp) + 1 for -1 <= temp < 2^22: rounding temp + 1.5 * 2^23 down
+                // lands on an integer (unit spacing there), so both steps are exact
+                const float of = __fsub_rn(__fadd_rd(temp, 12582912.0f), 12582911.0f);
+                u = __fsub_rn(of, temp);
+                sc[i] = of;
+            }
+        }
+        __syncthreads();
+        // exclusive offsets of this tile's counts, four per thread
+        uint32_t v[4], run = 0;
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * threadIdx.x + k;
+            v[k] = i < t ? (uint32_t)sc[i] : 0u;
+            run += v[k];
+        }
+        uint32_t x = run;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        uint32_t woff = 0, tile_total = 0;
+        for (int k = 0; k < kChainThreads / 32; ++k) {
+            if (k < warp) woff += warp_tot[k];
+            tile_total += warp_tot[k];
+        }
+        uint32_t o = s_base + woff + x - run;
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * threadIdx.x + k;
+            if (i < t) {
+                cnt[base + i] = v[k];
+                off[base + i] = o;
+            }
+            o += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_base += tile_total;
+            if (s_base >= (1u << 31)) *err = 1;   // offsets stay 32-bit
+        }
+        __syncthreads();
+        if (*err) {
+            if (threadIdx.x == 0) *total = s_base;
+            return;
+        }
+    }
+    if (threadIdx.x == 0) *total = s_base;
+}
+
+// Copies particle m (7 floats) to its cnt[m] output slots below cap, or writes
+// its index there; thread 0 reports the count (and the chain's failure).
+__global__ void resample_scatter_kernel(const float* particles, int M, const uint32_t* cnt, const uint32_t* off,
+                                        const unsigned long long* total, const int* err, const int* run,
+                                        float* out, uint32_t* idx_out, long long cap, uint32_t* count_out,
+                                        int32_t* status)
+{
+    if (run && !*run) return;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (*err) {
+        if (m == 0) {
+            *count_out = (uint32_t)*total;
+            atomicExch(status, TSDFL_ERR_UNSUPPORTED);
+        }
+        return;
+    }
+    if (m == 0) {
+        *count_out = (uint32_t)*total;
+        if ((long long)*total > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
+    }
+    if (m >= M) return;
+    const long long o = off[m];
+    for (long long j = o; j < o + (long long)cnt[m] && j < cap; ++j) {
+        if (idx_out) idx_out[j] = (uint32_t)m;
+        if (out) {
+            const float* src = particles + 7 * (size_t)m;
+            float* dst = out + 7 * (size_t)j;
+            for (int k = 0; k < 7; ++k) dst[k] = src[k];
+        }
+    }
 }
 
 __global__ void set_int_kernel(int* p, int v) { *p = v; }
@@ -1243,7 +1493,7 @@ int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s)
 size_t resample_workspace_bytes(size_t M)
 {
     size_t tiles = (M + kScanTile - 1) / kScanTile + 1;
-    return 8 * (M + 2 * tiles) + sizeof(Segment) * kMaxSegments + 64;
+    return 8 * (M + 2 * tiles) + sizeof(Segment) * kMaxSegments + 64;   // flags: 16 + 16 + 8 + 4 + 4 <= 64
 }
 
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
@@ -1259,15 +1509,47 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     ws.segs = reinterpret_cast<Segment*>(p); p += sizeof(Segment) * kMaxSegments;
     ws.nseg = reinterpret_cast<int*>(p); p += 16;
     ws.exact_ok = reinterpret_cast<int*>(p); p += 16;
-    ws.total = reinterpret_cast<long long*>(p);
-    set_int_kernel<<<1, 1, 0, s>>>(ws.exact_ok, 1);
+    ws.total = reinterpret_cast<long long*>(p); p += 8;
+    int* err = reinterpret_cast<int*>(p); p += 4;
+    ws.serial = reinterpret_cast<int*>(p);
+    ws.sums = reinterpret_cast<double*>(ws.cdf);
+    // the literal loop reuses the prefix-sum array for counts and offsets
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(ws.cdf);
+    uint32_t* off = cnt + M;
+    unsigned long long* total = reinterpret_cast<unsigned long long*>(ws.total);
+    const unsigned blocks = (unsigned)((M + 255) / 256);
+    set_flags_kernel<<<1, 1, 0, s>>>(ws.exact_ok, ws.serial, err);
     resample_scan_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(w, stride, (int)M, ws);
     resample_segments_kernel<<<1, 32, 0, s>>>((int)M, u0, (int)tiles, ws);
-    resample_assign_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(particles, (int)M, out, idx_out,
-                                                                        (long long)cap, count_out, ws, status);
-    resample_serial_kernel<<<1, 1, 0, s>>>(particles, w, stride, (int)M, u0, out, idx_out, (long long)cap,
-                                          count_out, ws, status);
-    g_launches += 5;
+    resample_assign_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out, ws,
+                                                  status);
+    // exact fallbacks: serial double sums + parallel assignment, else the literal loop
+    resample_sums_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, ws);
+    resample_segments_sums_kernel<<<1, 32, 0, s>>>((int)M, u0, ws);
+    resample_assign_sums_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out,
+                                                       ws, status);
+    systematic_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err, ws.serial);
+    resample_scatter_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, cnt, off, total, err, ws.serial, out,
+                                                   idx_out, (long long)cap, count_out, status);
+    g_launches += 9;
+    return check(cudaGetLastError());
+}
+
+int launch_resample_residual(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
+                             uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
+                             cudaStream_t s)
+{
+    char* p = static_cast<char*>(workspace);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(p);
+    uint32_t* off = cnt + M;
+    unsigned long long* total = reinterpret_cast<unsigned long long*>(p + ((8 * M + 15) / 16) * 16);
+    int* err = reinterpret_cast<int*>(total + 1);
+    set_int_kernel<<<1, 1, 0, s>>>(err, 0);
+    residual_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err);
+    resample_scatter_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(particles, (int)M, cnt, off, total, err,
+                                                                         nullptr, out, idx_out, (long long)cap,
+                                                                         count_out, status);
+    g_launches += 3;
     return check(cudaGetLastError());
 }
 

@@ -178,6 +178,10 @@ size_t resample_workspace_bytes(size_t M);
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
                          uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
                          cudaStream_t s);
+// ResidualSystematicResampler on the device; workspace: resample_workspace_bytes(M).
+int launch_resample_residual(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
+                             uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
+                             cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
 // Fills the compact layout: brick b (of n) copies sub3 codes from codes[src[b]]

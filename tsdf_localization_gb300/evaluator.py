@@ -198,6 +198,35 @@ class SystematicResampler:
         return particles[idx].copy()
 
 
+class ResidualSystematicResampler:
+    """ResidualSystematicResampler (novel_resampling.h:76-104, mcl_3d's default)
+    on the GPU.  The draw u0 ~ U[0, 1) comes from a seeded numpy generator
+    unless given."""
+
+    def __init__(self, ctx: Context, seed: int | None = None):
+        self.ctx = ctx
+        self.rng = np.random.default_rng(seed)
+
+    def draw(self) -> float:
+        return float(np.float32(self.rng.random()))
+
+    def resample_indices(self, weights: np.ndarray, u0: float | None = None, cap: int | None = None) -> np.ndarray:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        m = w.shape[0]
+        if u0 is None:
+            u0 = self.draw()
+        cap = cap if cap is not None else 2 * m + 16
+        out = np.zeros(max(cap, 1), np.uint32)
+        cnt = C.c_size_t()
+        N.check(N.lib().tsdfl_resample_residual_systematic(self.ctx.handle, _ptr(w), m, np.float32(u0), _ptr(out),
+                                                           cap, C.byref(cnt)))
+        return out[: cnt.value]
+
+    def resample(self, particles: np.ndarray, u0: float | None = None) -> np.ndarray:
+        idx = self.resample_indices(particles[:, 6], u0)
+        return particles[idx].copy()
+
+
 def code_values(sigma: float = 0.1, init_value: float = 0.0) -> np.ndarray:
     out = np.zeros(601, np.float32)
     N.check(N.lib().tsdfl_code_values(sigma, init_value, _ptr(out)))
