@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="building", choices=["building", "room"])
+    ap.add_argument("--workload", default="building", choices=["building", "room", "global"])
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
     ap.add_argument("--layout", default="compact", choices=["compact", "brick"])
@@ -54,6 +54,8 @@ def make_workload(args):
     from tsdf_localization_gb300 import synth
     if args.workload == "room":
         wl = synth.room_workload(seed=1, n_particles=args.particles or 1000, n_points=args.points or 2048)
+    elif args.workload == "global":
+        wl = synth.global_workload(seed=3, n_particles=args.particles or 1_000_000, n_points=args.points or 2048)
     else:
         wl = synth.building_workload(seed=2, n_particles=args.particles or 100_000, n_points=args.points or 8192)
     return wl

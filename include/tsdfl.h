@@ -192,6 +192,12 @@ int tsdfl_resample_residual_systematic(tsdfl_ctx* ctx, const float* weights, siz
 int tsdfl_resample_residual_systematic_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,
                                               float* d_particles_out, size_t cap, uint32_t* d_count);
 
+/* ---- best particle ----
+ * mcl_3d.cpp:382-394: the index of the first particle with the largest weight
+ * above 0, written to *d_index (device; 0xFFFFFFFF when no weight is above 0,
+ * where the reference would index with -1).  d_particles: M x 7 floats. */
+int tsdfl_best_particle_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint32_t* d_index);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about

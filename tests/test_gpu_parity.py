@@ -314,3 +314,39 @@ def test_residual_resample_device_form_and_errors(ctx):
         ResidualSystematicResampler(ctx).resample_indices(bad, u0)
     # the context stays usable
     assert np.array_equal(ResidualSystematicResampler(ctx).resample_indices(parts[:, 6], u0), idx)
+
+
+def test_best_particle(ctx):
+    """mcl_3d.cpp:382-394: first index of the largest weight above 0."""
+    import ctypes as C
+    from tsdf_localization_gb300 import _native as N
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(8)
+
+    def best_gpu(parts):
+        d_in = torch.from_numpy(np.ascontiguousarray(parts)).cuda()
+        d_idx = torch.zeros(1, dtype=torch.int32, device="cuda")
+        N.check(N.lib().tsdfl_best_particle_device(ctx.handle, C.c_void_p(d_in.data_ptr()), parts.shape[0],
+                                                   C.c_void_p(d_idx.data_ptr())))
+        ctx.sync()
+        return int(d_idx.item()) & 0xFFFFFFFF
+
+    def best_ref(w):
+        best, idx = np.float32(0.0), -1
+        for i, v in enumerate(w):
+            if v > best:
+                best, idx = v, i
+        return idx & 0xFFFFFFFF
+
+    for m, kind in [(1, "one"), (1000, "random"), (300001, "random"), (5000, "ties"), (64, "zero"), (100, "neg")]:
+        parts = rng.normal(size=(m, 7)).astype(np.float32)
+        w = rng.random(m).astype(np.float32)
+        if kind == "ties":
+            w[[17, 4000, 99]] = np.float32(2.0)
+        elif kind == "zero":
+            w[:] = 0.0
+        elif kind == "neg":
+            w = -w
+            w[50] = np.float32(1e-30)
+        parts[:, 6] = w
+        assert best_gpu(parts) == best_ref(parts[:, 6])

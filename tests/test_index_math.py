@@ -44,3 +44,18 @@ def test_sub_index_exhaustive(tmp_path):
     for ln in lines:
         f = dict(kv.split("=") for kv in ln.split()[1:])
         assert f["bad"] == "0" and f["mode"] in ("1", "2")
+
+
+def test_binade_prefix_sums_match_serial_double(tmp_path):
+    """The parallel, binade-wise form of the resampler's serial double prefix
+    sum equals plain serial double additions (random, tiny, zero and tie-heavy
+    weights)."""
+    exe = tmp_path / "binade_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", str(ROOT / "tests" / "native" / "binade_check.cpp"),
+                    "-o", str(exe)], check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True)
+    print(res.stdout)
+    assert res.returncode == 0, res.stdout
+    assert " 0 mismatches" in res.stdout
+    ties = int(res.stdout.split(" ties")[0].split()[-1])
+    assert ties > 0

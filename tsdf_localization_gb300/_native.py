@@ -95,6 +95,7 @@ SIGNATURES = [
     ("tsdfl_resample_systematic_static", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_residual_systematic", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_residual_systematic_device", I, [P, P, SZ, F, P, SZ, P]),
+    ("tsdfl_best_particle_device", I, [P, P, SZ, P]),
 ]
 
 SYNTH_SIGNATURES = [

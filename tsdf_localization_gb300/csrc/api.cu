@@ -871,6 +871,23 @@ int tsdfl_resample_residual_systematic_device(tsdfl_ctx* c, const float* d_parti
                                     c->rs_ws, c->status, c->stream);
 }
 
+int tsdfl_best_particle_device(tsdfl_ctx* c, const float* d_particles, size_t M, uint32_t* d_index)
+{
+    if (!c || (M && !d_particles) || !d_index) {
+        set_error("tsdfl_best_particle_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (M >= (1ull << 31)) {
+        set_error("tsdfl_best_particle_device: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    // status words 2-3 hold the 64-bit reduction key
+    return launch_best_particle(d_particles, M, reinterpret_cast<unsigned long long*>(c->status + 2), d_index,
+                                c->sm_count, c->stream);
+}
+
 }  // extern "C"
 
 // ------------------------------------------------ resampling without allocation

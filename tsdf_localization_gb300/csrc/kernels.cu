@@ -1036,39 +1036,168 @@ constexpr int kChainThreads = 512;
 
 // Fallback of the parallel systematic path for weights that are not exact
 // multiples of 2^-52 (tiny or huge) but non-negative and finite: the serial
-// double sums s_m = s_{m-1} + w_m of the reference loop are formed by one
-// thread over tiles staged in shared memory (one dependent double addition a
-// particle); with s monotone, the draws each particle emits follow from the
-// draw segments in parallel (resample_assign_sums_kernel).  Negative or
-// non-finite weights set *ws.serial: only the literal loop reproduces them.
-__global__ void __launch_bounds__(kChainThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
-                                                                      ResampleWs ws)
+// double sums s_m = s_{m-1} + w_m of the reference loop (novel_resampling.h:
+// 53-56), formed in parallel.  While the sum stays in one binade [2^b, 2^(b+1))
+// every result is a multiple of u = 2^(b-52), so s_k = s_{k-1} + r_k u with
+// r_k = floor(w_k / u) + [frac > 1/2] -- independent of s -- except at ties
+// (frac == 1/2), which round to the even multiple.  The sum after a tie is
+// always even, so the parity before a tie is that of the last tie (or the
+// binade's start) XOR the low bits of the increments since: a segmented XOR
+// scan.  Where the exact sum leaves the binade (or a weight reaches 2^(b+1))
+// one ordinary double addition is made and the scan restarts; that happens
+// about once per binade.  One block walks the weights in chunks staged in
+// shared memory.  Negative or non-finite weights set *ws.serial: only the
+// literal loop reproduces them.  With s monotone, the draws each particle emits
+// then follow from the draw segments in parallel (resample_assign_sums_kernel).
+constexpr int kSumsThreads = 1024;
+constexpr int kSumsItems = 4;
+constexpr int kSumsChunk = kSumsThreads * kSumsItems;
+
+struct ParityPrefix {   // segmented XOR: the parity state after a run of items
+    uint32_t reset;     // a tie occurred in the run: the parity restarted at 0 there
+    uint32_t x;         // XOR of the increments' low bits since the start or the last tie
+};
+
+__device__ __forceinline__ ParityPrefix parity_combine(ParityPrefix a, ParityPrefix b)
 {
-    __shared__ float sw[kChainTile];
-    __shared__ double sd[kChainTile];
+    return b.reset ? b : ParityPrefix{a.reset, a.x ^ b.x};
+}
+
+__global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
+                                                                     ResampleWs ws)
+{
+    __shared__ float sw[kSumsChunk];
+    __shared__ unsigned long long red_sum[kSumsThreads / 32];
+    __shared__ ParityPrefix red_par[kSumsThreads / 32];
+    __shared__ double s_s, s_prev;
+    __shared__ int s_pos, s_e;
     if (*ws.exact_ok) return;
-    double s = 0.0;
-    for (int base = 0; base < M; base += kChainTile) {
-        const int t = min(kChainTile, M - base);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_s = 0.0;
+    for (int c0 = 0; c0 < M; c0 += kSumsChunk) {
+        const int t = min(kSumsChunk, M - c0);
         bool bad = false;
-        for (int i = threadIdx.x; i < t; i += blockDim.x) {
-            const float x = w[(size_t)(base + i) * stride];
-            bad |= !(x >= 0.0f) || !(fabsf(x) < INFINITY);
+        for (int i = tid; i < t; i += kSumsThreads) {
+            const float x = w[(size_t)(c0 + i) * stride];
+            bad |= !(x >= 0.0f) || !(x < INFINITY);
             sw[i] = x;
         }
+        if (tid == 0) s_pos = 0;
         if (__syncthreads_or(bad ? 1 : 0)) {
-            if (threadIdx.x == 0) *ws.serial = 1;
+            if (tid == 0) *ws.serial = 1;
             return;
         }
-        if (threadIdx.x == 0) {
-#pragma unroll 8
-            for (int i = 0; i < t; ++i) {
-                s += (double)sw[i];
-                sd[i] = s;
+        for (int guard = 0; guard <= kSumsChunk; ++guard) {   // one pass per event: at most t + 1
+            const int pos = s_pos;
+            if (pos >= t) break;
+            const double s = s_s;
+            if (tid == 0) s_e = t;
+            __syncthreads();
+            if (s == 0.0) {   // leading zero weights keep the sum 0; the first positive one is the sum
+                for (int i = pos + tid; i < t; i += kSumsThreads)
+                    if (sw[i] > 0.0f) atomicMin(&s_e, i);
+                __syncthreads();
+                const int z = s_e;
+                for (int i = pos + tid; i < z; i += kSumsThreads) ws.sums[c0 + i] = 0.0;
+                if (tid == 0) {
+                    if (z < t) {
+                        s_s = (double)sw[z];
+                        ws.sums[c0 + z] = s_s;
+                    }
+                    s_pos = z < t ? z + 1 : t;
+                }
+                __syncthreads();
+                continue;
             }
+            const int b = (int)((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;   // s in [2^b, 2^(b+1))
+            const double u = pow2(b - 52), uinv = pow2(52 - b), top = pow2(b + 1);
+            const unsigned long long P0 = (unsigned long long)(s * uinv);   // in [2^52, 2^53)
+            const unsigned long long LIM = 1ull << 53;
+            unsigned long long q[kSumsItems], r[kSumsItems];
+            bool tie[kSumsItems], big[kSumsItems], valid[kSumsItems];
+            ParityPrefix agg{0u, 0u};
+            for (int j = 0; j < kSumsItems; ++j) {
+                const int i = pos + kSumsItems * tid + j;
+                valid[j] = i < t;
+                const double wd = valid[j] ? (double)sw[i] : 0.0;
+                big[j] = valid[j] && wd >= top;
+                q[j] = 0;
+                r[j] = 0;
+                tie[j] = false;
+                if (valid[j] && !big[j]) {
+                    const double tt = wd * uinv;   // exact scaling
+                    q[j] = (unsigned long long)tt;
+                    const double f = tt - (double)q[j];
+                    tie[j] = f == 0.5;
+                    r[j] = q[j] + (f > 0.5 ? 1ull : 0ull);
+                }
+                agg = parity_combine(agg, tie[j] ? ParityPrefix{1u, 0u} : ParityPrefix{0u, (uint32_t)(r[j] & 1)});
+            }
+            // exclusive segmented-XOR scan of the threads' aggregates
+            ParityPrefix px = agg;
+            for (int o = 1; o < 32; o <<= 1) {
+                ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, o), __shfl_up_sync(0xffffffffu, px.x, o)};
+                if (lane >= o) px = parity_combine(y, px);
+            }
+            if (lane == 31) red_par[warp] = px;
+            __syncthreads();
+            ParityPrefix before{0u, 0u};
+            for (int k = 0; k < warp; ++k) before = parity_combine(before, red_par[k]);
+            {
+                ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, 1), __shfl_up_sync(0xffffffffu, px.x, 1)};
+                if (lane > 0) before = parity_combine(before, y);
+            }
+            uint32_t par = before.reset ? before.x : (uint32_t)(P0 & 1) ^ before.x;   // parity before the first item
+            unsigned long long tsum = 0;
+            for (int j = 0; j < kSumsItems; ++j) {
+                if (tie[j]) {   // round half to even: +1 when the sum before plus q is odd
+                    r[j] = q[j] + ((par ^ (uint32_t)(q[j] & 1)) & 1u);
+                    par = 0u;
+                } else {
+                    par ^= (uint32_t)(r[j] & 1);
+                }
+                if (r[j] > LIM) r[j] = LIM;   // the sum leaves the binade there anyway
+                tsum += r[j];
+            }
+            // exclusive sum scan of the threads' increments
+            unsigned long long xs = tsum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, xs, o);
+                if (lane >= o) xs += y;
+            }
+            if (lane == 31) red_sum[warp] = xs;
+            __syncthreads();
+            unsigned long long run = xs - tsum;
+            for (int k = 0; k < warp; ++k) run += red_sum[k];
+            unsigned long long incl[kSumsItems];
+            for (int j = 0; j < kSumsItems; ++j) {
+                const int i = pos + kSumsItems * tid + j;
+                if (valid[j] && (big[j] || P0 + run + q[j] >= LIM)) atomicMin(&s_e, i);   // leaves the binade
+                run += r[j];
+                incl[j] = run;
+            }
+            __syncthreads();
+            const int e = s_e;
+            for (int j = 0; j < kSumsItems; ++j) {
+                const int i = pos + kSumsItems * tid + j;
+                if (i < e) ws.sums[c0 + i] = (double)(P0 + incl[j]) * u;
+                if (i == e - 1) s_prev = (double)(P0 + incl[j]) * u;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                const double prev = e > pos ? s_prev : s;
+                if (e < t) {
+                    const double nx = prev + (double)sw[e];   // one ordinary double addition
+                    ws.sums[c0 + e] = nx;
+                    s_s = nx;
+                    s_pos = e + 1;
+                } else {
+                    s_s = prev;
+                    s_pos = t;
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < t; i += blockDim.x) ws.sums[base + i] = sd[i];
         __syncthreads();
     }
 }
@@ -1302,6 +1431,32 @@ __global__ void resample_scatter_kernel(const float* particles, int M, const uin
 
 __global__ void set_int_kernel(int* p, int v) { *p = v; }
 
+// Best particle of mcl_3d.cpp:382-394: the first index with the largest weight
+// above 0 (strict comparison from max_value = 0).  Keys (weight bits, ~index)
+// order positive floats by value and equal weights by the lower index.
+__global__ void best_particle_kernel(const float* particles, int M, unsigned long long* key)
+{
+    unsigned long long best = 0ull;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        const float w = particles[7 * (size_t)i + 6];
+        if (w > 0.0f) {
+            const unsigned long long k = ((unsigned long long)__float_as_uint(w) << 32) | (0xffffffffu - (uint32_t)i);
+            best = k > best ? k : best;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, best, o);
+        best = y > best ? y : best;
+    }
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(key, best);
+}
+
+__global__ void best_index_kernel(const unsigned long long* key, uint32_t* index_out)
+{
+    const unsigned long long k = *key;
+    *index_out = k ? 0xffffffffu - (uint32_t)(k & 0xffffffffu) : 0xffffffffu;
+}
+
 // Carries a per-evaluation error into the context's sticky status word.
 __global__ void fold_status_kernel(int32_t* ev, int32_t* sticky)
 {
@@ -1524,7 +1679,7 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     resample_assign_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out, ws,
                                                   status);
     // exact fallbacks: serial double sums + parallel assignment, else the literal loop
-    resample_sums_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, ws);
+    resample_sums_kernel<<<1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
     resample_segments_sums_kernel<<<1, 32, 0, s>>>((int)M, u0, ws);
     resample_assign_sums_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out,
                                                        ws, status);
@@ -1550,6 +1705,19 @@ int launch_resample_residual(const float* particles, const float* w, int stride,
                                                                          nullptr, out, idx_out, (long long)cap,
                                                                          count_out, status);
     g_launches += 3;
+    return check(cudaGetLastError());
+}
+
+int launch_best_particle(const float* particles, size_t M, unsigned long long* key, uint32_t* index_out, int sm_count,
+                         cudaStream_t s)
+{
+    cudaMemsetAsync(key, 0, sizeof(unsigned long long), s);
+    unsigned blocks = (unsigned)((M + 255) / 256);
+    if (blocks > (unsigned)(4 * sm_count)) blocks = (unsigned)(4 * sm_count);
+    if (blocks == 0) blocks = 1;
+    best_particle_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, key);
+    best_index_kernel<<<1, 1, 0, s>>>(key, index_out);
+    g_launches += 2;
     return check(cudaGetLastError());
 }
 

@@ -182,6 +182,8 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
 int launch_resample_residual(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
                              uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
                              cudaStream_t s);
+int launch_best_particle(const float* particles, size_t M, unsigned long long* key, uint32_t* index_out, int sm_count,
+                         cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
 // Fills the compact layout: brick b (of n) copies sub3 codes from codes[src[b]]

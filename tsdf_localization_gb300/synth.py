@@ -160,6 +160,19 @@ def room_workload(seed: int = 1, n_particles: int = 1000, n_points: int = 2048) 
     return make_workload(ROOM, seed, 64, n_points, n_particles, 16, 1024, edge=64, name="room20x20x4@0.064")
 
 
+def global_workload(seed: int = 3, n_particles: int = 1_000_000, n_points: int = 2048) -> Workload:
+    """Global localisation in the 100x100x10 m building at 0.05 m: a 2,048-point
+    scan (64x2048 ray-cast, 1 % dropouts) and particles uniform over free space
+    (0.3 m clearance, sensor heights of the lower storey), yaw uniform, roll and
+    pitch within +-3 deg."""
+    wl = building_workload(seed=seed, n_particles=1, n_points=n_points)
+    w = World(BUILDING, seed)
+    z = float(wl.true_pose[2])
+    parts = w.particles_free_space(n_particles, 0.3, z - 0.3, z + 0.3, float(np.deg2rad(3.0)), seed + 7)
+    return Workload("building100x100x10@0.05/global", wl.coef, wl.grid_occ, wl.codes, wl.points, parts, wl.tf,
+                    wl.true_pose, wl.voxel_mm, dict(wl.extra, global_particles=n_particles))
+
+
 def building_workload(seed: int = 2, n_particles: int = 100_000, n_points: int = 8192) -> Workload:
     """100x100x10 m building at 0.05 m in sparse 8^3 bricks, 64x2048 scan with 1%
     dropouts reduced to n_points, particles with sigma 0.3 m / 5 deg."""
