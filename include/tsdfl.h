@@ -198,6 +198,41 @@ int tsdfl_resample_residual_systematic_device(tsdfl_ctx* ctx, const float* d_par
  * where the reference would index with -1).  d_particles: M x 7 floats. */
 int tsdfl_best_particle_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint32_t* d_index);
 
+/* ---- scan reduction ----
+ * The pre-processing of TSDFEvaluator::evaluateParticles
+ * (tsdf_evaluator.cpp:304-376) on a PointCloud2's data: points closer than
+ * 1 m are dropped; of the kept points sharing (ring, reduction cell centre)
+ * the first stays; the survivors come out ring by ring (0..63), in cloud
+ * order within a ring, as their original x, y, z (N x 3 floats, the points
+ * argument of tsdfl_evaluate).  Same points in the same order as the reference.
+ * cloud: n_points records of point_step bytes; x, y, z are consecutive floats
+ *   at x_offset (iter_x[0..2], :313-315), the ring an int16 at ring_offset.
+ * cell: reduction_cell_size (> 0), centre = floor(v / cell) * cell + cell / 2.
+ * The k-th kept point takes the ring field of the k-th cloud point, as the
+ * reference's ring iterator does (:319-332); TSDFL_SCAN_OWN_RING takes the
+ * point's own ring instead.  A ring outside [0, 64) gives
+ * TSDFL_ERR_INVALID_ARG (the reference indexes past its 64 ring lists).
+ * Writes min(count, cap) points; count > cap gives TSDFL_ERR_CAPACITY with
+ * *count_out still the full count. */
+#define TSDFL_SCAN_OWN_RING 1u
+int tsdfl_reduce_scan(tsdfl_ctx* ctx, const void* cloud, size_t n_points, uint32_t point_step, uint32_t x_offset,
+                      uint32_t ring_offset, float cell, uint32_t flags, float* points_out, size_t cap,
+                      size_t* count_out);
+/* Device form: d_cloud and d_points_out on the device, the count written to
+ * *d_count (device); stream-ordered, device-side errors by tsdfl_ctx_sync. */
+int tsdfl_reduce_scan_device(tsdfl_ctx* ctx, const void* d_cloud, size_t n_points, uint32_t point_step,
+                             uint32_t x_offset, uint32_t ring_offset, float cell, uint32_t flags,
+                             float* d_points_out, size_t cap, uint32_t* d_count);
+/* TSDFEvaluator::evaluateParticles (tsdf_evaluator.cpp:247-376) after its tf
+ * lookup: the scan reduction above and tsdfl_evaluate on the reduced points,
+ * with the cloud copied to the device once and the reduced points kept there.
+ * scan_flags: TSDFL_SCAN_*; flags: TSDFL_SUM_* / TSDFL_EVAL_*.  *n_reduced
+ * (optional) receives the number of reduced points. */
+int tsdfl_evaluate_cloud(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles, size_t P,
+                         const void* cloud, size_t n_points, uint32_t point_step, uint32_t x_offset,
+                         uint32_t ring_offset, float cell, uint32_t scan_flags, const float tf[16], uint32_t flags,
+                         float pose_out[6], size_t* n_reduced);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about

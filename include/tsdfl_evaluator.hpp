@@ -9,6 +9,8 @@
  *       (include/tsdf_localization/resampling/novel_resampling.h:38-74)
  *   tsdf_localization::GpuResidualSystematicResampler replaces
  *       ResidualSystematicResampler (novel_resampling.h:76-104)
+ *   tsdf_localization::gpu_reduce_scan replaces the scan reduction block of
+ *       TSDFEvaluator::evaluateParticles (src/evaluation/tsdf_evaluator.cpp:304-374)
  *
  * Errors surface as std::runtime_error carrying libtsdfl's message, as the
  * reference's evaluators throw them ("No particle is valid!" for a zero
@@ -117,6 +119,30 @@ public:
         return true;
     }
 
+    // The scan reduction (ScanReducer) and evaluate() in one call on a
+    // PointCloud2's data; false when no point survives the reduction.
+    template <class ParticleT>
+    bool evaluate_cloud(std::vector<ParticleT>& particles, const void* data, size_t n_points, uint32_t point_step,
+                        uint32_t x_offset, uint32_t ring_offset, float reduction_cell_size, uint32_t scan_flags,
+                        const float tf[16], Pose6* pose, size_t* n_reduced = nullptr)
+    {
+        parts_.resize(7 * (particles.size() ? particles.size() : 1));
+        for (size_t i = 0; i < particles.size(); ++i) {
+            for (int k = 0; k < 6; ++k) parts_[7 * i + k] = particles[i].first[k];
+            parts_[7 * i + 6] = particles[i].second;
+        }
+        float out[6];
+        size_t m = 0;
+        check(tsdfl_evaluate_cloud(ctx_.get(), map_.get(), &model_, parts_.data(), particles.size(), data, n_points,
+                                   point_step, x_offset, ring_offset, reduction_cell_size, scan_flags, tf, flags_,
+                                   out, &m));
+        if (n_reduced) *n_reduced = m;
+        if (m == 0) return false;
+        for (size_t i = 0; i < particles.size(); ++i) particles[i].second = parts_[7 * i + 6];
+        if (pose) *pose = Pose6{out[0], out[1], out[2], out[3], out[4], out[5]};
+        return true;
+    }
+
 private:
     Context& ctx_;
     Map& map_;
@@ -170,6 +196,48 @@ void resample_residual_systematic(Context& ctx, std::vector<ParticleT>& particle
     particles = std::move(out);
 }
 
+// The scan reduction of TSDFEvaluator::evaluateParticles
+// (tsdf_evaluator.cpp:304-376) on the device: the points it hands to evaluate,
+// in its order, from a PointCloud2's data.
+class ScanReducer {
+public:
+    ScanReducer(Context& ctx, float reduction_cell_size = 0.064f, uint32_t flags = 0)
+        : ctx_(ctx), cell_(reduction_cell_size), flags_(flags)
+    {
+    }
+
+    float cell() const { return cell_; }
+    uint32_t flags() const { return flags_; }
+
+    // data: n_points records of point_step bytes, x, y, z floats at x_offset,
+    // the ring an int16 at ring_offset.
+    template <class PointT>
+    std::vector<PointT> reduce(const void* data, size_t n_points, uint32_t point_step, uint32_t x_offset,
+                               uint32_t ring_offset)
+    {
+        buf_.resize(3 * (n_points ? n_points : 1));
+        size_t m = 0;
+        check(tsdfl_reduce_scan(ctx_.get(), data, n_points, point_step, x_offset, ring_offset, cell_, flags_,
+                                buf_.data(), n_points, &m));
+        std::vector<PointT> out;
+        out.reserve(m);
+        for (size_t i = 0; i < m; ++i) {
+            PointT p;
+            p.x = buf_[3 * i];
+            p.y = buf_[3 * i + 1];
+            p.z = buf_[3 * i + 2];
+            out.push_back(p);
+        }
+        return out;
+    }
+
+private:
+    Context& ctx_;
+    float cell_;
+    uint32_t flags_;
+    std::vector<float> buf_;
+};
+
 // Cell-centre reduction of a scan as CudaEvaluator's point-cloud overload
 // performs it (cuda_evaluator.cu:77-115): every point maps to the centre of its
 // 0.064 m cell, each centre kept once.  Order does not matter downstream: the
@@ -207,6 +275,23 @@ std::vector<PointT> reduce_to_cells(const std::vector<PointT>& points)
 
 namespace tsdf_localization {
 
+// Byte offset of a PointCloud2 field; a missing field throws as
+// PointCloud2ConstIterator's constructor does.
+inline uint32_t tsdfl_field_offset(const sensor_msgs::PointCloud2& cloud, const std::string& name)
+{
+    for (const auto& f : cloud.fields)
+        if (f.name == name) return f.offset;
+    throw std::runtime_error("Field " + name + " does not exist");
+}
+
+// The points TSDFEvaluator::evaluateParticles scores (its ordered_points,
+// tsdf_evaluator.cpp:304-374), reduced on the device: same points, same order.
+inline std::vector<CudaPoint> gpu_reduce_scan(tsdfl::ScanReducer& reducer, const sensor_msgs::PointCloud2& cloud)
+{
+    return reducer.reduce<CudaPoint>(cloud.data.data(), (size_t)cloud.width * cloud.height, cloud.point_step,
+                                     tsdfl_field_offset(cloud, "x"), tsdfl_field_offset(cloud, "ring"));
+}
+
 // Drop-in for CudaEvaluator: same constructor arguments (per_point is accepted;
 // both reference modes give the same weights here) and the same two evaluate
 // overloads.  The map's slots are copied to the device once, here.
@@ -241,6 +326,30 @@ public:
         geometry_msgs::PoseWithCovariance out;
         tsdfl::Pose6 p;
         if (!update_->evaluate(particles, points, tf_matrix, &p)) return out;
+        return to_msg(p);
+    }
+
+    // TSDFEvaluator::evaluateParticles after its tf lookup
+    // (tsdf_evaluator.cpp:304-376): the scan reduction and the update in one
+    // call, the reduced points staying on the device.
+    geometry_msgs::PoseWithCovariance evaluateCloud(std::vector<Particle>& particles,
+                                                    const sensor_msgs::PointCloud2& cloud, FLOAT_T tf_matrix[16],
+                                                    FLOAT_T reduction_cell_size = 0.064, uint32_t scan_flags = 0)
+    {
+        geometry_msgs::PoseWithCovariance out;
+        tsdfl::Pose6 p;
+        if (!update_->evaluate_cloud(particles, cloud.data.data(), (size_t)cloud.width * cloud.height,
+                                     cloud.point_step, tsdfl_field_offset(cloud, "x"),
+                                     tsdfl_field_offset(cloud, "ring"), reduction_cell_size, scan_flags, tf_matrix,
+                                     &p))
+            return out;
+        return to_msg(p);
+    }
+
+private:
+    static geometry_msgs::PoseWithCovariance to_msg(const tsdfl::Pose6& p)
+    {
+        geometry_msgs::PoseWithCovariance out;
         out.pose.position.x = p.x;
         out.pose.position.y = p.y;
         out.pose.position.z = p.z;

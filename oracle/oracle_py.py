@@ -73,6 +73,8 @@ def oracle() -> C.CDLL:
                                                 C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
         L.orc_resample_systematic.restype = SZ
         L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
+        L.orc_reduce_scan.restype = SZ
+        L.orc_reduce_scan.argtypes = [P, P, SZ, C.c_float, C.c_int, P, SZ]
         L.orc_resample_residual_systematic.restype = SZ
         L.orc_resample_residual_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
         _orc = L
@@ -112,6 +114,8 @@ def reference() -> C.CDLL:
         L.ref_draw_u01.argtypes = [C.c_uint32]
         L.ref_resample_residual_systematic.restype = SZ
         L.ref_resample_residual_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
+        L.ref_reduce_scan.restype = SZ
+        L.ref_reduce_scan.argtypes = [P, P, SZ, C.c_float, P, SZ]
         L.ref_omp_threads.restype = C.c_int
         _ref = L
     return _ref
@@ -226,6 +230,27 @@ def resample_residual_systematic(weights: np.ndarray, u0: float, cap: int | None
     if n == (1 << 64) - 1:
         raise RuntimeError("a particle count reaches 2^32")
     return out[: min(n, cap)] if n > cap else out[:n]
+
+
+def reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064, own_ring: bool = False) -> np.ndarray:
+    """tsdf_evaluator.cpp:304-376: the reduced points, ring-major, cloud order."""
+    x = np.ascontiguousarray(xyz, np.float32)
+    r = np.ascontiguousarray(ring, np.int16)
+    out = np.zeros((max(x.shape[0], 1), 3), np.float32)
+    n = oracle().orc_reduce_scan(_ptr(x), _ptr(r), x.shape[0], np.float32(cell), int(own_ring), _ptr(out),
+                                 out.shape[0])
+    if n == (1 << 64) - 1:
+        raise ValueError("ring outside [0, 64)")
+    return out[:n].copy()
+
+
+def ref_reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064) -> np.ndarray:
+    """The reference's own evaluateParticles reduction (oracle/_ref)."""
+    x = np.ascontiguousarray(xyz, np.float32)
+    r = np.ascontiguousarray(ring, np.int16)
+    out = np.zeros((max(x.shape[0], 1), 3), np.float32)
+    n = reference().ref_reduce_scan(_ptr(x), _ptr(r), x.shape[0], np.float32(cell), _ptr(out), out.shape[0])
+    return out[:n].copy()
 
 
 def likelihood_value(mm: int, sigma: float = 0.1) -> float:

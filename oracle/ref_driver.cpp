@@ -74,6 +74,19 @@ struct ProbeEvaluator : TSDFEvaluator {
     }
 };
 
+// Captures the point list evaluateParticles hands to evaluate (its scan
+// reduction, tsdf_evaluator.cpp:300-376) instead of scoring it.
+struct ScanProbe : TSDFEvaluator {
+    using TSDFEvaluator::TSDFEvaluator;
+    std::vector<CudaPoint> captured;
+    geometry_msgs::PoseWithCovariance evaluate(std::vector<Particle>&, const std::vector<CudaPoint>& points,
+                                               FLOAT_T*, bool) override
+    {
+        captured = points;
+        return geometry_msgs::PoseWithCovariance();
+    }
+};
+
 struct SeededSystematic : SystematicResampler {
     explicit SeededSystematic(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
 };
@@ -241,6 +254,40 @@ size_t ref_resample_residual_systematic(const float* w, size_t M, uint32_t seed,
     size_t n = cloud.particles().size();
     for (size_t i = 0; i < n && i < cap; ++i) idx_out[i] = (uint32_t)cloud.particles()[i].first[0];
     return n;
+}
+
+// TSDFEvaluator::evaluateParticles' scan reduction (ignore_tf) on a cloud with
+// float fields x, y, z and a short field ring; writes the reduced points in the
+// order evaluate receives them.  Returns their number.
+size_t ref_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float cell, float* out, size_t cap)
+{
+    auto map = std::make_shared<Map>(0.0f, 0.0f, 0.0f, 1.0f, 1.0f, 1.0f, 0.1f, 0.0f);
+    ScanProbe ev(map, false, 0.9f, 0.1f, 0.0f, 100.0f, cell);
+    sensor_msgs::PointCloud2 cloud;
+    cloud.height = 1;
+    cloud.width = (uint32_t)n;
+    cloud.point_step = 16;
+    cloud.row_step = 16 * (uint32_t)n;
+    const char* names[4] = {"x", "y", "z", "ring"};
+    for (int f = 0; f < 4; ++f) {
+        sensor_msgs::PointField pf;
+        pf.name = names[f];
+        pf.offset = 4 * f;
+        cloud.fields.push_back(pf);
+    }
+    cloud.data.resize(16 * n);
+    for (size_t i = 0; i < n; ++i) {
+        std::memcpy(&cloud.data[16 * i], xyz + 3 * i, 12);
+        std::memcpy(&cloud.data[16 * i + 12], ring + i, 2);
+    }
+    ParticleCloud pc;
+    ev.evaluateParticles(pc, cloud, "base", "scan", false, true);
+    for (size_t i = 0; i < ev.captured.size() && i < cap; ++i) {
+        out[3 * i] = ev.captured[i].x;
+        out[3 * i + 1] = ev.captured[i].y;
+        out[3 * i + 2] = ev.captured[i].z;
+    }
+    return ev.captured.size();
 }
 
 int ref_omp_threads(void) { return (int)OMP_THREADS; }

@@ -389,3 +389,67 @@ size_t orc_resample_residual_systematic(const float* w, size_t M, float u0, uint
     }
     return n;
 }
+
+/* tsdf_evaluator.cpp:300-376 */
+typedef struct {
+    int32_t ring, index;
+    float cx, cy, cz;
+    size_t src;
+} orc_scan_pt;
+
+static int orc_scan_key_cmp(const void* a, const void* b)
+{
+    const orc_scan_pt* p = (const orc_scan_pt*)a;
+    const orc_scan_pt* q = (const orc_scan_pt*)b;
+    uint32_t pb[3], qb[3];
+    memcpy(&pb[0], &p->cx, 4); memcpy(&pb[1], &p->cy, 4); memcpy(&pb[2], &p->cz, 4);
+    memcpy(&qb[0], &q->cx, 4); memcpy(&qb[1], &q->cy, 4); memcpy(&qb[2], &q->cz, 4);
+    if (p->ring != q->ring) return p->ring < q->ring ? -1 : 1;
+    for (int k = 0; k < 3; ++k)
+        if (pb[k] != qb[k]) return pb[k] < qb[k] ? -1 : 1;
+    return p->index < q->index ? -1 : (p->index > q->index ? 1 : 0);
+}
+
+static int orc_scan_out_cmp(const void* a, const void* b)
+{
+    const orc_scan_pt* p = (const orc_scan_pt*)a;
+    const orc_scan_pt* q = (const orc_scan_pt*)b;
+    if (p->ring != q->ring) return p->ring < q->ring ? -1 : 1;
+    return p->index < q->index ? -1 : (p->index > q->index ? 1 : 0);
+}
+
+size_t orc_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float cell, int own_ring, float* out,
+                       size_t cap)
+{
+    const float half = cell / 2;
+    orc_scan_pt* pts = (orc_scan_pt*)malloc(sizeof(orc_scan_pt) * (n ? n : 1));
+    size_t k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        const float dist = sqrtf(x * x + y * y + z * z);
+        if (dist < 1.0) continue;
+        orc_scan_pt p;
+        p.ring = own_ring ? ring[i] : ring[k];   /* the ring iterator advances once per kept point */
+        p.index = (int32_t)k;
+        p.cx = floorf(x / cell) * cell + half;
+        p.cy = floorf(y / cell) * cell + half;
+        p.cz = floorf(z / cell) * cell + half;
+        p.src = i;
+        if (p.ring < 0 || p.ring >= 64) { free(pts); return (size_t)-1; }
+        pts[k++] = p;
+    }
+    /* first (lowest index) of every (ring, centre); NaN centres never compare equal */
+    qsort(pts, k, sizeof(orc_scan_pt), orc_scan_key_cmp);
+    size_t m = 0;
+    for (size_t t = 0; t < k; ++t) {
+        int nan = pts[t].cx != pts[t].cx || pts[t].cy != pts[t].cy || pts[t].cz != pts[t].cz;
+        if (t > 0 && !nan && pts[t].ring == pts[t - 1].ring && pts[t].cx == pts[t - 1].cx &&
+            pts[t].cy == pts[t - 1].cy && pts[t].cz == pts[t - 1].cz)
+            continue;
+        pts[m++] = pts[t];
+    }
+    qsort(pts, m, sizeof(orc_scan_pt), orc_scan_out_cmp);
+    for (size_t t = 0; t < m && t < cap; ++t) memcpy(out + 3 * t, xyz + 3 * pts[t].src, 12);
+    free(pts);
+    return m;
+}

@@ -112,6 +112,18 @@ uint64_t orc_d2u_x86(double v);
  * reaches 2^32 (the reference would try to allocate it). */
 size_t orc_resample_residual_systematic(const float* w, size_t M, float u0, uint32_t* idx_out, size_t cap);
 
+/* The scan reduction of TSDFEvaluator::evaluateParticles
+ * (tsdf_evaluator.cpp:300-376): points closer than 1 m (float sqrt of the float
+ * sum of squares) are dropped; the k-th kept point takes ring[k] (the ring
+ * iterator advances only for kept points) and index k; the first kept point of
+ * every (ring, cell centre) stays, centre = floor(v / cell) * cell + cell / 2 in
+ * float per axis; the survivors come out ring by ring (0..63), by index within a
+ * ring, with their original coordinates.  Returns the number of survivors, or
+ * (size_t)-1 for a ring outside [0, 64) (the reference indexes past its table).
+ * own_ring != 0: every kept point takes its own ring instead. */
+size_t orc_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float cell, int own_ring, float* out,
+                       size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,8 +7,10 @@ points, sensor transform, query points, weight vectors, generator seeds) and
 what the reference computes from them: the map's coefficients and brick table
 and a digest of its slots (CudaSubVoxelMap ctor + setData), getEntry at the
 query points, TSDFEvaluator::evaluate's un-normalised and normalised weights,
-laser poses and mean pose (serial, in point order), and SystematicResampler's
-and ResidualSystematicResampler's output indices for seeded draws.
+laser poses and mean pose (serial, in point order), SystematicResampler's
+and ResidualSystematicResampler's output indices for seeded draws, and the
+point list TSDFEvaluator::evaluateParticles' scan reduction hands to evaluate
+for a set of clouds (x, y, z, ring).
 
     python tests/golden/make_golden.py
 """
@@ -107,6 +109,55 @@ def resample_case(seed):
     return out
 
 
+def scan_cloud(kind, rng):
+    """A cloud (xyz float32, ring int16) of one of several kinds."""
+    if kind == "lidar":
+        # 16 rings x 200 columns on walls 2-9 m away, some returns inside 1 m
+        rings, cols = 16, 200
+        el = np.deg2rad(np.linspace(-15, 15, rings))[:, None]
+        az = np.linspace(-np.pi, np.pi, cols, endpoint=False)[None, :]
+        r = rng.uniform(2.0, 9.0, (rings, cols))
+        r[rng.random((rings, cols)) < 0.05] = rng.uniform(0.2, 1.2, 1)[0]
+        xyz = np.stack([r * np.cos(el) * np.cos(az), r * np.cos(el) * np.sin(az), r * np.sin(el)], -1)
+        ring = np.broadcast_to(np.arange(rings)[:, None], (rings, cols))
+        # column-major order, as a spinning sensor emits it
+        return xyz.transpose(1, 0, 2).reshape(-1, 3).astype(np.float32), ring.T.reshape(-1).astype(np.int16)
+    if kind == "dense":
+        # many points per cell and ring: the first per (ring, cell) survives
+        d = rng.normal(0, 1, (2000, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        xyz = d * rng.uniform(1.0, 1.6, (2000, 1))
+        xyz = (np.round(xyz * 4) / 4 + 0.025 + rng.uniform(-0.004, 0.004, xyz.shape)).astype(np.float32)
+        return xyz, rng.integers(0, 2, 2000).astype(np.int16)
+    if kind == "edge":
+        # points at |p| ~ 1 m, non-finite values, large and negative coordinates
+        n = 1500
+        d = rng.normal(0, 1, (n, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        xyz = (d * rng.choice([0.9999999, 1.0, 1.0000001, 1.5, 40.0], (n, 1))).astype(np.float32)
+        xyz[rng.random(n) < 0.03, 0] = np.nan
+        xyz[rng.random(n) < 0.01, 1] = np.inf
+        xyz[rng.random(n) < 0.01, 2] = -np.inf
+        big = rng.random(n) < 0.05
+        xyz[big] = rng.uniform(-3e6, 3e6, (big.sum(), 3)).astype(np.float32)
+        xyz[:50] = xyz[50:100]            # exact duplicates of other points
+        return xyz, rng.integers(0, 64, n).astype(np.int16)
+    raise ValueError(kind)
+
+
+def scan_case(seed):
+    rng = np.random.default_rng(seed)
+    out = {}
+    for kind, cell in (("lidar", 0.064), ("lidar", 0.25), ("dense", 0.05), ("edge", 0.064), ("edge", 0.5)):
+        xyz, ring = scan_cloud(kind, rng)
+        key = f"scan/{kind}_{int(round(cell * 1000)):04d}"
+        out[f"{key}/xyz"] = xyz
+        out[f"{key}/ring"] = ring
+        out[f"{key}/cell"] = np.float32(cell)
+        out[f"{key}/reduced"] = O.ref_reduce_scan(xyz, ring, cell)
+    return out
+
+
 def main():
     if not O.reference_available():
         raise SystemExit("oracle/_ref/libref.so is not built: the reference tree is needed")
@@ -114,6 +165,7 @@ def main():
     fx.update(map_case("map_0064", 0.064, (-1.3, -0.7, -0.45), (5.1, 4.3, 2.6), 6000, 11))
     fx.update(map_case("map_005", 0.05, (0.0, 0.0, 0.0), (4.2, 3.6, 2.2), 6000, 12))
     fx.update(resample_case(13))
+    fx.update(scan_case(14))
     np.savez_compressed(OUT / "reference_cases.npz", **fx)
     print("wrote", OUT / "reference_cases.npz", (OUT / "reference_cases.npz").stat().st_size, "bytes")
 

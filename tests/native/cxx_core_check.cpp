@@ -82,6 +82,23 @@ int main(int argc, char** argv)
             out[7 * i + 6] = parts[i].second;
         }
         save(d + "/resampled_out.bin", out.data(), out.size());
+        // scan reduction of a PointCloud2-style record array (x, y, z, ring)
+        auto cloud = load<char>(d + "/cloud.bin");
+        const size_t n_cloud = cloud.size() / 16;
+        tsdfl::ScanReducer reducer(ctx, 0.064f);
+        std::vector<MyPoint> red = reducer.reduce<MyPoint>(cloud.data(), n_cloud, 16, 0, 12);
+        save(d + "/reduced_out.bin", &red.data()->x, 3 * red.size());
+        std::vector<MyParticle> parts_c(pf.size() / 7);
+        for (size_t i = 0; i < parts_c.size(); ++i) {
+            for (int k = 0; k < 6; ++k) parts_c[i].first[k] = pf[7 * i + k];
+            parts_c[i].second = pf[7 * i + 6];
+        }
+        tsdfl::Pose6 pose_c;
+        size_t n_red = 0;
+        upd.evaluate_cloud(parts_c, cloud.data(), n_cloud, 16, 0, 12, 0.064f, 0, tf.data(), &pose_c, &n_red);
+        std::vector<float> wc(parts_c.size());
+        for (size_t i = 0; i < parts_c.size(); ++i) wc[i] = parts_c[i].second;
+        save(d + "/cloud_weights_out.bin", wc.data(), wc.size());
         bool threw = false;
         try {   // an empty cloud: the reference's "No particle is valid!"
             std::vector<MyParticle> none;
@@ -89,8 +106,8 @@ int main(int argc, char** argv)
         } catch (const std::runtime_error& e) {
             threw = std::string(e.what()).find("No particle is valid!") != std::string::npos;
         }
-        std::printf("cxx core ok P=%zu N=%zu resampled=%zu empty_cloud_throws=%d\n", w.size(), pts.size(), parts.size(),
-                    threw ? 1 : 0);
+        std::printf("cxx core ok P=%zu N=%zu resampled=%zu reduced=%zu/%zu empty_cloud_throws=%d\n", w.size(),
+                    pts.size(), parts.size(), red.size(), n_red, threw ? 1 : 0);
         return threw ? 0 : 4;
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());

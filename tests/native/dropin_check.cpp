@@ -10,6 +10,7 @@
 #include "tsdfl_evaluator.hpp"
 
 #include <cstdio>
+#include <cstring>
 #include <tuple>
 #include <vector>
 
@@ -47,6 +48,31 @@ int main()
         GpuResidualSystematicResampler rr(0);
         rr.resample(cloud);
         std::printf("residual resampled %zu\n", cloud.size());
+        // a PointCloud2 with the fields evaluateParticles reads
+        sensor_msgs::PointCloud2 pc;
+        pc.height = 1;
+        pc.width = 3;
+        pc.point_step = 16;
+        const char* names[4] = {"x", "y", "z", "ring"};
+        for (int f = 0; f < 4; ++f) {
+            sensor_msgs::PointField field;
+            field.name = names[f];
+            field.offset = 4 * f;
+            pc.fields.push_back(field);
+        }
+        const float xyz[3][3] = {{1.5f, 1.0f, 1.0f}, {1.5f, 1.0f, 1.0f}, {0.2f, 0.1f, 0.0f}};
+        pc.data.resize(48);
+        for (int i = 0; i < 3; ++i) {
+            std::memcpy(&pc.data[16 * i], xyz[i], 12);
+            const int16_t ring = 1;
+            std::memcpy(&pc.data[16 * i + 12], &ring, 2);
+        }
+        tsdfl::Context sctx(0);
+        tsdfl::ScanReducer reducer(sctx, 0.064f);
+        std::vector<CudaPoint> reduced = gpu_reduce_scan(reducer, pc);
+        std::printf("reduced %zu\n", reduced.size());
+        pose = ev.evaluateCloud(parts, pc, tf, 0.064f);
+        std::printf("cloud evaluated w0=%.9g\n", parts[0].second);
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         status = 0;

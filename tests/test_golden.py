@@ -80,3 +80,43 @@ def test_residual_resample_random_weights_match_reference():
         seed = int(rng.integers(1, 2 ** 31))
         assert np.array_equal(O.resample_residual_systematic(w, O.ref_draw_u01(seed), cap=4 * m + 16),
                               O.ref_resample_residual_systematic(w, seed, cap=4 * m + 16))
+
+
+SCANS = sorted({k.rsplit("/", 1)[0] for k in GOLD.files if k.startswith("scan/")})
+
+
+@pytest.mark.parametrize("case", SCANS)
+def test_scan_reduction_matches_reference(case):
+    got = O.reduce_scan(GOLD[f"{case}/xyz"], GOLD[f"{case}/ring"], float(GOLD[f"{case}/cell"]))
+    assert np.array_equal(got, GOLD[f"{case}/reduced"], equal_nan=True)
+
+
+def test_scan_reduction_random_clouds_match_reference():
+    if not O.reference_available():
+        pytest.skip("the reference sources are not on this machine")
+    rng = np.random.default_rng(21)
+    for t in range(30):
+        n = int(rng.integers(1, 3000))
+        x = rng.normal(0, 3, (n, 3)).astype(np.float32)
+        x[rng.random(n) < 0.05] = np.nan
+        x[rng.random(n) < 0.1] *= np.float32(0.1)
+        if t % 3 == 0:
+            x = (np.round(x * 8) / 8).astype(np.float32)
+        r = rng.integers(0, 64, n).astype(np.int16)
+        cell = float(rng.choice([0.05, 0.064, 0.2]))
+        assert np.array_equal(O.reduce_scan(x, r, cell), O.ref_reduce_scan(x, r, cell), equal_nan=True)
+
+
+def test_scan_reduction_ring_skip_and_errors():
+    # the k-th kept point takes the ring of the k-th cloud point
+    xyz = np.array([[0.1, 0, 0], [2, 0, 0], [2, 0, 0]], np.float32)
+    ring = np.array([5, 3, 63], np.int16)
+    got = O.reduce_scan(xyz, ring, 0.1)         # kept: #1 -> ring 5, #2 -> ring 3 (different rings)
+    assert got.shape == (2, 3)
+    assert O.reduce_scan(xyz, ring, 0.1, own_ring=True).shape == (2, 3)
+    ring2 = np.array([7, 7, 63], np.int16)      # both kept points get ring 7: one survives
+    assert O.reduce_scan(xyz, ring2, 0.1).shape == (1, 3)
+    assert O.reduce_scan(xyz, ring2, 0.1, own_ring=True).shape == (2, 3)
+    with pytest.raises(ValueError):
+        O.reduce_scan(xyz, np.array([64, 0, 0], np.int16), 0.1)
+    assert O.reduce_scan(np.zeros((0, 3), np.float32), np.zeros(0, np.int16), 0.1).shape == (0, 3)

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle_py as O
-from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator, synth
+from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator, pack_cloud, synth
 
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
@@ -34,6 +34,9 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     np.asarray(wl.tf, np.float32).tofile(tmp_path / "tf.bin")
     u1 = np.float32(0.618)
     np.array([u0, u1], np.float32).tofile(tmp_path / "u0.bin")
+    cxyz, cring = synth.World(synth.ROOM, 21).scan(wl.true_pose, 16, 700, sigma=0.01, dropout=0.02, seed=8)
+    cxyz[::37] *= np.float32(0.1)       # some returns inside 1 m
+    pack_cloud(cxyz, cring).tofile(tmp_path / "cloud.bin")
     res = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     print(res.stdout, res.stderr)
     assert res.returncode == 0, res.stdout + res.stderr
@@ -58,3 +61,10 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     assert np.array_equal(idx, O.resample_systematic(p[:, 6], float(u0)))
     ridx = O.resample_residual_systematic(p[:, 6], float(u1))
     assert np.array_equal(rr_cxx, p[ridx])
+
+    red = np.fromfile(tmp_path / "reduced_out.bin", np.float32).reshape(-1, 3)
+    want = O.reduce_scan(cxyz, cring, 0.064)
+    assert np.array_equal(red, want)
+    pc = wl.particles.copy()
+    TSDFEvaluator(dmap).evaluate(pc, want, wl.tf)
+    assert np.array_equal(np.fromfile(tmp_path / "cloud_weights_out.bin", np.float32), pc[:, 6])

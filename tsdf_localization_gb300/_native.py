@@ -24,6 +24,7 @@ TSDFL_MAP_FORCE_F32 = 2
 TSDFL_SUM_EXACT = 0
 TSDFL_SUM_SERIAL = 1
 TSDFL_EVAL_GENERIC = 4
+TSDFL_SCAN_OWN_RING = 1
 
 
 class MapCoef(C.Structure):
@@ -65,6 +66,7 @@ P = C.c_void_p
 SZ = C.c_size_t
 I = C.c_int
 F = C.c_float
+U32 = C.c_uint32
 
 # (name, restype, argtypes) of every entry point include/tsdfl.h declares
 SIGNATURES = [
@@ -96,6 +98,10 @@ SIGNATURES = [
     ("tsdfl_resample_residual_systematic", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_residual_systematic_device", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_best_particle_device", I, [P, P, SZ, P]),
+    ("tsdfl_reduce_scan", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, C.POINTER(SZ)]),
+    ("tsdfl_reduce_scan_device", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, P]),
+    ("tsdfl_evaluate_cloud", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, U32, U32, U32, F, U32, P, U32, P,
+                                 C.POINTER(SZ)]),
 ]
 
 SYNTH_SIGNATURES = [

@@ -66,6 +66,8 @@ struct tsdfl_ctx {
     size_t ws_bytes = 0;
     void* rs_ws = nullptr;       // resampling workspace
     size_t rs_bytes = 0;
+    void* scan_ws = nullptr;     // scan reduction workspace
+    size_t scan_bytes = 0;
     void* io = nullptr;          // device copies of host inputs (host API)
     size_t io_bytes = 0;
     int32_t* status = nullptr;   // [0] sticky status, [1] per-evaluation status
@@ -176,6 +178,41 @@ int ensure_resample_ws(tsdfl_ctx* c, size_t M)
     if (c->rs_ws) cudaFree(c->rs_ws);
     c->rs_ws = p;
     c->rs_bytes = need;
+    return TSDFL_OK;
+}
+
+int ensure_scan_ws(tsdfl_ctx* c, size_t n)
+{
+    size_t need = scan_workspace_bytes(n);
+    if (need <= c->scan_bytes) return TSDFL_OK;
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, need));
+    if (c->scan_ws) cudaFree(c->scan_ws);
+    c->scan_ws = p;
+    c->scan_bytes = need;
+    return TSDFL_OK;
+}
+
+// Arguments of the scan reduction (tsdfl_reduce_scan*).
+int check_scan_args(const char* fn, size_t n, uint32_t step, uint32_t x_offset, uint32_t ring_offset, float cell,
+                    uint32_t flags)
+{
+    if (n >= (1ull << 31)) {
+        set_error("%s: at most 2^31-1 cloud points", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    if ((uint64_t)x_offset + 12 > step || (uint64_t)ring_offset + 2 > step) {
+        set_error("%s: x, y, z (12 bytes at x_offset) and ring (2 bytes) must lie inside point_step", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (!(cell > 0.0f) || !std::isfinite(cell)) {
+        set_error("%s: cell must be positive and finite", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (flags & ~TSDFL_SCAN_OWN_RING) {
+        set_error("%s: unknown flags", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
     return TSDFL_OK;
 }
 
@@ -488,6 +525,7 @@ int tsdfl_ctx_destroy(tsdfl_ctx* c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->ws);
     cudaFree(c->rs_ws);
+    cudaFree(c->scan_ws);
     cudaFree(c->io);
     cudaFree(c->status);
     cudaFreeHost(c->h_status);
@@ -549,6 +587,7 @@ int tsdfl_ctx_sync(tsdfl_ctx* c)
     if (st == TSDFL_ERR_DEGENERATE) set_error("No particle is valid!");
     else if (st == TSDFL_ERR_TIMEOUT) set_error("a device wait timed out");
     else if (st == TSDFL_ERR_CAPACITY) set_error("output capacity exceeded");
+    else if (st == TSDFL_ERR_INVALID_ARG) set_error("invalid device input (a scan ring outside [0, 64))");
     else if (st) set_error("device status %d", st);
     return st;
 }
@@ -886,6 +925,126 @@ int tsdfl_best_particle_device(tsdfl_ctx* c, const float* d_particles, size_t M,
     // status words 2-3 hold the 64-bit reduction key
     return launch_best_particle(d_particles, M, reinterpret_cast<unsigned long long*>(c->status + 2), d_index,
                                 c->sm_count, c->stream);
+}
+
+int tsdfl_reduce_scan_device(tsdfl_ctx* c, const void* d_cloud, size_t n, uint32_t step, uint32_t x_offset,
+                             uint32_t ring_offset, float cell, uint32_t flags, float* d_points_out, size_t cap,
+                             uint32_t* d_count)
+{
+    if (!c || (n && !d_cloud) || (cap && !d_points_out) || !d_count) {
+        set_error("tsdfl_reduce_scan_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_scan_args("tsdfl_reduce_scan_device", n, step, x_offset, ring_offset, cell, flags);
+    if (rc) return rc;
+    rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_scan_ws(c, n);
+    if (rc) return rc;
+    return launch_reduce_scan(static_cast<const uint8_t*>(d_cloud), n, step, x_offset, ring_offset, cell,
+                              (flags & TSDFL_SCAN_OWN_RING) != 0, d_points_out, cap, d_count, c->scan_ws, c->status,
+                              c->stream);
+}
+
+int tsdfl_reduce_scan(tsdfl_ctx* c, const void* cloud, size_t n, uint32_t step, uint32_t x_offset,
+                      uint32_t ring_offset, float cell, uint32_t flags, float* points_out, size_t cap,
+                      size_t* count_out)
+{
+    if (!c || (n && !cloud) || (cap && !points_out) || !count_out) {
+        set_error("tsdfl_reduce_scan: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *count_out = 0;
+    int rc = check_scan_args("tsdfl_reduce_scan", n, step, x_offset, ring_offset, cell, flags);
+    if (rc) return rc;
+    if (n == 0) return TSDFL_OK;
+    rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_scan_ws(c, n);
+    if (rc) return rc;
+    const size_t cloud_b = align_up((size_t)step * n, 256);
+    const size_t out_b = align_up(sizeof(float) * 3 * (cap ? cap : 1), 256);
+    rc = ensure_io(c, cloud_b + out_b + 256);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    uint8_t* d_cloud = reinterpret_cast<uint8_t*>(io);
+    float* d_out = reinterpret_cast<float*>(io + cloud_b);
+    uint32_t* d_cnt = reinterpret_cast<uint32_t*>(io + cloud_b + out_b);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_cloud, cloud, (size_t)step * n, cudaMemcpyHostToDevice, s));
+    rc = launch_reduce_scan(d_cloud, n, step, x_offset, ring_offset, cell, (flags & TSDFL_SCAN_OWN_RING) != 0, d_out,
+                            cap, d_cnt, c->scan_ws, c->status, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->h_count, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    *count_out = c->h_count[0];
+    if (st && st != TSDFL_ERR_CAPACITY) return st;
+    size_t m = *count_out < cap ? *count_out : cap;
+    if (m) {
+        CUDA_TRY(cudaMemcpyAsync(points_out, d_out, sizeof(float) * 3 * m, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    return st;
+}
+
+int tsdfl_evaluate_cloud(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* particles, size_t P,
+                         const void* cloud, size_t n, uint32_t step, uint32_t x_offset, uint32_t ring_offset,
+                         float cell, uint32_t scan_flags, const float tf[16], uint32_t flags, float pose_out[6],
+                         size_t* n_reduced)
+{
+    if (n_reduced) *n_reduced = 0;
+    if (!c || !map || !tf || (P && !particles) || (n && !cloud)) {
+        set_error("tsdfl_evaluate_cloud: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(mdl);
+    if (rc) return rc;
+    rc = check_scan_args("tsdfl_evaluate_cloud", n, step, x_offset, ring_offset, cell, scan_flags);
+    if (rc) return rc;
+    if (n == 0) return TSDFL_OK;
+    if (P >= (1ull << 31)) {
+        set_error("tsdfl_evaluate_cloud: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    rc = set_device(c->device);
+    if (rc) return rc;
+    rc = ensure_scan_ws(c, n);
+    if (rc) return rc;
+    const size_t part_b = align_up(sizeof(float) * 7 * (P ? P : 1), 256);
+    const size_t cloud_b = align_up((size_t)step * n, 256);
+    const size_t pts_b = align_up(sizeof(float) * 3 * n, 256);
+    rc = ensure_io(c, part_b + cloud_b + pts_b + 512);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_part = reinterpret_cast<float*>(io);
+    uint8_t* d_cloud = reinterpret_cast<uint8_t*>(io + part_b);
+    float* d_pts = reinterpret_cast<float*>(io + part_b + cloud_b);
+    uint32_t* d_cnt = reinterpret_cast<uint32_t*>(io + part_b + cloud_b + pts_b);
+    float* d_pose = reinterpret_cast<float*>(io + part_b + cloud_b + pts_b + 256);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_cloud, cloud, (size_t)step * n, cudaMemcpyHostToDevice, s));
+    if (P) CUDA_TRY(cudaMemcpyAsync(d_part, particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice, s));
+    rc = launch_reduce_scan(d_cloud, n, step, x_offset, ring_offset, cell, (scan_flags & TSDFL_SCAN_OWN_RING) != 0,
+                            d_pts, n, d_cnt, c->scan_ws, c->status, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->h_count, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    if (st) return st;
+    const size_t N = c->h_count[0];
+    if (n_reduced) *n_reduced = N;
+    if (N == 0) return TSDFL_OK;
+    if (P == 0) {
+        set_error("No particle is valid!");
+        return TSDFL_ERR_DEGENERATE;
+    }
+    rc = run_eval(c, map, mdl, d_part, P, d_pts, N, tf, flags, d_pose, nullptr);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(particles, d_part, sizeof(float) * 7 * P, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(c->h_pose, d_pose, sizeof(float) * 6, cudaMemcpyDeviceToHost, s));
+    st = tsdfl_ctx_sync(c);
+    if (st) return st;
+    if (pose_out) std::memcpy(pose_out, c->h_pose, sizeof(float) * 6);
+    return TSDFL_OK;
 }
 
 }  // extern "C"

@@ -192,4 +192,10 @@ int launch_codes_from_floats(const float* data, size_t n, const float* code_valu
 int launch_compact_fill(const uint16_t* codes, const int64_t* src, const int64_t* dst, const uint8_t* skirt,
                         uint32_t n, uint32_t sub3, uint16_t* dense, cudaStream_t s);
 
+// Scan reduction of a PointCloud2 (scan.cu); workspace: scan_workspace_bytes(n).
+size_t scan_workspace_bytes(size_t n);
+int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t off_x, uint32_t off_ring, float cell,
+                       bool own_ring, float* out, size_t cap, uint32_t* count, void* workspace, int32_t* status,
+                       cudaStream_t s);
+
 }  // namespace tsdfl

@@ -149,6 +149,30 @@ class TSDFEvaluator:
         N.check(rc)
         return Pose(*[float(v) for v in pose])
 
+    def evaluate_cloud(self, particles: np.ndarray, cloud: np.ndarray, n_points: int, point_step: int, tf_matrix,
+                       x_offset: int = 0, ring_offset: int = 12, reduction_cell_size: float = 0.064,
+                       own_ring: bool = False):
+        """TSDFEvaluator::evaluateParticles (tsdf_evaluator.cpp:247-376) after its
+        tf lookup: reduces the PointCloud2 data on the GPU and scores the reduced
+        points.  Returns (pose or None, number of reduced points)."""
+        if not (isinstance(particles, np.ndarray) and particles.dtype == np.float32 and particles.flags.c_contiguous
+                and particles.ndim == 2 and particles.shape[1] == 7):
+            raise ValueError("particles must be a C-contiguous (P, 7) float32 array")
+        blob = np.ascontiguousarray(cloud, np.uint8).reshape(-1)
+        if blob.shape[0] < n_points * point_step:
+            raise ValueError("cloud holds fewer than n_points * point_step bytes")
+        tf = np.ascontiguousarray(np.asarray(tf_matrix, dtype=np.float32).reshape(16))
+        pose = np.zeros(6, dtype=np.float32)
+        nred = C.c_size_t(0)
+        N.check(N.lib().tsdfl_evaluate_cloud(self.ctx.handle, self.map.handle, C.byref(self.model), _ptr(particles),
+                                             particles.shape[0], _ptr(blob), n_points, point_step, x_offset,
+                                             ring_offset, reduction_cell_size,
+                                             N.TSDFL_SCAN_OWN_RING if own_ring else 0, _ptr(tf), self.flags,
+                                             _ptr(pose), C.byref(nred)))
+        if nred.value == 0:
+            return None, 0
+        return Pose(*[float(v) for v in pose]), nred.value
+
     def evaluate_debug(self, particles: np.ndarray, points: np.ndarray, tf_matrix, voxel_index: bool = False):
         """evaluate() plus per-particle raw weights, hit counts, laser poses and,
         for small cases, per particle*point: the slot index (serial sums, and
@@ -168,6 +192,54 @@ class TSDFEvaluator:
                                              P, _ptr(pts), Nn, _ptr(tf), self.flags, _ptr(pose), C.byref(dbg)))
         return {"pose": pose, "raw": raw, "hits": hits, "laser_pose": lp, "voxel_index": idx,
                 "weight_sum": dbg.weight_sum}
+
+
+def pack_cloud(xyz: np.ndarray, ring: np.ndarray, point_step: int = 16, x_offset: int = 0,
+               ring_offset: int = 12) -> np.ndarray:
+    """PointCloud2 data bytes: per point x, y, z floats at x_offset and an int16
+    ring at ring_offset, point_step bytes per point (other bytes zero)."""
+    x = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    r = np.ascontiguousarray(ring, np.int16).reshape(-1)
+    if r.shape[0] != x.shape[0]:
+        raise ValueError("xyz and ring differ in length")
+    if x_offset + 12 > point_step or ring_offset + 2 > point_step:
+        raise ValueError("fields must lie inside point_step")
+    if ring_offset + 2 > x_offset and x_offset + 12 > ring_offset:
+        raise ValueError("x, y, z and ring overlap")
+    blob = np.zeros((x.shape[0], point_step), np.uint8)
+    blob[:, x_offset:x_offset + 12] = x.view(np.uint8).reshape(-1, 12)
+    blob[:, ring_offset:ring_offset + 2] = r.view(np.uint8).reshape(-1, 2)
+    return blob.reshape(-1)
+
+
+class ScanReducer:
+    """The scan reduction of TSDFEvaluator::evaluateParticles
+    (tsdf_evaluator.cpp:304-376) on the GPU: range filter (< 1 m dropped),
+    first point per (ring, reduction cell), ring-major output in cloud order.
+    own_ring=False follows the reference's ring iterator, which advances only
+    for kept points (:319-332); True gives every point its own ring."""
+
+    def __init__(self, ctx: Context, reduction_cell_size: float = 0.064, own_ring: bool = False):
+        self.ctx = ctx
+        self.cell = float(reduction_cell_size)
+        self.flags = N.TSDFL_SCAN_OWN_RING if own_ring else 0
+
+    def reduce(self, cloud: np.ndarray, n_points: int, point_step: int, x_offset: int = 0,
+               ring_offset: int = 12) -> np.ndarray:
+        """cloud: the PointCloud2 data (uint8, n_points * point_step bytes).
+        Returns the reduced points as an (M, 3) float32 array."""
+        blob = np.ascontiguousarray(cloud, np.uint8).reshape(-1)
+        if blob.shape[0] < n_points * point_step:
+            raise ValueError("cloud holds fewer than n_points * point_step bytes")
+        out = np.zeros((max(n_points, 1), 3), np.float32)
+        cnt = C.c_size_t(0)
+        N.check(N.lib().tsdfl_reduce_scan(self.ctx.handle, _ptr(blob), n_points, point_step, x_offset, ring_offset,
+                                          self.cell, self.flags, _ptr(out), out.shape[0], C.byref(cnt)))
+        return out[:cnt.value].copy()
+
+    def reduce_xyz(self, xyz: np.ndarray, ring: np.ndarray) -> np.ndarray:
+        blob = pack_cloud(xyz, ring)
+        return self.reduce(blob, blob.shape[0] // 16, 16, 0, 12)
 
 
 class SystematicResampler:

@@ -74,7 +74,10 @@ class World:
 
 
 def reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064) -> np.ndarray:
-    """Scan reduction of tsdf_evaluator.cpp:304-376 (one point per ring and cell)."""
+    """Host scan reduction used to make synthetic workloads: one point per ring and
+    cell as in tsdf_evaluator.cpp:304-376, with every point's own ring (the
+    TSDFL_SCAN_OWN_RING form; the reference's ring iterator skips with the range
+    filter)."""
     lib = N.synth_lib()
     x = np.ascontiguousarray(xyz, np.float32)
     r = np.ascontiguousarray(ring, np.int16)
