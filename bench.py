@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-scan", action="store_true", help="skip the scan-reduction side measurement")
     return ap.parse_args()
 
 
@@ -172,6 +173,59 @@ def cpu_baseline(wl, target_s: float = 10.0) -> dict:
 def _reference_map(O, wl):
     """The map loaded into the reference's own CudaSubVoxelMap."""
     return O.RefMap.from_slots(wl.coef, wl.grid_occ, wl.float_data())
+
+
+def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 100) -> dict:
+    """Times the scan reduction (evaluateParticles' pre-processing) on the raw
+    64 x 2048 ray-cast cloud the workload's points come from: the device form
+    with CUDA events on the context's stream, the host form (pageable cloud in,
+    points out) with a host clock, and the oracle on one host core."""
+    import torch
+
+    from tsdf_localization_gb300 import _native as N
+    from tsdf_localization_gb300 import pack_cloud, synth
+    xyz, ring = synth.World(synth.BUILDING, 2).scan(wl.true_pose, 64, 2048, dropout=0.01, seed=2)
+    n = int(xyz.shape[0])
+    blob_h = pack_cloud(xyz, ring)
+    blob = torch.from_numpy(blob_h).to(device)
+    out = torch.empty((n, 3), dtype=torch.float32, device=device)
+    cnt = torch.zeros(1, dtype=torch.int32, device=device)
+    vp = C.c_void_p
+
+    def dev():
+        N.check(lib.tsdfl_reduce_scan_device(ctx.handle, vp(blob.data_ptr()), n, 16, 0, 12, 0.05, 0,
+                                             vp(out.data_ptr()), n, vp(cnt.data_ptr())))
+
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            dev()
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            dev()
+        e1.record(stream)
+        e1.synchronize()
+        ctx.sync()
+    m = int(cnt.item())
+    ho = np.empty((n, 3), np.float32)
+    hc = C.c_size_t()
+    tt = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        N.check(lib.tsdfl_reduce_scan(ctx.handle, blob_h.ctypes.data_as(vp), n, 16, 0, 12, 0.05, 0,
+                                      ho.ctypes.data_as(vp), n, C.byref(hc)))
+        tt.append(time.perf_counter() - t0)
+    res = {"cloud": "64x2048 ray-cast, building at 0.05 m, 16-byte records", "raw_points": n, "reduced_points": m,
+           "cell_m": 0.05, "device_us": 1000.0 * e0.elapsed_time(e1) / reps,
+           "host_api_us": 1e6 * float(np.median(tt)), "launches_per_call": 6}
+    if with_cpu:
+        from oracle import oracle_py as O
+        t0 = time.perf_counter()
+        ref = O.reduce_scan(xyz, ring, 0.05)
+        res["cpu_oracle_ms"] = 1000.0 * (time.perf_counter() - t0)
+        res["matches_oracle"] = bool(np.array_equal(ho[:hc.value], ref))
+    return res
 
 
 def max_over_ranks(x: float, device=None) -> float:
@@ -361,6 +415,9 @@ def main():
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base, _ = cpu_baseline(wl)
+    scan = None
+    if not args.no_scan:
+        scan = scan_reduction_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -373,7 +430,7 @@ def main():
                           "step": "sensor update + normalise + mean pose + systematic resample",
                           "form": "plain single filter", "parallelism": f"replicas x{world}"},
                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
-               "latency_ms": latency, "clocks": clocks}
+               "latency_ms": latency, "clocks": clocks, "scan_reduction": scan}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
