@@ -233,6 +233,42 @@ int tsdfl_evaluate_cloud(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model
                          uint32_t ring_offset, float cell, uint32_t scan_flags, const float tf[16], uint32_t flags,
                          float pose_out[6], size_t* n_reduced);
 
+/* ---- motion update ----
+ * ParticleCloud::apply_model (particle_cloud.cpp:499-617), the loop every
+ * motion-update overload runs: each particle draws dx, dy, dz, roll, pitch,
+ * yaw from N(mean[k], stddev[k]), composes the odometry transform with its
+ * orientation and takes the translation and getAngleFromMat's angles
+ * (util.cpp:86-111) as its new pose; weights are kept.  The composition is the
+ * reference's bit for bit.  The draws cannot be: the reference pulls them from
+ * one serial std::mt19937 through std::normal_distribution.
+ * tsdfl_motion_update* draws them on the device (Philox4x64-10 keyed by seed,
+ * counter (particle, block, step), Box-Muller in FP64: the same distribution,
+ * independent per particle, reproducible per (seed, step));
+ * tsdfl_motion_apply* takes them from the caller (P x 6 doubles), e.g. the
+ * reference's own sequence drawn on the host. */
+typedef struct tsdfl_motion {
+    double mean[6];     /* dx, dy, dz, roll, pitch, yaw */
+    double stddev[6];   /* the reference's second std::normal_distribution argument */
+} tsdfl_motion;
+#define TSDFL_MOTION_ODOM 0       /* motionUpdate(const nav_msgs::Odometry&) (:153-197): in = linear.x, angular.z */
+#define TSDFL_MOTION_IMU 1        /* motionUpdate(const ImuAccumulator::Data&) (:335-378): in = linear_vel, angular_yaw */
+#define TSDFL_MOTION_SCALE 2      /* motionUpdate(lin_scale, ang_scale) (:380-413) */
+#define TSDFL_MOTION_SCALE_IMU 3  /* motionUpdate(lin_scale, imu) (:415-454): in = lin_scale, delta_roll, delta_pitch, delta_yaw */
+#define TSDFL_MOTION_DELTA 4      /* motion_update (:456-497): in = dx, dy, dz, roll, pitch, yaw, lin_base_noise, ang_base_noise */
+/* The distributions an overload sets up, with its own float/double
+ * arithmetic; a = a_1 .. a_12 (setMotionParameters), time_diff in seconds. */
+int tsdfl_motion_model(int kind, const float a[12], const double* in, size_t n_in, float time_diff,
+                       tsdfl_motion* out);
+/* Device forms, stream-ordered: d_particles P x 7 floats updated in place;
+ * d_draws_out (optional) receives the generated draws (P x 6 doubles). */
+int tsdfl_motion_update_device(tsdfl_ctx* ctx, float* d_particles, size_t P, const tsdfl_motion* motion,
+                               uint64_t seed, uint64_t step, double* d_draws_out);
+int tsdfl_motion_apply_device(tsdfl_ctx* ctx, float* d_particles, size_t P, const double* d_draws);
+/* Host forms (particles and draws in host memory). */
+int tsdfl_motion_update(tsdfl_ctx* ctx, float* particles, size_t P, const tsdfl_motion* motion, uint64_t seed,
+                        uint64_t step);
+int tsdfl_motion_apply(tsdfl_ctx* ctx, float* particles, size_t P, const double* draws);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about

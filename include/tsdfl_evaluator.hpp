@@ -11,6 +11,8 @@
  *       ResidualSystematicResampler (novel_resampling.h:76-104)
  *   tsdf_localization::gpu_reduce_scan replaces the scan reduction block of
  *       TSDFEvaluator::evaluateParticles (src/evaluation/tsdf_evaluator.cpp:304-374)
+ *   tsdf_localization::GpuMotionModel replaces ParticleCloud's motion-update
+ *       overloads (src/particle_cloud.cpp:153-617)
  *
  * Errors surface as std::runtime_error carrying libtsdfl's message, as the
  * reference's evaluators throw them ("No particle is valid!" for a zero
@@ -19,9 +21,11 @@
 #define TSDFL_EVALUATOR_HPP
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <random>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -238,6 +242,83 @@ private:
     std::vector<float> buf_;
 };
 
+// ParticleCloud's motion model (particle_cloud.cpp:153-617) on the device.
+// a_1 .. a_12 as setMotionParameters takes them (0.1 each by default).
+class MotionModel {
+public:
+    explicit MotionModel(Context& ctx, uint64_t seed = 0) : ctx_(ctx), seed_(seed)
+    {
+        for (int k = 0; k < 12; ++k) a_[k] = 0.1f;
+    }
+
+    void setMotionParameters(float a1, float a2, float a3, float a4, float a5, float a6, float a7, float a8,
+                             float a9, float a10, float a11, float a12)
+    {
+        const float v[12] = {a1, a2, a3, a4, a5, a6, a7, a8, a9, a10, a11, a12};
+        for (int k = 0; k < 12; ++k) a_[k] = v[k];
+    }
+
+    // The distributions of an overload (TSDFL_MOTION_*), see tsdfl_motion_model.
+    tsdfl_motion distributions(int kind, const double* in, size_t n_in, float time_diff) const
+    {
+        tsdfl_motion m;
+        check(tsdfl_motion_model(kind, a_, in, n_in, time_diff, &m));
+        return m;
+    }
+
+    // Device-drawn noise: one counter-based stream per call.
+    template <class ParticleT>
+    void update(std::vector<ParticleT>& particles, const tsdfl_motion& m)
+    {
+        to_floats(particles);
+        check(tsdfl_motion_update(ctx_.get(), parts_.data(), particles.size(), &m, seed_, step_++));
+        from_floats(particles);
+    }
+
+    // Noise from the caller's generator in the reference's order: six
+    // std::normal_distribution<> objects, x, y, z, roll, pitch, yaw per
+    // particle (particle_cloud.cpp:506-511), so a generator in the same state
+    // gives the reference's particles bit for bit.
+    template <class ParticleT, class Generator>
+    void update_with(std::vector<ParticleT>& particles, const tsdfl_motion& m, Generator& gen)
+    {
+        std::normal_distribution<> dist[6] = {
+            std::normal_distribution<>(m.mean[0], m.stddev[0]), std::normal_distribution<>(m.mean[1], m.stddev[1]),
+            std::normal_distribution<>(m.mean[2], m.stddev[2]), std::normal_distribution<>(m.mean[3], m.stddev[3]),
+            std::normal_distribution<>(m.mean[4], m.stddev[4]), std::normal_distribution<>(m.mean[5], m.stddev[5])};
+        draws_.resize(6 * particles.size());
+        for (size_t i = 0; i < particles.size(); ++i)
+            for (int k = 0; k < 6; ++k) draws_[6 * i + k] = dist[k](gen);
+        to_floats(particles);
+        check(tsdfl_motion_apply(ctx_.get(), parts_.data(), particles.size(), draws_.data()));
+        from_floats(particles);
+    }
+
+private:
+    template <class ParticleT>
+    void to_floats(const std::vector<ParticleT>& particles)
+    {
+        parts_.resize(7 * (particles.size() ? particles.size() : 1));
+        for (size_t i = 0; i < particles.size(); ++i) {
+            for (int k = 0; k < 6; ++k) parts_[7 * i + k] = particles[i].first[k];
+            parts_[7 * i + 6] = particles[i].second;
+        }
+    }
+    template <class ParticleT>
+    void from_floats(std::vector<ParticleT>& particles) const
+    {
+        for (size_t i = 0; i < particles.size(); ++i)
+            for (int k = 0; k < 6; ++k) particles[i].first[k] = parts_[7 * i + k];
+    }
+
+    Context& ctx_;
+    uint64_t seed_;
+    uint64_t step_ = 0;
+    float a_[12];
+    std::vector<float> parts_;
+    std::vector<double> draws_;
+};
+
 // Cell-centre reduction of a scan as CudaEvaluator's point-cloud overload
 // performs it (cuda_evaluator.cu:77-115): every point maps to the centre of its
 // 0.064 m cell, each centre kept once.  Order does not matter downstream: the
@@ -363,6 +444,115 @@ private:
     std::unique_ptr<tsdfl::Context> ctx_;
     std::unique_ptr<tsdfl::Map> map_;
     std::unique_ptr<tsdfl::SensorUpdate> update_;
+};
+
+// Drop-in for ParticleCloud's motion-update overloads (particle_cloud.cpp:153-497):
+// the same names and arguments, applied to a ParticleCloud's particles on the
+// device.  It keeps what ParticleCloud keeps for them -- a_1 .. a_12, the time
+// of the last update and the reference pose behind refDist / refAngle, with
+// ParticleCloud's expressions, compiled in the caller's build -- so mcl_3d
+// calls it where it called particle_cloud_.motionUpdate (mcl_3d.cpp:335-347)
+// and reads refDist / refAngle / resetRef from it.  Noise is drawn on the
+// device; with host_draws set it comes from an owned std::mt19937 seeded from
+// std::random_device as ParticleCloud's is, in the reference's order.
+class GpuMotionModel {
+public:
+    explicit GpuMotionModel(int device = 0, bool host_draws = false)
+        : ctx_(new tsdfl::Context(device)), model_(*ctx_, std::random_device{}()), host_draws_(host_draws)
+    {
+        std::random_device rd{};
+        gen_.seed(rd());
+        ref_pose_.fill(0);
+        m_last_time_ = ros::Time::now();
+    }
+
+    // ParticleCloud::initialize sets the time the first update measures from.
+    void resetTime() { m_last_time_ = ros::Time::now(); }
+
+    void setMotionParameters(FLOAT_T a_1, FLOAT_T a_2, FLOAT_T a_3, FLOAT_T a_4, FLOAT_T a_5, FLOAT_T a_6,
+                             FLOAT_T a_7, FLOAT_T a_8, FLOAT_T a_9, FLOAT_T a_10, FLOAT_T a_11, FLOAT_T a_12)
+    {
+        model_.setMotionParameters(a_1, a_2, a_3, a_4, a_5, a_6, a_7, a_8, a_9, a_10, a_11, a_12);
+    }
+
+    void motionUpdate(ParticleCloud& cloud, const nav_msgs::Odometry& odom)
+    {
+        auto linear_velocity = odom.twist.twist.linear.x;
+        auto angular_velocity = odom.twist.twist.angular.z;
+        FLOAT_T time_diff = elapsed();
+        ref_pose_[0] = ref_pose_[0] + linear_velocity * time_diff * cos(ref_pose_[5] + (angular_velocity / 2 * time_diff));
+        ref_pose_[1] = ref_pose_[1] + linear_velocity * time_diff * sin(ref_pose_[5] + (angular_velocity / 2 * time_diff));
+        ref_pose_[5] = ref_pose_[5] + angular_velocity * time_diff;
+        const double in[2] = {linear_velocity, angular_velocity};
+        run(cloud, model_.distributions(TSDFL_MOTION_ODOM, in, 2, time_diff));
+    }
+
+    void motionUpdate(ParticleCloud& cloud, const ImuAccumulator::Data& imu_data)
+    {
+        auto linear_velocity = imu_data.linear_vel;
+        auto angular_velocity = imu_data.angular_yaw;
+        FLOAT_T time_diff = elapsed();
+        ref_pose_[0] = ref_pose_[0] + linear_velocity * time_diff * cos(ref_pose_[5] + (angular_velocity / 2 * time_diff));
+        ref_pose_[1] = ref_pose_[1] + linear_velocity * time_diff * sin(ref_pose_[5] + (angular_velocity / 2 * time_diff));
+        ref_pose_[5] = ref_pose_[5] + angular_velocity * time_diff;
+        const double in[2] = {linear_velocity, angular_velocity};
+        run(cloud, model_.distributions(TSDFL_MOTION_IMU, in, 2, time_diff));
+    }
+
+    void motionUpdate(ParticleCloud& cloud, FLOAT_T lin_scale, FLOAT_T ang_scale)
+    {
+        FLOAT_T time_diff = elapsed();
+        const double in[2] = {lin_scale, ang_scale};
+        run(cloud, model_.distributions(TSDFL_MOTION_SCALE, in, 2, time_diff));
+    }
+
+    void motionUpdate(ParticleCloud& cloud, FLOAT_T lin_scale, const ImuAccumulator::Data& imu_data)
+    {
+        FLOAT_T time_diff = elapsed();
+        const double in[4] = {lin_scale, imu_data.delta_roll, imu_data.delta_pitch, imu_data.delta_yaw};
+        run(cloud, model_.distributions(TSDFL_MOTION_SCALE_IMU, in, 4, time_diff));
+    }
+
+    void motion_update(ParticleCloud& cloud, FLOAT_T dx, FLOAT_T dy, FLOAT_T dz, FLOAT_T roll, FLOAT_T pitch,
+                       FLOAT_T yaw, FLOAT_T lin_base_noise = 0, FLOAT_T ang_base_noise = 0)
+    {
+        elapsed();
+        ref_pose_[0] = ref_pose_[0] + dx * cos(ref_pose_[5] + yaw);
+        ref_pose_[1] = ref_pose_[1] + dx * sin(ref_pose_[5] + yaw);
+        ref_pose_[5] = ref_pose_[5] + yaw;
+        const double in[8] = {dx, dy, dz, roll, pitch, yaw, lin_base_noise, ang_base_noise};
+        run(cloud, model_.distributions(TSDFL_MOTION_DELTA, in, 8, 0.0f));
+    }
+
+    const std::array<FLOAT_T, 6>& refPose() { return ref_pose_; }
+    void resetRef() { ref_pose_.fill(0); }
+    FLOAT_T refDist()
+    {
+        return std::sqrt(ref_pose_[0] * ref_pose_[0] + ref_pose_[1] * ref_pose_[1] + ref_pose_[2] * ref_pose_[2]);
+    }
+    FLOAT_T refAngle() { return std::fabs(ref_pose_[5]); }
+
+private:
+    FLOAT_T elapsed()
+    {
+        ros::Time current_time = ros::Time::now();
+        FLOAT_T time_diff = (current_time - m_last_time_).toSec();
+        m_last_time_ = current_time;
+        return time_diff;
+    }
+
+    void run(ParticleCloud& cloud, const tsdfl_motion& m)
+    {
+        if (host_draws_) model_.update_with(cloud.particles(), m, gen_);
+        else model_.update(cloud.particles(), m);
+    }
+
+    std::unique_ptr<tsdfl::Context> ctx_;
+    tsdfl::MotionModel model_;
+    bool host_draws_;
+    std::mt19937 gen_;
+    std::array<FLOAT_T, 6> ref_pose_;
+    ros::Time m_last_time_;
 };
 
 // Drop-in for SystematicResampler: draws U ~ U[0, 1/M) from the inherited

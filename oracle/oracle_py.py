@@ -73,6 +73,8 @@ def oracle() -> C.CDLL:
                                                 C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
         L.orc_resample_systematic.restype = SZ
         L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
+        L.orc_motion_apply.restype = None
+        L.orc_motion_apply.argtypes = [P, SZ, P]
         L.orc_reduce_scan.restype = SZ
         L.orc_reduce_scan.argtypes = [P, P, SZ, C.c_float, C.c_int, P, SZ]
         L.orc_resample_residual_systematic.restype = SZ
@@ -114,6 +116,8 @@ def reference() -> C.CDLL:
         L.ref_draw_u01.argtypes = [C.c_uint32]
         L.ref_resample_residual_systematic.restype = SZ
         L.ref_resample_residual_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
+        L.ref_motion_update.restype = None
+        L.ref_motion_update.argtypes = [P, SZ, P]
         L.ref_reduce_scan.restype = SZ
         L.ref_reduce_scan.argtypes = [P, P, SZ, C.c_float, P, SZ]
         L.ref_omp_threads.restype = C.c_int
@@ -242,6 +246,48 @@ def reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064, own_ring
     if n == (1 << 64) - 1:
         raise ValueError("ring outside [0, 64)")
     return out[:n].copy()
+
+
+def motion_apply(particles: np.ndarray, draws: np.ndarray) -> np.ndarray:
+    """particle_cloud.cpp:499-617 on given draws (P x 6 doubles); returns new particles."""
+    p = np.ascontiguousarray(particles, np.float32).copy()
+    d = np.ascontiguousarray(draws, np.float64)
+    assert d.shape == (p.shape[0], 6)
+    oracle().orc_motion_apply(_ptr(p), p.shape[0], _ptr(d))
+    return p
+
+
+def ref_motion_update(particles: np.ndarray, delta) -> np.ndarray:
+    """The reference's ParticleCloud::motion_update with zero noise: every
+    particle moves by exactly delta = (dx, dy, dz, roll, pitch, yaw) (floats)."""
+    p = np.ascontiguousarray(particles, np.float32).copy()
+    d = np.ascontiguousarray(delta, np.float32)
+    reference().ref_motion_update(_ptr(p), p.shape[0], _ptr(d))
+    return p
+
+
+PHILOX_M = (0xD2E7470EE14C6C93, 0xCA5A826395121157)
+PHILOX_W = (0x9E3779B97F4A7C15, 0xBB67AE8584CAA73B)
+
+
+def philox4x64_10(counter, key):
+    """Philox4x64-10 (Salmon et al., SC 2011) of one counter block, vectorised
+    over numpy uint64 arrays: counter 4 arrays, key 2 arrays or ints."""
+    m64 = (1 << 64) - 1
+
+    def as_int(v):
+        a = np.asarray(v)
+        return np.vectorize(int, otypes=[object])(a) if a.ndim else int(a)
+
+    c = [as_int(v) for v in counter]
+    k0, k1 = int(key[0]), int(key[1])
+    for _ in range(10):
+        p0 = c[0] * PHILOX_M[0]
+        p1 = c[2] * PHILOX_M[1]
+        c = [(p1 >> 64) ^ c[1] ^ k0, p1 & m64, (p0 >> 64) ^ c[3] ^ k1, p0 & m64]
+        k0 = (k0 + PHILOX_W[0]) & m64
+        k1 = (k1 + PHILOX_W[1]) & m64
+    return [np.asarray(v, dtype=object).astype(np.uint64) for v in c]
 
 
 def ref_reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064) -> np.ndarray:

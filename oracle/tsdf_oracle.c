@@ -453,3 +453,73 @@ size_t orc_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float ce
     free(pts);
     return m;
 }
+
+/* util.cpp:86-111, getAngleFromMat; unqualified fabs/atan2/asin/cos on floats
+ * bind to the double functions in the reference's build. */
+static void orc_angles_from_mat(const float m[16], float* roll, float* pitch, float* yaw)
+{
+    if (fabs((double)m[8]) >= 1) {
+        *yaw = 0;
+        double delta = atan2((double)m[9], (double)m[10]);
+        *pitch = m[8] < 0 ? (float)(M_PI / 2.0) : (float)(-M_PI / 2.0);
+        *roll = (float)delta;
+    } else {
+        *pitch = (float)(-asin((double)m[8]));
+        *roll = (float)atan2((double)m[9] / cos((double)*pitch), (double)m[10] / cos((double)*pitch));
+        *yaw = (float)atan2((double)m[4] / cos((double)*pitch), (double)m[0] / cos((double)*pitch));
+    }
+}
+
+/* particle_cloud.cpp:530-614 */
+void orc_motion_apply(float* particles, size_t P, const double* draws)
+{
+    for (size_t i = 0; i < P; ++i) {
+        float* p = particles + 7 * i;
+        const double* d = draws + 6 * i;
+        float sr = (float)sin(d[3]), cr = (float)cos(d[3]);
+        float sp = (float)sin(d[4]), cp = (float)cos(d[4]);
+        float sy = (float)sin(d[5]), cy = (float)cos(d[5]);
+        float o[16], q[16], t[16];
+        o[0] = cp * cy;
+        o[4] = cp * sy;
+        o[8] = -sp;
+        o[3] = (float)d[0];
+        o[1] = sr * sp * cy - cr * sy;
+        o[5] = sr * sp * sy + cr * cy;
+        o[9] = sr * cp;
+        o[7] = (float)d[1];
+        o[2] = cr * sp * cy + sr * sy;
+        o[6] = cr * sp * sy - sr * cy;
+        o[10] = cr * cp;
+        o[11] = (float)d[2];
+        float sa = (float)sin((double)p[3]), ca = (float)cos((double)p[3]);
+        float sb = (float)sin((double)p[4]), cb = (float)cos((double)p[4]);
+        float sg = (float)sin((double)p[5]), cg = (float)cos((double)p[5]);
+        q[0] = cb * cg;
+        q[4] = cb * sg;
+        q[8] = -sb;
+        q[3] = 0;
+        q[1] = sa * sb * cg - ca * sg;
+        q[5] = sa * sb * sg + ca * cg;
+        q[9] = sa * cb;
+        q[7] = 0;
+        q[2] = ca * sb * cg + sa * sg;
+        q[6] = ca * sb * sg - sa * cg;
+        q[10] = ca * cb;
+        q[11] = 0;
+        for (int r = 0; r < 3; ++r) {
+            t[4 * r] = q[4 * r] * o[0] + q[4 * r + 1] * o[4] + q[4 * r + 2] * o[8];
+            t[4 * r + 1] = q[4 * r] * o[1] + q[4 * r + 1] * o[5] + q[4 * r + 2] * o[9];
+            t[4 * r + 2] = q[4 * r] * o[2] + q[4 * r + 1] * o[6] + q[4 * r + 2] * o[10];
+            t[4 * r + 3] = q[4 * r] * o[3] + q[4 * r + 1] * o[7] + q[4 * r + 2] * o[11] + q[4 * r + 3];
+        }
+        float roll, pitch, yaw;
+        orc_angles_from_mat(t, &roll, &pitch, &yaw);
+        p[0] = p[0] + t[3];
+        p[1] = p[1] + t[7];
+        p[2] = p[2] + t[11];
+        p[3] = roll;
+        p[4] = pitch;
+        p[5] = yaw;
+    }
+}

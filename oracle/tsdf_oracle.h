@@ -124,6 +124,11 @@ size_t orc_resample_residual_systematic(const float* w, size_t M, float u0, uint
 size_t orc_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float cell, int own_ring, float* out,
                        size_t cap);
 
+/* ParticleCloud::apply_model (particle_cloud.cpp:499-617) on given draws:
+ * particles P x 7 floats updated in place, draws P x 6 doubles (dx, dy, dz,
+ * roll, pitch, yaw), trig through the double overloads. */
+void orc_motion_apply(float* particles, size_t P, const double* draws);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,7 +10,8 @@ query points, TSDFEvaluator::evaluate's un-normalised and normalised weights,
 laser poses and mean pose (serial, in point order), SystematicResampler's
 and ResidualSystematicResampler's output indices for seeded draws, and the
 point list TSDFEvaluator::evaluateParticles' scan reduction hands to evaluate
-for a set of clouds (x, y, z, ring).
+for a set of clouds (x, y, z, ring), and the particles ParticleCloud's motion
+model produces from given increments (motion_update with zero noise).
 
     python tests/golden/make_golden.py
 """
@@ -158,6 +159,24 @@ def scan_case(seed):
     return out
 
 
+def motion_case(seed):
+    rng = np.random.default_rng(seed)
+    P = 600
+    parts = np.zeros((P, 7), np.float32)
+    parts[:, :3] = rng.uniform(-60, 60, (P, 3))
+    parts[:, 3:5] = rng.uniform(-0.6, 0.6, (P, 2))
+    parts[:, 5] = rng.uniform(-np.pi, np.pi, P)
+    parts[:40, 4] = np.float32(np.pi / 2)       # getAngleFromMat's |m[8]| >= 1 branch
+    parts[40:80, 4] = -np.float32(np.pi / 2)
+    parts[:, 6] = rng.random(P)
+    deltas = np.array([[0, 0, 0, 0, 0, 0],
+                       [0.35, -0.02, 0.01, 0.004, -0.003, 0.12],
+                       [-1.2, 0.4, -0.3, 0.3, -0.25, -2.9]], np.float32)
+    out = {"motion/particles": parts, "motion/deltas": deltas}
+    out["motion/moved"] = np.stack([O.ref_motion_update(parts, d) for d in deltas])
+    return out
+
+
 def main():
     if not O.reference_available():
         raise SystemExit("oracle/_ref/libref.so is not built: the reference tree is needed")
@@ -166,6 +185,7 @@ def main():
     fx.update(map_case("map_005", 0.05, (0.0, 0.0, 0.0), (4.2, 3.6, 2.2), 6000, 12))
     fx.update(resample_case(13))
     fx.update(scan_case(14))
+    fx.update(motion_case(15))
     np.savez_compressed(OUT / "reference_cases.npz", **fx)
     print("wrote", OUT / "reference_cases.npz", (OUT / "reference_cases.npz").stat().st_size, "bytes")
 

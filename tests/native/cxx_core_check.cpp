@@ -5,6 +5,8 @@
 // the resampled particles back there.
 #include "tsdfl_evaluator.hpp"
 
+using tsdfl::check;
+
 #include <cstdio>
 #include <fstream>
 #include <iterator>
@@ -99,6 +101,26 @@ int main(int argc, char** argv)
         std::vector<float> wc(parts_c.size());
         for (size_t i = 0; i < parts_c.size(); ++i) wc[i] = parts_c[i].second;
         save(d + "/cloud_weights_out.bin", wc.data(), wc.size());
+        // motion model on given draws and on device-drawn noise
+        auto draws = load<double>(d + "/draws.bin");
+        std::vector<MyParticle> parts_m(pf.size() / 7);
+        for (size_t i = 0; i < parts_m.size(); ++i) {
+            for (int k = 0; k < 6; ++k) parts_m[i].first[k] = pf[7 * i + k];
+            parts_m[i].second = pf[7 * i + 6];
+        }
+        tsdfl::MotionModel motion(ctx, 42);
+        std::vector<float> pm(pf);
+        check(tsdfl_motion_apply(ctx.get(), pm.data(), parts_m.size(), draws.data()));
+        save(d + "/motion_apply_out.bin", pm.data(), pm.size());
+        const double odom_in[2] = {0.6, -0.3};
+        tsdfl_motion m = motion.distributions(TSDFL_MOTION_ODOM, odom_in, 2, 0.1f);
+        motion.update(parts_m, m);   // step 0 of seed 42
+        std::vector<float> out_m(7 * parts_m.size());
+        for (size_t i = 0; i < parts_m.size(); ++i) {
+            for (int k = 0; k < 6; ++k) out_m[7 * i + k] = parts_m[i].first[k];
+            out_m[7 * i + 6] = parts_m[i].second;
+        }
+        save(d + "/motion_update_out.bin", out_m.data(), out_m.size());
         bool threw = false;
         try {   // an empty cloud: the reference's "No particle is valid!"
             std::vector<MyParticle> none;

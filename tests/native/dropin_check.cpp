@@ -73,6 +73,14 @@ int main()
         std::printf("reduced %zu\n", reduced.size());
         pose = ev.evaluateCloud(parts, pc, tf, 0.064f);
         std::printf("cloud evaluated w0=%.9g\n", parts[0].second);
+        GpuMotionModel motion(0);
+        motion.setMotionParameters(0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f, 0.1f);
+        nav_msgs::Odometry odom;
+        odom.twist.twist.linear.x = 0.5;
+        odom.twist.twist.angular.z = 0.1;
+        motion.motionUpdate(cloud, odom);
+        motion.motion_update(cloud, 0.1f, 0.0f, 0.0f, 0.0f, 0.0f, 0.05f);
+        std::printf("moved %zu, ref dist %.9g\n", cloud.size(), motion.refDist());
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         status = 0;

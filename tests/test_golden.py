@@ -120,3 +120,36 @@ def test_scan_reduction_ring_skip_and_errors():
     with pytest.raises(ValueError):
         O.reduce_scan(xyz, np.array([64, 0, 0], np.int16), 0.1)
     assert O.reduce_scan(np.zeros((0, 3), np.float32), np.zeros(0, np.int16), 0.1).shape == (0, 3)
+
+
+def test_motion_composition_matches_reference():
+    parts, deltas, moved = GOLD["motion/particles"], GOLD["motion/deltas"], GOLD["motion/moved"]
+    for d, want in zip(deltas, moved):
+        got = O.motion_apply(parts, np.tile(d.astype(np.float64), (parts.shape[0], 1)))
+        assert np.array_equal(got, want)
+
+
+def test_motion_composition_random_matches_reference():
+    if not O.reference_available():
+        pytest.skip("the reference sources are not on this machine")
+    rng = np.random.default_rng(23)
+    P = 5000
+    parts = np.zeros((P, 7), np.float32)
+    parts[:, :3] = rng.uniform(-100, 100, (P, 3))
+    parts[:, 3:6] = rng.uniform(-np.pi, np.pi, (P, 3))
+    parts[:50, 4] = np.float32(np.pi / 2)
+    parts[:, 6] = rng.random(P)
+    for _ in range(15):
+        d = rng.normal(0, [0.5, 0.2, 0.1, 0.1, 0.1, 0.5]).astype(np.float32)
+        assert np.array_equal(O.motion_apply(parts, np.tile(d.astype(np.float64), (P, 1))),
+                              O.ref_motion_update(parts, d))
+
+
+def test_philox_restatement_matches_numpy():
+    for key in ((0, 0), (12345, 0x6D6F74696F6E0001), (2 ** 64 - 1, 7)):
+        g = np.random.Philox(key=np.array(key, np.uint64), counter=np.zeros(4, np.uint64))
+        raw = g.random_raw(12)
+        # numpy advances the counter before each block: blocks 1, 2, 3
+        for b in range(3):
+            got = O.philox4x64_10([np.uint64(b + 1), np.uint64(0), np.uint64(0), np.uint64(0)], key)
+            assert [int(v) for v in got] == [int(v) for v in raw[4 * b:4 * b + 4]]

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle_py as O
-from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator, pack_cloud, synth
+from tsdf_localization_gb300 import (Context, DeviceMap, MotionModel, SystematicResampler, TSDFEvaluator, pack_cloud,
+                                     synth)
 
 pytestmark = pytest.mark.gpu
 ROOT = Path(__file__).resolve().parent.parent
@@ -37,6 +38,8 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     cxyz, cring = synth.World(synth.ROOM, 21).scan(wl.true_pose, 16, 700, sigma=0.01, dropout=0.02, seed=8)
     cxyz[::37] *= np.float32(0.1)       # some returns inside 1 m
     pack_cloud(cxyz, cring).tofile(tmp_path / "cloud.bin")
+    draws = np.random.default_rng(3).normal(0, [0.3, 0.1, 0.05, 0.05, 0.05, 0.3], (wl.particles.shape[0], 6))
+    draws.tofile(tmp_path / "draws.bin")
     res = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     print(res.stdout, res.stderr)
     assert res.returncode == 0, res.stdout + res.stderr
@@ -68,3 +71,10 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     pc = wl.particles.copy()
     TSDFEvaluator(dmap).evaluate(pc, want, wl.tf)
     assert np.array_equal(np.fromfile(tmp_path / "cloud_weights_out.bin", np.float32), pc[:, 6])
+
+    moved = np.fromfile(tmp_path / "motion_apply_out.bin", np.float32).reshape(-1, 7)
+    assert np.array_equal(moved, O.motion_apply(wl.particles, draws))
+    mm = MotionModel(ctx, seed=42)
+    pm = wl.particles.copy()
+    mm.update(pm, mm.distributions("odom", [0.6, -0.3], 0.1), step=0)
+    assert np.array_equal(np.fromfile(tmp_path / "motion_update_out.bin", np.float32).reshape(-1, 7), pm)

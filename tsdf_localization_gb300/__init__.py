@@ -5,8 +5,8 @@ ABI in include/tsdfl.h); this package binds it for tests, benchmarks and Python
 callers.  Build with `python -c "import __graft_entry__ as g; g.build()"`.
 """
 from ._native import TsdflError
-from .evaluator import (Context, DeviceMap, Pose, ResidualSystematicResampler, ScanReducer, SystematicResampler,
-                        TSDFEvaluator, build_map_codes, code_values, pack_cloud)
+from .evaluator import (Context, DeviceMap, MotionModel, Pose, ResidualSystematicResampler, ScanReducer,
+                        SystematicResampler, TSDFEvaluator, build_map_codes, code_values, pack_cloud)
 
-__all__ = ["Context", "DeviceMap", "Pose", "ResidualSystematicResampler", "ScanReducer", "SystematicResampler",
-           "TSDFEvaluator", "TsdflError", "build_map_codes", "code_values", "pack_cloud"]
+__all__ = ["Context", "DeviceMap", "MotionModel", "Pose", "ResidualSystematicResampler", "ScanReducer",
+           "SystematicResampler", "TSDFEvaluator", "TsdflError", "build_map_codes", "code_values", "pack_cloud"]

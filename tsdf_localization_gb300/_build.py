@@ -56,7 +56,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
     headers = sorted(CSRC.glob("*.h")) + [ROOT / "include" / "tsdfl.h"]
     cu = sorted(CSRC.glob("*.cu"))
-    cpp_lib = [CSRC / "map_build.cpp"]
+    cpp_lib = [CSRC / "map_build.cpp", CSRC / "motion_model.cpp"]
     jobs = []
     objs = []
     for src in cu:
@@ -87,7 +87,9 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         ref_dir.mkdir(parents=True, exist_ok=True)
         ref = ref_dir / "libref.so"
         ref_srcs = [REFERENCE / "src" / "evaluation" / "tsdf_evaluator.cpp",
-                    REFERENCE / "src" / "evaluation" / "model" / "likelihood_evaluation.cpp"]
+                    REFERENCE / "src" / "evaluation" / "model" / "likelihood_evaluation.cpp",
+                    REFERENCE / "src" / "particle_cloud.cpp",
+                    REFERENCE / "src" / "util" / "util.cpp"]
         if force or _stale(ref, [ORACLE / "ref_driver.cpp"] + ref_srcs + sorted((ORACLE / "shim").rglob("*"))):
             jobs.append(["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fopenmp", "-shared",
                          f"-DTSDFL_REF_OMP_THREADS={os.cpu_count() or 8}",

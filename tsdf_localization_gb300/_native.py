@@ -25,6 +25,7 @@ TSDFL_SUM_EXACT = 0
 TSDFL_SUM_SERIAL = 1
 TSDFL_EVAL_GENERIC = 4
 TSDFL_SCAN_OWN_RING = 1
+TSDFL_MOTION_ODOM, TSDFL_MOTION_IMU, TSDFL_MOTION_SCALE, TSDFL_MOTION_SCALE_IMU, TSDFL_MOTION_DELTA = range(5)
 
 
 class MapCoef(C.Structure):
@@ -55,6 +56,10 @@ class MapInfo(C.Structure):
     _fields_ = [("grid_occ_size", C.c_uint64), ("data_size", C.c_uint64), ("bricks", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("storage", C.c_int32), ("dense", C.c_int32),
                 ("fast_index", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Motion(C.Structure):
+    _fields_ = [("mean", C.c_double * 6), ("stddev", C.c_double * 6)]
 
 
 class EvalDebug(C.Structure):
@@ -100,6 +105,11 @@ SIGNATURES = [
     ("tsdfl_best_particle_device", I, [P, P, SZ, P]),
     ("tsdfl_reduce_scan", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, C.POINTER(SZ)]),
     ("tsdfl_reduce_scan_device", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, P]),
+    ("tsdfl_motion_model", I, [I, P, P, SZ, F, C.POINTER(Motion)]),
+    ("tsdfl_motion_update_device", I, [P, P, SZ, C.POINTER(Motion), C.c_uint64, C.c_uint64, P]),
+    ("tsdfl_motion_apply_device", I, [P, P, SZ, P]),
+    ("tsdfl_motion_update", I, [P, P, SZ, C.POINTER(Motion), C.c_uint64, C.c_uint64]),
+    ("tsdfl_motion_apply", I, [P, P, SZ, P]),
     ("tsdfl_evaluate_cloud", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, U32, U32, U32, F, U32, P, U32, P,
                                  C.POINTER(SZ)]),
 ]

@@ -1047,6 +1047,87 @@ int tsdfl_evaluate_cloud(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* 
     return TSDFL_OK;
 }
 
+int tsdfl_motion_update_device(tsdfl_ctx* c, float* d_particles, size_t P, const tsdfl_motion* m, uint64_t seed,
+                               uint64_t step, double* d_draws_out)
+{
+    if (!c || !m || (P && !d_particles)) {
+        set_error("tsdfl_motion_update_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P >= (1ull << 32)) {
+        set_error("tsdfl_motion_update_device: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    return launch_motion(d_particles, P, m->mean, m->stddev, seed, step, nullptr, d_draws_out, c->stream);
+}
+
+int tsdfl_motion_apply_device(tsdfl_ctx* c, float* d_particles, size_t P, const double* d_draws)
+{
+    if (!c || (P && (!d_particles || !d_draws))) {
+        set_error("tsdfl_motion_apply_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P >= (1ull << 32)) {
+        set_error("tsdfl_motion_apply_device: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    return launch_motion(d_particles, P, nullptr, nullptr, 0, 0, d_draws, nullptr, c->stream);
+}
+
+namespace {
+
+int motion_host(tsdfl_ctx* c, float* particles, size_t P, const tsdfl_motion* m, uint64_t seed, uint64_t step,
+                const double* draws, const char* fn)
+{
+    if (!c || (P && !particles) || (!m && !draws && P)) {
+        set_error("%s: invalid argument", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P == 0) return TSDFL_OK;
+    if (P >= (1ull << 32)) {
+        set_error("%s: too many particles", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    const size_t part_b = align_up(sizeof(float) * 7 * P, 256);
+    const size_t draw_b = draws ? align_up(sizeof(double) * 6 * P, 256) : 0;
+    rc = ensure_io(c, part_b + draw_b);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_part = reinterpret_cast<float*>(io);
+    double* d_draws = draws ? reinterpret_cast<double*>(io + part_b) : nullptr;
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_part, particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice, s));
+    if (draws) CUDA_TRY(cudaMemcpyAsync(d_draws, draws, sizeof(double) * 6 * P, cudaMemcpyHostToDevice, s));
+    rc = draws ? launch_motion(d_part, P, nullptr, nullptr, 0, 0, d_draws, nullptr, s)
+               : launch_motion(d_part, P, m->mean, m->stddev, seed, step, nullptr, nullptr, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(particles, d_part, sizeof(float) * 7 * P, cudaMemcpyDeviceToHost, s));
+    return tsdfl_ctx_sync(c);
+}
+
+}  // namespace
+
+int tsdfl_motion_update(tsdfl_ctx* c, float* particles, size_t P, const tsdfl_motion* m, uint64_t seed,
+                        uint64_t step)
+{
+    if (!m) {
+        set_error("tsdfl_motion_update: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    return motion_host(c, particles, P, m, seed, step, nullptr, "tsdfl_motion_update");
+}
+
+int tsdfl_motion_apply(tsdfl_ctx* c, float* particles, size_t P, const double* draws)
+{
+    return motion_host(c, particles, P, nullptr, 0, 0, draws, "tsdfl_motion_apply");
+}
+
 }  // extern "C"
 
 // ------------------------------------------------ resampling without allocation

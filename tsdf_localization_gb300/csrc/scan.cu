@@ -14,8 +14,8 @@
 //
 // Layout: the cloud stays in its PointCloud2 byte layout (point_step bytes per
 // point, x, y, z as consecutive floats at x_offset as iter_x[0..2] reads them,
-// ring as int16 at ring_offset).  One tile = 1024 cloud points = one block of
-// 256 threads, 4 rounds of 256 consecutive points.  The (ring, centre) set is
+// ring as int16 at ring_offset).  One tile = 256 consecutive cloud points = one
+// block of 256 threads.  The (ring, centre) set is
 // an open-addressing hash table of 128-bit keys claimed with one 128-bit CAS
 // (empty = all ones; a key's high word holds the ring, < 64), load <= 1/2, with
 // the smallest index per key kept by atomicMin.
@@ -26,8 +26,8 @@
 //   scan_insert_kernel  index k, ring, centre; inserts (ring, centre) -> min k
 //   scan_winner_kernel  survivors (the key's minimum is the point's k); per-tile
 //                       survivors per ring
-//   scan_rings_kernel   output offset of every (ring, tile); total count (one block)
-//   scan_write_kernel   stable multi-split by ring: writes the survivors' x, y, z
+//   scan_rings_kernel   output offset of every (ring, tile) within its ring (a block per ring)
+//   scan_write_kernel   ring starts; stable multi-split by ring: writes the survivors' x, y, z
 #include <stdint.h>
 
 #include <atomic>
@@ -42,7 +42,7 @@ namespace {
 
 constexpr int kScanRings = 64;
 constexpr int kScanBlock = 256;
-constexpr int kScanRounds = 4;
+constexpr int kScanRounds = 1;
 constexpr int kScanTilePts = kScanBlock * kScanRounds;
 constexpr int kScanWarps = kScanBlock / 32;
 constexpr uint32_t kNotKept = 0xffffffffu;
@@ -70,7 +70,7 @@ struct ScanParams {
     uint32_t* slot;       // n: hash slot, kAlwaysStays
     int8_t* ring8;        // n: ring of kept points (-1 otherwise); after the winner pass: survivors only
     uint32_t* hist;       // kScanRings x tiles: survivors per (ring, tile), then their offsets
-    uint32_t* ring_base;  // kScanRings + 1: first output position of each ring; [kScanRings] = total
+    uint32_t* ring_base;  // kScanRings: survivors of each ring
     float* out;
     unsigned long long cap;
     uint32_t* count;
@@ -277,40 +277,40 @@ __global__ void __launch_bounds__(kScanBlock) scan_winner_kernel(ScanParams p)
     if (threadIdx.x < kScanRings) p.hist[(size_t)threadIdx.x * p.tiles + blockIdx.x] = s_hist[threadIdx.x];
 }
 
-// hist[ring][tile] -> first output position of the tile's survivors of that
-// ring, relative to the ring's start; ring_base[ring] = the ring's start.
-__global__ void __launch_bounds__(1024) scan_rings_kernel(ScanParams p)
+// One block per ring: hist[ring][tile] -> first output position of the
+// tile's survivors of that ring relative to the ring's start; ring_total[ring].
+__global__ void __launch_bounds__(kScanBlock) scan_rings_kernel(ScanParams p)
 {
-    __shared__ uint32_t s_tot[kScanRings];
+    __shared__ uint32_t s_warp[kScanWarps];
+    __shared__ uint32_t s_run;
+    const int ring = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int ring = w; ring < kScanRings; ring += 32) {
-        uint32_t* h = p.hist + (size_t)ring * p.tiles;
-        uint32_t run = 0;
-        for (uint32_t base = 0; base < p.tiles; base += 32) {
-            const uint32_t t = base + lane;
-            const uint32_t v = t < p.tiles ? h[t] : 0;
-            uint32_t inc = v;
+    uint32_t* h = p.hist + (size_t)ring * p.tiles;
+    if (threadIdx.x == 0) s_run = 0;
+    for (uint32_t base = 0; base < p.tiles; base += kScanBlock) {
+        const uint32_t t = base + threadIdx.x;
+        const uint32_t v = t < p.tiles ? h[t] : 0;
+        uint32_t inc = v;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += u;
-            }
-            if (t < p.tiles) h[t] = run + inc - v;
-            run += __shfl_sync(0xffffffffu, inc, 31);
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
         }
-        if (lane == 0) s_tot[ring] = run;
+        __syncthreads();   // s_run and s_warp of the previous chunk have been read
+        if (lane == 31) s_warp[w] = inc;
+        __syncthreads();
+        uint32_t before = s_run, total = 0;
+#pragma unroll
+        for (int q = 0; q < kScanWarps; ++q) {
+            before += q < w ? s_warp[q] : 0;
+            total += s_warp[q];
+        }
+        if (t < p.tiles) h[t] = before + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_run += total;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int ring = 0; ring < kScanRings; ++ring) {
-            p.ring_base[ring] = run;
-            run += s_tot[ring];
-        }
-        p.ring_base[kScanRings] = run;
-        *p.count = run;
-        if (run > p.cap) atomicExch(p.status, TSDFL_ERR_CAPACITY);
-    }
+    if (threadIdx.x == 0) p.ring_base[ring] = s_run;   // the ring's total; scan_write_kernel scans them
 }
 
 __global__ void __launch_bounds__(kScanBlock) scan_write_kernel(ScanParams p)
@@ -319,9 +319,24 @@ __global__ void __launch_bounds__(kScanBlock) scan_write_kernel(ScanParams p)
     __shared__ uint32_t s_run[kScanRings];
     __shared__ uint32_t s_off[kScanRings];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x < kScanRings) s_off[threadIdx.x] = p.ring_base[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {   // the rings' starts: exclusive prefix of their totals
+        uint32_t run = 0;
+        for (int r = 0; r < kScanRings; ++r) {
+            const uint32_t c = s_off[r];
+            s_off[r] = run;
+            run += c;
+        }
+        if (blockIdx.x == 0) {
+            *p.count = run;
+            if (run > p.cap) atomicExch(p.status, TSDFL_ERR_CAPACITY);
+        }
+    }
+    __syncthreads();
     if (threadIdx.x < kScanRings) {
         s_run[threadIdx.x] = 0;
-        s_off[threadIdx.x] = p.ring_base[threadIdx.x] + p.hist[(size_t)threadIdx.x * p.tiles + blockIdx.x];
+        s_off[threadIdx.x] += p.hist[(size_t)threadIdx.x * p.tiles + blockIdx.x];
     }
     const uint32_t t0 = blockIdx.x * kScanTilePts;
     for (int r = 0; r < kScanRounds; ++r) {
@@ -376,7 +391,7 @@ size_t scan_workspace_bytes(size_t n)
     const size_t slots = table_slots(n);
     auto a = [](size_t v) { return (v + 255) / 256 * 256; };
     return a(16 * slots) + a(4 * slots) + a(4 * (tiles + 1)) + a(4 * n) + a(4 * n) + a(n) +
-           a(4 * kScanRings * (tiles ? tiles : 1)) + a(4 * (kScanRings + 1));
+           a(4 * kScanRings * (tiles ? tiles : 1)) + a(4 * kScanRings);
 }
 
 int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t off_x, uint32_t off_ring, float cell,
@@ -422,7 +437,7 @@ int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t o
     scan_tiles_kernel<<<1, 1024, 0, s>>>(p);
     scan_insert_kernel<<<g, kScanBlock, 0, s>>>(p);
     scan_winner_kernel<<<g, kScanBlock, 0, s>>>(p);
-    scan_rings_kernel<<<1, 1024, 0, s>>>(p);
+    scan_rings_kernel<<<kScanRings, kScanBlock, 0, s>>>(p);
     scan_write_kernel<<<g, kScanBlock, 0, s>>>(p);
     g_launches += 6;
     return check(cudaGetLastError());

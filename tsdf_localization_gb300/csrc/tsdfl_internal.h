@@ -198,4 +198,8 @@ int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t o
                        bool own_ring, float* out, size_t cap, uint32_t* count, void* workspace, int32_t* status,
                        cudaStream_t s);
 
+// Motion update (motion.cu): draws from the generator when draws is null.
+int launch_motion(float* particles, size_t P, const double mean[6], const double stddev[6], uint64_t seed,
+                  uint64_t step, const double* draws, double* draws_out, cudaStream_t s);
+
 }  // namespace tsdfl

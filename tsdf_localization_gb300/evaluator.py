@@ -299,6 +299,58 @@ class ResidualSystematicResampler:
         return particles[idx].copy()
 
 
+class MotionModel:
+    """ParticleCloud's motion update (particle_cloud.cpp:153-617) on the GPU.
+
+    a = a_1 .. a_12 as setMotionParameters takes them (0.1 each by default,
+    particle_cloud.h:59-70).  update() draws on the device from a counter-based
+    generator keyed by the seed (one stream per step); apply() takes the draws
+    (P x 6: dx, dy, dz, roll, pitch, yaw) from the caller.  Either way the pose
+    composition is the reference's bit for bit."""
+
+    KINDS = {"odom": N.TSDFL_MOTION_ODOM, "imu": N.TSDFL_MOTION_IMU, "scale": N.TSDFL_MOTION_SCALE,
+             "scale_imu": N.TSDFL_MOTION_SCALE_IMU, "delta": N.TSDFL_MOTION_DELTA}
+
+    def __init__(self, ctx: Context, a=(0.1,) * 12, seed: int = 0):
+        self.ctx = ctx
+        self.set_motion_parameters(*a)
+        self.seed = int(seed)
+        self.step = 0
+
+    def set_motion_parameters(self, *a) -> None:
+        if len(a) != 12:
+            raise ValueError("12 motion parameters")
+        self.a = np.asarray(a, np.float32)
+
+    def distributions(self, kind: str, inputs, time_diff: float = 0.0) -> N.Motion:
+        """(mean, stddev) of the six draws as the overload `kind` sets them up:
+        odom (linear.x, angular.z), imu (linear_vel, angular_yaw), scale
+        (lin_scale, ang_scale), scale_imu (lin_scale, delta_roll, delta_pitch,
+        delta_yaw), delta (dx, dy, dz, roll, pitch, yaw, lin_base_noise,
+        ang_base_noise)."""
+        x = np.ascontiguousarray(inputs, np.float64)
+        m = N.Motion()
+        N.check(N.lib().tsdfl_motion_model(self.KINDS[kind], _ptr(self.a), _ptr(x), x.shape[0], time_diff,
+                                           C.byref(m)))
+        return m
+
+    def update(self, particles: np.ndarray, motion: N.Motion, step: int | None = None) -> np.ndarray:
+        """Moves particles (P, 7) float32 in place with device-drawn noise."""
+        if step is None:
+            step = self.step
+            self.step += 1
+        N.check(N.lib().tsdfl_motion_update(self.ctx.handle, _ptr(particles), particles.shape[0], C.byref(motion),
+                                            self.seed, int(step)))
+        return particles
+
+    def apply(self, particles: np.ndarray, draws: np.ndarray) -> np.ndarray:
+        d = np.ascontiguousarray(draws, np.float64)
+        if d.shape != (particles.shape[0], 6):
+            raise ValueError("draws must be (P, 6)")
+        N.check(N.lib().tsdfl_motion_apply(self.ctx.handle, _ptr(particles), particles.shape[0], _ptr(d)))
+        return particles
+
+
 def code_values(sigma: float = 0.1, init_value: float = 0.0) -> np.ndarray:
     out = np.zeros(601, np.float32)
     N.check(N.lib().tsdfl_code_values(sigma, init_value, _ptr(out)))
