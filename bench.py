@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-scan", action="store_true", help="skip the scan-reduction side measurement")
+    ap.add_argument("--no-scan", action="store_true", help="skip the scan-reduction and motion side measurements")
     return ap.parse_args()
 
 
@@ -175,11 +175,12 @@ def _reference_map(O, wl):
     return O.RefMap.from_slots(wl.coef, wl.grid_occ, wl.float_data())
 
 
-def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 100) -> dict:
+def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 20) -> dict:
     """Times the scan reduction (evaluateParticles' pre-processing) on the raw
     64 x 2048 ray-cast cloud the workload's points come from: the device form
-    with CUDA events on the context's stream, the host form (pageable cloud in,
-    points out) with a host clock, and the oracle on one host core."""
+    replayed from a CUDA graph of `reps` calls (CUDA events on the context's
+    stream, so host launch costs are excluded), the host form (pageable cloud
+    in, points out) with a host clock, and the oracle on one host core."""
     import torch
 
     from tsdf_localization_gb300 import _native as N
@@ -191,6 +192,7 @@ def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps:
     out = torch.empty((n, 3), dtype=torch.float32, device=device)
     cnt = torch.zeros(1, dtype=torch.int32, device=device)
     vp = C.c_void_p
+    torch.cuda.synchronize()
 
     def dev():
         N.check(lib.tsdfl_reduce_scan_device(ctx.handle, vp(blob.data_ptr()), n, 16, 0, 12, 0.05, 0,
@@ -200,10 +202,16 @@ def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps:
         for _ in range(5):
             dev()
         ctx.sync()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            for _ in range(reps):
+                dev()
+        for _ in range(3):
+            graph.replay()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(reps):
-            dev()
+        for _ in range(10):
+            graph.replay()
         e1.record(stream)
         e1.synchronize()
         ctx.sync()
@@ -217,7 +225,7 @@ def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps:
                                       ho.ctypes.data_as(vp), n, C.byref(hc)))
         tt.append(time.perf_counter() - t0)
     res = {"cloud": "64x2048 ray-cast, building at 0.05 m, 16-byte records", "raw_points": n, "reduced_points": m,
-           "cell_m": 0.05, "device_us": 1000.0 * e0.elapsed_time(e1) / reps,
+           "cell_m": 0.05, "device_us": 1000.0 * e0.elapsed_time(e1) / (10 * reps),
            "host_api_us": 1e6 * float(np.median(tt)), "launches_per_call": 6}
     if with_cpu:
         from oracle import oracle_py as O
@@ -225,6 +233,39 @@ def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps:
         ref = O.reduce_scan(xyz, ring, 0.05)
         res["cpu_oracle_ms"] = 1000.0 * (time.perf_counter() - t0)
         res["matches_oracle"] = bool(np.array_equal(ho[:hc.value], ref))
+    return res
+
+
+def motion_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 20) -> dict:
+    """Times the motion update (ParticleCloud::apply_model with device-drawn
+    noise, odometry 0.8 m/s, 0.2 rad/s, 0.1 s) on the workload's particles."""
+    import torch
+
+    from tsdf_localization_gb300 import MotionModel
+    from tsdf_localization_gb300 import _native as N
+    P = int(wl.particles.shape[0])
+    mm = MotionModel(ctx)
+    m = mm.distributions("odom", [0.8, 0.2], 0.1)
+    d = torch.from_numpy(wl.particles.copy()).to(device)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(3):
+            N.check(lib.tsdfl_motion_update_device(ctx.handle, C.c_void_p(d.data_ptr()), P, C.byref(m), 1, i, None))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(reps):
+            N.check(lib.tsdfl_motion_update_device(ctx.handle, C.c_void_p(d.data_ptr()), P, C.byref(m), 1, 10 + i,
+                                                   None))
+        e1.record(stream)
+        e1.synchronize()
+        ctx.sync()
+    res = {"particles": P, "device_us": 1000.0 * e0.elapsed_time(e1) / reps, "rng": "Philox4x64-10, Box-Muller FP64"}
+    if with_cpu:
+        from oracle import oracle_py as O
+        draws = np.random.default_rng(0).normal(0, 0.01, (P, 6))
+        t0 = time.perf_counter()
+        O.motion_apply(wl.particles, draws)
+        res["cpu_oracle_ms"] = 1000.0 * (time.perf_counter() - t0)
     return res
 
 
@@ -415,9 +456,10 @@ def main():
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base, _ = cpu_baseline(wl)
-    scan = None
+    scan = motion = None
     if not args.no_scan:
         scan = scan_reduction_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)
+        motion = motion_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -430,7 +472,8 @@ def main():
                           "step": "sensor update + normalise + mean pose + systematic resample",
                           "form": "plain single filter", "parallelism": f"replicas x{world}"},
                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
-               "latency_ms": latency, "clocks": clocks, "scan_reduction": scan}
+               "latency_ms": latency, "clocks": clocks, "scan_reduction": scan,
+               "motion_update": motion}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
