@@ -198,6 +198,46 @@ int tsdfl_resample_residual_systematic_device(tsdfl_ctx* ctx, const float* d_par
  * where the reference would index with -1).  d_particles: M x 7 floats. */
 int tsdfl_best_particle_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint32_t* d_index);
 
+/* ---- the reference's other resamplers ----
+ * WheelResampler (src/resampling/wheel_resampler.cpp:6-33), ResidualResampler
+ * (novel_resampling.h:9-35), MetropolisResampler (:106-143) and
+ * RejectionResampler (:146-187), all emitting exactly M particles.  Random
+ * draws come from the caller -- the reference's own sequence drawn on the host
+ * in its order, which makes the output the reference's bit for bit -- or, when
+ * the draw pointer is NULL, from Philox4x64-10 on the device keyed by seed.
+ * Host forms: weights[M] in, the source index of every output particle out
+ * (idx_out[M]).  Device forms: M x 7 particles gathered into d_out.
+ *
+ * wheel: draws[M] doubles in [0, 1) (uniform_distribution(0.0, 1.0)); output
+ *   i takes the first particle whose float running weight sum reaches
+ *   (float)draw, and stays itself when none does.
+ * residual: draws[n_draws] particle indices (uniform_int_distribution(0, M-1));
+ *   each drawn particle is copied ceil(M * w) times until M are emitted.  Too
+ *   few draws (or, generated, more than 4M + 4096 needed) -> TSDFL_ERR_UNSUPPORTED.
+ * metropolis: `steps` proposals per output (the reference's sampling_steps, 50
+ *   in mcl_3d.cpp:258); u_draws[M*steps] floats, j_draws[M*steps] indices, in
+ *   the reference's order (output-major, u before j); acceptance u <= w_j / w_0
+ *   (the reference keeps particle 0 as the comparison particle).
+ * rejection: device draws only (how many the reference consumes depends on the
+ *   outcomes); u <= w_j / max(0, max w) accepts; an output still rejecting after
+ *   2^20 proposals stops with TSDFL_ERR_UNSUPPORTED. */
+int tsdfl_resample_wheel(tsdfl_ctx* ctx, const float* weights, size_t M, const double* draws, uint64_t seed,
+                         uint32_t* idx_out);
+int tsdfl_resample_wheel_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, const double* d_draws,
+                                uint64_t seed, float* d_out);
+int tsdfl_resample_residual(tsdfl_ctx* ctx, const float* weights, size_t M, const uint32_t* draws, size_t n_draws,
+                            uint64_t seed, uint32_t* idx_out);
+int tsdfl_resample_residual_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, const uint32_t* d_draws,
+                                   size_t n_draws, uint64_t seed, float* d_out);
+int tsdfl_resample_metropolis(tsdfl_ctx* ctx, const float* weights, size_t M, uint32_t steps, const float* u_draws,
+                              const uint32_t* j_draws, uint64_t seed, uint32_t* idx_out);
+int tsdfl_resample_metropolis_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint32_t steps,
+                                     const float* d_u_draws, const uint32_t* d_j_draws, uint64_t seed,
+                                     float* d_out);
+int tsdfl_resample_rejection(tsdfl_ctx* ctx, const float* weights, size_t M, uint64_t seed, uint32_t* idx_out);
+int tsdfl_resample_rejection_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint64_t seed,
+                                    float* d_out);
+
 /* ---- scan reduction ----
  * The pre-processing of TSDFEvaluator::evaluateParticles
  * (tsdf_evaluator.cpp:304-376) on a PointCloud2's data: points closer than

@@ -13,6 +13,9 @@
  *       TSDFEvaluator::evaluateParticles (src/evaluation/tsdf_evaluator.cpp:304-374)
  *   tsdf_localization::GpuMotionModel replaces ParticleCloud's motion-update
  *       overloads (src/particle_cloud.cpp:153-617)
+ *   tsdf_localization::GpuWheelResampler, GpuResidualResampler,
+ *       GpuMetropolisResampler, GpuRejectionResampler replace the other
+ *       resamplers mcl_3d selects (mcl_3d.cpp:246-261)
  *
  * Errors surface as std::runtime_error carrying libtsdfl's message, as the
  * reference's evaluators throw them ("No particle is valid!" for a zero
@@ -198,6 +201,118 @@ void resample_residual_systematic(Context& ctx, std::vector<ParticleT>& particle
     out.reserve(count);
     for (size_t k = 0; k < count; ++k) out.push_back(particles[idx[k]]);
     particles = std::move(out);
+}
+
+// The reference's other resamplers (Wheel, Residual, Metropolis, Rejection) on
+// a caller's particle vector.  With a generator, the draws are taken from it
+// with the reference's distributions and in its order (Rejection excepted, see
+// below), so the same generator state gives the reference's particles bit for
+// bit and leaves the generator where the reference leaves it; without one, the
+// device draws them from Philox keyed by seed.
+namespace detail {
+template <class ParticleT>
+std::vector<float> weights_of(const std::vector<ParticleT>& particles)
+{
+    std::vector<float> w(particles.size());
+    for (size_t i = 0; i < particles.size(); ++i) w[i] = particles[i].second;
+    return w;
+}
+template <class ParticleT>
+void take(std::vector<ParticleT>& particles, const std::vector<uint32_t>& idx)
+{
+    std::vector<ParticleT> out;
+    out.reserve(idx.size());
+    for (uint32_t k : idx) out.push_back(particles[k]);
+    particles = std::move(out);
+}
+}  // namespace detail
+
+// WheelResampler (wheel_resampler.cpp:6-33): one uniform_real_distribution<>
+// draw per particle.
+template <class ParticleT, class Generator>
+void resample_wheel(Context& ctx, std::vector<ParticleT>& particles, Generator* gen, uint64_t seed = 0)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    const std::vector<float> w = detail::weights_of(particles);
+    std::vector<double> draws;
+    if (gen) {
+        std::uniform_real_distribution<> d(0.0, 1.0);
+        draws.resize(M);
+        for (size_t i = 0; i < M; ++i) draws[i] = d(*gen);
+    }
+    std::vector<uint32_t> idx(M);
+    check(tsdfl_resample_wheel(ctx.get(), w.data(), M, gen ? draws.data() : nullptr, seed, idx.data()));
+    detail::take(particles, idx);
+}
+
+// ResidualResampler (novel_resampling.h:9-35): uniform_int_distribution
+// draws, as many as the reference takes (counted on the host from the
+// weights, novel_resampling.h:19-30), then the copies on the device.
+template <class ParticleT, class Generator>
+void resample_residual(Context& ctx, std::vector<ParticleT>& particles, Generator* gen, uint64_t seed = 0)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    const std::vector<float> w = detail::weights_of(particles);
+    std::vector<uint32_t> draws;
+    if (gen) {
+        std::uniform_int_distribution<size_t> d(0, M - 1);
+        size_t filled = 0;
+        while (filled < M) {
+            const size_t r = d(*gen);
+            draws.push_back((uint32_t)r);
+            const float expected = w[r] * M;
+            const size_t left = M - filled;
+            const float insertions = expected <= left ? expected : left;
+            for (size_t k = 0; k < insertions; ++k) ++filled;
+        }
+    }
+    std::vector<uint32_t> idx(M);
+    check(tsdfl_resample_residual(ctx.get(), w.data(), M, gen ? draws.data() : nullptr, draws.size(), seed,
+                                  idx.data()));
+    detail::take(particles, idx);
+}
+
+// MetropolisResampler(steps) (novel_resampling.h:106-143): per output and
+// step, a uniform_real_distribution<float> then a uniform_int_distribution draw.
+template <class ParticleT, class Generator>
+void resample_metropolis(Context& ctx, std::vector<ParticleT>& particles, uint32_t steps, Generator* gen,
+                         uint64_t seed = 0)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    const std::vector<float> w = detail::weights_of(particles);
+    std::vector<float> u;
+    std::vector<uint32_t> j;
+    if (gen) {
+        std::uniform_real_distribution<float> du(0.0, 1.0);
+        std::uniform_int_distribution<size_t> dj(0, M - 1);
+        u.resize(M * steps);
+        j.resize(M * steps);
+        for (size_t k = 0; k < M * steps; ++k) {
+            u[k] = du(*gen);
+            j[k] = (uint32_t)dj(*gen);
+        }
+    }
+    std::vector<uint32_t> idx(M);
+    check(tsdfl_resample_metropolis(ctx.get(), w.data(), M, steps, gen ? u.data() : nullptr,
+                                    gen ? j.data() : nullptr, seed, idx.data()));
+    detail::take(particles, idx);
+}
+
+// RejectionResampler (novel_resampling.h:146-187) with device draws: how many
+// draws the reference takes depends on its outcomes, so its sequence cannot
+// be handed over in advance.
+template <class ParticleT>
+void resample_rejection(Context& ctx, std::vector<ParticleT>& particles, uint64_t seed)
+{
+    const size_t M = particles.size();
+    if (M == 0) return;
+    const std::vector<float> w = detail::weights_of(particles);
+    std::vector<uint32_t> idx(M);
+    check(tsdfl_resample_rejection(ctx.get(), w.data(), M, seed, idx.data()));
+    detail::take(particles, idx);
 }
 
 // The scan reduction of TSDFEvaluator::evaluateParticles
@@ -444,6 +559,63 @@ private:
     std::unique_ptr<tsdfl::Context> ctx_;
     std::unique_ptr<tsdfl::Map> map_;
     std::unique_ptr<tsdfl::SensorUpdate> update_;
+};
+
+// Drop-ins for the other resamplers mcl_3d can select (mcl_3d.cpp:246-261).
+// Wheel, Residual and Metropolis draw from the inherited generator in the
+// reference's order (same generator state: same particles, generator left
+// where the reference leaves it); Rejection seeds the device generator from it.
+class GpuWheelResampler : public Resampler {
+public:
+    explicit GpuWheelResampler(int device = 0) : ctx_(new tsdfl::Context(device)) {}
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        tsdfl::resample_wheel(*ctx_, particle_cloud.particles(), m_generator_ptr.get());
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+};
+
+class GpuResidualResampler : public Resampler {
+public:
+    explicit GpuResidualResampler(int device = 0) : ctx_(new tsdfl::Context(device)) {}
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        tsdfl::resample_residual(*ctx_, particle_cloud.particles(), m_generator_ptr.get());
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+};
+
+class GpuMetropolisResampler : public Resampler {
+public:
+    explicit GpuMetropolisResampler(size_t sampling_steps, int device = 0)
+        : ctx_(new tsdfl::Context(device)), steps_((uint32_t)sampling_steps)
+    {
+    }
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        tsdfl::resample_metropolis(*ctx_, particle_cloud.particles(), steps_, m_generator_ptr.get());
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
+    uint32_t steps_;
+};
+
+class GpuRejectionResampler : public Resampler {
+public:
+    explicit GpuRejectionResampler(int device = 0) : ctx_(new tsdfl::Context(device)) {}
+    void resample(ParticleCloud& particle_cloud) override
+    {
+        const uint64_t seed = ((uint64_t)(*m_generator_ptr)() << 32) | (*m_generator_ptr)();
+        tsdfl::resample_rejection(*ctx_, particle_cloud.particles(), seed);
+    }
+
+private:
+    std::unique_ptr<tsdfl::Context> ctx_;
 };
 
 // Drop-in for ParticleCloud's motion-update overloads (particle_cloud.cpp:153-497):

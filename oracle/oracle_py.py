@@ -73,6 +73,14 @@ def oracle() -> C.CDLL:
                                                 C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
         L.orc_resample_systematic.restype = SZ
         L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
+        L.orc_resample_wheel.restype = None
+        L.orc_resample_wheel.argtypes = [P, SZ, P, P]
+        L.orc_resample_residual.restype = SZ
+        L.orc_resample_residual.argtypes = [P, SZ, P, SZ, P]
+        L.orc_resample_metropolis.restype = None
+        L.orc_resample_metropolis.argtypes = [P, SZ, C.c_uint32, P, P, P]
+        L.orc_resample_rejection.restype = C.c_int
+        L.orc_resample_rejection.argtypes = [P, SZ, P, P, P, C.c_uint32, P]
         L.orc_motion_apply.restype = None
         L.orc_motion_apply.argtypes = [P, SZ, P]
         L.orc_reduce_scan.restype = SZ
@@ -116,6 +124,19 @@ def reference() -> C.CDLL:
         L.ref_draw_u01.argtypes = [C.c_uint32]
         L.ref_resample_residual_systematic.restype = SZ
         L.ref_resample_residual_systematic.argtypes = [P, SZ, C.c_uint32, P, SZ]
+        for name in ("ref_resample_wheel", "ref_resample_residual", "ref_resample_rejection"):
+            getattr(L, name).restype = SZ
+            getattr(L, name).argtypes = [P, SZ, C.c_uint32, P, SZ]
+        L.ref_resample_metropolis.restype = SZ
+        L.ref_resample_metropolis.argtypes = [P, SZ, C.c_uint32, C.c_uint32, P, SZ]
+        L.ref_resample_next.restype = C.c_uint32
+        L.ref_resample_next.argtypes = [C.c_int, P, SZ, C.c_uint32, C.c_uint32]
+        L.ref_draws_wheel.argtypes = [C.c_uint32, SZ, P]
+        L.ref_draws_residual.argtypes = [C.c_uint32, SZ, SZ, P]
+        L.ref_draws_metropolis.argtypes = [C.c_uint32, SZ, C.c_uint32, P, P]
+        L.ref_draw_source_create.restype = P
+        L.ref_draw_source_create.argtypes = [C.c_uint32, SZ]
+        L.ref_draw_source_destroy.argtypes = [P]
         L.ref_motion_update.restype = None
         L.ref_motion_update.argtypes = [P, SZ, P]
         L.ref_reduce_scan.restype = SZ
@@ -264,6 +285,154 @@ def ref_motion_update(particles: np.ndarray, delta) -> np.ndarray:
     d = np.ascontiguousarray(delta, np.float32)
     reference().ref_motion_update(_ptr(p), p.shape[0], _ptr(d))
     return p
+
+
+def resample_wheel(w: np.ndarray, draws: np.ndarray) -> np.ndarray:
+    """WheelResampler on given draws (doubles in [0, 1)): source index per output."""
+    w = np.ascontiguousarray(w, np.float32)
+    d = np.ascontiguousarray(draws, np.float64)
+    out = np.zeros(w.shape[0], np.uint32)
+    oracle().orc_resample_wheel(_ptr(w), w.shape[0], _ptr(d), _ptr(out))
+    return out
+
+
+def resample_residual(w: np.ndarray, draws: np.ndarray):
+    """ResidualResampler on given draws (particle indices): (indices, draws used)."""
+    w = np.ascontiguousarray(w, np.float32)
+    d = np.ascontiguousarray(draws, np.uint32)
+    out = np.zeros(w.shape[0], np.uint32)
+    used = oracle().orc_resample_residual(_ptr(w), w.shape[0], _ptr(d), d.shape[0], _ptr(out))
+    if used == (1 << 64) - 1:
+        raise ValueError("the draws ran out")
+    return out, used
+
+
+def resample_metropolis(w: np.ndarray, steps: int, u: np.ndarray, j: np.ndarray) -> np.ndarray:
+    w = np.ascontiguousarray(w, np.float32)
+    u = np.ascontiguousarray(u, np.float32)
+    j = np.ascontiguousarray(j, np.uint32)
+    out = np.zeros(w.shape[0], np.uint32)
+    oracle().orc_resample_metropolis(_ptr(w), w.shape[0], steps, _ptr(u), _ptr(j), _ptr(out))
+    return out
+
+
+REJECTION_ROUNDS = 1 << 20
+STREAMS = {"motion": 0x6D6F74696F6E0001, "wheel": 0x776865656C000001, "residual": 0x7265736964000001,
+           "metropolis": 0x6D6574726F000001, "rejection": 0x72656A6563000001}
+
+
+def resample_rejection_philox(w: np.ndarray, seed: int) -> np.ndarray:
+    """RejectionResampler with the device's Philox draws (counter (i, t), key (seed, stream))."""
+    w = np.ascontiguousarray(w, np.float32)
+    src = np.array([seed, STREAMS["rejection"], w.shape[0]], np.uint64)
+    out = np.zeros(w.shape[0], np.uint32)
+    L = oracle()
+    rc = L.orc_resample_rejection(_ptr(w), w.shape[0], C.cast(L.orc_philox_u, P), C.cast(L.orc_philox_j, P),
+                                  _ptr(src), REJECTION_ROUNDS, _ptr(out))
+    if rc:
+        raise ValueError("an output exceeded the proposal limit")
+    return out
+
+
+def resample_rejection_reference_draws(w: np.ndarray, seed: int) -> np.ndarray:
+    """The oracle's RejectionResampler drawing from the reference's own generator
+    and distributions (seeded mt19937), in the reference's order."""
+    w = np.ascontiguousarray(w, np.float32)
+    R = reference()
+    src = R.ref_draw_source_create(seed, w.shape[0])
+    try:
+        out = np.zeros(w.shape[0], np.uint32)
+        rc = oracle().orc_resample_rejection(_ptr(w), w.shape[0], C.cast(R.ref_draw_source_u, P),
+                                             C.cast(R.ref_draw_source_j, P), src, REJECTION_ROUNDS, _ptr(out))
+        if rc:
+            raise ValueError("an output exceeded the proposal limit")
+        return out
+    finally:
+        R.ref_draw_source_destroy(src)
+
+
+_DRAW_U = C.CFUNCTYPE(C.c_float, C.c_void_p, C.c_size_t, C.c_uint32)
+_DRAW_J = C.CFUNCTYPE(C.c_uint32, C.c_void_p, C.c_size_t, C.c_uint32)
+
+
+def resample_rejection_arrays(w: np.ndarray, u_seq, j_seq, record: bool = False):
+    """The oracle's RejectionResampler consuming u and j draws from two sequences
+    in order (the reference's consumption order).  With record=True the
+    sequences are callables producing the next draw, and the draws consumed are
+    returned alongside the indices."""
+    w = np.ascontiguousarray(w, np.float32)
+    used_u, used_j = [], []
+    it_u = iter(u_seq) if not callable(u_seq) else None
+    it_j = iter(j_seq) if not callable(j_seq) else None
+
+    def du(_src, _i, _t):
+        v = float(u_seq() if it_u is None else next(it_u))
+        used_u.append(v)
+        return v
+
+    def dj(_src, _i, _t):
+        v = int(j_seq() if it_j is None else next(it_j))
+        used_j.append(v)
+        return v
+
+    fu, fj = _DRAW_U(du), _DRAW_J(dj)
+    out = np.zeros(w.shape[0], np.uint32)
+    rc = oracle().orc_resample_rejection(_ptr(w), w.shape[0], C.cast(fu, P), C.cast(fj, P), None,
+                                         REJECTION_ROUNDS, _ptr(out))
+    if rc:
+        raise ValueError("an output exceeded the proposal limit")
+    if record:
+        return out, np.array(used_u, np.float32), np.array(used_j, np.uint32)
+    return out
+
+
+def ref_rejection_draw_callables(seed: int, M: int):
+    """next-u and next-j callables over the reference's generator and distributions."""
+    R = reference()
+    src = R.ref_draw_source_create(seed, M)
+    R.ref_draw_source_u.restype = C.c_float
+    R.ref_draw_source_u.argtypes = [P, SZ, C.c_uint32]
+    R.ref_draw_source_j.restype = C.c_uint32
+    R.ref_draw_source_j.argtypes = [P, SZ, C.c_uint32]
+    return (lambda: R.ref_draw_source_u(src, 0, 0)), (lambda: R.ref_draw_source_j(src, 0, 0)), \
+        (lambda: R.ref_draw_source_destroy(src))
+
+
+def ref_resample(kind: str, w: np.ndarray, seed: int, steps: int = 50) -> np.ndarray:
+    """The reference's own Wheel/Residual/Metropolis/Rejection resampler, seeded."""
+    w = np.ascontiguousarray(w, np.float32)
+    out = np.zeros(w.shape[0], np.uint32)
+    R = reference()
+    if kind == "metropolis":
+        n = R.ref_resample_metropolis(_ptr(w), w.shape[0], steps, seed, _ptr(out), out.shape[0])
+    else:
+        n = getattr(R, f"ref_resample_{kind}")(_ptr(w), w.shape[0], seed, _ptr(out), out.shape[0])
+    assert n == w.shape[0]
+    return out
+
+
+def ref_resample_next(kind: int, w: np.ndarray, seed: int, steps: int = 50) -> int:
+    """The seeded generator's next output after the reference's Wheel (0),
+    Residual (1) or Metropolis (2) resampler ran."""
+    w = np.ascontiguousarray(w, np.float32)
+    return int(reference().ref_resample_next(kind, _ptr(w), w.shape[0], steps, seed))
+
+
+def ref_draws(kind: str, seed: int, M: int, K: int = 0, steps: int = 50):
+    """The draws the reference's resampler takes from mt19937(seed), in its order."""
+    R = reference()
+    if kind == "wheel":
+        d = np.zeros(M, np.float64)
+        R.ref_draws_wheel(seed, M, _ptr(d))
+        return d
+    if kind == "residual":
+        d = np.zeros(K, np.uint32)
+        R.ref_draws_residual(seed, M, K, _ptr(d))
+        return d
+    u = np.zeros(M * steps, np.float32)
+    j = np.zeros(M * steps, np.uint32)
+    R.ref_draws_metropolis(seed, M, steps, _ptr(u), _ptr(j))
+    return u, j
 
 
 PHILOX_M = (0xD2E7470EE14C6C93, 0xCA5A826395121157)

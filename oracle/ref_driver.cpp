@@ -12,6 +12,7 @@
 #include <tsdf_localization/evaluation/tsdf_evaluator.h>
 #include <tsdf_localization/particle_cloud.h>
 #include <tsdf_localization/resampling/novel_resampling.h>
+#include <tsdf_localization/resampling/wheel_resampler.h>
 #include <tsdf_localization/util/constant.h>
 
 #include <omp.h>
@@ -86,6 +87,56 @@ struct SeededSystematic : SystematicResampler {
 struct SeededResidualSystematic : ResidualSystematicResampler {
     explicit SeededResidualSystematic(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
 };
+
+struct SeededWheel : WheelResampler {
+    explicit SeededWheel(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
+    uint32_t next() { return (*m_generator_ptr)(); }
+};
+
+struct SeededResidual : ResidualResampler {
+    explicit SeededResidual(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
+    uint32_t next() { return (*m_generator_ptr)(); }
+};
+
+struct SeededMetropolis : MetropolisResampler {
+    SeededMetropolis(size_t steps, uint32_t seed) : MetropolisResampler(steps)
+    {
+        m_generator_ptr.reset(new std::mt19937(seed));
+    }
+    uint32_t next() { return (*m_generator_ptr)(); }
+};
+
+struct SeededRejection : RejectionResampler {
+    explicit SeededRejection(uint32_t seed) { m_generator_ptr.reset(new std::mt19937(seed)); }
+    uint32_t next() { return (*m_generator_ptr)(); }
+};
+
+// The same generator and distributions as the reference's resamplers, drawn
+// on demand in the order the caller asks for them.
+struct DrawSource {
+    std::mt19937 gen;
+    std::uniform_real_distribution<FLOAT_T> u01{0.0, 1.0};
+    std::uniform_int_distribution<size_t> index;
+    DrawSource(uint32_t seed, size_t M) : gen(seed), index(0, M - 1) {}
+};
+
+// Runs a resampler on particles whose x holds their index; writes the indices.
+template <class R>
+size_t run_indexed(R& r, const float* w, size_t M, uint32_t* idx_out, size_t cap)
+{
+    ParticleCloud cloud;
+    auto& v = cloud.particles();
+    v.resize(M);
+    for (size_t i = 0; i < M; ++i) {
+        for (int k = 0; k < 6; ++k) v[i].first[k] = 0.0f;
+        v[i].first[0] = (float)i;
+        v[i].second = w[i];
+    }
+    r.resample(cloud);
+    size_t n = cloud.particles().size();
+    for (size_t i = 0; i < n && i < cap; ++i) idx_out[i] = (uint32_t)cloud.particles()[i].first[0];
+    return n;
+}
 
 struct MapHandle {
     std::shared_ptr<Map> map;
@@ -280,6 +331,85 @@ size_t ref_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float ce
         out[3 * i + 2] = ev.captured[i].z;
     }
     return ev.captured.size();
+}
+
+// The reference's other resamplers with generators seeded by seed (outputs as indices).
+size_t ref_resample_wheel(const float* w, size_t M, uint32_t seed, uint32_t* idx_out, size_t cap)
+{
+    SeededWheel r(seed);
+    return run_indexed(r, w, M, idx_out, cap);
+}
+size_t ref_resample_residual(const float* w, size_t M, uint32_t seed, uint32_t* idx_out, size_t cap)
+{
+    SeededResidual r(seed);
+    return run_indexed(r, w, M, idx_out, cap);
+}
+size_t ref_resample_metropolis(const float* w, size_t M, uint32_t steps, uint32_t seed, uint32_t* idx_out,
+                               size_t cap)
+{
+    SeededMetropolis r(steps, seed);
+    return run_indexed(r, w, M, idx_out, cap);
+}
+size_t ref_resample_rejection(const float* w, size_t M, uint32_t seed, uint32_t* idx_out, size_t cap)
+{
+    SeededRejection r(seed);
+    return run_indexed(r, w, M, idx_out, cap);
+}
+
+// The generator's next output after the seeded resampler ran (kind 0 wheel,
+// 1 residual, 2 metropolis).
+uint32_t ref_resample_next(int kind, const float* w, size_t M, uint32_t steps, uint32_t seed)
+{
+    std::vector<uint32_t> idx(M);
+    if (kind == 0) {
+        SeededWheel r(seed);
+        run_indexed(r, w, M, idx.data(), M);
+        return r.next();
+    }
+    if (kind == 1) {
+        SeededResidual r(seed);
+        run_indexed(r, w, M, idx.data(), M);
+        return r.next();
+    }
+    SeededMetropolis r(steps, seed);
+    run_indexed(r, w, M, idx.data(), M);
+    return r.next();
+}
+
+// The draws those resamplers take from a generator seeded by seed, in their order.
+void ref_draws_wheel(uint32_t seed, size_t M, double* out)
+{
+    std::mt19937 g(seed);
+    std::uniform_real_distribution<> d(0.0, 1.0);
+    for (size_t i = 0; i < M; ++i) out[i] = d(g);
+}
+void ref_draws_residual(uint32_t seed, size_t M, size_t K, uint32_t* out)
+{
+    std::mt19937 g(seed);
+    std::uniform_int_distribution<size_t> d(0, M - 1);
+    for (size_t k = 0; k < K; ++k) out[k] = (uint32_t)d(g);
+}
+void ref_draws_metropolis(uint32_t seed, size_t M, uint32_t steps, float* u, uint32_t* j)
+{
+    std::mt19937 g(seed);
+    std::uniform_real_distribution<FLOAT_T> du(0.0, 1.0);
+    std::uniform_int_distribution<size_t> dj(0, M - 1);
+    for (size_t i = 0; i < (size_t)M * steps; ++i) {
+        u[i] = du(g);
+        j[i] = (uint32_t)dj(g);
+    }
+}
+void* ref_draw_source_create(uint32_t seed, size_t M) { return new DrawSource(seed, M); }
+void ref_draw_source_destroy(void* s) { delete static_cast<DrawSource*>(s); }
+float ref_draw_source_u(void* s, size_t, uint32_t)
+{
+    auto* d = static_cast<DrawSource*>(s);
+    return d->u01(d->gen);
+}
+uint32_t ref_draw_source_j(void* s, size_t, uint32_t)
+{
+    auto* d = static_cast<DrawSource*>(s);
+    return (uint32_t)d->index(d->gen);
 }
 
 // ParticleCloud::motion_update (particle_cloud.cpp:456-497) with every noise

@@ -523,3 +523,108 @@ void orc_motion_apply(float* particles, size_t P, const double* draws)
         p[5] = yaw;
     }
 }
+
+/* wheel_resampler.cpp:13-30 */
+void orc_resample_wheel(const float* w, size_t M, const double* draws, uint32_t* idx)
+{
+    for (size_t i = 0; i < M; ++i) {
+        float random_value = (float)draws[i];
+        float weight_sum = 0.0f;
+        idx[i] = (uint32_t)i;
+        for (size_t m = 0; m < M; ++m) {
+            weight_sum += w[m];
+            if (random_value <= weight_sum) {
+                idx[i] = (uint32_t)m;
+                break;
+            }
+        }
+    }
+}
+
+/* novel_resampling.h:14-31 */
+size_t orc_resample_residual(const float* w, size_t M, const uint32_t* draws, size_t K, uint32_t* idx)
+{
+    size_t filled = 0, used = 0;
+    while (filled < M) {
+        if (used >= K) return (size_t)-1;
+        size_t r = draws[used++];
+        float expected = w[r] * (float)M;
+        size_t left = M - filled;
+        float insertions = expected <= (float)left ? expected : (float)left;
+        for (size_t k = 0; (float)k < insertions; ++k) idx[filled++] = (uint32_t)r;
+    }
+    return used;
+}
+
+/* novel_resampling.h:118-139: particle_k stays particle 0 */
+void orc_resample_metropolis(const float* w, size_t M, uint32_t steps, const float* u, const uint32_t* j,
+                             uint32_t* idx)
+{
+    for (size_t i = 0; i < M; ++i) {
+        size_t k = 0;
+        for (uint32_t n = 0; n < steps; ++n) {
+            float un = u[i * steps + n];
+            uint32_t jn = j[i * steps + n];
+            if (un <= w[jn] / w[0]) k = jn;
+        }
+        idx[i] = (uint32_t)k;
+    }
+}
+
+/* novel_resampling.h:158-183 */
+int orc_resample_rejection(const float* w, size_t M, orc_draw_u_fn du, orc_draw_j_fn dj, void* src,
+                           uint32_t max_rounds, uint32_t* idx)
+{
+    double sup_w = 0.0;
+    for (size_t m = 0; m < M; ++m)
+        if (sup_w < w[m]) sup_w = w[m];
+    int rc = 0;
+    for (size_t i = 0; i < M; ++i) {
+        size_t j = i;
+        float u = du(src, i, 0);
+        uint32_t t = 1;
+        while (u > (w[j] / sup_w)) {
+            if (t > max_rounds) {
+                rc = -1;
+                break;
+            }
+            j = dj(src, i, t);
+            u = du(src, i, t);
+            ++t;
+        }
+        idx[i] = (uint32_t)j;
+    }
+    return rc;
+}
+
+void orc_philox4x64_10(uint64_t c[4], uint64_t k0, uint64_t k1)
+{
+    const uint64_t m0 = 0xD2E7470EE14C6C93ull, m1 = 0xCA5A826395121157ull;
+    const uint64_t w0 = 0x9E3779B97F4A7C15ull, w1 = 0xBB67AE8584CAA73Bull;
+    for (int r = 0; r < 10; ++r) {
+        unsigned __int128 p0 = (unsigned __int128)m0 * c[0], p1 = (unsigned __int128)m1 * c[2];
+        uint64_t n0 = (uint64_t)(p1 >> 64) ^ c[1] ^ k0, n2 = (uint64_t)(p0 >> 64) ^ c[3] ^ k1;
+        c[1] = (uint64_t)p1;
+        c[3] = (uint64_t)p0;
+        c[0] = n0;
+        c[2] = n2;
+        k0 += w0;
+        k1 += w1;
+    }
+}
+
+float orc_philox_u(void* src, size_t i, uint32_t t)
+{
+    const uint64_t* s = (const uint64_t*)src;
+    uint64_t c[4] = {i, t, 0, 0};
+    orc_philox4x64_10(c, s[0], s[1]);
+    return (float)(c[t == 0 ? 0 : 1] >> 40) * 0x1.0p-24f;
+}
+
+uint32_t orc_philox_j(void* src, size_t i, uint32_t t)
+{
+    const uint64_t* s = (const uint64_t*)src;
+    uint64_t c[4] = {i, t, 0, 0};
+    orc_philox4x64_10(c, s[0], s[1]);
+    return (uint32_t)(((unsigned __int128)c[0] * s[2]) >> 64);
+}

@@ -129,6 +129,31 @@ size_t orc_reduce_scan(const float* xyz, const int16_t* ring, size_t n, float ce
  * roll, pitch, yaw), trig through the double overloads. */
 void orc_motion_apply(float* particles, size_t P, const double* draws);
 
+/* WheelResampler::resample (wheel_resampler.cpp:6-33), literally (O(M^2)):
+ * idx[i] = source of output i for the draws (doubles in [0, 1)). */
+void orc_resample_wheel(const float* w, size_t M, const double* draws, uint32_t* idx);
+/* ResidualResampler::resample (novel_resampling.h:12-34) consuming draws[0..K)
+ * (particle indices); returns the number consumed, or (size_t)-1 when they run out. */
+size_t orc_resample_residual(const float* w, size_t M, const uint32_t* draws, size_t K, uint32_t* idx);
+/* MetropolisResampler::resample (novel_resampling.h:113-142), steps proposals
+ * per output, u and j draws output-major. */
+void orc_resample_metropolis(const float* w, size_t M, uint32_t steps, const float* u, const uint32_t* j,
+                             uint32_t* idx);
+/* RejectionResampler::resample (novel_resampling.h:149-186) with draws taken
+ * from callbacks in the reference's order (u for output i; then j, u per
+ * proposal); t counts the proposals of output i (0 for its first u).  Returns 0,
+ * or -1 when an output exceeds max_rounds proposals. */
+typedef float (*orc_draw_u_fn)(void* src, size_t i, uint32_t t);
+typedef uint32_t (*orc_draw_j_fn)(void* src, size_t i, uint32_t t);
+int orc_resample_rejection(const float* w, size_t M, orc_draw_u_fn du, orc_draw_j_fn dj, void* src,
+                           uint32_t max_rounds, uint32_t* idx);
+/* Philox4x64-10 (Salmon et al., SC 2011) of one counter block. */
+void orc_philox4x64_10(uint64_t c[4], uint64_t k0, uint64_t k1);
+/* A draw source for orc_resample_rejection with the device's keying
+ * (counter (i, t, 0, 0), key (seed, stream)): src points at two uint64 {seed, stream, M}. */
+float orc_philox_u(void* src, size_t i, uint32_t t);
+uint32_t orc_philox_j(void* src, size_t i, uint32_t t);
+
 #ifdef __cplusplus
 }
 #endif

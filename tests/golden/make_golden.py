@@ -11,7 +11,9 @@ laser poses and mean pose (serial, in point order), SystematicResampler's
 and ResidualSystematicResampler's output indices for seeded draws, and the
 point list TSDFEvaluator::evaluateParticles' scan reduction hands to evaluate
 for a set of clouds (x, y, z, ring), and the particles ParticleCloud's motion
-model produces from given increments (motion_update with zero noise).
+model produces from given increments (motion_update with zero noise), and the
+Wheel, Residual, Metropolis and Rejection resamplers' outputs with the draws
+they took from a seeded generator.
 
     python tests/golden/make_golden.py
 """
@@ -177,6 +179,42 @@ def motion_case(seed):
     return out
 
 
+def other_resamplers_case(seed):
+    rng = np.random.default_rng(seed)
+    M, steps = 300, 10
+    sets = {
+        "random": (lambda w: (w / w.sum()).astype(np.float32))(rng.random(M) ** 3),
+        "sparse": (lambda w: (w / w.sum()).astype(np.float32))(np.where(rng.random(M) < 0.1, rng.random(M) + 0.01,
+                                                                        0.0)),
+        "unnormalised": rng.uniform(0.0, 1.6 / M, M).astype(np.float32),
+    }
+    out = {}
+    for k, w in sets.items():
+        s = int(rng.integers(1, 2 ** 31))
+        key = f"others/{k}"
+        out[f"{key}/weights"] = w
+        out[f"{key}/seed"] = np.int64(s)
+        out[f"{key}/wheel_draws"] = O.ref_draws("wheel", s, M)
+        out[f"{key}/wheel"] = O.ref_resample("wheel", w, s)
+        draws = O.ref_draws("residual", s, M, K=50 * M)
+        _, used = O.resample_residual(w, draws)
+        out[f"{key}/residual_draws"] = draws[:used]
+        out[f"{key}/residual"] = O.ref_resample("residual", w, s)
+        u, j = O.ref_draws("metropolis", s, M, steps=steps)
+        out[f"{key}/metropolis_u"], out[f"{key}/metropolis_j"] = u, j
+        out[f"{key}/metropolis"] = O.ref_resample("metropolis", w, s, steps=steps)
+        nu, nj, close = O.ref_rejection_draw_callables(s, M)
+        idx, uu, jj = O.resample_rejection_arrays(w, nu, nj, record=True)
+        close()
+        out[f"{key}/rejection_u"], out[f"{key}/rejection_j"] = uu, jj
+        out[f"{key}/rejection"] = O.ref_resample("rejection", w, s)
+        assert np.array_equal(idx, out[f"{key}/rejection"])
+        out[f"{key}/generator_next"] = np.array([O.ref_resample_next(kind, w, s, steps) for kind in range(3)],
+                                                np.uint32)
+    out["others/steps"] = np.int64(steps)
+    return out
+
+
 def main():
     if not O.reference_available():
         raise SystemExit("oracle/_ref/libref.so is not built: the reference tree is needed")
@@ -186,6 +224,7 @@ def main():
     fx.update(resample_case(13))
     fx.update(scan_case(14))
     fx.update(motion_case(15))
+    fx.update(other_resamplers_case(16))
     np.savez_compressed(OUT / "reference_cases.npz", **fx)
     print("wrote", OUT / "reference_cases.npz", (OUT / "reference_cases.npz").stat().st_size, "bytes")
 

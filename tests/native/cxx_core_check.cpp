@@ -10,6 +10,7 @@ using tsdfl::check;
 #include <cstdio>
 #include <fstream>
 #include <iterator>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -121,6 +122,30 @@ int main(int argc, char** argv)
             out_m[7 * i + 6] = parts_m[i].second;
         }
         save(d + "/motion_update_out.bin", out_m.data(), out_m.size());
+        // the other resamplers with the reference's seeded generator
+        auto ow = load<float>(d + "/others_w.bin");
+        auto oseed = load<uint32_t>(d + "/others_seed.bin");
+        auto run_other = [&](int kind) {
+            std::vector<MyParticle> ps(ow.size());
+            for (size_t i = 0; i < ps.size(); ++i) {
+                for (int k = 0; k < 6; ++k) ps[i].first[k] = 0.0f;
+                ps[i].first[0] = (float)i;
+                ps[i].second = ow[i];
+            }
+            std::mt19937 gen(oseed.at(0));
+            if (kind == 0) tsdfl::resample_wheel(ctx, ps, &gen);
+            if (kind == 1) tsdfl::resample_residual(ctx, ps, &gen);
+            if (kind == 2) tsdfl::resample_metropolis(ctx, ps, 10, &gen);
+            std::vector<uint32_t> idx(ps.size());
+            for (size_t i = 0; i < ps.size(); ++i) idx[i] = (uint32_t)ps[i].first[0];
+            // the generator is where the reference leaves it: report its next output
+            idx.push_back(gen());
+            return idx;
+        };
+        for (int kind = 0; kind < 3; ++kind) {
+            auto idx = run_other(kind);
+            save(d + "/others_out_" + std::to_string(kind) + ".bin", idx.data(), idx.size());
+        }
         bool threw = false;
         try {   // an empty cloud: the reference's "No particle is valid!"
             std::vector<MyParticle> none;

@@ -5,6 +5,7 @@
 // with libtsdfl's message; with a GPU, one update and one resample run.
 #include <tsdf_localization/cuda/cuda_evaluator.h>
 #include <tsdf_localization/resampling/novel_resampling.h>
+#include <tsdf_localization/resampling/wheel_resampler.h>
 
 #define TSDFL_WITH_TSDF_LOCALIZATION
 #include "tsdfl_evaluator.hpp"
@@ -81,6 +82,15 @@ int main()
         motion.motionUpdate(cloud, odom);
         motion.motion_update(cloud, 0.1f, 0.0f, 0.0f, 0.0f, 0.0f, 0.05f);
         std::printf("moved %zu, ref dist %.9g\n", cloud.size(), motion.refDist());
+        GpuWheelResampler wheel(0);
+        wheel.resample(cloud);
+        GpuResidualResampler residual(0);
+        residual.resample(cloud);
+        GpuMetropolisResampler metropolis(50, 0);
+        metropolis.resample(cloud);
+        GpuRejectionResampler rejection(0);
+        rejection.resample(cloud);
+        std::printf("other resamplers %zu\n", cloud.size());
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         status = 0;

@@ -153,3 +153,36 @@ def test_philox_restatement_matches_numpy():
         for b in range(3):
             got = O.philox4x64_10([np.uint64(b + 1), np.uint64(0), np.uint64(0), np.uint64(0)], key)
             assert [int(v) for v in got] == [int(v) for v in raw[4 * b:4 * b + 4]]
+
+
+OTHERS = sorted({k.split("/")[1] for k in GOLD.files if k.startswith("others/") and k.count("/") == 2})
+
+
+@pytest.mark.parametrize("wset", OTHERS)
+def test_other_resamplers_match_reference(wset):
+    g = lambda name: GOLD[f"others/{wset}/{name}"]  # noqa: E731
+    w = g("weights")
+    assert np.array_equal(O.resample_wheel(w, g("wheel_draws")), g("wheel"))
+    idx, used = O.resample_residual(w, g("residual_draws"))
+    assert np.array_equal(idx, g("residual")) and used == g("residual_draws").shape[0]
+    assert np.array_equal(O.resample_metropolis(w, int(GOLD["others/steps"]), g("metropolis_u"), g("metropolis_j")),
+                          g("metropolis"))
+    assert np.array_equal(O.resample_rejection_arrays(w, g("rejection_u"), g("rejection_j")), g("rejection"))
+
+
+def test_other_resamplers_random_weights_match_reference():
+    if not O.reference_available():
+        pytest.skip("the reference sources are not on this machine")
+    rng = np.random.default_rng(31)
+    for M in (1, 2, 50, 1500):
+        for t in range(3):
+            w = (rng.random(M) ** (1 + 4 * t)).astype(np.float32)
+            if t == 1:
+                w /= w.sum()
+            seed = int(rng.integers(1, 2 ** 31))
+            assert np.array_equal(O.ref_resample("wheel", w, seed), O.resample_wheel(w, O.ref_draws("wheel", seed, M)))
+            assert np.array_equal(O.ref_resample("residual", w, seed),
+                                  O.resample_residual(w, O.ref_draws("residual", seed, M, K=100 * M + 100))[0])
+            u, j = O.ref_draws("metropolis", seed, M, steps=50)
+            assert np.array_equal(O.ref_resample("metropolis", w, seed), O.resample_metropolis(w, 50, u, j))
+            assert np.array_equal(O.ref_resample("rejection", w, seed), O.resample_rejection_reference_draws(w, seed))

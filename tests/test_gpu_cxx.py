@@ -40,6 +40,9 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     pack_cloud(cxyz, cring).tofile(tmp_path / "cloud.bin")
     draws = np.random.default_rng(3).normal(0, [0.3, 0.1, 0.05, 0.05, 0.05, 0.3], (wl.particles.shape[0], 6))
     draws.tofile(tmp_path / "draws.bin")
+    gold = np.load(ROOT / "tests" / "golden" / "reference_cases.npz")
+    gold["others/random/weights"].astype(np.float32).tofile(tmp_path / "others_w.bin")
+    np.array([gold["others/random/seed"]], np.uint32).tofile(tmp_path / "others_seed.bin")
     res = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
     print(res.stdout, res.stderr)
     assert res.returncode == 0, res.stdout + res.stderr
@@ -78,3 +81,9 @@ def test_cxx_host_layer_matches_python_and_oracle(tmp_path):
     pm = wl.particles.copy()
     mm.update(pm, mm.distributions("odom", [0.6, -0.3], 0.1), step=0)
     assert np.array_equal(np.fromfile(tmp_path / "motion_update_out.bin", np.float32).reshape(-1, 7), pm)
+
+    # Wheel, Residual, Metropolis from a seeded std::mt19937: the reference's particles
+    for kind, name in enumerate(("wheel", "residual", "metropolis")):
+        got = np.fromfile(tmp_path / f"others_out_{kind}.bin", np.uint32)
+        assert np.array_equal(got[:-1], gold[f"others/random/{name}"])
+        assert got[-1] == gold["others/random/generator_next"][kind]   # the generator left where the reference leaves it

@@ -89,7 +89,8 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         ref_srcs = [REFERENCE / "src" / "evaluation" / "tsdf_evaluator.cpp",
                     REFERENCE / "src" / "evaluation" / "model" / "likelihood_evaluation.cpp",
                     REFERENCE / "src" / "particle_cloud.cpp",
-                    REFERENCE / "src" / "util" / "util.cpp"]
+                    REFERENCE / "src" / "util" / "util.cpp",
+                    REFERENCE / "src" / "resampling" / "wheel_resampler.cpp"]
         if force or _stale(ref, [ORACLE / "ref_driver.cpp"] + ref_srcs + sorted((ORACLE / "shim").rglob("*"))):
             jobs.append(["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fopenmp", "-shared",
                          f"-DTSDFL_REF_OMP_THREADS={os.cpu_count() or 8}",

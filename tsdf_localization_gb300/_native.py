@@ -105,6 +105,14 @@ SIGNATURES = [
     ("tsdfl_best_particle_device", I, [P, P, SZ, P]),
     ("tsdfl_reduce_scan", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, C.POINTER(SZ)]),
     ("tsdfl_reduce_scan_device", I, [P, P, SZ, U32, U32, U32, F, U32, P, SZ, P]),
+    ("tsdfl_resample_wheel", I, [P, P, SZ, P, C.c_uint64, P]),
+    ("tsdfl_resample_wheel_device", I, [P, P, SZ, P, C.c_uint64, P]),
+    ("tsdfl_resample_residual", I, [P, P, SZ, P, SZ, C.c_uint64, P]),
+    ("tsdfl_resample_residual_device", I, [P, P, SZ, P, SZ, C.c_uint64, P]),
+    ("tsdfl_resample_metropolis", I, [P, P, SZ, U32, P, P, C.c_uint64, P]),
+    ("tsdfl_resample_metropolis_device", I, [P, P, SZ, U32, P, P, C.c_uint64, P]),
+    ("tsdfl_resample_rejection", I, [P, P, SZ, C.c_uint64, P]),
+    ("tsdfl_resample_rejection_device", I, [P, P, SZ, C.c_uint64, P]),
     ("tsdfl_motion_model", I, [I, P, P, SZ, F, C.POINTER(Motion)]),
     ("tsdfl_motion_update_device", I, [P, P, SZ, C.POINTER(Motion), C.c_uint64, C.c_uint64, P]),
     ("tsdfl_motion_apply_device", I, [P, P, SZ, P]),

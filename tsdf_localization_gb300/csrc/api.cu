@@ -68,6 +68,8 @@ struct tsdfl_ctx {
     size_t rs_bytes = 0;
     void* scan_ws = nullptr;     // scan reduction workspace
     size_t scan_bytes = 0;
+    void* aux_ws = nullptr;      // workspace of the other resamplers
+    size_t aux_bytes = 0;
     void* io = nullptr;          // device copies of host inputs (host API)
     size_t io_bytes = 0;
     int32_t* status = nullptr;   // [0] sticky status, [1] per-evaluation status
@@ -190,6 +192,17 @@ int ensure_scan_ws(tsdfl_ctx* c, size_t n)
     if (c->scan_ws) cudaFree(c->scan_ws);
     c->scan_ws = p;
     c->scan_bytes = need;
+    return TSDFL_OK;
+}
+
+int ensure_aux_ws(tsdfl_ctx* c, size_t need)
+{
+    if (need <= c->aux_bytes) return TSDFL_OK;
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, need));
+    if (c->aux_ws) cudaFree(c->aux_ws);
+    c->aux_ws = p;
+    c->aux_bytes = need;
     return TSDFL_OK;
 }
 
@@ -526,6 +539,7 @@ int tsdfl_ctx_destroy(tsdfl_ctx* c)
     cudaFree(c->ws);
     cudaFree(c->rs_ws);
     cudaFree(c->scan_ws);
+    cudaFree(c->aux_ws);
     cudaFree(c->io);
     cudaFree(c->status);
     cudaFreeHost(c->h_status);
@@ -1045,6 +1059,186 @@ int tsdfl_evaluate_cloud(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* 
     if (st) return st;
     if (pose_out) std::memcpy(pose_out, c->h_pose, sizeof(float) * 6);
     return TSDFL_OK;
+}
+
+// ------------------------------------------------ the reference's other resamplers
+
+namespace {
+
+enum class Rs { Wheel, Residual, Metropolis, Rejection };
+
+struct RsCall {
+    Rs kind;
+    size_t M;
+    const void* draws;      // wheel: double[M]; residual: uint32[n_draws]; metropolis: float[M*steps]
+    const void* draws2;     // metropolis: uint32[M*steps]
+    size_t n_draws;
+    uint32_t steps;
+    uint64_t seed;
+};
+
+constexpr uint32_t kRejectionRounds = 1u << 20;
+
+size_t residual_draws(const RsCall& r) { return r.draws ? r.n_draws : 4 * r.M + 4096; }
+
+int rs_launch(tsdfl_ctx* c, const RsCall& r, const float* particles, const float* w, int stride, float* out,
+              uint32_t* idx_out)
+{
+    const size_t K = r.kind == Rs::Residual ? residual_draws(r) : 0;
+    int rc = ensure_aux_ws(c, resamplers_workspace_bytes(r.M, K));
+    if (rc) return rc;
+    cudaStream_t s = c->stream;
+    switch (r.kind) {
+    case Rs::Wheel:
+        return launch_resample_wheel(particles, w, stride, r.M, static_cast<const double*>(r.draws), r.seed, out,
+                                     idx_out, c->aux_ws, s);
+    case Rs::Residual:
+        return launch_resample_residual_random(particles, w, stride, r.M, static_cast<const uint32_t*>(r.draws), K,
+                                               r.seed, out, idx_out, c->aux_ws, c->status, s);
+    case Rs::Metropolis:
+        return launch_resample_metropolis(particles, w, stride, r.M, r.steps, static_cast<const float*>(r.draws),
+                                          static_cast<const uint32_t*>(r.draws2), r.seed, out, idx_out, c->status,
+                                          s);
+    case Rs::Rejection:
+        return launch_resample_rejection(particles, w, stride, r.M, r.seed, kRejectionRounds, out, idx_out,
+                                         c->aux_ws, c->status, c->sm_count, s);
+    }
+    return TSDFL_ERR_INVALID_ARG;
+}
+
+int rs_check(const char* fn, tsdfl_ctx* c, const RsCall& r, bool have_in, bool have_out)
+{
+    if (!c || (r.M && (!have_in || !have_out))) {
+        set_error("%s: invalid argument", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (r.M >= (1ull << 31)) {
+        set_error("%s: too many particles", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    if (r.kind == Rs::Residual && r.draws && r.M && r.n_draws == 0) {
+        set_error("%s: no draws", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (r.kind == Rs::Residual && residual_draws(r) >= (1ull << 32)) {
+        set_error("%s: too many draws", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    if (r.kind == Rs::Metropolis && (!r.draws) != (!r.draws2)) {
+        set_error("%s: give both draw arrays or neither", fn);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (r.kind == Rs::Metropolis && (uint64_t)r.M * r.steps >= (1ull << 40)) {
+        set_error("%s: too many draws", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    return set_device(c->device);
+}
+
+const char* rs_message(int st)
+{
+    if (st == TSDFL_ERR_UNSUPPORTED) return "the draws ran out before every particle was emitted";
+    if (st == TSDFL_ERR_INVALID_ARG) return "a drawn particle index is not below M";
+    return nullptr;
+}
+
+int rs_host(const char* fn, tsdfl_ctx* c, const RsCall& r, const float* weights, uint32_t* idx_out)
+{
+    int rc = rs_check(fn, c, r, weights != nullptr, idx_out != nullptr);
+    if (rc || r.M == 0) return rc;
+    size_t db = 0, db2 = 0;
+    if (r.draws) {
+        if (r.kind == Rs::Wheel) db = sizeof(double) * r.M;
+        if (r.kind == Rs::Residual) db = sizeof(uint32_t) * r.n_draws;
+        if (r.kind == Rs::Metropolis) {
+            db = sizeof(float) * r.M * r.steps;
+            db2 = sizeof(uint32_t) * r.M * r.steps;
+        }
+    }
+    const size_t w_b = align_up(sizeof(float) * r.M, 256), i_b = align_up(sizeof(uint32_t) * r.M, 256);
+    const size_t d_b = align_up(db, 256), d2_b = align_up(db2, 256);
+    rc = ensure_io(c, w_b + i_b + d_b + d2_b);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_w = reinterpret_cast<float*>(io);
+    uint32_t* d_idx = reinterpret_cast<uint32_t*>(io + w_b);
+    void* d_dr = db ? io + w_b + i_b : nullptr;
+    void* d_dr2 = db2 ? io + w_b + i_b + d_b : nullptr;
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_w, weights, sizeof(float) * r.M, cudaMemcpyHostToDevice, s));
+    if (db) CUDA_TRY(cudaMemcpyAsync(d_dr, r.draws, db, cudaMemcpyHostToDevice, s));
+    if (db2) CUDA_TRY(cudaMemcpyAsync(d_dr2, r.draws2, db2, cudaMemcpyHostToDevice, s));
+    RsCall dr = r;
+    dr.draws = d_dr;
+    dr.draws2 = d_dr2;
+    rc = rs_launch(c, dr, nullptr, d_w, 1, nullptr, d_idx);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(idx_out, d_idx, sizeof(uint32_t) * r.M, cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    if (st && rs_message(st)) set_error("%s: %s", fn, rs_message(st));
+    return st;
+}
+
+int rs_device(const char* fn, tsdfl_ctx* c, const RsCall& r, const float* d_particles, float* d_out)
+{
+    int rc = rs_check(fn, c, r, d_particles != nullptr, d_out != nullptr);
+    if (rc || r.M == 0) return rc;
+    return rs_launch(c, r, d_particles, d_particles + 6, 7, d_out, nullptr);
+}
+
+}  // namespace
+
+int tsdfl_resample_wheel(tsdfl_ctx* c, const float* weights, size_t M, const double* draws, uint64_t seed,
+                         uint32_t* idx_out)
+{
+    return rs_host("tsdfl_resample_wheel", c, RsCall{Rs::Wheel, M, draws, nullptr, 0, 0, seed}, weights, idx_out);
+}
+
+int tsdfl_resample_wheel_device(tsdfl_ctx* c, const float* d_particles, size_t M, const double* d_draws,
+                                uint64_t seed, float* d_out)
+{
+    return rs_device("tsdfl_resample_wheel_device", c, RsCall{Rs::Wheel, M, d_draws, nullptr, 0, 0, seed},
+                     d_particles, d_out);
+}
+
+int tsdfl_resample_residual(tsdfl_ctx* c, const float* weights, size_t M, const uint32_t* draws, size_t n_draws,
+                            uint64_t seed, uint32_t* idx_out)
+{
+    return rs_host("tsdfl_resample_residual", c, RsCall{Rs::Residual, M, draws, nullptr, n_draws, 0, seed}, weights,
+                   idx_out);
+}
+
+int tsdfl_resample_residual_device(tsdfl_ctx* c, const float* d_particles, size_t M, const uint32_t* d_draws,
+                                   size_t n_draws, uint64_t seed, float* d_out)
+{
+    return rs_device("tsdfl_resample_residual_device", c,
+                     RsCall{Rs::Residual, M, d_draws, nullptr, n_draws, 0, seed}, d_particles, d_out);
+}
+
+int tsdfl_resample_metropolis(tsdfl_ctx* c, const float* weights, size_t M, uint32_t steps, const float* u_draws,
+                              const uint32_t* j_draws, uint64_t seed, uint32_t* idx_out)
+{
+    return rs_host("tsdfl_resample_metropolis", c, RsCall{Rs::Metropolis, M, u_draws, j_draws, 0, steps, seed},
+                   weights, idx_out);
+}
+
+int tsdfl_resample_metropolis_device(tsdfl_ctx* c, const float* d_particles, size_t M, uint32_t steps,
+                                     const float* d_u_draws, const uint32_t* d_j_draws, uint64_t seed, float* d_out)
+{
+    return rs_device("tsdfl_resample_metropolis_device", c,
+                     RsCall{Rs::Metropolis, M, d_u_draws, d_j_draws, 0, steps, seed}, d_particles, d_out);
+}
+
+int tsdfl_resample_rejection(tsdfl_ctx* c, const float* weights, size_t M, uint64_t seed, uint32_t* idx_out)
+{
+    return rs_host("tsdfl_resample_rejection", c, RsCall{Rs::Rejection, M, nullptr, nullptr, 0, 0, seed}, weights,
+                   idx_out);
+}
+
+int tsdfl_resample_rejection_device(tsdfl_ctx* c, const float* d_particles, size_t M, uint64_t seed, float* d_out)
+{
+    return rs_device("tsdfl_resample_rejection_device", c, RsCall{Rs::Rejection, M, nullptr, nullptr, 0, 0, seed},
+                     d_particles, d_out);
 }
 
 int tsdfl_motion_update_device(tsdfl_ctx* c, float* d_particles, size_t P, const tsdfl_motion* m, uint64_t seed,

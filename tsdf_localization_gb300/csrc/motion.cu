@@ -22,6 +22,7 @@
 
 #include <atomic>
 
+#include "philox.h"
 #include "tsdfl_internal.h"
 
 namespace tsdfl {
@@ -40,33 +41,6 @@ struct MotionParams {
     const double* draws;     // P x 6 given draws, or null: generate
     double* draws_out;       // optional: the generated draws
 };
-
-__device__ __forceinline__ void mulhilo64(unsigned long long a, unsigned long long b, unsigned long long& hi,
-                                          unsigned long long& lo)
-{
-    lo = a * b;
-    hi = __umul64hi(a, b);
-}
-
-// Philox4x64 with 10 rounds (multipliers and Weyl increments of the paper).
-__device__ __forceinline__ void philox4x64_10(unsigned long long c[4], unsigned long long k0, unsigned long long k1)
-{
-    const unsigned long long m0 = 0xD2E7470EE14C6C93ull, m1 = 0xCA5A826395121157ull;
-    const unsigned long long w0 = 0x9E3779B97F4A7C15ull, w1 = 0xBB67AE8584CAA73Bull;
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        unsigned long long hi0, lo0, hi1, lo1;
-        mulhilo64(m0, c[0], hi0, lo0);
-        mulhilo64(m1, c[2], hi1, lo1);
-        const unsigned long long n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
-        c[0] = n0;
-        c[1] = lo1;
-        c[2] = n2;
-        c[3] = lo0;
-        k0 += w0;
-        k1 += w1;
-    }
-}
 
 // A standard normal pair from two 64-bit words: u1 in (0, 1], u2 in [0, 1),
 // r = sqrt(-2 ln u1), (r cos 2 pi u2, r sin 2 pi u2).
@@ -211,10 +185,8 @@ int launch_motion(float* particles, size_t P, const double mean[6], const double
         mp.mean[k] = mean ? mean[k] : 0.0;
         mp.stddev[k] = stddev ? stddev[k] : 0.0;
     }
-    // the seed keys the generator; the second key word separates it from other
-    // streams of this library
     mp.key0 = seed;
-    mp.key1 = 0x6D6F74696F6E0001ull;
+    mp.key1 = kStreamMotion;
     mp.step = step;
     mp.draws = draws;
     mp.draws_out = draws_out;

@@ -202,4 +202,18 @@ int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t o
 int launch_motion(float* particles, size_t P, const double mean[6], const double stddev[6], uint64_t seed,
                   uint64_t step, const double* draws, double* draws_out, cudaStream_t s);
 
+// The reference's other resamplers (resamplers.cu).  K: residual draws.
+size_t resamplers_workspace_bytes(size_t M, size_t K);
+int launch_resample_wheel(const float* particles, const float* w, int stride, size_t M, const double* draws,
+                          uint64_t seed, float* out, uint32_t* idx_out, void* ws, cudaStream_t s);
+int launch_resample_residual_random(const float* particles, const float* w, int stride, size_t M,
+                                    const uint32_t* draws, size_t K, uint64_t seed, float* out, uint32_t* idx_out,
+                                    void* ws, int32_t* status, cudaStream_t s);
+int launch_resample_metropolis(const float* particles, const float* w, int stride, size_t M, uint32_t steps,
+                               const float* u_draws, const uint32_t* j_draws, uint64_t seed, float* out,
+                               uint32_t* idx_out, int32_t* status, cudaStream_t s);
+int launch_resample_rejection(const float* particles, const float* w, int stride, size_t M, uint64_t seed,
+                              uint32_t max_rounds, float* out, uint32_t* idx_out, void* ws, int32_t* status,
+                              int sm_count, cudaStream_t s);
+
 }  // namespace tsdfl

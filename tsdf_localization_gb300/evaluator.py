@@ -299,6 +299,73 @@ class ResidualSystematicResampler:
         return particles[idx].copy()
 
 
+class _DrawnResampler:
+    """Common host form of the reference's Wheel/Residual/Metropolis/Rejection
+    resamplers: exactly M outputs; draws from the caller (the reference's
+    own sequence gives its output bit for bit) or from the device generator."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        self.seed = int(seed)
+
+    def resample(self, particles: np.ndarray, *draws) -> np.ndarray:
+        return particles[self.resample_indices(particles[:, 6], *draws)]
+
+
+class WheelResampler(_DrawnResampler):
+    """WheelResampler (wheel_resampler.cpp:6-33); draws: M doubles in [0, 1)."""
+
+    def resample_indices(self, weights: np.ndarray, draws: np.ndarray | None = None) -> np.ndarray:
+        w = _f32(weights)
+        d = None if draws is None else np.ascontiguousarray(draws, np.float64)
+        if d is not None and d.shape != w.shape:
+            raise ValueError("one draw per particle")
+        out = np.zeros(w.shape[0], np.uint32)
+        N.check(N.lib().tsdfl_resample_wheel(self.ctx.handle, _ptr(w), w.shape[0], _ptr(d), self.seed, _ptr(out)))
+        return out
+
+
+class ResidualResampler(_DrawnResampler):
+    """ResidualResampler (novel_resampling.h:9-35); draws: particle indices."""
+
+    def resample_indices(self, weights: np.ndarray, draws: np.ndarray | None = None) -> np.ndarray:
+        w = _f32(weights)
+        d = None if draws is None else np.ascontiguousarray(draws, np.uint32)
+        out = np.zeros(w.shape[0], np.uint32)
+        N.check(N.lib().tsdfl_resample_residual(self.ctx.handle, _ptr(w), w.shape[0], _ptr(d),
+                                                0 if d is None else d.shape[0], self.seed, _ptr(out)))
+        return out
+
+
+class MetropolisResampler(_DrawnResampler):
+    """MetropolisResampler(sampling_steps) (novel_resampling.h:106-143); draws:
+    u (float) and j (index) arrays of M * steps, output-major."""
+
+    def __init__(self, ctx: Context, sampling_steps: int = 50, seed: int = 0):
+        super().__init__(ctx, seed)
+        self.steps = int(sampling_steps)
+
+    def resample_indices(self, weights: np.ndarray, u: np.ndarray | None = None,
+                         j: np.ndarray | None = None) -> np.ndarray:
+        w = _f32(weights)
+        uu = None if u is None else np.ascontiguousarray(u, np.float32)
+        jj = None if j is None else np.ascontiguousarray(j, np.uint32)
+        out = np.zeros(w.shape[0], np.uint32)
+        N.check(N.lib().tsdfl_resample_metropolis(self.ctx.handle, _ptr(w), w.shape[0], self.steps, _ptr(uu),
+                                                  _ptr(jj), self.seed, _ptr(out)))
+        return out
+
+
+class RejectionResampler(_DrawnResampler):
+    """RejectionResampler (novel_resampling.h:146-187); device draws only."""
+
+    def resample_indices(self, weights: np.ndarray) -> np.ndarray:
+        w = _f32(weights)
+        out = np.zeros(w.shape[0], np.uint32)
+        N.check(N.lib().tsdfl_resample_rejection(self.ctx.handle, _ptr(w), w.shape[0], self.seed, _ptr(out)))
+        return out
+
+
 class MotionModel:
     """ParticleCloud's motion update (particle_cloud.cpp:153-617) on the GPU.
 
