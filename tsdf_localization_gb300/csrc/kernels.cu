@@ -1344,11 +1344,26 @@ __global__ void __launch_bounds__(kChainThreads) residual_chain_kernel(const flo
             return;
         }
         if (threadIdx.x == 0) {
-#pragma unroll 8
-            for (int i = 0; i < t; ++i) {
+            // 32 products to registers at a time, so that only the chain is serial
+            int i = 0;
+            for (; i + 32 <= t; i += 32) {
+                float v[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) v[k] = sc[i + k];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    const float temp = __fsub_rn(v[k], u);
+                    // floor(temp) + 1 for -1 <= temp < 2^22: rounding temp + 1.5 * 2^23 down
+                    // lands on an integer (unit spacing there), so both steps are exact
+                    const float of = __fsub_rn(__fadd_rd(temp, 12582912.0f), 12582911.0f);
+                    u = __fsub_rn(of, temp);
+                    v[k] = of;
+                }
+#pragma unroll
+                for (int k = 0; k < 32; ++k) sc[i + k] = v[k];
+            }
+            for (; i < t; ++i) {
                 const float temp = __fsub_rn(sc[i], u);
-                // floor(temp) + 1 for -1 <= temp < 2^22: rounding temp + 1.5 * 2^23 down
-                // lands on an integer (unit spacing there), so both steps are exact
                 const float of = __fsub_rn(__fadd_rd(temp, 12582912.0f), 12582911.0f);
                 u = __fsub_rn(of, temp);
                 sc[i] = of;

@@ -47,31 +47,73 @@ __device__ __forceinline__ void gather(const float* particles, uint32_t src, siz
 // ------------------------------------------------------------------ wheel
 
 // wheel_resampler.cpp:22-30: weight_sum += w_m in float, in particle order.
-// One thread walks the sums over weights staged in shared memory and writes
-// their running maximum R_m (over the sums before the first NaN): the first m
-// with draw <= sum_m is the first m with draw <= R_m, so a binary search
-// over R finds it.
+// One thread walks the sums over weights staged in shared memory (only the
+// additions chain); the block then forms their running maximum R_m with
+// fmaxf, which skips NaN (a NaN sum stays NaN, so R stops growing at the first
+// one).  The first m with draw <= sum_m is the first m with draw <= R_m, so a
+// binary search over R finds it.
 __global__ void __launch_bounds__(kWheelThreads) wheel_sums_kernel(const float* __restrict__ w, int stride,
                                                                    uint32_t M, float* __restrict__ R)
 {
+    static_assert(kWheelTile == 4 * kWheelThreads, "four sums per thread in the running maximum");
     __shared__ float sw[kWheelTile];
-    float s = 0.0f, rmax = -INFINITY;
-    bool dead = false;
+    __shared__ float sr[kWheelTile];
+    __shared__ float warp_max[kWheelThreads / 32];
+    __shared__ float s_carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float s = 0.0f;
+    if (threadIdx.x == 0) s_carry = -INFINITY;
     for (uint32_t base = 0; base < M; base += kWheelTile) {
         const uint32_t t = min((uint32_t)kWheelTile, M - base);
-        for (uint32_t i = threadIdx.x; i < t; i += blockDim.x) sw[i] = w[(size_t)(base + i) * stride];
+        for (uint32_t i = threadIdx.x; i < kWheelTile; i += blockDim.x)
+            sw[i] = i < t ? w[(size_t)(base + i) * stride] : 0.0f;
         __syncthreads();
         if (threadIdx.x == 0) {
-#pragma unroll 8
-            for (uint32_t i = 0; i < t; ++i) {
-                s = __fadd_rn(s, sw[i]);
-                dead |= s != s;
-                if (!dead && s > rmax) rmax = s;
-                sw[i] = rmax;
+            // 32 weights to registers at a time (one load latency per 32 additions)
+            for (uint32_t i = 0; i < t; i += 32) {
+                float v[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) v[k] = sw[i + k];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) {
+                    s = __fadd_rn(s, v[k]);
+                    v[k] = s;
+                }
+#pragma unroll
+                for (int k = 0; k < 32; ++k) sr[i + k] = v[k];
             }
         }
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < t; i += blockDim.x) R[base + i] = sw[i];
+        // running maximum of this tile's sums, four per thread, from the carry
+        float m[4], run = -INFINITY;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = 4 * threadIdx.x + k;
+            run = fmaxf(run, i < t ? sr[i] : -INFINITY);
+            m[k] = run;
+        }
+        float x = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = fmaxf(x, y);
+        }
+        if (lane == 31) warp_max[warp] = x;
+        __syncthreads();
+        float before = s_carry, tile_max = s_carry;
+        for (int k = 0; k < kWheelThreads / 32; ++k) {
+            if (k < warp) before = fmaxf(before, warp_max[k]);
+            tile_max = fmaxf(tile_max, warp_max[k]);
+        }
+        const float xprev = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane > 0) before = fmaxf(before, xprev);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = 4 * threadIdx.x + k;
+            if (i < t) R[base + i] = fmaxf(before, m[k]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = tile_max;
         __syncthreads();
     }
 }
@@ -134,41 +176,80 @@ __global__ void residual_counts_kernel(const float* __restrict__ w, int stride, 
     }
 }
 
-// Inclusive sums of c[0..K) in place, one block walking chunks.
-__global__ void __launch_bounds__(kScanThreads) inclusive_scan_u64_kernel(unsigned long long* c, uint32_t K)
+// Inclusive sums of c[0..K) in place: per-tile sums (kScanTile values a
+// block), one block scanning the tile sums, each tile rescanned from its offset.
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ unsigned long long block_exclusive(unsigned long long v, unsigned long long* warp_tot,
+                                                              unsigned long long& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    unsigned long long off = 0;
+    total = 0;
+    for (int k = 0; k < kScanThreads / 32; ++k) {
+        if (k < warp) off += warp_tot[k];
+        total += warp_tot[k];
+    }
+    return off + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) tile_sums_u64_kernel(const unsigned long long* __restrict__ c,
+                                                                     uint32_t K, unsigned long long* tile_sum)
+{
+    __shared__ unsigned long long warp_tot[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanTile;
+    unsigned long long run = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint32_t i = base + kScanItems * threadIdx.x + k;
+        run += i < K ? c[i] : 0;
+    }
+    unsigned long long total;
+    block_exclusive(run, warp_tot, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// Exclusive prefix of tile_sum[0..tiles) in place (one block).
+__global__ void __launch_bounds__(kScanThreads) scan_tile_sums_kernel(unsigned long long* tile_sum, uint32_t tiles)
 {
     __shared__ unsigned long long warp_tot[kScanThreads / 32];
     __shared__ unsigned long long s_base;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_base = 0;
-    for (uint32_t base = 0; base < K; base += kScanThreads * kScanItems) {
-        unsigned long long v[kScanItems], run = 0;
-        for (int k = 0; k < kScanItems; ++k) {
-            const uint32_t i = base + kScanItems * threadIdx.x + k;
-            v[k] = i < K ? c[i] : 0;
-            run += v[k];
-        }
-        unsigned long long x = run;
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        __syncthreads();   // s_base and warp_tot of the previous chunk have been read
-        if (lane == 31) warp_tot[warp] = x;
+    for (uint32_t base = 0; base < tiles; base += kScanThreads) {
+        const uint32_t t = base + threadIdx.x;
+        const unsigned long long v = t < tiles ? tile_sum[t] : 0;
+        unsigned long long total;
+        const unsigned long long ex = block_exclusive(v, warp_tot, total);
+        if (t < tiles) tile_sum[t] = s_base + ex;
         __syncthreads();
-        unsigned long long off = s_base, tot = 0;
-        for (int k = 0; k < kScanThreads / 32; ++k) {
-            if (k < warp) off += warp_tot[k];
-            tot += warp_tot[k];
-        }
-        off += x - run;
-        for (int k = 0; k < kScanItems; ++k) {
-            const uint32_t i = base + kScanItems * threadIdx.x + k;
-            off += v[k];
-            if (i < K) c[i] = off;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_base += tot;
+        if (threadIdx.x == 0) s_base += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) tile_rescan_u64_kernel(unsigned long long* c, uint32_t K,
+                                                                       const unsigned long long* tile_off)
+{
+    __shared__ unsigned long long warp_tot[kScanThreads / 32];
+    const uint32_t base = blockIdx.x * kScanTile;
+    unsigned long long v[kScanItems], run = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint32_t i = base + kScanItems * threadIdx.x + k;
+        v[k] = i < K ? c[i] : 0;
+        run += v[k];
+    }
+    unsigned long long total;
+    unsigned long long off = tile_off[blockIdx.x] + block_exclusive(run, warp_tot, total);
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint32_t i = base + kScanItems * threadIdx.x + k;
+        off += v[k];
+        if (i < K) c[i] = off;
     }
 }
 
@@ -276,7 +357,7 @@ size_t resamplers_workspace_bytes(size_t M, size_t K)
 {
     auto a = [](size_t v) { return (v + 255) / 256 * 256; };
     const size_t wheel = a(4 * M);
-    const size_t residual = a(4 * K) + a(8 * K);
+    const size_t residual = a(4 * K) + a(8 * K) + a(8 * ((K + 4095) / 4096 + 1));
     return (wheel > residual ? wheel : residual) + 256;
 }
 
@@ -300,13 +381,17 @@ int launch_resample_residual_random(const float* particles, const float* w, int 
     auto a = [](size_t v) { return (v + 255) / 256 * 256; };
     uint32_t* r = static_cast<uint32_t*>(ws);
     unsigned long long* C = reinterpret_cast<unsigned long long*>(static_cast<char*>(ws) + a(4 * K));
+    unsigned long long* tile = reinterpret_cast<unsigned long long*>(static_cast<char*>(ws) + a(4 * K) + a(8 * K));
     const size_t quads = (K + 3) / 4;
+    const unsigned tiles = (unsigned)((K + kScanTile - 1) / kScanTile);
     residual_counts_kernel<<<(unsigned)((quads + 255) / 256), 256, 0, s>>>(w, stride, (uint32_t)M, draws,
                                                                           (uint32_t)K, seed, r, C, status);
-    inclusive_scan_u64_kernel<<<1, kScanThreads, 0, s>>>(C, (uint32_t)K);
+    tile_sums_u64_kernel<<<tiles, kScanThreads, 0, s>>>(C, (uint32_t)K, tile);
+    scan_tile_sums_kernel<<<1, kScanThreads, 0, s>>>(tile, tiles);
+    tile_rescan_u64_kernel<<<tiles, kScanThreads, 0, s>>>(C, (uint32_t)K, tile);
     residual_assign_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(particles, (uint32_t)M, r, C, (uint32_t)K,
                                                                         out, idx_out, status);
-    g_launches += 3;
+    g_launches += 5;
     return check(cudaGetLastError());
 }
 
