@@ -309,6 +309,15 @@ int tsdfl_motion_update(tsdfl_ctx* ctx, float* particles, size_t P, const tsdfl_
                         uint64_t step);
 int tsdfl_motion_apply(tsdfl_ctx* ctx, float* particles, size_t P, const double* draws);
 
+/* ---- particle output ----
+ * mcl_3d.cpp:429-449: every particle as a geometry_msgs::Pose -- position x,
+ * y, z, then the quaternion x, y, z, w tf2::Quaternion::setRPY forms from its
+ * roll, pitch, yaw (half angles, ZYX, in double) -- 7 doubles per particle, in
+ * particle order, ready for a PoseArray.  Device form on device buffers; host
+ * form copies P x 7 floats in and P x 7 doubles out. */
+int tsdfl_pose_array_device(tsdfl_ctx* ctx, const float* d_particles, size_t P, double* d_poses);
+int tsdfl_pose_array(tsdfl_ctx* ctx, const float* particles, size_t P, double* poses);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about

@@ -315,6 +315,21 @@ void resample_rejection(Context& ctx, std::vector<ParticleT>& particles, uint64_
     detail::take(particles, idx);
 }
 
+// mcl_3d.cpp:429-449: the particles as Pose records (position, setRPY
+// quaternion x, y, z, w), 7 doubles each.
+template <class ParticleT>
+std::vector<double> pose_array(Context& ctx, const std::vector<ParticleT>& particles)
+{
+    std::vector<float> p(7 * particles.size());
+    for (size_t i = 0; i < particles.size(); ++i) {
+        for (int k = 0; k < 6; ++k) p[7 * i + k] = particles[i].first[k];
+        p[7 * i + 6] = particles[i].second;
+    }
+    std::vector<double> out(7 * particles.size());
+    check(tsdfl_pose_array(ctx.get(), p.data(), particles.size(), out.data()));
+    return out;
+}
+
 // The scan reduction of TSDFEvaluator::evaluateParticles
 // (tsdf_evaluator.cpp:304-376) on the device: the points it hands to evaluate,
 // in its order, from a PointCloud2's data.
@@ -560,6 +575,24 @@ private:
     std::unique_ptr<tsdfl::Map> map_;
     std::unique_ptr<tsdfl::SensorUpdate> update_;
 };
+
+// The particle cloud as the poses of mcl_3d's PoseArray (mcl_3d.cpp:429-449):
+// pose_array.poses = gpu_particle_poses(ctx, particle_cloud_.particles()).
+inline std::vector<geometry_msgs::Pose> gpu_particle_poses(tsdfl::Context& ctx, const std::vector<Particle>& particles)
+{
+    const std::vector<double> v = tsdfl::pose_array(ctx, particles);
+    std::vector<geometry_msgs::Pose> poses(particles.size());
+    for (size_t i = 0; i < particles.size(); ++i) {
+        poses[i].position.x = v[7 * i];
+        poses[i].position.y = v[7 * i + 1];
+        poses[i].position.z = v[7 * i + 2];
+        poses[i].orientation.x = v[7 * i + 3];
+        poses[i].orientation.y = v[7 * i + 4];
+        poses[i].orientation.z = v[7 * i + 5];
+        poses[i].orientation.w = v[7 * i + 6];
+    }
+    return poses;
+}
 
 // Drop-ins for the other resamplers mcl_3d can select (mcl_3d.cpp:246-261).
 // Wheel, Residual and Metropolis draw from the inherited generator in the

@@ -81,6 +81,8 @@ def oracle() -> C.CDLL:
         L.orc_resample_metropolis.argtypes = [P, SZ, C.c_uint32, P, P, P]
         L.orc_resample_rejection.restype = C.c_int
         L.orc_resample_rejection.argtypes = [P, SZ, P, P, P, C.c_uint32, P]
+        L.orc_pose_array.restype = None
+        L.orc_pose_array.argtypes = [P, SZ, P]
         L.orc_motion_apply.restype = None
         L.orc_motion_apply.argtypes = [P, SZ, P]
         L.orc_reduce_scan.restype = SZ
@@ -267,6 +269,14 @@ def reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064, own_ring
     if n == (1 << 64) - 1:
         raise ValueError("ring outside [0, 64)")
     return out[:n].copy()
+
+
+def pose_array(particles: np.ndarray) -> np.ndarray:
+    """mcl_3d.cpp:433-449: (P, 7) doubles, position and setRPY quaternion (x, y, z, w)."""
+    p = np.ascontiguousarray(particles, np.float32)
+    out = np.zeros((p.shape[0], 7), np.float64)
+    oracle().orc_pose_array(_ptr(p), p.shape[0], _ptr(out))
+    return out
 
 
 def motion_apply(particles: np.ndarray, draws: np.ndarray) -> np.ndarray:

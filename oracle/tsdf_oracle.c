@@ -628,3 +628,21 @@ uint32_t orc_philox_j(void* src, size_t i, uint32_t t)
     orc_philox4x64_10(c, s[0], s[1]);
     return (uint32_t)(((unsigned __int128)c[0] * s[2]) >> 64);
 }
+
+/* mcl_3d.cpp:433-449 with tf2::Quaternion::setRPY's half-angle ZYX form */
+void orc_pose_array(const float* particles, size_t P, double* poses)
+{
+    for (size_t i = 0; i < P; ++i) {
+        const float* p = particles + 7 * i;
+        double hr = (double)p[3] * 0.5, hp = (double)p[4] * 0.5, hy = (double)p[5] * 0.5;
+        double sr = sin(hr), cr = cos(hr), sp = sin(hp), cp = cos(hp), sy = sin(hy), cy = cos(hy);
+        double* o = poses + 7 * i;
+        o[0] = p[0];
+        o[1] = p[1];
+        o[2] = p[2];
+        o[3] = sr * cp * cy - cr * sp * sy;
+        o[4] = cr * sp * cy + sr * cp * sy;
+        o[5] = cr * cp * sy - sr * sp * cy;
+        o[6] = cr * cp * cy + sr * sp * sy;
+    }
+}

@@ -147,6 +147,9 @@ typedef float (*orc_draw_u_fn)(void* src, size_t i, uint32_t t);
 typedef uint32_t (*orc_draw_j_fn)(void* src, size_t i, uint32_t t);
 int orc_resample_rejection(const float* w, size_t M, orc_draw_u_fn du, orc_draw_j_fn dj, void* src,
                            uint32_t max_rounds, uint32_t* idx);
+/* mcl_3d.cpp:433-449: particles (P x 7 floats) as Pose records (P x 7
+ * doubles: position, quaternion x, y, z, w of setRPY in double). */
+void orc_pose_array(const float* particles, size_t P, double* poses);
 /* Philox4x64-10 (Salmon et al., SC 2011) of one counter block. */
 void orc_philox4x64_10(uint64_t c[4], uint64_t k0, uint64_t k1);
 /* A draw source for orc_resample_rejection with the device's keying

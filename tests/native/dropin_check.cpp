@@ -91,6 +91,8 @@ int main()
         GpuRejectionResampler rejection(0);
         rejection.resample(cloud);
         std::printf("other resamplers %zu\n", cloud.size());
+        std::vector<geometry_msgs::Pose> poses = gpu_particle_poses(sctx, cloud.particles());
+        std::printf("poses %zu\n", poses.size());
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         status = 0;

@@ -129,3 +129,15 @@ def test_gpu_motion_empty_and_errors(ctx):
     m = mm.distributions("scale", [1.0, 1.0], 0.1)
     mm.update(empty, m)
     assert N.lib().tsdfl_motion_apply_device(ctx.handle, None, 5, None) == N.TSDFL_ERR_INVALID_ARG
+
+
+def test_gpu_pose_array_matches_oracle(ctx):
+    from tsdf_localization_gb300 import pose_array
+    parts = random_particles(50_000, 12)
+    got = pose_array(ctx, parts)
+    want = O.pose_array(parts)
+    assert np.array_equal(got[:, :3], want[:, :3])
+    # double sin/cos of the device and of the host may differ in the last bit
+    assert np.allclose(got[:, 3:], want[:, 3:], rtol=0, atol=1e-15)
+    assert np.allclose(np.linalg.norm(got[:, 3:], axis=1), 1.0, atol=1e-12)
+    assert pose_array(ctx, np.zeros((0, 7), np.float32)).shape == (0, 7)

@@ -113,6 +113,8 @@ SIGNATURES = [
     ("tsdfl_resample_metropolis_device", I, [P, P, SZ, U32, P, P, C.c_uint64, P]),
     ("tsdfl_resample_rejection", I, [P, P, SZ, C.c_uint64, P]),
     ("tsdfl_resample_rejection_device", I, [P, P, SZ, C.c_uint64, P]),
+    ("tsdfl_pose_array_device", I, [P, P, SZ, P]),
+    ("tsdfl_pose_array", I, [P, P, SZ, P]),
     ("tsdfl_motion_model", I, [I, P, P, SZ, F, C.POINTER(Motion)]),
     ("tsdfl_motion_update_device", I, [P, P, SZ, C.POINTER(Motion), C.c_uint64, C.c_uint64, P]),
     ("tsdfl_motion_apply_device", I, [P, P, SZ, P]),

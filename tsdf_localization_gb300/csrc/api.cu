@@ -1241,6 +1241,48 @@ int tsdfl_resample_rejection_device(tsdfl_ctx* c, const float* d_particles, size
                      d_particles, d_out);
 }
 
+int tsdfl_pose_array_device(tsdfl_ctx* c, const float* d_particles, size_t P, double* d_poses)
+{
+    if (!c || (P && (!d_particles || !d_poses))) {
+        set_error("tsdfl_pose_array_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P >= (1ull << 32)) {
+        set_error("tsdfl_pose_array_device: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    return launch_pose_array(d_particles, P, d_poses, c->stream);
+}
+
+int tsdfl_pose_array(tsdfl_ctx* c, const float* particles, size_t P, double* poses)
+{
+    if (!c || (P && (!particles || !poses))) {
+        set_error("tsdfl_pose_array: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P == 0) return TSDFL_OK;
+    if (P >= (1ull << 32)) {
+        set_error("tsdfl_pose_array: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    const size_t part_b = align_up(sizeof(float) * 7 * P, 256);
+    rc = ensure_io(c, part_b + sizeof(double) * 7 * P);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_part = reinterpret_cast<float*>(io);
+    double* d_poses = reinterpret_cast<double*>(io + part_b);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_part, particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice, s));
+    rc = launch_pose_array(d_part, P, d_poses, s);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(poses, d_poses, sizeof(double) * 7 * P, cudaMemcpyDeviceToHost, s));
+    return tsdfl_ctx_sync(c);
+}
+
 int tsdfl_motion_update_device(tsdfl_ctx* c, float* d_particles, size_t P, const tsdfl_motion* m, uint64_t seed,
                                uint64_t step, double* d_draws_out)
 {

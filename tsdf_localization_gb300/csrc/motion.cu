@@ -170,9 +170,39 @@ __global__ void __launch_bounds__(kMotionBlock) motion_kernel(MotionParams mp)
     for (int k = 0; k < 6; ++k) src[k] = p[k];
 }
 
+// mcl_3d.cpp:433-449: a particle as geometry_msgs::Pose (position, then the
+// orientation quaternion x, y, z, w of tf2::Quaternion::setRPY(roll, pitch,
+// yaw): half angles, ZYX composition, in double).
+__global__ void pose_array_kernel(const float* __restrict__ particles, uint32_t P, double* __restrict__ poses)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const float* p = particles + 7 * (size_t)i;
+    double sr, cr, sp, cp, sy, cy;
+    sincos(__dmul_rn((double)p[3], 0.5), &sr, &cr);
+    sincos(__dmul_rn((double)p[4], 0.5), &sp, &cp);
+    sincos(__dmul_rn((double)p[5], 0.5), &sy, &cy);
+    double* o = poses + 7 * (size_t)i;
+    o[0] = p[0];
+    o[1] = p[1];
+    o[2] = p[2];
+    o[3] = __dsub_rn(__dmul_rn(__dmul_rn(sr, cp), cy), __dmul_rn(__dmul_rn(cr, sp), sy));
+    o[4] = __dadd_rn(__dmul_rn(__dmul_rn(cr, sp), cy), __dmul_rn(__dmul_rn(sr, cp), sy));
+    o[5] = __dsub_rn(__dmul_rn(__dmul_rn(cr, cp), sy), __dmul_rn(__dmul_rn(sr, sp), cy));
+    o[6] = __dadd_rn(__dmul_rn(__dmul_rn(cr, cp), cy), __dmul_rn(__dmul_rn(sr, sp), sy));
+}
+
 int check(cudaError_t e) { return e == cudaSuccess ? TSDFL_OK : TSDFL_ERR_DEVICE; }
 
 }  // namespace
+
+int launch_pose_array(const float* particles, size_t P, double* poses, cudaStream_t s)
+{
+    if (P == 0) return TSDFL_OK;
+    pose_array_kernel<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(particles, (uint32_t)P, poses);
+    g_launches += 1;
+    return check(cudaGetLastError());
+}
 
 int launch_motion(float* particles, size_t P, const double mean[6], const double stddev[6], uint64_t seed,
                   uint64_t step, const double* draws, double* draws_out, cudaStream_t s)

@@ -202,6 +202,9 @@ int launch_reduce_scan(const uint8_t* cloud, size_t n, uint32_t step, uint32_t o
 int launch_motion(float* particles, size_t P, const double mean[6], const double stddev[6], uint64_t seed,
                   uint64_t step, const double* draws, double* draws_out, cudaStream_t s);
 
+// Particles as geometry_msgs::Pose records (7 doubles each) (motion.cu).
+int launch_pose_array(const float* particles, size_t P, double* poses, cudaStream_t s);
+
 // The reference's other resamplers (resamplers.cu).  K: residual draws.
 size_t resamplers_workspace_bytes(size_t M, size_t K);
 int launch_resample_wheel(const float* particles, const float* w, int stride, size_t M, const double* draws,

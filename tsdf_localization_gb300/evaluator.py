@@ -418,6 +418,15 @@ class MotionModel:
         return particles
 
 
+def pose_array(ctx: Context, particles: np.ndarray) -> np.ndarray:
+    """mcl_3d.cpp:429-449: the particles as geometry_msgs::Pose records, (P, 7)
+    doubles: position, then the setRPY quaternion x, y, z, w."""
+    p = _f32(particles, 7)
+    out = np.zeros((p.shape[0], 7), np.float64)
+    N.check(N.lib().tsdfl_pose_array(ctx.handle, _ptr(p), p.shape[0], _ptr(out)))
+    return out
+
+
 def code_values(sigma: float = 0.1, init_value: float = 0.0) -> np.ndarray:
     out = np.zeros(601, np.float32)
     N.check(N.lib().tsdfl_code_values(sigma, init_value, _ptr(out)))
