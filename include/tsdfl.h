@@ -198,6 +198,52 @@ int tsdfl_resample_residual_systematic_device(tsdfl_ctx* ctx, const float* d_par
  * where the reference would index with -1).  d_particles: M x 7 floats. */
 int tsdfl_best_particle_device(tsdfl_ctx* ctx, const float* d_particles, size_t M, uint32_t* d_index);
 
+/* ---- batched filters ----
+ * No single call of the reference does this: many independent filters (each
+ * one TSDFEvaluator::evaluate + SystematicResampler::resample, as the single
+ * calls above) updated together.  Their scoring runs in ONE persistent launch
+ * over a (filter, pass, point chunk, particle group) work queue; preparation,
+ * normalisation and resampling are per-filter launches in the same stream.
+ * The whole update can be captured once as a CUDA graph and replayed.  Every
+ * filter's results are the same as its single-filter tsdfl_evaluate_device +
+ * tsdfl_resample_systematic_device results (exact sums; same draws).  All
+ * buffers are device buffers fixed at creation: write new particles, points
+ * and draws into them between runs.  Exact sums only (flags 0). */
+typedef struct tsdfl_batch tsdfl_batch;
+typedef struct tsdfl_filter {
+    const tsdfl_map* map;
+    tsdfl_model model;
+    float tf[16];             /* sensor-to-base transform, row-major */
+    float* d_particles;       /* P x 7; weights overwritten with the normalised weights */
+    size_t P;
+    const float* d_points;    /* N x 3 */
+    size_t N;
+    float* d_pose_out;        /* 6 floats, or NULL */
+    const float* d_u0;        /* systematic draw in [0, 1/P), read when the batch runs; NULL: no resampling */
+    float* d_resampled;       /* resample_cap x 7 */
+    size_t resample_cap;
+    uint32_t* d_count;        /* particles the resampler emitted */
+} tsdfl_filter;
+int tsdfl_batch_create(tsdfl_ctx* ctx, const tsdfl_filter* filters, size_t n_filters, uint32_t flags,
+                       tsdfl_batch** out);
+int tsdfl_batch_destroy(tsdfl_batch* batch);
+/* One update of every filter, stream-ordered on the context's stream (the
+ * captured graph when there is one).  Device-side errors: tsdfl_ctx_sync. */
+int tsdfl_batch_run(tsdfl_batch* batch);
+/* Captures one update as a CUDA graph; later runs launch the graph. */
+int tsdfl_batch_capture(tsdfl_batch* batch);
+/* Work-item shape of the persistent scoring launch: chunk scan points (a
+ * multiple of 64) x group particles.  Results do not depend on it. */
+int tsdfl_batch_set_tiles(tsdfl_batch* batch, int chunk, int group);
+/* Times the scoring launch for a set of shapes and keeps the fastest. */
+int tsdfl_batch_autotune(tsdfl_batch* batch, int* chunk_out, int* group_out, float* best_ms);
+/* Hit counts (points whose slot index is inside the map data) of filter i's
+ * last update, P values copied to the host. */
+int tsdfl_batch_hits(tsdfl_batch* batch, size_t i, uint32_t* hits);
+/* Work in the persistent launch: segments, batches of work items, and the
+ * filters scored outside it (maps without the tiled path). */
+int tsdfl_batch_info(const tsdfl_batch* batch, uint32_t* segments, uint32_t* batches, uint32_t* outside);
+
 /* ---- the reference's other resamplers ----
  * WheelResampler (src/resampling/wheel_resampler.cpp:6-33), ResidualResampler
  * (novel_resampling.h:9-35), MetropolisResampler (:106-143) and

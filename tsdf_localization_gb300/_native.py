@@ -62,6 +62,13 @@ class Motion(C.Structure):
     _fields_ = [("mean", C.c_double * 6), ("stddev", C.c_double * 6)]
 
 
+class Filter(C.Structure):
+    _fields_ = [("map", C.c_void_p), ("model", Model), ("tf", C.c_float * 16), ("d_particles", C.c_void_p),
+                ("P", C.c_size_t), ("d_points", C.c_void_p), ("N", C.c_size_t), ("d_pose_out", C.c_void_p),
+                ("d_u0", C.c_void_p), ("d_resampled", C.c_void_p), ("resample_cap", C.c_size_t),
+                ("d_count", C.c_void_p)]
+
+
 class EvalDebug(C.Structure):
     _fields_ = [("raw_weights", C.c_void_p), ("hits", C.c_void_p), ("voxel_index", C.c_void_p),
                 ("laser_pose", C.c_void_p), ("weight_sum", C.c_double)]
@@ -113,6 +120,14 @@ SIGNATURES = [
     ("tsdfl_resample_metropolis_device", I, [P, P, SZ, U32, P, P, C.c_uint64, P]),
     ("tsdfl_resample_rejection", I, [P, P, SZ, C.c_uint64, P]),
     ("tsdfl_resample_rejection_device", I, [P, P, SZ, C.c_uint64, P]),
+    ("tsdfl_batch_create", I, [P, C.POINTER(Filter), SZ, U32, C.POINTER(P)]),
+    ("tsdfl_batch_destroy", I, [P]),
+    ("tsdfl_batch_run", I, [P]),
+    ("tsdfl_batch_capture", I, [P]),
+    ("tsdfl_batch_set_tiles", I, [P, I, I]),
+    ("tsdfl_batch_autotune", I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(F)]),
+    ("tsdfl_batch_hits", I, [P, SZ, P]),
+    ("tsdfl_batch_info", I, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     ("tsdfl_pose_array_device", I, [P, P, SZ, P]),
     ("tsdfl_pose_array", I, [P, P, SZ, P]),
     ("tsdfl_motion_model", I, [I, P, P, SZ, F, C.POINTER(Motion)]),

@@ -105,12 +105,10 @@ int set_device(int dev)
     return TSDFL_OK;
 }
 
-// Carves the per-evaluation workspace for P particles and N points.
-int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
+// Layout of one evaluation's workspace for nP particles and nN points: the
+// bytes it takes, and (base non-null) the buffers carved from base.
+size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** sum_f64)
 {
-    if (P <= c->cap_P && N <= c->cap_N && c->ws) return TSDFL_OK;
-    size_t nP = P > c->cap_P ? P : c->cap_P;
-    size_t nN = N > c->cap_N ? N : c->cap_N;
     if (nP < 1) nP = 1;
     if (nN < 4) nN = 4;
     size_t npad = align_up(nN, 4);
@@ -139,33 +137,48 @@ int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
     size_t o_part = take(sizeof(double) * 256 * 10);
     size_t o_sums = take(sizeof(double) * 16);
     size_t o_wsf = take(sizeof(float) * 4);
-    size_t total = off;
+    size_t o_st = take(sizeof(int32_t) * 4);
+    if (base) {
+        char* b = base;
+        e->pose12 = reinterpret_cast<float*>(b + o_pose);
+        e->trig6 = reinterpret_cast<float*>(b + o_trig);
+        e->sum_fx = reinterpret_cast<long long*>(b + o_fx);
+        *sum_f64 = reinterpret_cast<double*>(b + o_f64);
+        e->raw = reinterpret_cast<float*>(b + o_raw);
+        e->hits = reinterpret_cast<uint32_t*>(b + o_hits);
+        e->xs = reinterpret_cast<float*>(b + o_xs);
+        e->ys = reinterpret_cast<float*>(b + o_ys);
+        e->zs = reinterpret_cast<float*>(b + o_zs);
+        e->cs = reinterpret_cast<float*>(b + o_cs);
+        e->pxy = reinterpret_cast<float4*>(b + o_pxy);
+        e->pz = reinterpret_cast<float2*>(b + o_pz);
+        e->lut_fx = reinterpret_cast<long long*>(b + o_lfx);
+        e->lut_f = reinterpret_cast<float*>(b + o_lf);
+        e->counts = reinterpret_cast<int32_t*>(b + o_cnt);
+        e->partials = reinterpret_cast<double*>(b + o_part);
+        e->sums = reinterpret_cast<double*>(b + o_sums);
+        e->weight_sum_f = reinterpret_cast<float*>(b + o_wsf);
+        e->status = reinterpret_cast<int32_t*>(b + o_st);
+    }
+    return off;
+}
+
+// Carves the per-evaluation workspace for P particles and N points.
+int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
+{
+    if (P <= c->cap_P && N <= c->cap_N && c->ws) return TSDFL_OK;
+    size_t nP = P > c->cap_P ? P : c->cap_P;
+    size_t nN = N > c->cap_N ? N : c->cap_N;
+    if (nP < 1) nP = 1;
+    if (nN < 4) nN = 4;
+    size_t total = eval_layout(nP, nN, nullptr, nullptr, nullptr);
     void* ws = nullptr;
     CUDA_TRY(cudaMalloc(&ws, total));
     if (c->ws) cudaFree(c->ws);
     c->ws = ws;
     c->ws_bytes = total;
-    char* b = static_cast<char*>(ws);
-    EvalBuffers& e = c->buf;
-    e.pose12 = reinterpret_cast<float*>(b + o_pose);
-    e.trig6 = reinterpret_cast<float*>(b + o_trig);
-    e.sum_fx = reinterpret_cast<long long*>(b + o_fx);
-    c->sum_f64 = reinterpret_cast<double*>(b + o_f64);
-    e.raw = reinterpret_cast<float*>(b + o_raw);
-    e.hits = reinterpret_cast<uint32_t*>(b + o_hits);
-    e.xs = reinterpret_cast<float*>(b + o_xs);
-    e.ys = reinterpret_cast<float*>(b + o_ys);
-    e.zs = reinterpret_cast<float*>(b + o_zs);
-    e.cs = reinterpret_cast<float*>(b + o_cs);
-    e.pxy = reinterpret_cast<float4*>(b + o_pxy);
-    e.pz = reinterpret_cast<float2*>(b + o_pz);
-    e.lut_fx = reinterpret_cast<long long*>(b + o_lfx);
-    e.lut_f = reinterpret_cast<float*>(b + o_lf);
-    e.counts = reinterpret_cast<int32_t*>(b + o_cnt);
-    e.partials = reinterpret_cast<double*>(b + o_part);
-    e.sums = reinterpret_cast<double*>(b + o_sums);
-    e.weight_sum_f = reinterpret_cast<float*>(b + o_wsf);
-    e.status = c->status + 1;
+    eval_layout(nP, nN, static_cast<char*>(ws), &c->buf, &c->sum_f64);
+    c->buf.status = c->status + 1;
     c->cap_P = nP;
     c->cap_N = nN;
     return TSDFL_OK;
@@ -1058,6 +1071,376 @@ int tsdfl_evaluate_cloud(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* 
     st = tsdfl_ctx_sync(c);
     if (st) return st;
     if (pose_out) std::memcpy(pose_out, c->h_pose, sizeof(float) * 6);
+    return TSDFL_OK;
+}
+
+// ------------------------------------------------ batched filters
+
+struct tsdfl_batch {
+    tsdfl_ctx* ctx = nullptr;
+    std::vector<tsdfl_filter> f;
+    struct Per {
+        EvalBuffers b{};
+        double* sum_f64 = nullptr;
+        void* rs_ws = nullptr;
+        int shift = 40;
+        int npad = 4;
+        bool tiled = false;
+        bool dense = false;
+        size_t pass = 0;
+    };
+    std::vector<Per> per;
+    void* ws = nullptr;
+    void* d_segs = nullptr;
+    std::vector<BatchSegSpec> specs;
+    uint32_t batches = 0;
+    uint32_t* d_counter = nullptr;
+    int chunk = 1024, group = 4;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int batch_build_segments(tsdfl_batch* B)
+{
+    std::vector<char> host(B->specs.size() * batch_seg_bytes() + 1);
+    B->batches = build_batch_segs(B->specs.data(), (int)B->specs.size(), B->chunk, B->group, host.data());
+    if (!B->specs.empty())
+        CUDA_TRY(cudaMemcpy(B->d_segs, host.data(), B->specs.size() * batch_seg_bytes(), cudaMemcpyHostToDevice));
+    return TSDFL_OK;
+}
+
+// Scoring of every filter: the persistent launch, then the filters it does not take.
+int batch_score(tsdfl_batch* B, cudaStream_t s)
+{
+    tsdfl_ctx* c = B->ctx;
+    for (size_t i = 0; i < B->f.size(); ++i) {
+        if (!B->per[i].tiled || B->f[i].N == 0) continue;
+        CUDA_TRY(cudaMemsetAsync(B->per[i].b.sum_fx, 0, sizeof(long long) * B->f[i].P, s));
+        CUDA_TRY(cudaMemsetAsync(B->per[i].b.hits, 0, sizeof(uint32_t) * B->f[i].P, s));
+    }
+    int rc = launch_eval_batch(B->d_segs, (int)B->specs.size(), B->batches, B->d_counter, c->status, c->sm_count, s);
+    if (rc) return rc;
+    for (size_t i = 0; i < B->f.size(); ++i) {
+        const tsdfl_filter& F = B->f[i];
+        const tsdfl_batch::Per& q = B->per[i];
+        if (q.tiled || F.N == 0) continue;
+        for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
+            size_t n1 = n0 + q.pass < F.N ? n0 + q.pass : F.N;
+            rc = launch_eval_pass(F.map->view, F.model.a_hit, (int)F.P, (int)n0, (int)n1, (int)F.N, n0 == 0, false,
+                                  q.dense, true, q.b, q.sum_f64, c->sm_count, s);
+            if (rc) return rc;
+        }
+    }
+    return TSDFL_OK;
+}
+
+int batch_record(tsdfl_batch* B)
+{
+    tsdfl_ctx* c = B->ctx;
+    cudaStream_t s = c->stream;
+    for (size_t i = 0; i < B->f.size(); ++i) {
+        const tsdfl_filter& F = B->f[i];
+        tsdfl_batch::Per& q = B->per[i];
+        if (F.N == 0) continue;
+        const float inv_max_range = (float)(1.0 / (double)F.model.max_range);
+        const float c_in = F.model.a_range * inv_max_range;
+        int rc = launch_prepare(F.d_points, (int)F.N, q.npad, F.model.max_range * F.model.max_range, c_in,
+                                F.model.a_max, F.map->values, q.shift, q.b, s);
+        if (rc) return rc;
+        rc = launch_pose_kernel(F.tf, (int)F.P, q.b, s);
+        if (rc) return rc;
+    }
+    int rc = batch_score(B, s);
+    if (rc) return rc;
+    for (size_t i = 0; i < B->f.size(); ++i) {
+        const tsdfl_filter& F = B->f[i];
+        tsdfl_batch::Per& q = B->per[i];
+        if (F.N == 0) continue;
+        const float inv_max_range = (float)(1.0 / (double)F.model.max_range);
+        const float c_in = F.model.a_range * inv_max_range;
+        const int mode = F.map->view.storage == 1 ? 1 : 0;
+        rc = launch_norm((int)F.P, mode, q.shift, (double)F.model.a_hit, (double)c_in, (double)F.model.a_max,
+                         (int)F.N, q.sum_f64, F.d_particles, F.d_pose_out, q.b, s);
+        if (rc) return rc;
+        rc = launch_fold_status(q.b.status, c->status, s);
+        if (rc) return rc;
+        if (F.d_u0 && F.d_resampled && F.P)
+            rc = launch_resample_impl(F.d_particles, F.d_particles + 6, 7, F.P, 0.0f, F.d_resampled, nullptr,
+                                      F.resample_cap, F.d_count, q.rs_ws, c->status, s, F.d_u0);
+        if (rc) return rc;
+    }
+    return TSDFL_OK;
+}
+
+}  // namespace
+
+int tsdfl_batch_create(tsdfl_ctx* c, const tsdfl_filter* filters, size_t n, uint32_t flags, tsdfl_batch** out)
+{
+    if (!c || !out || (n && !filters)) {
+        set_error("tsdfl_batch_create: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (flags != 0) {
+        set_error("tsdfl_batch_create: batches use exact sums (flags 0)");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        const tsdfl_filter& F = filters[i];
+        if (!F.map || (F.P && !F.d_particles) || (F.N && !F.d_points) ||
+            (F.d_u0 && (!F.d_resampled || !F.d_count))) {
+            set_error("tsdfl_batch_create: filter %zu: invalid argument", i);
+            return TSDFL_ERR_INVALID_ARG;
+        }
+        int rc = check_model(&F.model);
+        if (rc) return rc;
+        if (F.N && F.P == 0) {
+            set_error("tsdfl_batch_create: filter %zu: no particles", i);
+            return TSDFL_ERR_DEGENERATE;
+        }
+        if (F.P >= (1ull << 24) || F.N >= (1ull << 31)) {
+            set_error("tsdfl_batch_create: filter %zu: too many particles or points", i);
+            return TSDFL_ERR_UNSUPPORTED;
+        }
+        if (F.map->device != c->device) {
+            set_error("tsdfl_batch_create: filter %zu: map on another device", i);
+            return TSDFL_ERR_INVALID_ARG;
+        }
+    }
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    auto* B = new (std::nothrow) tsdfl_batch;
+    if (!B) return TSDFL_ERR_OUT_OF_MEMORY;
+    B->ctx = c;
+    B->f.assign(filters, filters + n);
+    B->per.resize(n);
+    std::vector<size_t> eval_off(n), rs_off(n);
+    size_t total = 0;
+    for (size_t i = 0; i < n; ++i) {
+        eval_off[i] = total;
+        total = align_up(total + eval_layout(B->f[i].P, B->f[i].N, nullptr, nullptr, nullptr), 256);
+        rs_off[i] = total;
+        total = align_up(total + resample_workspace_bytes(B->f[i].P ? B->f[i].P : 1), 256);
+    }
+    cudaError_t e = cudaMalloc(&B->ws, total ? total : 256);
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, 256);
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_segs, (2 * n + 1) * batch_seg_bytes() + 256);
+    if (e != cudaSuccess) {
+        set_error("tsdfl_batch_create: %s", cudaGetErrorString(e));
+        tsdfl_batch_destroy(B);
+        return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
+    }
+    char* base = static_cast<char*>(B->ws);
+    for (size_t i = 0; i < n; ++i) {
+        tsdfl_filter& F = B->f[i];
+        tsdfl_batch::Per& q = B->per[i];
+        eval_layout(F.P, F.N, base + eval_off[i], &q.b, &q.sum_f64);
+        q.b.particles = F.d_particles;
+        q.rs_ws = base + rs_off[i];
+        q.npad = (int)align_up(F.N, 4);
+        double bound = std::fmax((double)F.map->max_value, 1e-30) * (double)(F.N + 1);
+        int need = (int)std::ceil(std::log2(bound));
+        q.shift = 62 - need < 40 ? 62 - need : 40;
+        const MapView& m = F.map->view;
+        q.dense = F.map->dense != nullptr;
+        q.tiled = m.storage == 0 && m.sub_fast != 0;
+        if (q.tiled) {
+            int tp = tiled_pass_points(m, q.dense);
+            if (tp < 1024 && q.dense) {
+                q.dense = false;
+                tp = tiled_pass_points(m, false);
+            }
+            if (tp < 64) q.tiled = false;
+            q.pass = (size_t)(tp > 0 ? tp : kMaxPassPoints);
+        }
+        if (!q.tiled) q.pass = (size_t)kMaxPassPoints;
+        if (q.tiled && F.N) {
+            for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
+                BatchSegSpec sp;
+                sp.m = m;
+                sp.a_hit = F.model.a_hit;
+                sp.P = (int)F.P;
+                sp.n0 = (int)n0;
+                sp.n1 = (int)(n0 + q.pass < F.N ? n0 + q.pass : F.N);
+                sp.n_total = (int)F.N;
+                sp.dense = q.dense;
+                sp.b = q.b;
+                B->specs.push_back(sp);
+            }
+        }
+    }
+    if (B->specs.size() > 2 * n + 1) {   // more passes than the segment buffer holds: grow it
+        cudaFree(B->d_segs);
+        if (cudaMalloc(&B->d_segs, B->specs.size() * batch_seg_bytes() + 256) != cudaSuccess) {
+            set_error("tsdfl_batch_create: out of memory");
+            tsdfl_batch_destroy(B);
+            return TSDFL_ERR_OUT_OF_MEMORY;
+        }
+    }
+    rc = batch_build_segments(B);
+    if (rc) {
+        tsdfl_batch_destroy(B);
+        return rc;
+    }
+    *out = B;
+    return TSDFL_OK;
+}
+
+int tsdfl_batch_destroy(tsdfl_batch* B)
+{
+    if (!B) return TSDFL_OK;
+    cudaSetDevice(B->ctx->device);
+    if (B->ctx->stream) cudaStreamSynchronize(B->ctx->stream);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    cudaFree(B->ws);
+    cudaFree(B->d_counter);
+    cudaFree(B->d_segs);
+    delete B;
+    return TSDFL_OK;
+}
+
+int tsdfl_batch_run(tsdfl_batch* B)
+{
+    if (!B) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(B->ctx->device);
+    if (rc) return rc;
+    if (B->exec) {
+        CUDA_TRY(cudaGraphLaunch(B->exec, B->ctx->stream));
+        g_launches += 1;
+        return TSDFL_OK;
+    }
+    return batch_record(B);
+}
+
+int tsdfl_batch_capture(tsdfl_batch* B)
+{
+    if (!B) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(B->ctx->device);
+    if (rc) return rc;
+    if (B->exec) {
+        cudaGraphExecDestroy(B->exec);
+        B->exec = nullptr;
+    }
+    cudaStream_t s = B->ctx->stream;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    rc = batch_record(B);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_error("tsdfl_batch_capture: %s", cudaGetErrorString(e));
+        return TSDFL_ERR_DEVICE;
+    }
+    e = cudaGraphInstantiate(&B->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        B->exec = nullptr;
+        set_error("tsdfl_batch_capture: %s", cudaGetErrorString(e));
+        return TSDFL_ERR_DEVICE;
+    }
+    return TSDFL_OK;
+}
+
+int tsdfl_batch_set_tiles(tsdfl_batch* B, int chunk, int group)
+{
+    if (!B || chunk < 64 || chunk % 64 || group < 1 || group > 64) {
+        set_error("tsdfl_batch_set_tiles: chunk must be a positive multiple of 64, group in [1, 64]");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = set_device(B->ctx->device);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(B->ctx->stream));   // the segment table is read by queued work
+    B->chunk = chunk;
+    B->group = group;
+    rc = batch_build_segments(B);
+    if (rc) return rc;
+    if (B->exec) return tsdfl_batch_capture(B);   // the graph holds the old batch count
+    return TSDFL_OK;
+}
+
+int tsdfl_batch_autotune(tsdfl_batch* B, int* chunk_out, int* group_out, float* best_ms)
+{
+    if (!B) return TSDFL_ERR_INVALID_ARG;
+    int rc = set_device(B->ctx->device);
+    if (rc) return rc;
+    cudaStream_t s = B->ctx->stream;
+    const bool had_graph = B->exec != nullptr;
+    static const int shapes[][2] = {{1024, 4}, {512, 4}, {2048, 4}, {1024, 2}, {1024, 8}, {512, 8}, {2048, 2}};
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    // the points and poses the scoring reads
+    const int keep_chunk = B->chunk, keep_group = B->group;
+    cudaGraphExec_t keep_exec = B->exec;
+    B->exec = nullptr;
+    rc = batch_record(B);
+    float best = 1e30f;
+    int bc = keep_chunk, bg = keep_group;
+    for (const auto& sh : shapes) {
+        if (rc) break;
+        CUDA_TRY(cudaStreamSynchronize(s));
+        B->chunk = sh[0];
+        B->group = sh[1];
+        rc = batch_build_segments(B);
+        if (rc) break;
+        float t = 0;
+        for (int rep = 0; rep < 3 && !rc; ++rep) {
+            cudaEventRecord(e0, s);
+            rc = batch_score(B, s);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) t += ms;   // the first is a warm-up
+        }
+        if (!rc && t / 2 < best) {
+            best = t / 2;
+            bc = sh[0];
+            bg = sh[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->exec = keep_exec;
+    B->chunk = bc;
+    B->group = bg;
+    int rc2 = batch_build_segments(B);
+    if (!rc) rc = rc2;
+    if (!rc && had_graph) rc = tsdfl_batch_capture(B);
+    if (chunk_out) *chunk_out = bc;
+    if (group_out) *group_out = bg;
+    if (best_ms) *best_ms = best;
+    return rc ? rc : tsdfl_ctx_sync(B->ctx);
+}
+
+int tsdfl_batch_hits(tsdfl_batch* B, size_t i, uint32_t* hits)
+{
+    if (!B || i >= B->f.size() || (B->f[i].P && !hits)) {
+        set_error("tsdfl_batch_hits: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = set_device(B->ctx->device);
+    if (rc) return rc;
+    if (B->f[i].P)
+        CUDA_TRY(cudaMemcpyAsync(hits, B->per[i].b.hits, sizeof(uint32_t) * B->f[i].P, cudaMemcpyDeviceToHost,
+                                 B->ctx->stream));
+    return tsdfl_ctx_sync(B->ctx);
+}
+
+int tsdfl_batch_info(const tsdfl_batch* B, uint32_t* segments, uint32_t* batches, uint32_t* outside)
+{
+    if (!B) return TSDFL_ERR_INVALID_ARG;
+    if (segments) *segments = (uint32_t)B->specs.size();
+    if (batches) *batches = B->batches;
+    if (outside) {
+        uint32_t o = 0;
+        for (size_t i = 0; i < B->f.size(); ++i) o += (!B->per[i].tiled && B->f[i].N) ? 1u : 0u;
+        *outside = o;
+    }
     return TSDFL_OK;
 }
 

@@ -494,6 +494,130 @@ struct TiledParams {
 // independent of order, so results equal eval_exact_kernel's bit for bit.
 // TWO: the sub-voxel index needs the two-term multiplier (sub_fast 1);
 // DBG: per-point codes are written to the debug buffer.
+// One work item of the tiled scoring: the points [c0, c0 + chunk_pts) of the
+// staged pass (pair layout in sxy/spz) against the particles of group grp.
+// Sums go to p.sum_fx / p.hits with one integer atomic per particle.
+template <bool DENSE, bool TWO, bool DBG>
+__device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m, const MapView* s_map,
+                                           const uint32_t* occ, const float4* sxy, const float2* spz,
+                                           const long long* lut, float4* ring, int n, int chunk_pts, int group,
+                                           int chunk, int grp, int lane)
+{
+    const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
+    const f2_t MAG = pk(8388608.0f, 8388608.0f);
+    const f2_t INV = pk(m.sub_inv, m.sub_inv);
+    const f2_t INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
+    const f2_t ABS = 0x7fffffff7fffffffull;
+    uint32_t head = 0, tail = 0;
+    const int c0 = chunk * chunk_pts;
+    const int cn = min(chunk_pts, n - c0);
+    const int b0 = c0 >> 6, nblk = (cn + 63) >> 6, nfull = cn >> 6;
+    for (int k = 0; k < group; ++k) {
+        const int pi = grp * group + k;
+        if (pi >= p.P) break;
+        const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
+        const float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
+        const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
+        long long acc = 0;
+        uint32_t hits = 0;
+        uint32_t* dbg_row = DBG ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
+        // one step: the two points of block blk held by this lane (the
+        // chunk's partial last block masks its padding points)
+        auto step = [&](int blk, bool partial) {
+            const float4 xy = sxy[(b0 + blk) * 32 + lane];
+            const float2 zz = spz[(b0 + blk) * 32 + lane];
+            // tsdf_evaluator.cpp:44-46 for two points: ((r0 x + r1 y) + r2 z) + r3
+            const f2_t TX = add2(add2(add2(pk(__fmul_rn(a.x, xy.x), __fmul_rn(a.x, xy.y)),
+                                           pk(__fmul_rn(a.y, xy.z), __fmul_rn(a.y, xy.w))),
+                                      pk(__fmul_rn(a.z, zz.x), __fmul_rn(a.z, zz.y))),
+                                 R3);
+            const f2_t TY = add2(add2(add2(pk(__fmul_rn(b4.x, xy.x), __fmul_rn(b4.x, xy.y)),
+                                           pk(__fmul_rn(b4.y, xy.z), __fmul_rn(b4.y, xy.w))),
+                                      pk(__fmul_rn(b4.z, zz.x), __fmul_rn(b4.z, zz.y))),
+                                 R7);
+            const f2_t TZ = add2(add2(add2(pk(__fmul_rn(c4.x, xy.x), __fmul_rn(c4.x, xy.y)),
+                                           pk(__fmul_rn(c4.y, xy.z), __fmul_rn(c4.y, xy.w))),
+                                      pk(__fmul_rn(c4.z, zz.x), __fmul_rn(c4.z, zz.y))),
+                                 R11);
+            const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
+            const f2_t AZ = and2(OZ, ABS);   // |oz|
+            const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(AZ, MAG);  // 2^23 + trunc
+            const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(AZ, sub2(MZ, MAG));
+            f2_t CX, CY, CZ;   // 2^23 + sub-voxel index
+            if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
+                CX = add2_rz(fma2_rn(SX, INV, mul2(SX, INVLO)), MAG);
+                CY = add2_rz(fma2_rn(SY, INV, mul2(SY, INVLO)), MAG);
+                CZ = add2_rz(fma2_rn(SZ, INV, mul2(SZ, INVLO)), MAG);
+            } else {           // floor(s * inv), the product unrounded
+                CX = fma2_rz(SX, INV, MAG);
+                CY = fma2_rz(SY, INV, MAG);
+                CZ = fma2_rz(SZ, INV, MAG);
+            }
+            FastIn i0, i1;
+            upk(OX, i0.ox, i1.ox); upk(OY, i0.oy, i1.oy); upk(OZ, i0.oz, i1.oz);
+            {
+                float a0, a1;
+                upk(MX, a0, a1); i0.bmx = __float_as_uint(a0); i1.bmx = __float_as_uint(a1);
+                upk(MY, a0, a1); i0.bmy = __float_as_uint(a0); i1.bmy = __float_as_uint(a1);
+                upk(MZ, a0, a1); i0.bmz = __float_as_uint(a0); i1.bmz = __float_as_uint(a1);
+                upk(CX, a0, a1); i0.bcx = __float_as_uint(a0); i1.bcx = __float_as_uint(a1);
+                upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
+                upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
+            }
+            uint32_t k0 = fast_code<DENSE>(m, occ, i0);
+            uint32_t k1 = fast_code<DENSE>(m, occ, i1);
+            if (partial) {
+                if (64 * blk + lane >= cn) k0 = kCodeNone;
+                if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
+            }
+            // lanes the fast path cannot decide are deferred to the warp's ring and
+            // scored 32 at a time (kCodeLater contributes nothing here), so no warp
+            // diverges into the slow tiers; at most 31 entries wait between steps,
+            // so each append of <= 32 fits the ring
+            if (__any_sync(0xffffffffu, k0 == kCodeSlow || k1 == kCodeSlow)) {
+                float tx, ty, tz, u;
+                upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
+                defer(ring, head, tail, k0 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + lane, lane);
+                if (tail - head >= 32) {
+                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
+                    acc += d.acc;
+                    hits += d.hits;
+                    head += 32;
+                }
+                upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
+                defer(ring, head, tail, k1 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
+                if (tail - head >= 32) {
+                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
+                    acc += d.acc;
+                    hits += d.hits;
+                    head += 32;
+                }
+            }
+            if (DBG) {
+                const int j = c0 + 64 * blk + lane;
+                if (k0 < (uint32_t)kCodeNone) dbg_row[j] = k0;
+                if (k1 < (uint32_t)kCodeNone) dbg_row[j + 32] = k1;
+            }
+            acc += lut[k0] + lut[k1];
+            hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
+        };
+        for (int blk = 0; blk < nfull; ++blk) step(blk, false);
+        if (nfull < nblk) step(nfull, true);
+        if (tail != head) {
+            const Partial d = drain(s_map, lut, ring, head, (int)(tail - head), lane, dbg_row);
+            acc += d.acc;
+            hits += d.hits;
+            head = tail;
+        }
+        acc = warp_sum_ll(acc);
+        hits = warp_sum_u32(hits);
+        if (lane == 0) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(p.sum_fx + pi), (unsigned long long)acc);
+            atomicAdd(p.hits + pi, hits);
+        }
+    }
+}
+
 template <bool DENSE, bool TWO, bool DBG>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
@@ -525,123 +649,110 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
 
     const int lane = threadIdx.x & 31;
     float4* ring = reinterpret_cast<float4*>(spz + npairs) + (threadIdx.x >> 5) * kRing;
-    uint32_t head = 0, tail = 0;
     const int gwarp = blockIdx.x * kTiledWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kTiledWarps;
-    const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
-    const f2_t MAG = pk(8388608.0f, 8388608.0f);
-    const f2_t INV = pk(m.sub_inv, m.sub_inv);
-    const f2_t INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
-    const f2_t ABS = 0x7fffffff7fffffffull;
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
-        const int c0 = chunk * tp.chunk;
-        const int cn = min(tp.chunk, n - c0);
-        const int b0 = c0 >> 6, nblk = (cn + 63) >> 6, nfull = cn >> 6;
-        for (int k = 0; k < tp.group; ++k) {
-            const int pi = grp * tp.group + k;
-            if (pi >= p.P) break;
-            const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
-            const float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
-            const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
-            long long acc = 0;
-            uint32_t hits = 0;
-            uint32_t* dbg_row = DBG ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
-            // one step: the two points of block blk held by this lane (the
-            // chunk's partial last block masks its padding points)
-            auto step = [&](int blk, bool partial) {
-                const float4 xy = sxy[(b0 + blk) * 32 + lane];
-                const float2 zz = spz[(b0 + blk) * 32 + lane];
-                // tsdf_evaluator.cpp:44-46 for two points: ((r0 x + r1 y) + r2 z) + r3
-                const f2_t TX = add2(add2(add2(pk(__fmul_rn(a.x, xy.x), __fmul_rn(a.x, xy.y)),
-                                               pk(__fmul_rn(a.y, xy.z), __fmul_rn(a.y, xy.w))),
-                                          pk(__fmul_rn(a.z, zz.x), __fmul_rn(a.z, zz.y))),
-                                     R3);
-                const f2_t TY = add2(add2(add2(pk(__fmul_rn(b4.x, xy.x), __fmul_rn(b4.x, xy.y)),
-                                               pk(__fmul_rn(b4.y, xy.z), __fmul_rn(b4.y, xy.w))),
-                                          pk(__fmul_rn(b4.z, zz.x), __fmul_rn(b4.z, zz.y))),
-                                     R7);
-                const f2_t TZ = add2(add2(add2(pk(__fmul_rn(c4.x, xy.x), __fmul_rn(c4.x, xy.y)),
-                                               pk(__fmul_rn(c4.y, xy.z), __fmul_rn(c4.y, xy.w))),
-                                          pk(__fmul_rn(c4.z, zz.x), __fmul_rn(c4.z, zz.y))),
-                                     R11);
-                const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
-                const f2_t AZ = and2(OZ, ABS);   // |oz|
-                const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(AZ, MAG);  // 2^23 + trunc
-                const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(AZ, sub2(MZ, MAG));
-                f2_t CX, CY, CZ;   // 2^23 + sub-voxel index
-                if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
-                    CX = add2_rz(fma2_rn(SX, INV, mul2(SX, INVLO)), MAG);
-                    CY = add2_rz(fma2_rn(SY, INV, mul2(SY, INVLO)), MAG);
-                    CZ = add2_rz(fma2_rn(SZ, INV, mul2(SZ, INVLO)), MAG);
-                } else {           // floor(s * inv), the product unrounded
-                    CX = fma2_rz(SX, INV, MAG);
-                    CY = fma2_rz(SY, INV, MAG);
-                    CZ = fma2_rz(SZ, INV, MAG);
-                }
-                FastIn i0, i1;
-                upk(OX, i0.ox, i1.ox); upk(OY, i0.oy, i1.oy); upk(OZ, i0.oz, i1.oz);
-                {
-                    float a0, a1;
-                    upk(MX, a0, a1); i0.bmx = __float_as_uint(a0); i1.bmx = __float_as_uint(a1);
-                    upk(MY, a0, a1); i0.bmy = __float_as_uint(a0); i1.bmy = __float_as_uint(a1);
-                    upk(MZ, a0, a1); i0.bmz = __float_as_uint(a0); i1.bmz = __float_as_uint(a1);
-                    upk(CX, a0, a1); i0.bcx = __float_as_uint(a0); i1.bcx = __float_as_uint(a1);
-                    upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
-                    upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
-                }
-                uint32_t k0 = fast_code<DENSE>(m, occ, i0);
-                uint32_t k1 = fast_code<DENSE>(m, occ, i1);
-                if (partial) {
-                    if (64 * blk + lane >= cn) k0 = kCodeNone;
-                    if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
-                }
-                // lanes the fast path cannot decide are deferred to the warp's ring and
-                // scored 32 at a time (kCodeLater contributes nothing here), so no warp
-                // diverges into the slow tiers; at most 31 entries wait between steps,
-                // so each append of <= 32 fits the ring
-                if (__any_sync(0xffffffffu, k0 == kCodeSlow || k1 == kCodeSlow)) {
-                    float tx, ty, tz, u;
-                    upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
-                    defer(ring, head, tail, k0 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + lane, lane);
-                    if (tail - head >= 32) {
-                        const Partial d = drain(&s_map, lut, ring, head, 32, lane, dbg_row);
-                        acc += d.acc;
-                        hits += d.hits;
-                        head += 32;
-                    }
-                    upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
-                    defer(ring, head, tail, k1 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
-                    if (tail - head >= 32) {
-                        const Partial d = drain(&s_map, lut, ring, head, 32, lane, dbg_row);
-                        acc += d.acc;
-                        hits += d.hits;
-                        head += 32;
-                    }
-                }
-                if (DBG) {
-                    const int j = c0 + 64 * blk + lane;
-                    if (k0 < (uint32_t)kCodeNone) dbg_row[j] = k0;
-                    if (k1 < (uint32_t)kCodeNone) dbg_row[j + 32] = k1;
-                }
-                acc += lut[k0] + lut[k1];
-                hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
-            };
-            for (int blk = 0; blk < nfull; ++blk) step(blk, false);
-            if (nfull < nblk) step(nfull, true);
-            if (tail != head) {
-                const Partial d = drain(&s_map, lut, ring, head, (int)(tail - head), lane, dbg_row);
-                acc += d.acc;
-                hits += d.hits;
-                head = tail;
+        tiled_item<DENSE, TWO, DBG>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp, lane);
+    }
+}
+
+struct BatchSeg {
+    EvalParams e;
+    int chunk, group, groups, items;
+    int dense, two;
+    uint32_t first_batch;
+};
+
+// Many filters in one persistent launch.  The work queue is the filters'
+// (filter, pass) segments one after another, each cut into batches of
+// kTiledWarps (point chunk, particle group) items -- one per warp of a CTA.  A
+// CTA takes the next batch with one atomic; when the batch belongs to another
+// segment than the one staged, the CTA stages that segment (the filter's code
+// LUT, its map's occupancy bitmap, the pass's scan points) before its warps
+// score the items.  Per-item scoring is eval_tiled_kernel's, so every filter's
+// sums equal its single-filter sums bit for bit.
+__global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const BatchSeg* __restrict__ segs, int nseg,
+                                                                      uint32_t total_batches, uint32_t* counter,
+                                                                      int32_t* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ BatchSeg s_seg;
+    __shared__ uint32_t s_batch;
+    __shared__ int s_segi;
+    long long* lut = reinterpret_cast<long long*>(smem);
+    uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    int cur = -1;
+    uint32_t phase = 0;
+    float4* sxy = nullptr;
+    float2* spz = nullptr;
+    float4* ring = nullptr;
+    int n = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t b = atomicAdd(counter, 1u);
+            int lo = 0, hi = nseg - 1;   // last segment whose first batch is <= b
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (segs[mid].first_batch <= b) lo = mid;
+                else hi = mid - 1;
             }
-            acc = warp_sum_ll(acc);
-            hits = warp_sum_u32(hits);
-            if (lane == 0) {
-                atomicAdd(reinterpret_cast<unsigned long long*>(p.sum_fx + pi), (unsigned long long)acc);
-                atomicAdd(p.hits + pi, hits);
+            s_batch = b;
+            s_segi = lo;
+        }
+        __syncthreads();
+        const uint32_t b = s_batch;
+        const int segi = s_segi;
+        if (b >= total_batches) break;
+        if (segi != cur) {
+            if (threadIdx.x == 0) s_seg = segs[segi];
+            __syncthreads();
+            const EvalParams& p = s_seg.e;
+            n = p.n1 - p.n0;
+            const int npairs = ((n + 63) >> 6) * 32;
+            const uint32_t occ_words = s_seg.dense ? 2u * p.m.occ_words : 0u;
+            sxy = reinterpret_cast<float4*>(occ + occ_words);
+            spz = reinterpret_cast<float2*>(sxy + npairs);
+            ring = reinterpret_cast<float4*>(spz + npairs) + warp * kRing;
+            for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
+            if (threadIdx.x == 0) {
+                mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_words * 4u);
+                bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
+                bulk_g2s(spz, p.pz + p.n0 / 2, (uint32_t)npairs * 8u, &bar);
+                if (occ_words) bulk_g2s(occ, p.m.occ, occ_words * 4u, &bar);
+            }
+            bool staged = mbar_wait_bounded(&bar, phase);
+            if (!staged) staged = mbar_wait_bounded(&bar, phase);   // give copies in flight a second bound
+            phase ^= 1u;
+            if (!staged && threadIdx.x == 0) atomicExch(status, TSDFL_ERR_TIMEOUT);
+            if (__syncthreads_and(staged ? 1 : 0) == 0) return;
+            cur = segi;
+        }
+        const int item = (int)(b - s_seg.first_batch) * kTiledWarps + warp;
+        if (item < s_seg.items) {
+            const EvalParams& p = s_seg.e;
+            const int chunk = item / s_seg.groups, grp = item - chunk * s_seg.groups;
+            if (s_seg.dense) {
+                if (s_seg.two)
+                    tiled_item<true, true, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group,
+                                                  chunk, grp, lane);
+                else
+                    tiled_item<true, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
+                                                   s_seg.group, chunk, grp, lane);
+            } else {
+                if (s_seg.two)
+                    tiled_item<false, true, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
+                                                   s_seg.group, chunk, grp, lane);
+                else
+                    tiled_item<false, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
+                                                    s_seg.group, chunk, grp, lane);
             }
         }
+        __syncthreads();   // every warp is done with s_batch and the staged segment
     }
 }
 
@@ -817,6 +928,7 @@ struct ResampleWs {
     long long* total;
     int* serial;            // 1 when only the literal loop reproduces it
     double* sums;           // M serial double prefix sums (aliases cdf; used when !exact_ok)
+    const float* u0p;       // the draw in device memory (replaces u0 when set)
 };
 
 // Weight as an exact multiple of 2^-52 (its value in those units), or -1 when
@@ -956,6 +1068,7 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
 // prefix offsets, lane 0 walks the binades (scalings by powers of two only).
 __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs ws)
 {
+    if (ws.u0p) u0 = *ws.u0p;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x >= 32 || blockIdx.x != 0) return;
     const int per = (tiles + 31) / 32, t0 = min(tiles, lane * per), t1 = min(tiles, t0 + per);
@@ -1205,6 +1318,7 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
 // Draw segments up to the serial sum's total, for the fallback above.
 __global__ void resample_segments_sums_kernel(int M, float u0, ResampleWs ws)
 {
+    if (ws.u0p) u0 = *ws.u0p;
     if (threadIdx.x != 0 || blockIdx.x != 0 || *ws.exact_ok || *ws.serial) return;
     if (!build_segments(M, u0, ws.sums[M - 1], ws)) *ws.serial = 1;
 }
@@ -1255,8 +1369,9 @@ __global__ void __launch_bounds__(kChainThreads) systematic_chain_kernel(const f
                                                                          uint32_t* __restrict__ cnt,
                                                                          uint32_t* __restrict__ off,
                                                                          unsigned long long* total, int* err,
-                                                                         const int* run)
+                                                                         const int* run, const float* u0p)
 {
+    if (u0p) u0 = *u0p;
     __shared__ float sw[kChainTile];
     __shared__ uint32_t sc[kChainTile], so[kChainTile];
     __shared__ int s_stop;
@@ -1639,6 +1754,58 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
     return check(cudaGetLastError());
 }
 
+size_t batch_seg_bytes() { return sizeof(BatchSeg); }
+
+uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out)
+{
+    BatchSeg* out = static_cast<BatchSeg*>(host_out);
+    uint32_t batches = 0;
+    for (int i = 0; i < nseg; ++i) {
+        const BatchSegSpec& sp = specs[i];
+        const EvalBuffers& b = sp.b;
+        BatchSeg g{};
+        EvalParams& p = g.e;
+        p.m = sp.m;
+        p.pose12 = b.pose12;
+        p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
+        p.pxy = b.pxy; p.pz = b.pz;
+        p.lut_fx = b.lut_fx;
+        p.lut_f = b.lut_f;
+        p.sum_fx = b.sum_fx;
+        p.hits = b.hits;
+        p.status = b.status;
+        p.P = sp.P; p.n0 = sp.n0; p.n1 = sp.n1; p.n_total = sp.n_total; p.first_pass = sp.n0 == 0 ? 1 : 0;
+        p.a_hit = sp.a_hit;
+        g.chunk = chunk;
+        g.group = group;
+        g.groups = (sp.P + group - 1) / group;
+        g.items = ((sp.n1 - sp.n0 + chunk - 1) / chunk) * g.groups;
+        g.dense = sp.dense ? 1 : 0;
+        g.two = sp.m.sub_fast == 1 ? 1 : 0;
+        g.first_batch = batches;
+        batches += (uint32_t)((g.items + kTiledWarps - 1) / kTiledWarps);
+        out[i] = g;
+    }
+    return batches;
+}
+
+size_t batch_smem_bytes() { return 227 * 1024 - 1024; }
+
+int launch_eval_batch(const void* d_segs, int nseg, uint32_t total_batches, uint32_t* counter, int32_t* status,
+                      int sm_count, cudaStream_t s)
+{
+    if (nseg == 0 || total_batches == 0) return TSDFL_OK;
+    const size_t smem = batch_smem_bytes();
+    cudaFuncSetAttribute(eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
+    unsigned blocks = (unsigned)sm_count;
+    if (total_batches < blocks) blocks = total_batches;
+    eval_batch_kernel<<<blocks, kTiledThreads, smem, s>>>(static_cast<const BatchSeg*>(d_segs), nseg, total_batches,
+                                                          counter, status);
+    g_launches += 1;
+    return check(cudaGetLastError());
+}
+
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s)
 {
@@ -1668,7 +1835,7 @@ size_t resample_workspace_bytes(size_t M)
 
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
                          uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
-                         cudaStream_t s)
+                         cudaStream_t s, const float* u0p)
 {
     size_t tiles = (M + kScanTile - 1) / kScanTile;
     char* p = static_cast<char*>(workspace);
@@ -1683,6 +1850,7 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     int* err = reinterpret_cast<int*>(p); p += 4;
     ws.serial = reinterpret_cast<int*>(p);
     ws.sums = reinterpret_cast<double*>(ws.cdf);
+    ws.u0p = u0p;
     // the literal loop reuses the prefix-sum array for counts and offsets
     uint32_t* cnt = reinterpret_cast<uint32_t*>(ws.cdf);
     uint32_t* off = cnt + M;
@@ -1698,7 +1866,8 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     resample_segments_sums_kernel<<<1, 32, 0, s>>>((int)M, u0, ws);
     resample_assign_sums_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out,
                                                        ws, status);
-    systematic_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err, ws.serial);
+    systematic_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err, ws.serial,
+                                                         u0p);
     resample_scatter_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, cnt, off, total, err, ws.serial, out,
                                                    idx_out, (long long)cap, count_out, status);
     g_launches += 9;

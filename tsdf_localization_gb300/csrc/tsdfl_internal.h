@@ -174,10 +174,28 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s);
 int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s);
+
+// Many filters' scoring in one persistent launch (eval_batch_kernel).  One
+// segment per (filter, pass) of a filter whose map takes the tiled path.
+struct BatchSegSpec {
+    MapView m;
+    float a_hit;
+    int P, n0, n1, n_total;
+    bool dense;
+    EvalBuffers b;
+};
+size_t batch_seg_bytes();
+// Writes nseg segment records (nseg * batch_seg_bytes() bytes at host_out)
+// with work items of `chunk` points x `group` particles; returns the number
+// of batches in the queue.
+uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out);
+int launch_eval_batch(const void* d_segs, int nseg, uint32_t total_batches, uint32_t* counter, int32_t* status,
+                      int sm_count, cudaStream_t s);
 size_t resample_workspace_bytes(size_t M);
+// u0p (optional): the draw read from device memory when the kernels run.
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
                          uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,
-                         cudaStream_t s);
+                         cudaStream_t s, const float* u0p = nullptr);
 // ResidualSystematicResampler on the device; workspace: resample_workspace_bytes(M).
 int launch_resample_residual(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
                              uint32_t* idx_out, size_t cap, uint32_t* count_out, void* workspace, int32_t* status,

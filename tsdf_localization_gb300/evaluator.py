@@ -418,6 +418,76 @@ class MotionModel:
         return particles
 
 
+class FilterBatch:
+    """Many independent filters updated together (tsdfl_batch): scoring in one
+    persistent launch, optionally replayed from a captured CUDA graph.  Each
+    filter is a dict of device buffers given as integer pointers -- particles
+    (P x 7 float32), points (N x 3), pose_out (6 floats or 0), u0 (1 float or 0
+    for no resampling), resampled (cap x 7), count (1 uint32) -- plus map
+    (DeviceMap), P, N, cap, tf (16 floats) and model (a_hit, a_range, a_max,
+    max_range)."""
+
+    def __init__(self, ctx: Context, filters):
+        self.ctx = ctx
+        arr = (N.Filter * max(len(filters), 1))()
+        self._maps = []
+        for i, f in enumerate(filters):
+            d = arr[i]
+            d.map = f["map"].handle
+            self._maps.append(f["map"])
+            d.model = N.Model(*f.get("model", (0.9, 0.1, 0.0, 100.0)))
+            tf = np.asarray(f["tf"], np.float32).reshape(16)
+            for k in range(16):
+                d.tf[k] = float(tf[k])
+            d.d_particles = f["particles"]
+            d.P = f["P"]
+            d.d_points = f["points"]
+            d.N = f["N"]
+            d.d_pose_out = f.get("pose_out") or None
+            d.d_u0 = f.get("u0") or None
+            d.d_resampled = f.get("resampled") or None
+            d.resample_cap = f.get("cap", 0)
+            d.d_count = f.get("count") or None
+        h = C.c_void_p()
+        N.check(N.lib().tsdfl_batch_create(ctx.handle, arr, len(filters), 0, C.byref(h)))
+        self.handle = h
+
+    def run(self) -> None:
+        N.check(N.lib().tsdfl_batch_run(self.handle))
+
+    def capture(self) -> None:
+        N.check(N.lib().tsdfl_batch_capture(self.handle))
+
+    def set_tiles(self, chunk: int, group: int) -> None:
+        N.check(N.lib().tsdfl_batch_set_tiles(self.handle, chunk, group))
+
+    def autotune(self):
+        c, g, t = C.c_int(), C.c_int(), C.c_float()
+        N.check(N.lib().tsdfl_batch_autotune(self.handle, C.byref(c), C.byref(g), C.byref(t)))
+        return c.value, g.value, t.value
+
+    def hits(self, i: int, P: int) -> np.ndarray:
+        out = np.zeros(P, np.uint32)
+        N.check(N.lib().tsdfl_batch_hits(self.handle, i, _ptr(out)))
+        return out
+
+    def info(self):
+        a, b, o = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        N.check(N.lib().tsdfl_batch_info(self.handle, C.byref(a), C.byref(b), C.byref(o)))
+        return {"segments": a.value, "batches": b.value, "outside": o.value}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            N.lib().tsdfl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def pose_array(ctx: Context, particles: np.ndarray) -> np.ndarray:
     """mcl_3d.cpp:429-449: the particles as geometry_msgs::Pose records, (P, 7)
     doubles: position, then the setRPY quaternion x, y, z, w."""
