@@ -1094,6 +1094,7 @@ struct tsdfl_batch {
     void* d_segs = nullptr;
     std::vector<BatchSegSpec> specs;
     uint32_t batches = 0;
+    BatchKinds kinds{};
     uint32_t* d_counter = nullptr;
     int chunk = 1024, group = 4;
     cudaGraphExec_t exec = nullptr;
@@ -1104,7 +1105,7 @@ namespace {
 int batch_build_segments(tsdfl_batch* B)
 {
     std::vector<char> host(B->specs.size() * batch_seg_bytes() + 1);
-    B->batches = build_batch_segs(B->specs.data(), (int)B->specs.size(), B->chunk, B->group, host.data());
+    B->batches = build_batch_segs(B->specs.data(), (int)B->specs.size(), B->chunk, B->group, host.data(), &B->kinds);
     if (!B->specs.empty())
         CUDA_TRY(cudaMemcpy(B->d_segs, host.data(), B->specs.size() * batch_seg_bytes(), cudaMemcpyHostToDevice));
     return TSDFL_OK;
@@ -1119,7 +1120,7 @@ int batch_score(tsdfl_batch* B, cudaStream_t s)
         CUDA_TRY(cudaMemsetAsync(B->per[i].b.sum_fx, 0, sizeof(long long) * B->f[i].P, s));
         CUDA_TRY(cudaMemsetAsync(B->per[i].b.hits, 0, sizeof(uint32_t) * B->f[i].P, s));
     }
-    int rc = launch_eval_batch(B->d_segs, (int)B->specs.size(), B->batches, B->d_counter, c->status, c->sm_count, s);
+    int rc = launch_eval_batch(B->d_segs, B->kinds, B->d_counter, c->status, c->sm_count, s);
     if (rc) return rc;
     for (size_t i = 0; i < B->f.size(); ++i) {
         const tsdfl_filter& F = B->f[i];

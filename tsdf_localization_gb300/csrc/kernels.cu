@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
+#include <vector>
 
 #include "index_math.h"
 #include "tsdfl_internal.h"
@@ -657,6 +659,12 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     }
 }
 
+// Work items per batch of the persistent multi-filter launch: the CTA's warps
+// take them one at a time from a shared counter, so uneven items even out
+// before the CTA's next barrier.
+constexpr int kBatchDepth = 8;
+constexpr int kBatchItems = kTiledWarps * kBatchDepth;
+
 struct BatchSeg {
     EvalParams e;
     int chunk, group, groups, items;
@@ -664,14 +672,18 @@ struct BatchSeg {
     uint32_t first_batch;
 };
 
-// Many filters in one persistent launch.  The work queue is the filters'
+// Many filters in one persistent launch (one per map-layout kind present:
+// compact or brick table, one- or two-term sub-voxel multiplier -- the same
+// specialisations as eval_tiled_kernel).  The work queue is the filters'
 // (filter, pass) segments one after another, each cut into batches of
-// kTiledWarps (point chunk, particle group) items -- one per warp of a CTA.  A
-// CTA takes the next batch with one atomic; when the batch belongs to another
+// kBatchItems (point chunk, particle group) items.  A CTA takes the next batch
+// with one atomic, its warps take the batch's items from a shared counter;
+// when the batch belongs to another
 // segment than the one staged, the CTA stages that segment (the filter's code
 // LUT, its map's occupancy bitmap, the pass's scan points) before its warps
 // score the items.  Per-item scoring is eval_tiled_kernel's, so every filter's
 // sums equal its single-filter sums bit for bit.
+template <bool DENSE, bool TWO>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const BatchSeg* __restrict__ segs, int nseg,
                                                                       uint32_t total_batches, uint32_t* counter,
                                                                       int32_t* status)
@@ -680,6 +692,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
     __shared__ uint64_t bar;
     __shared__ BatchSeg s_seg;
     __shared__ uint32_t s_batch;
+    __shared__ uint32_t s_next;
     __shared__ int s_segi;
     long long* lut = reinterpret_cast<long long*>(smem);
     uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
@@ -703,6 +716,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             }
             s_batch = b;
             s_segi = lo;
+            s_next = 0;
         }
         __syncthreads();
         const uint32_t b = s_batch;
@@ -714,7 +728,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             const EvalParams& p = s_seg.e;
             n = p.n1 - p.n0;
             const int npairs = ((n + 63) >> 6) * 32;
-            const uint32_t occ_words = s_seg.dense ? 2u * p.m.occ_words : 0u;
+            const uint32_t occ_words = DENSE ? 2u * p.m.occ_words : 0u;
             sxy = reinterpret_cast<float4*>(occ + occ_words);
             spz = reinterpret_cast<float2*>(sxy + npairs);
             ring = reinterpret_cast<float4*>(spz + npairs) + warp * kRing;
@@ -732,25 +746,17 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             if (__syncthreads_and(staged ? 1 : 0) == 0) return;
             cur = segi;
         }
-        const int item = (int)(b - s_seg.first_batch) * kTiledWarps + warp;
-        if (item < s_seg.items) {
+        const int base = (int)(b - s_seg.first_batch) * kBatchItems;
+        for (;;) {
+            uint32_t j = 0;
+            if (lane == 0) j = atomicAdd(&s_next, 1u);
+            j = __shfl_sync(0xffffffffu, j, 0);
+            const int item = base + (int)j;
+            if (j >= (uint32_t)kBatchItems || item >= s_seg.items) break;
             const EvalParams& p = s_seg.e;
             const int chunk = item / s_seg.groups, grp = item - chunk * s_seg.groups;
-            if (s_seg.dense) {
-                if (s_seg.two)
-                    tiled_item<true, true, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group,
-                                                  chunk, grp, lane);
-                else
-                    tiled_item<true, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
-                                                   s_seg.group, chunk, grp, lane);
-            } else {
-                if (s_seg.two)
-                    tiled_item<false, true, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
-                                                   s_seg.group, chunk, grp, lane);
-                else
-                    tiled_item<false, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk,
-                                                    s_seg.group, chunk, grp, lane);
-            }
+            tiled_item<DENSE, TWO, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group, chunk,
+                                          grp, lane);
         }
         __syncthreads();   // every warp is done with s_batch and the staged segment
     }
@@ -1756,53 +1762,78 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
 
 size_t batch_seg_bytes() { return sizeof(BatchSeg); }
 
-uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out)
+uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out,
+                          BatchKinds* kinds)
 {
     BatchSeg* out = static_cast<BatchSeg*>(host_out);
-    uint32_t batches = 0;
-    for (int i = 0; i < nseg; ++i) {
-        const BatchSegSpec& sp = specs[i];
-        const EvalBuffers& b = sp.b;
-        BatchSeg g{};
-        EvalParams& p = g.e;
-        p.m = sp.m;
-        p.pose12 = b.pose12;
-        p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
-        p.pxy = b.pxy; p.pz = b.pz;
-        p.lut_fx = b.lut_fx;
-        p.lut_f = b.lut_f;
-        p.sum_fx = b.sum_fx;
-        p.hits = b.hits;
-        p.status = b.status;
-        p.P = sp.P; p.n0 = sp.n0; p.n1 = sp.n1; p.n_total = sp.n_total; p.first_pass = sp.n0 == 0 ? 1 : 0;
-        p.a_hit = sp.a_hit;
-        g.chunk = chunk;
-        g.group = group;
-        g.groups = (sp.P + group - 1) / group;
-        g.items = ((sp.n1 - sp.n0 + chunk - 1) / chunk) * g.groups;
-        g.dense = sp.dense ? 1 : 0;
-        g.two = sp.m.sub_fast == 1 ? 1 : 0;
-        g.first_batch = batches;
-        batches += (uint32_t)((g.items + kTiledWarps - 1) / kTiledWarps);
-        out[i] = g;
+    // within a kind, the segments of one map follow each other, so that the L2
+    // holds one map's footprint at a time
+    std::vector<int> order(nseg);
+    for (int i = 0; i < nseg; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return reinterpret_cast<uintptr_t>(specs[a].m.codes) < reinterpret_cast<uintptr_t>(specs[b].m.codes);
+    });
+    uint32_t total = 0;
+    int o = 0;
+    for (int kind = 0; kind < 4; ++kind) {   // bit 1: compact layout, bit 0: two-term multiplier
+        kinds->first[kind] = o;
+        kinds->count[kind] = 0;
+        uint32_t batches = 0;
+        for (int oi = 0; oi < nseg; ++oi) {
+            const BatchSegSpec& sp = specs[order[oi]];
+            const int k = (sp.dense ? 2 : 0) + (sp.m.sub_fast == 1 ? 1 : 0);
+            if (k != kind) continue;
+            const EvalBuffers& b = sp.b;
+            BatchSeg g{};
+            EvalParams& p = g.e;
+            p.m = sp.m;
+            p.pose12 = b.pose12;
+            p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
+            p.pxy = b.pxy; p.pz = b.pz;
+            p.lut_fx = b.lut_fx;
+            p.lut_f = b.lut_f;
+            p.sum_fx = b.sum_fx;
+            p.hits = b.hits;
+            p.status = b.status;
+            p.P = sp.P; p.n0 = sp.n0; p.n1 = sp.n1; p.n_total = sp.n_total; p.first_pass = sp.n0 == 0 ? 1 : 0;
+            p.a_hit = sp.a_hit;
+            g.chunk = chunk;
+            g.group = group;
+            g.groups = (sp.P + group - 1) / group;
+            g.items = ((sp.n1 - sp.n0 + chunk - 1) / chunk) * g.groups;
+            g.dense = sp.dense ? 1 : 0;
+            g.two = sp.m.sub_fast == 1 ? 1 : 0;
+            g.first_batch = batches;
+            batches += (uint32_t)((g.items + kBatchItems - 1) / kBatchItems);
+            out[o++] = g;
+            kinds->count[kind]++;
+        }
+        kinds->batches[kind] = batches;
+        total += batches;
     }
-    return batches;
+    return total;
 }
 
 size_t batch_smem_bytes() { return 227 * 1024 - 1024; }
 
-int launch_eval_batch(const void* d_segs, int nseg, uint32_t total_batches, uint32_t* counter, int32_t* status,
+int launch_eval_batch(const void* d_segs, const BatchKinds& kinds, uint32_t* counter, int32_t* status,
                       int sm_count, cudaStream_t s)
 {
-    if (nseg == 0 || total_batches == 0) return TSDFL_OK;
+    const BatchSeg* segs = static_cast<const BatchSeg*>(d_segs);
     const size_t smem = batch_smem_bytes();
-    cudaFuncSetAttribute(eval_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
-    unsigned blocks = (unsigned)sm_count;
-    if (total_batches < blocks) blocks = total_batches;
-    eval_batch_kernel<<<blocks, kTiledThreads, smem, s>>>(static_cast<const BatchSeg*>(d_segs), nseg, total_batches,
-                                                          counter, status);
-    g_launches += 1;
+    for (int kind = 0; kind < 4; ++kind) {
+        if (kinds.count[kind] == 0 || kinds.batches[kind] == 0) continue;
+        auto k = kind == 3 ? eval_batch_kernel<true, true>
+                           : kind == 2 ? eval_batch_kernel<true, false>
+                                       : kind == 1 ? eval_batch_kernel<false, true> : eval_batch_kernel<false, false>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
+        unsigned blocks = (unsigned)sm_count;
+        if (kinds.batches[kind] < blocks) blocks = kinds.batches[kind];
+        k<<<blocks, kTiledThreads, smem, s>>>(segs + kinds.first[kind], kinds.count[kind], kinds.batches[kind],
+                                              counter, status);
+        g_launches += 1;
+    }
     return check(cudaGetLastError());
 }
 

@@ -184,13 +184,20 @@ struct BatchSegSpec {
     bool dense;
     EvalBuffers b;
 };
+// The segments of each map-layout kind (bit 1: compact layout, bit 0:
+// two-term sub-voxel multiplier) form one queue and one persistent launch.
+struct BatchKinds {
+    int first[4], count[4];
+    uint32_t batches[4];
+};
 size_t batch_seg_bytes();
-// Writes nseg segment records (nseg * batch_seg_bytes() bytes at host_out)
-// with work items of `chunk` points x `group` particles; returns the number
-// of batches in the queue.
-uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out);
-int launch_eval_batch(const void* d_segs, int nseg, uint32_t total_batches, uint32_t* counter, int32_t* status,
-                      int sm_count, cudaStream_t s);
+// Writes nseg segment records (nseg * batch_seg_bytes() bytes at host_out),
+// grouped by kind, with work items of `chunk` points x `group` particles;
+// returns the number of batches over all kinds.
+uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int group, void* host_out,
+                          BatchKinds* kinds);
+int launch_eval_batch(const void* d_segs, const BatchKinds& kinds, uint32_t* counter, int32_t* status, int sm_count,
+                      cudaStream_t s);
 size_t resample_workspace_bytes(size_t M);
 // u0p (optional): the draw read from device memory when the kernels run.
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
