@@ -244,6 +244,56 @@ int tsdfl_batch_hits(tsdfl_batch* batch, size_t i, uint32_t* hits);
  * filters scored outside it (maps without the tiled path). */
 int tsdfl_batch_info(const tsdfl_batch* batch, uint32_t* segments, uint32_t* batches, uint32_t* outside);
 
+/* ---- served sessions ----
+ * No counterpart in the reference (mcl_3d runs one filter per process).  A
+ * request loop for many robots on one GPU: every session's particles, map and
+ * random state stay on the device; scans are submitted as they arrive and
+ * queued; tsdfl_server_poll publishes finished updates and, whenever one of
+ * the two dispatch slots is free, launches every queued update of an idle
+ * session as one batch (continuous batching: updates that arrive while others
+ * run go out with the next batch, and two batches can be on the device at
+ * once).  One update = tsdfl_evaluate + tsdfl_resample_systematic of the
+ * session's particles, results identical to those single calls with the draw
+ * tsdfl_server_draw gives (exact sums).  Admission: a session opens only if
+ * its device memory fits the budget; a submission is refused when the work
+ * queued before it would take longer than max_wait_ms at the measured rate. */
+typedef struct tsdfl_server tsdfl_server;
+typedef struct tsdfl_server_config {
+    size_t hbm_budget;          /* bytes all sessions may hold on the device */
+    size_t max_sessions;
+    size_t max_points;          /* largest scan of one submission */
+    double max_wait_ms;         /* refuse submissions expected to wait longer (0: never refuse) */
+    uint32_t max_queue;         /* queued submissions per session (0: 4) */
+} tsdfl_server_config;
+int tsdfl_server_create(tsdfl_ctx* ctx, const tsdfl_server_config* cfg, tsdfl_server** out);
+int tsdfl_server_destroy(tsdfl_server* server);
+/* particles: P x 7 host floats; the session keeps at most 2P + 16 particles
+ * (the systematic resampler's count drifts).  TSDFL_ERR_OUT_OF_MEMORY: the
+ * budget cannot hold the session (refused). */
+int tsdfl_session_open(tsdfl_server* server, const tsdfl_map* map, const float* particles, size_t P,
+                       const float tf[16], const tsdfl_model* model, uint64_t seed, uint32_t* session);
+int tsdfl_session_close(tsdfl_server* server, uint32_t session);
+/* Queues one update with the scan points (N x 3 host floats, copied).  Refused
+ * with TSDFL_ERR_CAPACITY when the session's queue is full or the admission
+ * bound is exceeded. */
+int tsdfl_session_submit(tsdfl_server* server, uint32_t session, const float* points, size_t N, uint64_t* ticket);
+/* Non-blocking: publishes finished updates, launches queued ones; *completed
+ * (optional) receives the number published by this call. */
+int tsdfl_server_poll(tsdfl_server* server, size_t* completed);
+/* The result of a published ticket (once): mean pose, latency from submission
+ * to publication (host clock) and the update's status (TSDFL_OK, or e.g.
+ * TSDFL_ERR_DEGENERATE).  TSDFL_ERR_INVALID_ARG while not yet published. */
+int tsdfl_server_result(tsdfl_server* server, uint64_t ticket, float pose[6], double* latency_ms, int* status);
+/* The session's current particles (count x 7 host floats). */
+int tsdfl_session_particles(tsdfl_server* server, uint32_t session, float* out, size_t cap, size_t* count);
+/* The systematic draw of a session's k-th update (k from 0) with P particles:
+ * (float)(u / P), u = (splitmix64(seed + k * 0x9E3779B97F4A7C15) >> 11) * 2^-53. */
+float tsdfl_server_draw(uint64_t seed, uint64_t k, size_t P);
+/* Counters since creation: submissions accepted and refused, updates
+ * published, batches launched, and the measured rate (particle*points/s). */
+int tsdfl_server_stats(const tsdfl_server* server, uint64_t* accepted, uint64_t* refused, uint64_t* published,
+                       uint64_t* batches, double* rate);
+
 /* ---- the reference's other resamplers ----
  * WheelResampler (src/resampling/wheel_resampler.cpp:6-33), ResidualResampler
  * (novel_resampling.h:9-35), MetropolisResampler (:106-143) and

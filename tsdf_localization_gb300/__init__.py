@@ -5,10 +5,10 @@ ABI in include/tsdfl.h); this package binds it for tests, benchmarks and Python
 callers.  Build with `python -c "import __graft_entry__ as g; g.build()"`.
 """
 from ._native import TsdflError
-from .evaluator import (Context, DeviceMap, FilterBatch, MetropolisResampler, MotionModel, Pose, RejectionResampler,
+from .evaluator import (Context, DeviceMap, FilterBatch, LocalizationServer, MetropolisResampler, MotionModel, Pose, RejectionResampler,
                         ResidualResampler, ResidualSystematicResampler, ScanReducer, SystematicResampler,
                         TSDFEvaluator, WheelResampler, build_map_codes, code_values, pack_cloud, pose_array)
 
-__all__ = ["Context", "DeviceMap", "FilterBatch", "MetropolisResampler", "MotionModel", "Pose", "RejectionResampler",
+__all__ = ["Context", "DeviceMap", "FilterBatch", "LocalizationServer", "MetropolisResampler", "MotionModel", "Pose", "RejectionResampler",
            "ResidualResampler", "ResidualSystematicResampler", "ScanReducer", "SystematicResampler", "TSDFEvaluator",
            "TsdflError", "WheelResampler", "build_map_codes", "code_values", "pack_cloud", "pose_array"]

@@ -69,6 +69,11 @@ class Filter(C.Structure):
                 ("d_count", C.c_void_p)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_sessions", C.c_size_t), ("max_points", C.c_size_t),
+                ("max_wait_ms", C.c_double), ("max_queue", C.c_uint32)]
+
+
 class EvalDebug(C.Structure):
     _fields_ = [("raw_weights", C.c_void_p), ("hits", C.c_void_p), ("voxel_index", C.c_void_p),
                 ("laser_pose", C.c_void_p), ("weight_sum", C.c_double)]
@@ -128,6 +133,17 @@ SIGNATURES = [
     ("tsdfl_batch_autotune", I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(F)]),
     ("tsdfl_batch_hits", I, [P, SZ, P]),
     ("tsdfl_batch_info", I, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    ("tsdfl_server_create", I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
+    ("tsdfl_server_destroy", I, [P]),
+    ("tsdfl_session_open", I, [P, P, P, SZ, P, C.POINTER(Model), C.c_uint64, C.POINTER(U32)]),
+    ("tsdfl_session_close", I, [P, U32]),
+    ("tsdfl_session_submit", I, [P, U32, P, SZ, C.POINTER(C.c_uint64)]),
+    ("tsdfl_server_poll", I, [P, C.POINTER(SZ)]),
+    ("tsdfl_server_result", I, [P, C.c_uint64, P, C.POINTER(C.c_double), C.POINTER(I)]),
+    ("tsdfl_session_particles", I, [P, U32, P, SZ, C.POINTER(SZ)]),
+    ("tsdfl_server_draw", F, [C.c_uint64, C.c_uint64, SZ]),
+    ("tsdfl_server_stats", I, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                               C.POINTER(C.c_uint64), C.POINTER(C.c_double)]),
     ("tsdfl_pose_array_device", I, [P, P, SZ, P]),
     ("tsdfl_pose_array", I, [P, P, SZ, P]),
     ("tsdfl_motion_model", I, [I, P, P, SZ, F, C.POINTER(Motion)]),

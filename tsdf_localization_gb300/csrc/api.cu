@@ -11,6 +11,9 @@
 #include <new>
 #include <algorithm>
 #include <vector>
+#include <unordered_map>
+#include <deque>
+#include <chrono>
 
 #include "map_host.h"
 #include "tsdfl.h"
@@ -1088,8 +1091,10 @@ struct tsdfl_batch {
         bool tiled = false;
         bool dense = false;
         size_t pass = 0;
+        int32_t* sticky = nullptr;   // where device errors of this filter go (null: the context's status)
     };
     std::vector<Per> per;
+    cudaStream_t stream = nullptr;   // null: the context's stream
     void* ws = nullptr;
     void* d_segs = nullptr;
     std::vector<BatchSegSpec> specs;
@@ -1102,14 +1107,68 @@ struct tsdfl_batch {
 
 namespace {
 
-int batch_build_segments(tsdfl_batch* B)
+int batch_build_segments(tsdfl_batch* B, void* pinned = nullptr)
 {
-    std::vector<char> host(B->specs.size() * batch_seg_bytes() + 1);
-    B->batches = build_batch_segs(B->specs.data(), (int)B->specs.size(), B->chunk, B->group, host.data(), &B->kinds);
-    if (!B->specs.empty())
-        CUDA_TRY(cudaMemcpy(B->d_segs, host.data(), B->specs.size() * batch_seg_bytes(), cudaMemcpyHostToDevice));
+    std::vector<char> host;
+    char* h = static_cast<char*>(pinned);
+    if (!h) {
+        host.resize(B->specs.size() * batch_seg_bytes() + 1);
+        h = host.data();
+    }
+    B->batches = build_batch_segs(B->specs.data(), (int)B->specs.size(), B->chunk, B->group, h, &B->kinds);
+    if (B->specs.empty()) return TSDFL_OK;
+    if (pinned)
+        CUDA_TRY(cudaMemcpyAsync(B->d_segs, h, B->specs.size() * batch_seg_bytes(), cudaMemcpyHostToDevice,
+                                 B->stream));
+    else
+        CUDA_TRY(cudaMemcpy(B->d_segs, h, B->specs.size() * batch_seg_bytes(), cudaMemcpyHostToDevice));
     return TSDFL_OK;
 }
+
+// Per-filter settings that depend on the filter's map and scan size.
+void per_configure(tsdfl_batch::Per& q, const tsdfl_filter& F)
+{
+    q.b.particles = F.d_particles;
+    q.npad = (int)align_up(F.N, 4);
+    double bound = std::fmax((double)F.map->max_value, 1e-30) * (double)(F.N + 1);
+    int need = (int)std::ceil(std::log2(bound));
+    q.shift = 62 - need < 40 ? 62 - need : 40;
+    const MapView& m = F.map->view;
+    q.dense = F.map->dense != nullptr;
+    q.tiled = m.storage == 0 && m.sub_fast != 0;
+    if (q.tiled) {
+        int tp = tiled_pass_points(m, q.dense);
+        if (tp < 1024 && q.dense) {
+            q.dense = false;
+            tp = tiled_pass_points(m, false);
+        }
+        if (tp < 64) q.tiled = false;
+        q.pass = (size_t)(tp > 0 ? tp : kMaxPassPoints);
+    }
+    if (!q.tiled) q.pass = (size_t)kMaxPassPoints;
+}
+
+// The persistent launch's segments of filter i (one per pass).
+void append_specs(tsdfl_batch* B, size_t i)
+{
+    const tsdfl_filter& F = B->f[i];
+    const tsdfl_batch::Per& q = B->per[i];
+    if (!q.tiled || !F.N) return;
+    for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
+        BatchSegSpec sp;
+        sp.m = F.map->view;
+        sp.a_hit = F.model.a_hit;
+        sp.P = (int)F.P;
+        sp.n0 = (int)n0;
+        sp.n1 = (int)(n0 + q.pass < F.N ? n0 + q.pass : F.N);
+        sp.n_total = (int)F.N;
+        sp.dense = q.dense;
+        sp.b = q.b;
+        B->specs.push_back(sp);
+    }
+}
+
+cudaStream_t batch_stream(const tsdfl_batch* B) { return B->stream ? B->stream : B->ctx->stream; }
 
 // Scoring of every filter: the persistent launch, then the filters it does not take.
 int batch_score(tsdfl_batch* B, cudaStream_t s)
@@ -1139,7 +1198,7 @@ int batch_score(tsdfl_batch* B, cudaStream_t s)
 int batch_record(tsdfl_batch* B)
 {
     tsdfl_ctx* c = B->ctx;
-    cudaStream_t s = c->stream;
+    cudaStream_t s = batch_stream(B);
     for (size_t i = 0; i < B->f.size(); ++i) {
         const tsdfl_filter& F = B->f[i];
         tsdfl_batch::Per& q = B->per[i];
@@ -1164,11 +1223,12 @@ int batch_record(tsdfl_batch* B)
         rc = launch_norm((int)F.P, mode, q.shift, (double)F.model.a_hit, (double)c_in, (double)F.model.a_max,
                          (int)F.N, q.sum_f64, F.d_particles, F.d_pose_out, q.b, s);
         if (rc) return rc;
-        rc = launch_fold_status(q.b.status, c->status, s);
+        int32_t* sticky = q.sticky ? q.sticky : c->status;
+        rc = launch_fold_status(q.b.status, sticky, s);
         if (rc) return rc;
         if (F.d_u0 && F.d_resampled && F.P)
             rc = launch_resample_impl(F.d_particles, F.d_particles + 6, 7, F.P, 0.0f, F.d_resampled, nullptr,
-                                      F.resample_cap, F.d_count, q.rs_ws, c->status, s, F.d_u0);
+                                      F.resample_cap, F.d_count, q.rs_ws, sticky, s, F.d_u0);
         if (rc) return rc;
     }
     return TSDFL_OK;
@@ -1237,39 +1297,9 @@ int tsdfl_batch_create(tsdfl_ctx* c, const tsdfl_filter* filters, size_t n, uint
         tsdfl_filter& F = B->f[i];
         tsdfl_batch::Per& q = B->per[i];
         eval_layout(F.P, F.N, base + eval_off[i], &q.b, &q.sum_f64);
-        q.b.particles = F.d_particles;
         q.rs_ws = base + rs_off[i];
-        q.npad = (int)align_up(F.N, 4);
-        double bound = std::fmax((double)F.map->max_value, 1e-30) * (double)(F.N + 1);
-        int need = (int)std::ceil(std::log2(bound));
-        q.shift = 62 - need < 40 ? 62 - need : 40;
-        const MapView& m = F.map->view;
-        q.dense = F.map->dense != nullptr;
-        q.tiled = m.storage == 0 && m.sub_fast != 0;
-        if (q.tiled) {
-            int tp = tiled_pass_points(m, q.dense);
-            if (tp < 1024 && q.dense) {
-                q.dense = false;
-                tp = tiled_pass_points(m, false);
-            }
-            if (tp < 64) q.tiled = false;
-            q.pass = (size_t)(tp > 0 ? tp : kMaxPassPoints);
-        }
-        if (!q.tiled) q.pass = (size_t)kMaxPassPoints;
-        if (q.tiled && F.N) {
-            for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
-                BatchSegSpec sp;
-                sp.m = m;
-                sp.a_hit = F.model.a_hit;
-                sp.P = (int)F.P;
-                sp.n0 = (int)n0;
-                sp.n1 = (int)(n0 + q.pass < F.N ? n0 + q.pass : F.N);
-                sp.n_total = (int)F.N;
-                sp.dense = q.dense;
-                sp.b = q.b;
-                B->specs.push_back(sp);
-            }
-        }
+        per_configure(q, F);
+        append_specs(B, i);
     }
     if (B->specs.size() > 2 * n + 1) {   // more passes than the segment buffer holds: grow it
         cudaFree(B->d_segs);
@@ -1442,6 +1472,452 @@ int tsdfl_batch_info(const tsdfl_batch* B, uint32_t* segments, uint32_t* batches
         for (size_t i = 0; i < B->f.size(); ++i) o += (!B->per[i].tiled && B->f[i].N) ? 1u : 0u;
         *outside = o;
     }
+    return TSDFL_OK;
+}
+
+// ------------------------------------------------ served sessions
+
+struct tsdfl_server {
+    tsdfl_ctx* ctx = nullptr;
+    tsdfl_server_config cfg{};
+    size_t used = 0;
+    struct Request {
+        uint32_t session;
+        uint64_t ticket;
+        std::vector<float> points;
+        std::chrono::steady_clock::time_point t_submit;
+        uint64_t pp;
+    };
+    struct Session {
+        bool open = false;
+        const tsdfl_map* map = nullptr;
+        tsdfl_model model{};
+        float tf[16];
+        uint64_t seed = 0, step = 0;
+        size_t P = 0, cap = 0;
+        void* mem = nullptr;
+        size_t bytes = 0;
+        float* parts[2] = {nullptr, nullptr};
+        int cur = 0;
+        tsdfl_batch::Per per;
+        bool busy = false;
+        std::deque<Request> queue;
+    };
+    struct Result {
+        float pose[6];
+        double latency_ms;
+        int status;
+    };
+    struct Slot {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        tsdfl_batch batch;
+        std::vector<Request> reqs;
+        void* d_mem = nullptr;    // points, draws, poses, counts, statuses
+        float* d_points = nullptr;
+        float* d_u0 = nullptr;
+        float* d_pose = nullptr;
+        uint32_t* d_count = nullptr;
+        int32_t* d_status = nullptr;
+        void* h_mem = nullptr;    // pinned mirror
+        float* h_points = nullptr;
+        float* h_u0 = nullptr;
+        float* h_pose = nullptr;
+        uint32_t* h_count = nullptr;
+        int32_t* h_status = nullptr;
+        void* h_segs = nullptr;   // pinned segment records
+        size_t seg_cap = 0;
+        bool busy = false;
+        std::chrono::steady_clock::time_point t_launch;
+        uint64_t pp = 0;
+    };
+    std::vector<Session> sessions;
+    Slot slots[2];
+    std::unordered_map<uint64_t, Result> results;
+    uint64_t next_ticket = 1;
+    uint64_t queued_pp = 0, inflight_pp = 0;
+    double rate = 2.0e11;   // particle*points per second, refined from finished batches
+    uint64_t accepted = 0, refused = 0, published = 0, launched = 0;
+};
+
+namespace {
+
+uint64_t splitmix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+size_t session_bytes(size_t cap, size_t max_points)
+{
+    return align_up(2 * sizeof(float) * 7 * cap, 256) + align_up(eval_layout(cap, max_points, nullptr, nullptr, nullptr), 256) +
+           align_up(resample_workspace_bytes(cap), 256) + 256;
+}
+
+// Launches every queued update of an idle session as one batch on slot k.
+int server_dispatch(tsdfl_server* S, int k)
+{
+    tsdfl_server::Slot& sl = S->slots[k];
+    sl.reqs.clear();
+    for (size_t i = 0; i < S->sessions.size() && sl.reqs.size() < S->cfg.max_sessions; ++i) {
+        tsdfl_server::Session& se = S->sessions[i];
+        if (!se.open || se.busy || se.queue.empty()) continue;
+        sl.reqs.push_back(std::move(se.queue.front()));
+        se.queue.pop_front();
+        se.busy = true;
+    }
+    if (sl.reqs.empty()) return TSDFL_OK;
+    tsdfl_batch& B = sl.batch;
+    B.f.clear();
+    B.per.clear();
+    B.specs.clear();
+    const size_t n = sl.reqs.size();
+    sl.pp = 0;
+    for (size_t r = 0; r < n; ++r) {
+        const tsdfl_server::Request& q = sl.reqs[r];
+        tsdfl_server::Session& se = S->sessions[q.session];
+        const size_t N = q.points.size() / 3;
+        std::memcpy(sl.h_points + 3 * S->cfg.max_points * r, q.points.data(), sizeof(float) * 3 * N);
+        sl.h_u0[r] = tsdfl_server_draw(se.seed, se.step, se.P);
+        tsdfl_filter F{};
+        F.map = se.map;
+        F.model = se.model;
+        std::memcpy(F.tf, se.tf, sizeof(F.tf));
+        F.d_particles = se.parts[se.cur];
+        F.P = se.P;
+        F.d_points = sl.d_points + 3 * S->cfg.max_points * r;
+        F.N = N;
+        F.d_pose_out = sl.d_pose + 8 * r;
+        F.d_u0 = sl.d_u0 + r;
+        F.d_resampled = se.parts[se.cur ^ 1];
+        F.resample_cap = se.cap;
+        F.d_count = sl.d_count + r;
+        B.f.push_back(F);
+        tsdfl_batch::Per pq = se.per;
+        per_configure(pq, F);
+        pq.sticky = sl.d_status + r;
+        B.per.push_back(pq);
+        append_specs(&B, r);
+        sl.pp += (uint64_t)se.P * N;
+    }
+    if (B.specs.size() > sl.seg_cap) {   // more passes than the slot's tables hold
+        set_error("tsdfl_server_poll: too many scan passes in one batch");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    cudaStream_t s = sl.stream;
+    CUDA_TRY(cudaMemsetAsync(sl.d_status, 0, sizeof(int32_t) * n, s));
+    for (size_t r = 0; r < n; ++r)   // the scans sit at max_points strides
+        CUDA_TRY(cudaMemcpyAsync(sl.d_points + 3 * S->cfg.max_points * r, sl.h_points + 3 * S->cfg.max_points * r,
+                                 sizeof(float) * B.f[r].N * 3, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(sl.d_u0, sl.h_u0, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    int rc = batch_build_segments(&B, sl.h_segs);
+    if (rc) return rc;
+    rc = batch_record(&B);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(sl.h_pose, sl.d_pose, sizeof(float) * 8 * n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(sl.h_count, sl.d_count, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(sl.h_status, sl.d_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaEventRecord(sl.done, s));
+    sl.busy = true;
+    sl.t_launch = std::chrono::steady_clock::now();
+    S->queued_pp -= sl.pp;
+    S->inflight_pp += sl.pp;
+    S->launched += 1;
+    return TSDFL_OK;
+}
+
+// Publishes the updates of slot k once its batch is done; false while it runs.
+bool server_collect(tsdfl_server* S, int k, size_t* completed)
+{
+    tsdfl_server::Slot& sl = S->slots[k];
+    if (!sl.busy || cudaEventQuery(sl.done) != cudaSuccess) return false;
+    const auto now = std::chrono::steady_clock::now();
+    for (size_t r = 0; r < sl.reqs.size(); ++r) {
+        const tsdfl_server::Request& q = sl.reqs[r];
+        tsdfl_server::Session& se = S->sessions[q.session];
+        tsdfl_server::Result res;
+        std::memcpy(res.pose, sl.h_pose + 8 * r, sizeof(res.pose));
+        res.status = sl.h_status[r];
+        res.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_submit).count();
+        const uint32_t cnt = sl.h_count[r];
+        if (res.status == TSDFL_OK || res.status == TSDFL_ERR_CAPACITY) {
+            se.P = cnt < se.cap ? cnt : se.cap;
+            se.cur ^= 1;
+        }
+        se.step += 1;
+        se.busy = false;
+        S->results[q.ticket] = res;
+        S->published += 1;
+        if (completed) *completed += 1;
+    }
+    const double secs = std::chrono::duration<double>(now - sl.t_launch).count();
+    if (secs > 0 && sl.pp > 0) S->rate = 0.8 * S->rate + 0.2 * ((double)sl.pp / secs);
+    S->inflight_pp -= sl.pp;
+    sl.busy = false;
+    sl.reqs.clear();
+    return true;
+}
+
+}  // namespace
+
+float tsdfl_server_draw(uint64_t seed, uint64_t k, size_t P)
+{
+    const double u = (double)(splitmix64(seed + k * 0x9E3779B97F4A7C15ull) >> 11) * 0x1.0p-53;
+    return (float)(u / (double)(P ? P : 1));
+}
+
+int tsdfl_server_create(tsdfl_ctx* c, const tsdfl_server_config* cfg, tsdfl_server** out)
+{
+    if (!c || !cfg || !out || cfg->max_sessions == 0 || cfg->max_points == 0) {
+        set_error("tsdfl_server_create: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int rc = set_device(c->device);
+    if (rc) return rc;
+    auto* S = new (std::nothrow) tsdfl_server;
+    if (!S) return TSDFL_ERR_OUT_OF_MEMORY;
+    S->ctx = c;
+    S->cfg = *cfg;
+    if (S->cfg.max_queue == 0) S->cfg.max_queue = 4;
+    const size_t ns = cfg->max_sessions, np = cfg->max_points;
+    for (auto& sl : S->slots) {
+        sl.seg_cap = 4 * ns + 8;
+        const size_t pts_b = align_up(sizeof(float) * 3 * np * ns, 256);
+        const size_t u0_b = align_up(sizeof(float) * ns, 256), pose_b = align_up(sizeof(float) * 8 * ns, 256);
+        const size_t cnt_b = align_up(sizeof(uint32_t) * ns, 256), st_b = align_up(sizeof(int32_t) * ns, 256);
+        const size_t total = pts_b + u0_b + pose_b + cnt_b + st_b;
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.d_mem, total);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_mem, total);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.batch.d_segs, sl.seg_cap * batch_seg_bytes());
+        if (e == cudaSuccess) e = cudaMallocHost(&sl.h_segs, sl.seg_cap * batch_seg_bytes());
+        if (e == cudaSuccess) e = cudaMalloc(&sl.batch.d_counter, 256);
+        if (e != cudaSuccess) {
+            set_error("tsdfl_server_create: %s", cudaGetErrorString(e));
+            tsdfl_server_destroy(S);
+            return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
+        }
+        char* d = static_cast<char*>(sl.d_mem);
+        char* h = static_cast<char*>(sl.h_mem);
+        sl.d_points = reinterpret_cast<float*>(d);
+        sl.h_points = reinterpret_cast<float*>(h);
+        sl.d_u0 = reinterpret_cast<float*>(d + pts_b);
+        sl.h_u0 = reinterpret_cast<float*>(h + pts_b);
+        sl.d_pose = reinterpret_cast<float*>(d + pts_b + u0_b);
+        sl.h_pose = reinterpret_cast<float*>(h + pts_b + u0_b);
+        sl.d_count = reinterpret_cast<uint32_t*>(d + pts_b + u0_b + pose_b);
+        sl.h_count = reinterpret_cast<uint32_t*>(h + pts_b + u0_b + pose_b);
+        sl.d_status = reinterpret_cast<int32_t*>(d + pts_b + u0_b + pose_b + cnt_b);
+        sl.h_status = reinterpret_cast<int32_t*>(h + pts_b + u0_b + pose_b + cnt_b);
+        sl.batch.ctx = c;
+        sl.batch.stream = sl.stream;
+        S->used += total + 2 * sl.seg_cap * batch_seg_bytes();
+    }
+    if (S->used > cfg->hbm_budget) {
+        set_error("tsdfl_server_create: the dispatch buffers alone exceed the budget");
+        tsdfl_server_destroy(S);
+        return TSDFL_ERR_OUT_OF_MEMORY;
+    }
+    *out = S;
+    return TSDFL_OK;
+}
+
+int tsdfl_server_destroy(tsdfl_server* S)
+{
+    if (!S) return TSDFL_OK;
+    cudaSetDevice(S->ctx->device);
+    for (auto& sl : S->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.done) cudaEventDestroy(sl.done);
+        cudaFree(sl.d_mem);
+        cudaFreeHost(sl.h_mem);
+        cudaFree(sl.batch.d_segs);
+        cudaFreeHost(sl.h_segs);
+        cudaFree(sl.batch.d_counter);
+        sl.batch.d_segs = nullptr;
+        sl.batch.d_counter = nullptr;
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (auto& se : S->sessions) cudaFree(se.mem);
+    delete S;
+    return TSDFL_OK;
+}
+
+int tsdfl_session_open(tsdfl_server* S, const tsdfl_map* map, const float* particles, size_t P, const float tf[16],
+                       const tsdfl_model* model, uint64_t seed, uint32_t* session)
+{
+    if (!S || !map || !tf || !session || (P && !particles) || P == 0) {
+        set_error("tsdfl_session_open: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(model);
+    if (rc) return rc;
+    if (P >= (1ull << 23)) {
+        set_error("tsdfl_session_open: too many particles");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    size_t open = 0;
+    for (auto& se : S->sessions) open += se.open ? 1 : 0;
+    if (open >= S->cfg.max_sessions) {
+        set_error("tsdfl_session_open: the server holds max_sessions sessions");
+        return TSDFL_ERR_CAPACITY;
+    }
+    const size_t cap = 2 * P + 16;
+    const size_t bytes = session_bytes(cap, S->cfg.max_points);
+    if (S->used + bytes > S->cfg.hbm_budget) {
+        set_error("tsdfl_session_open: the device memory budget cannot hold the session");
+        return TSDFL_ERR_OUT_OF_MEMORY;
+    }
+    rc = set_device(S->ctx->device);
+    if (rc) return rc;
+    void* mem = nullptr;
+    CUDA_TRY(cudaMalloc(&mem, bytes));
+    tsdfl_server::Session se;
+    se.open = true;
+    se.map = map;
+    se.model = *model;
+    std::memcpy(se.tf, tf, sizeof(se.tf));
+    se.seed = seed;
+    se.P = P;
+    se.cap = cap;
+    se.mem = mem;
+    se.bytes = bytes;
+    char* b = static_cast<char*>(mem);
+    se.parts[0] = reinterpret_cast<float*>(b);
+    se.parts[1] = reinterpret_cast<float*>(b + sizeof(float) * 7 * cap);
+    char* ev = b + align_up(2 * sizeof(float) * 7 * cap, 256);
+    const size_t ev_b = align_up(eval_layout(cap, S->cfg.max_points, nullptr, nullptr, nullptr), 256);
+    eval_layout(cap, S->cfg.max_points, ev, &se.per.b, &se.per.sum_f64);
+    se.per.rs_ws = ev + ev_b;
+    CUDA_TRY(cudaMemcpy(se.parts[0], particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice));
+    S->used += bytes;
+    uint32_t id = (uint32_t)S->sessions.size();
+    for (uint32_t i = 0; i < S->sessions.size(); ++i)
+        if (!S->sessions[i].open && !S->sessions[i].busy) {
+            id = i;
+            break;
+        }
+    if (id == S->sessions.size()) S->sessions.push_back(std::move(se));
+    else S->sessions[id] = std::move(se);
+    *session = id;
+    return TSDFL_OK;
+}
+
+int tsdfl_session_close(tsdfl_server* S, uint32_t id)
+{
+    if (!S || id >= S->sessions.size() || !S->sessions[id].open) {
+        set_error("tsdfl_session_close: invalid session");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    tsdfl_server::Session& se = S->sessions[id];
+    if (se.busy) {   // its batch must finish before the memory goes
+        for (auto& sl : S->slots)
+            if (sl.busy) CUDA_TRY(cudaStreamSynchronize(sl.stream));
+        size_t done = 0;
+        for (int k = 0; k < 2; ++k) server_collect(S, k, &done);
+    }
+    for (auto& q : se.queue) S->queued_pp -= q.pp;
+    se.queue.clear();
+    cudaFree(se.mem);
+    S->used -= se.bytes;
+    se.mem = nullptr;
+    se.open = false;
+    return TSDFL_OK;
+}
+
+int tsdfl_session_submit(tsdfl_server* S, uint32_t id, const float* points, size_t N, uint64_t* ticket)
+{
+    if (!S || id >= S->sessions.size() || !S->sessions[id].open || (N && !points) || !ticket) {
+        set_error("tsdfl_session_submit: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    tsdfl_server::Session& se = S->sessions[id];
+    if (N > S->cfg.max_points) {
+        set_error("tsdfl_session_submit: more than max_points points");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    const uint64_t pp = (uint64_t)se.P * N;
+    const double wait_ms = 1e3 * (double)(S->queued_pp + S->inflight_pp + pp) / S->rate;
+    if (se.queue.size() >= S->cfg.max_queue || (S->cfg.max_wait_ms > 0 && wait_ms > S->cfg.max_wait_ms)) {
+        S->refused += 1;
+        set_error("tsdfl_session_submit: refused (session queue full or the server over its admission bound)");
+        return TSDFL_ERR_CAPACITY;
+    }
+    tsdfl_server::Request q;
+    q.session = id;
+    q.ticket = S->next_ticket++;
+    q.points.assign(points, points + 3 * N);
+    q.t_submit = std::chrono::steady_clock::now();
+    q.pp = pp;
+    se.queue.push_back(std::move(q));
+    S->queued_pp += pp;
+    S->accepted += 1;
+    *ticket = S->next_ticket - 1;
+    return TSDFL_OK;
+}
+
+int tsdfl_server_poll(tsdfl_server* S, size_t* completed)
+{
+    if (!S) return TSDFL_ERR_INVALID_ARG;
+    if (completed) *completed = 0;
+    int rc = set_device(S->ctx->device);
+    if (rc) return rc;
+    for (int k = 0; k < 2; ++k) server_collect(S, k, completed);
+    for (int k = 0; k < 2; ++k) {
+        if (S->slots[k].busy) continue;
+        rc = server_dispatch(S, k);
+        if (rc) return rc;
+    }
+    return TSDFL_OK;
+}
+
+int tsdfl_server_result(tsdfl_server* S, uint64_t ticket, float pose[6], double* latency_ms, int* status)
+{
+    if (!S) return TSDFL_ERR_INVALID_ARG;
+    auto it = S->results.find(ticket);
+    if (it == S->results.end()) {
+        set_error("tsdfl_server_result: ticket not published");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (pose) std::memcpy(pose, it->second.pose, sizeof(float) * 6);
+    if (latency_ms) *latency_ms = it->second.latency_ms;
+    if (status) *status = it->second.status;
+    S->results.erase(it);
+    return TSDFL_OK;
+}
+
+int tsdfl_session_particles(tsdfl_server* S, uint32_t id, float* out, size_t cap, size_t* count)
+{
+    if (!S || id >= S->sessions.size() || !S->sessions[id].open || !count) {
+        set_error("tsdfl_session_particles: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    tsdfl_server::Session& se = S->sessions[id];
+    *count = se.P;
+    if (se.busy) {
+        set_error("tsdfl_session_particles: an update of the session is on the device");
+        return TSDFL_ERR_CAPACITY;
+    }
+    int rc = set_device(S->ctx->device);
+    if (rc) return rc;
+    const size_t m = se.P < cap ? se.P : cap;
+    if (m) CUDA_TRY(cudaMemcpy(out, se.parts[se.cur], sizeof(float) * 7 * m, cudaMemcpyDeviceToHost));
+    return TSDFL_OK;
+}
+
+int tsdfl_server_stats(const tsdfl_server* S, uint64_t* accepted, uint64_t* refused, uint64_t* published,
+                       uint64_t* batches, double* rate)
+{
+    if (!S) return TSDFL_ERR_INVALID_ARG;
+    if (accepted) *accepted = S->accepted;
+    if (refused) *refused = S->refused;
+    if (published) *published = S->published;
+    if (batches) *batches = S->launched;
+    if (rate) *rate = S->rate;
     return TSDFL_OK;
 }
 

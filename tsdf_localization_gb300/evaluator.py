@@ -488,6 +488,89 @@ class FilterBatch:
             pass
 
 
+class LocalizationServer:
+    """Served sessions (tsdfl_server): particles, map and draws of every
+    session resident on the device; submissions queued and launched in
+    continuous batches by poll()."""
+
+    def __init__(self, ctx: Context, hbm_budget: int, max_sessions: int, max_points: int, max_wait_ms: float = 0.0,
+                 max_queue: int = 4):
+        self.ctx = ctx
+        cfg = N.ServerConfig(int(hbm_budget), int(max_sessions), int(max_points), float(max_wait_ms), int(max_queue))
+        h = C.c_void_p()
+        N.check(N.lib().tsdfl_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self._maps = []
+
+    def open(self, device_map, particles: np.ndarray, tf, model=(0.9, 0.1, 0.0, 100.0), seed: int = 0) -> int:
+        p = _f32(particles, 7)
+        t = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(16))
+        sid = C.c_uint32()
+        m = N.Model(*model)
+        N.check(N.lib().tsdfl_session_open(self.handle, device_map.handle, _ptr(p), p.shape[0], _ptr(t), C.byref(m),
+                                           int(seed), C.byref(sid)))
+        self._maps.append(device_map)
+        return sid.value
+
+    def close_session(self, sid: int) -> None:
+        N.check(N.lib().tsdfl_session_close(self.handle, sid))
+
+    def submit(self, sid: int, points: np.ndarray):
+        """The ticket, or None when the submission is refused."""
+        pts = _f32(points, 3)
+        t = C.c_uint64()
+        rc = N.lib().tsdfl_session_submit(self.handle, sid, _ptr(pts), pts.shape[0], C.byref(t))
+        if rc == N.TSDFL_ERR_CAPACITY:
+            return None
+        N.check(rc)
+        return t.value
+
+    def poll(self) -> int:
+        n = C.c_size_t()
+        N.check(N.lib().tsdfl_server_poll(self.handle, C.byref(n)))
+        return n.value
+
+    def result(self, ticket: int):
+        """(pose (6,), latency ms, status), or None while not published."""
+        pose = np.zeros(6, np.float32)
+        lat = C.c_double()
+        st = C.c_int()
+        rc = N.lib().tsdfl_server_result(self.handle, ticket, _ptr(pose), C.byref(lat), C.byref(st))
+        if rc != N.TSDFL_OK:
+            return None
+        return pose, lat.value, st.value
+
+    def particles(self, sid: int) -> np.ndarray:
+        cnt = C.c_size_t()
+        N.lib().tsdfl_session_particles(self.handle, sid, None, 0, C.byref(cnt))
+        out = np.zeros((max(cnt.value, 1), 7), np.float32)
+        N.check(N.lib().tsdfl_session_particles(self.handle, sid, _ptr(out), out.shape[0], C.byref(cnt)))
+        return out[:cnt.value]
+
+    def stats(self) -> dict:
+        a, r, p, b = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        rate = C.c_double()
+        N.check(N.lib().tsdfl_server_stats(self.handle, C.byref(a), C.byref(r), C.byref(p), C.byref(b),
+                                           C.byref(rate)))
+        return {"accepted": a.value, "refused": r.value, "published": p.value, "batches": b.value,
+                "rate": rate.value}
+
+    @staticmethod
+    def draw(seed: int, k: int, P: int) -> float:
+        return float(N.lib().tsdfl_server_draw(int(seed), int(k), int(P)))
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            N.lib().tsdfl_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def pose_array(ctx: Context, particles: np.ndarray) -> np.ndarray:
     """mcl_3d.cpp:429-449: the particles as geometry_msgs::Pose records, (P, 7)
     doubles: position, then the setRPY quaternion x, y, z, w."""
