@@ -40,7 +40,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="building", choices=["building", "room", "global", "batch"])
+    ap.add_argument("--workload", default="building", choices=["building", "room", "global", "batch", "served"])
+    ap.add_argument("--sessions", type=int, default=256, help="robots of the served workload")
+    ap.add_argument("--seconds", type=float, default=3.0, help="arrival window of the served workload")
+    ap.add_argument("--max-wait-ms", type=float, default=4.0, help="admission bound of the served workload")
     ap.add_argument("--filters", type=int, default=64, help="filters of the batch workload")
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
@@ -299,6 +302,154 @@ def batch_workload(n_filters: int, seed: int = 11):
     return worlds, filters
 
 
+def plain_rate(ctx, stream, dev: str, flush) -> float:
+    """The plain single-filter rate (particle*points/s) of one update plus
+    systematic resampling at 100k particles x 8,192 points on the building map,
+    L2 flushed before each of 5 timed repetitions (median)."""
+    import torch
+
+    from tsdf_localization_gb300 import DeviceMap
+    from tsdf_localization_gb300 import _native as N
+    from tsdf_localization_gb300 import synth
+    lib = N.lib()
+    wlp = synth.building_workload(seed=2, n_particles=100_000, n_points=8192)
+    dmp = DeviceMap(ctx, wlp.coef, wlp.grid_occ, codes=wlp.codes, dense=True)
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    tfp = np.ascontiguousarray(wlp.tf, np.float32)
+    dp = torch.from_numpy(wlp.particles).to(dev)
+    dq = torch.from_numpy(wlp.points).to(dev)
+    dpo = torch.zeros(8, dtype=torch.float32, device=dev)
+    dro = torch.zeros((200_016, 7), dtype=torch.float32, device=dev)
+    dcn = torch.zeros(4, dtype=torch.int32, device=dev)
+    vp = C.c_void_p
+    torch.cuda.synchronize()
+    pt = []
+    with torch.cuda.stream(stream):
+        for i in range(8):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            N.check(lib.tsdfl_evaluate_device(ctx.handle, dmp.handle, C.byref(model), vp(dp.data_ptr()), 100_000,
+                                              vp(dq.data_ptr()), 8192, tfp.ctypes.data_as(vp), 0,
+                                              vp(dpo.data_ptr())))
+            N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(dp.data_ptr()), 100_000,
+                                                         float(np.float32(0.37 / 100_000)), vp(dro.data_ptr()),
+                                                         200_016, vp(dcn.data_ptr())))
+            e1.record(stream)
+            e1.synchronize()
+            if i >= 3:
+                pt.append(e0.elapsed_time(e1))
+        ctx.sync()
+    return 100_000 * 8192 / (float(np.median(pt)) / 1000.0)
+
+
+def run_served(args, rank: int, world: int, local: int) -> None:
+    """Served localization: robots over the four maps submit scans as Poisson
+    arrivals (10-20 Hz each) to the native request loop for a fixed window;
+    particle counts log-uniform in [5k, 500k] (2 % of the robots at 1M), scans
+    uniform in [2k, 16k] points.  Reports the served aggregate rate, p50/p99
+    latency of the published updates (submission to publication, host clock),
+    and what admission refused."""
+    import torch
+
+    from tsdf_localization_gb300 import Context, DeviceMap, LocalizationServer
+    from tsdf_localization_gb300 import synth
+    dev = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    worlds, _ = batch_workload(1)
+    ctx = Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    maps = [DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True) for wl in worlds]
+    rng = np.random.default_rng(17 + rank)
+    srv = LocalizationServer(ctx, hbm_budget=150 << 30, max_sessions=args.sessions, max_points=16000,
+                             max_wait_ms=args.max_wait_ms, max_queue=2)
+    robots = []
+    refused_open = 0
+    for i in range(args.sessions):
+        mi = i % 4
+        wl = worlds[mi]
+        P = 1_000_000 if rng.random() < 0.02 else int(round(np.exp(rng.uniform(np.log(5000), np.log(500_000)))))
+        Nn = min(int(rng.integers(2000, 16001)), wl.points.shape[0])
+        parts = synth.particles_gaussian(wl.true_pose, 0.3, float(np.deg2rad(5.0)), P, 7000 + i)
+        try:
+            sid = srv.open(maps[mi], parts, wl.tf, seed=9000 + i)
+        except Exception:
+            refused_open += 1
+            continue
+        start = int(rng.integers(0, wl.points.shape[0] - Nn + 1))
+        robots.append({"sid": sid, "P": P, "N": Nn, "hz": float(rng.uniform(10, 20)),
+                       "pts": np.ascontiguousarray(wl.points[start:start + Nn]), "next": 0.0})
+    for r in robots:
+        r["next"] = float(rng.exponential(1.0 / r["hz"]))
+    # warm-up: one update per robot, not timed
+    warm = [srv.submit(r["sid"], r["pts"]) for r in robots]
+    pending = {t for t in warm if t is not None}
+    while pending:
+        srv.poll()
+        for t in list(pending):
+            if srv.result(t) is not None:
+                pending.discard(t)
+    base = srv.stats()
+    offered_pp = served_pp = 0
+    lat = []
+    tickets = {}
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        while True:
+            now = time.perf_counter() - t0
+            if now >= args.seconds:
+                break
+            for r in robots:
+                while r["next"] <= now:
+                    offered_pp += r["P"] * r["N"]
+                    t = srv.submit(r["sid"], r["pts"])
+                    if t is not None:
+                        tickets[t] = r["P"] * r["N"]
+                    r["next"] += float(rng.exponential(1.0 / r["hz"]))
+            srv.poll()
+            for t in list(tickets):
+                res = srv.result(t)
+                if res is not None:
+                    lat.append(res[1])
+                    served_pp += tickets.pop(t)
+        window = time.perf_counter() - t0
+        clocks = clk.summary()
+    # drain what was admitted in the window (its latency counts, its work does not extend the window)
+    t_drain = time.perf_counter()
+    while tickets and time.perf_counter() - t_drain < 60:
+        srv.poll()
+        for t in list(tickets):
+            res = srv.result(t)
+            if res is not None:
+                lat.append(res[1])
+                tickets.pop(t)
+    st = srv.stats()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    plain = plain_rate(ctx, stream, dev, flush)
+    value = served_pp / window
+    if rank == 0:
+        Pv = np.array([r["P"] for r in robots])
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": int(len(lat)),
+               "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": f"{args.sessions} served robots over room/building/warehouse/tunnel maps",
+                          "sessions_open": len(robots), "sessions_refused": refused_open,
+                          "particles_range": [int(Pv.min()), int(Pv.max())], "bursts_1M": int((Pv >= 1_000_000).sum()),
+                          "arrivals": "Poisson 10-20 Hz per robot", "window_s": window,
+                          "hbm_budget_gb": 150, "max_wait_ms": args.max_wait_ms, "form": "served: native request loop, "
+                          "continuous batching over two dispatch slots", "parallelism": f"replicas x{world}"},
+               "served": {"offered_pp_per_s": offered_pp / window, "served_pp_per_s": value,
+                          "submitted": st["accepted"] - base["accepted"] + st["refused"] - base["refused"],
+                          "refused": st["refused"] - base["refused"], "published": len(lat),
+                          "batches": st["batches"] - base["batches"]},
+               "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
+                              "p99": float(np.percentile(lat, 99)) if lat else None},
+               "vs_plain": value / plain, "plain_value": plain,
+               "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clocks}
+        print(json.dumps(out), flush=True)
+
+
 def run_batch(args, rank: int, world: int, local: int) -> None:
     """Batched uneven filters: one update of every filter per step (graph
     replay of prepare, the persistent scoring launch, normalise, resample),
@@ -373,37 +524,7 @@ def run_batch(args, rank: int, world: int, local: int) -> None:
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = max_over_ranks(float(np.sum(step_ms)), device=dev)
     value = total_pp * args.steps * world / (total_ms / 1000.0)
-    # the plain single-filter rate on the building map at 100k x 8,192 for the ratio
-    from tsdf_localization_gb300 import synth
-    wlp = synth.building_workload(seed=2, n_particles=100_000, n_points=8192)
-    dmp = DeviceMap(ctx, wlp.coef, wlp.grid_occ, codes=wlp.codes, dense=True)
-    model = N.Model(0.9, 0.1, 0.0, 100.0)
-    tfp = np.ascontiguousarray(wlp.tf, np.float32)
-    dp = torch.from_numpy(wlp.particles).to(dev)
-    dq = torch.from_numpy(wlp.points).to(dev)
-    dpo = torch.zeros(8, dtype=torch.float32, device=dev)
-    dro = torch.zeros((200_016, 7), dtype=torch.float32, device=dev)
-    dcn = torch.zeros(4, dtype=torch.int32, device=dev)
-    vp = C.c_void_p
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        pt = []
-        for i in range(8):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            N.check(lib.tsdfl_evaluate_device(ctx.handle, dmp.handle, C.byref(model), vp(dp.data_ptr()), 100_000,
-                                              vp(dq.data_ptr()), 8192, tfp.ctypes.data_as(vp), 0,
-                                              vp(dpo.data_ptr())))
-            N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(dp.data_ptr()), 100_000,
-                                                         float(np.float32(0.37 / 100_000)), vp(dro.data_ptr()),
-                                                         200_016, vp(dcn.data_ptr())))
-            e1.record(stream)
-            e1.synchronize()
-            if i >= 3:
-                pt.append(e0.elapsed_time(e1))
-        ctx.sync()
-    plain = 100_000 * 8192 / (float(np.median(pt)) / 1000.0)
+    plain = plain_rate(ctx, stream, dev, flush)
     peak, peak_src = measured_peaks()
     alg = 2.0 * total_pp + sum(56.0 * f["P"] + 12.0 * f["N"] for f in fs)
     achieved = alg / (score_ms / 1000.0) / 1e9
@@ -495,8 +616,8 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    if args.workload == "batch":
-        run_batch(args, rank, world, local)
+    if args.workload in ("batch", "served"):
+        (run_batch if args.workload == "batch" else run_served)(args, rank, world, local)
         if world > 1:
             dist.destroy_process_group()
         return
