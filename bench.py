@@ -240,6 +240,67 @@ def scan_reduction_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps:
     return res
 
 
+def tracking_side(lib, ctx, stream, wl, dmap, device: str, updates: int) -> dict:
+    """Consecutive filter steps on the device -- motion update (ParticleCloud's
+    lin_scale/ang_scale overload, 1 m/s and 0.5 rad/s scales over 0.1 s), sensor
+    update, systematic resampling into the other particle buffer -- for a robot
+    at rest at the workload's true pose; the mean pose's and the best
+    particle's errors against the true pose after every update."""
+    import torch
+
+    from tsdf_localization_gb300 import MotionModel
+    from tsdf_localization_gb300 import _native as N
+    vp = C.c_void_p
+    P0 = int(wl.particles.shape[0])
+    cap = 2 * P0 + 16
+    bufs = [torch.zeros((cap, 7), dtype=torch.float32, device=device) for _ in range(2)]
+    bufs[0][:P0].copy_(torch.from_numpy(wl.particles))
+    d_pose = torch.zeros(8, dtype=torch.float32, device=device)
+    d_cnt = torch.zeros(4, dtype=torch.int32, device=device)
+    d_best = torch.zeros(4, dtype=torch.int32, device=device)
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    tf = np.ascontiguousarray(wl.tf, np.float32)
+    mm = MotionModel(ctx, seed=77)
+    motion = mm.distributions("scale", [1.0, 0.5], 0.1)
+    Npts = int(wl.points.shape[0])
+    d_pts = torch.from_numpy(wl.points).to(device)
+    rng = np.random.default_rng(99)
+    ctx.reserve(cap, Npts)
+    true = np.asarray(wl.true_pose, np.float64)
+    P, cur = P0, 0
+    mean_err, best_err, yaw_err = [], [], []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(updates):
+            d = bufs[cur]
+            N.check(lib.tsdfl_motion_update_device(ctx.handle, vp(d.data_ptr()), P, C.byref(motion), 77, k, None))
+            N.check(lib.tsdfl_evaluate_device(ctx.handle, dmap.handle, C.byref(model), vp(d.data_ptr()), P,
+                                              vp(d_pts.data_ptr()), Npts, tf.ctypes.data_as(vp), 0,
+                                              vp(d_pose.data_ptr())))
+            N.check(lib.tsdfl_best_particle_device(ctx.handle, vp(d.data_ptr()), P, vp(d_best.data_ptr())))
+            N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(d.data_ptr()), P,
+                                                         float(np.float32(rng.random() / P)),
+                                                         vp(bufs[cur ^ 1].data_ptr()), cap, vp(d_cnt.data_ptr())))
+            ctx.sync()
+            pose = d_pose.cpu().numpy()[:6].astype(np.float64)
+            bi = int(d_best[0].item()) & 0xFFFFFFFF
+            b = d[min(bi, P - 1)].cpu().numpy().astype(np.float64)
+            mean_err.append(float(np.linalg.norm(pose[:3] - true[:3])))
+            best_err.append(float(np.linalg.norm(b[:3] - true[:3])))
+            yaw_err.append(float(np.rad2deg(abs((pose[5] - true[5] + np.pi) % (2 * np.pi) - np.pi))))
+            P = min(int(d_cnt[0].item()), cap)
+            cur ^= 1
+    secs = time.perf_counter() - t0
+    marks = sorted({0, 1, 4, 9, updates // 2, updates - 1})
+    return {"updates": updates, "particles": P0, "points": Npts,
+            "step": "motion + sensor update + best particle + systematic resample, count read back",
+            "ms_per_update": 1000.0 * secs / updates,
+            "mean_position_error_m": {str(i + 1): mean_err[i] for i in marks if i < updates},
+            "best_particle_error_m": {str(i + 1): best_err[i] for i in marks if i < updates},
+            "mean_yaw_error_deg": {str(i + 1): yaw_err[i] for i in marks if i < updates}}
+
+
 def motion_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 20) -> dict:
     """Times the motion update (ParticleCloud::apply_model with device-drawn
     noise, odometry 0.8 m/s, 0.2 rad/s, 0.1 s) on the workload's particles."""
@@ -744,10 +805,13 @@ def main():
     base = None
     if rank == 0 and not args.no_cpu_baseline:
         base, _ = cpu_baseline(wl)
-    scan = motion = None
+    scan = motion = tracking = None
     if not args.no_scan:
         scan = scan_reduction_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)
         motion = motion_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)
+        if args.workload in ("building", "global"):
+            tracking = tracking_side(lib, ctx, stream, wl, dmap, f"cuda:{local}",
+                                     100 if args.workload == "building" else 50)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -761,7 +825,7 @@ def main():
                           "form": "plain single filter", "parallelism": f"replicas x{world}"},
                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
                "latency_ms": latency, "clocks": clocks, "scan_reduction": scan,
-               "motion_update": motion}
+               "motion_update": motion, "tracking": tracking}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -170,8 +170,10 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
 int ensure_workspace(tsdfl_ctx* c, size_t P, size_t N)
 {
     if (P <= c->cap_P && N <= c->cap_N && c->ws) return TSDFL_OK;
-    size_t nP = P > c->cap_P ? P : c->cap_P;
-    size_t nN = N > c->cap_N ? N : c->cap_N;
+    // grow by at least a quarter, so that counts that drift upwards (the
+    // systematic resampler's) do not reallocate on every new maximum
+    size_t nP = P > c->cap_P ? std::max(P, c->cap_P + c->cap_P / 4) : c->cap_P;
+    size_t nN = N > c->cap_N ? std::max(N, c->cap_N + c->cap_N / 4) : c->cap_N;
     if (nP < 1) nP = 1;
     if (nN < 4) nN = 4;
     size_t total = eval_layout(nP, nN, nullptr, nullptr, nullptr);
@@ -191,6 +193,7 @@ int ensure_resample_ws(tsdfl_ctx* c, size_t M)
 {
     size_t need = resample_workspace_bytes(M);
     if (need <= c->rs_bytes) return TSDFL_OK;
+    need = std::max(need, c->rs_bytes + c->rs_bytes / 4);
     void* p = nullptr;
     CUDA_TRY(cudaMalloc(&p, need));
     if (c->rs_ws) cudaFree(c->rs_ws);
@@ -248,6 +251,7 @@ int check_scan_args(const char* fn, size_t n, uint32_t step, uint32_t x_offset, 
 int ensure_io(tsdfl_ctx* c, size_t bytes)
 {
     if (bytes <= c->io_bytes) return TSDFL_OK;
+    bytes = std::max(bytes, c->io_bytes + c->io_bytes / 4);
     void* p = nullptr;
     CUDA_TRY(cudaMalloc(&p, bytes));
     if (c->io) cudaFree(c->io);
