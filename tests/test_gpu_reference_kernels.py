@@ -1,0 +1,102 @@
+"""The reference's own CUDA kernels (cudaEvaluateParticlesOrdered, compiled
+from the reference tree for sm_103a and loaded through the driver API) beside
+ours on the same GPU, timed on the room (C1) and building (C2) workloads (run
+with -s to see the timings).  Their raw weights follow the reference's GPU
+semantics, which differ from its CPU path that we reproduce: float-to-unsigned
+conversions saturate negative map offsets to 0 (a slot of the first brick
+where the CPU path misses), and sinf/cosf and FMA contraction change the
+laser poses in the last bits.  So they are checked for what both paths share:
+finite positive weights that rank the particles alike."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import ref_gpu
+from tsdf_localization_gb300 import Context, DeviceMap, TSDFEvaluator
+from tsdf_localization_gb300 import _native as N
+from tsdf_localization_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+vp = C.c_void_p
+
+if not ref_gpu.available():
+    pytest.skip("the reference kernels were not built (no reference tree when the library was built)",
+                allow_module_level=True)
+
+
+def run_reference(rk, wl, parts, stream):
+    """Raw weights of the reference kernel and its time (ms, median of 3)."""
+    P = parts.shape[0]
+    data = torch.from_numpy(wl.float_data()).cuda()
+    occ = torch.from_numpy(np.ascontiguousarray(wl.grid_occ, np.int32)).cuda()
+    coef = bytes(wl.coef)
+    d_coef = torch.from_numpy(np.frombuffer(coef, np.uint8).copy()).cuda()
+    soa = torch.from_numpy(np.ascontiguousarray(parts[:, :6].T)).cuda()
+    pts = torch.from_numpy(np.ascontiguousarray(wl.points, np.float32)).cuda()
+    tf = torch.from_numpy(np.ascontiguousarray(wl.tf, np.float32).reshape(16)).cuda()
+    w = torch.zeros(P, dtype=torch.float32, device="cuda")
+    rk.set_model(coef, wl.tf)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rk.evaluate(occ.data_ptr(), data.data_ptr(), d_coef.data_ptr(), pts.data_ptr(), pts.shape[0], soa.data_ptr(),
+                    P, tf.data_ptr(), w.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return w.cpu().numpy(), float(np.median(times[1:]))
+
+
+def ours(ctx, wl, parts):
+    """Our serial-mode raw weights (the reference CPU path's float sums) and our
+    exact-mode scoring kernel time (ms, median of 3)."""
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True)
+    raw = TSDFEvaluator(dmap, serial_sums=True).evaluate_debug(parts.copy(), wl.points, wl.tf)["raw"]
+    d = torch.from_numpy(parts.copy()).cuda()
+    q = torch.from_numpy(np.ascontiguousarray(wl.points, np.float32)).cuda()
+    pose = torch.zeros(8, dtype=torch.float32, device="cuda")
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    tf = np.ascontiguousarray(wl.tf, np.float32)
+    N.check(N.lib().tsdfl_ctx_set_timing(ctx.handle, 1))
+    times = []
+    for _ in range(4):
+        N.check(N.lib().tsdfl_evaluate_device(ctx.handle, dmap.handle, C.byref(model), vp(d.data_ptr()),
+                                              parts.shape[0], vp(q.data_ptr()), q.shape[0], tf.ctypes.data_as(vp), 0,
+                                              vp(pose.data_ptr())))
+        ctx.sync()
+        k = C.c_float()
+        N.check(N.lib().tsdfl_ctx_last_timing(ctx.handle, C.byref(k)))
+        times.append(k.value)
+    N.check(N.lib().tsdfl_ctx_set_timing(ctx.handle, 0))
+    return raw, float(np.median(times[1:]))
+
+
+@pytest.mark.parametrize("name", ["room", "building"])
+def test_reference_kernels_beside_ours(name):
+    if name == "room":
+        wl = synth.room_workload(seed=1, n_particles=1024, n_points=2048)
+    else:
+        wl = synth.building_workload(seed=2, n_particles=100_032, n_points=8192)
+    parts = np.ascontiguousarray(wl.particles, np.float32)
+    assert parts.shape[0] % 64 == 0   # the reference kernel has no thread-index bound check
+    ctx = Context(0)
+    stream = torch.cuda.Stream()
+    N.check(N.lib().tsdfl_ctx_set_stream(ctx.handle, vp(stream.cuda_stream)))
+    with torch.cuda.stream(stream):
+        rk = ref_gpu.ReferenceKernels()
+        w_ref, ms_ref = run_reference(rk, wl, parts, stream)
+        raw, ms_ours = ours(ctx, wl, parts)
+    rel = np.abs(w_ref.astype(np.float64) - raw) / np.abs(raw)
+    print(f"\n{name}: P={parts.shape[0]} N={wl.points.shape[0]} reference cudaEvaluateParticlesOrdered "
+          f"{ms_ref:.3f} ms, ours (exact-mode scoring) {ms_ours:.3f} ms, {ms_ref / ms_ours:.1f}x; raw weight "
+          f"rel. difference median {np.median(rel):.2e}, p99 {np.percentile(rel, 99):.2e}, max {rel.max():.2e}")
+    assert np.all(np.isfinite(w_ref)) and np.all(w_ref > 0)
+    rank_ref = np.argsort(np.argsort(w_ref))
+    rank_ours = np.argsort(np.argsort(raw))
+    assert np.corrcoef(rank_ref, rank_ours)[0, 1] > 0.9
+    assert ms_ours < ms_ref
+    ctx.close()

@@ -7,6 +7,7 @@ Test infrastructure built by the same call:
   oracle/_build/liboracle.so   CPU restatement of the reference sensor update
   oracle/_ref/libref.so        the reference's own CPU sources, compiled from the
                                reference tree when it is present on this machine
+  oracle/_ref/ref_gpu.cubin    the reference's own CUDA kernels (device code), same
 """
 from __future__ import annotations
 
@@ -97,6 +98,11 @@ def build(verbose: bool = False, force: bool = False) -> dict:
                          "-I", str(ORACLE / "shim"), "-I", str(REFERENCE / "include"),
                          str(ORACLE / "ref_driver.cpp"), *map(str, ref_srcs), "-o", str(ref)])
         ref_built = str(ref)
+        # the reference's CUDA kernels as device code only (loaded through the driver API)
+        cubin = ref_dir / "ref_gpu.cubin"
+        if force or _stale(cubin, [ORACLE / "ref_gpu_kernels.cu"] + sorted((REFERENCE / "include").rglob("*.h"))):
+            jobs.append([nvcc, "-cubin", *ARCH, "-O3", "-std=c++17", "-I", str(ORACLE / "shim"), "-I",
+                         str(REFERENCE / "include"), str(ORACLE / "ref_gpu_kernels.cu"), "-o", str(cubin)])
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
