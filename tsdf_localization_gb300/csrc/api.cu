@@ -1560,8 +1560,30 @@ size_t session_bytes(size_t cap, size_t max_points)
            align_up(resample_workspace_bytes(cap), 256) + 256;
 }
 
-// Launches every queued update of an idle session as one batch on slot k.
+// Returns the slot's requests to the front of their sessions' queues (a
+// dispatch that could not be launched).
+void server_requeue(tsdfl_server* S, tsdfl_server::Slot& sl)
+{
+    for (size_t r = sl.reqs.size(); r-- > 0;) {
+        tsdfl_server::Session& se = S->sessions[sl.reqs[r].session];
+        se.busy = false;
+        se.queue.push_front(std::move(sl.reqs[r]));
+    }
+    sl.reqs.clear();
+}
+
+int server_launch(tsdfl_server* S, int k);
+
+// Launches every queued update of an idle session as one batch on slot k; on
+// failure the updates go back to their queues.
 int server_dispatch(tsdfl_server* S, int k)
+{
+    const int rc = server_launch(S, k);
+    if (rc && !S->slots[k].busy) server_requeue(S, S->slots[k]);
+    return rc;
+}
+
+int server_launch(tsdfl_server* S, int k)
 {
     tsdfl_server::Slot& sl = S->slots[k];
     sl.reqs.clear();
