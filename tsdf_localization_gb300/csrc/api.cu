@@ -91,6 +91,7 @@ struct tsdfl_map {
     uint16_t* codes = nullptr;
     float* data = nullptr;
     uint16_t* dense = nullptr;    // compact layout (TSDFL_MAP_DENSE)
+    uint64_t dense_slots = 0;     // its slots before the sentinels
     uint32_t* occ = nullptr;      // its bitmap and prefix counts
     uint32_t occ_words = 0;
     uint32_t n0 = 0;
@@ -329,6 +330,16 @@ void fill_view(tsdfl_map* m)
     v.occ = m->occ;
     v.occ_words = m->occ_words;
     v.n0 = m->n0;
+    v.codes_sent = (uint32_t)c.data_size;
+    v.dense_sent = (uint32_t)m->dense_slots;
+}
+
+// The kSentinels codes after the last slot of a code array (MapView::codes_sent).
+cudaError_t write_sentinels(uint16_t* arr, size_t at, cudaStream_t s)
+{
+    static const uint16_t kSent[kSentinels] = {(uint16_t)kCodeMiss, (uint16_t)kCodeLater, (uint16_t)kCodeNone,
+                                               (uint16_t)kCodeNone};
+    return cudaMemcpyAsync(arr + at, kSent, sizeof(kSent), cudaMemcpyHostToDevice, s);
 }
 
 // Largest sub-voxel index trunc(fl(s / res)) over floats s in [0, 1).
@@ -354,14 +365,14 @@ int build_compact(tsdfl_ctx* ctx, tsdfl_map* m)
     uint64_t nb = 0, n0 = 0;
     for (uint64_t up = 0; up < gos; ++up) {
         if (go[up] < 0) continue;
-        occ[up / 32] |= 1u << (up % 32);
+        occ[2 * (up / 32)] |= 1u << (up % 32);
         ++nb;
         if (up < c.up_dim_2) ++n0;
     }
     uint32_t run = 0;
     for (uint32_t w = 0; w < words; ++w) {
-        occ[words + w] = run;
-        run += (uint32_t)__builtin_popcount(occ[w]);
+        occ[2 * w + 1] = run;
+        run += (uint32_t)__builtin_popcount(occ[2 * w]);
     }
     const uint64_t slots = (nb + n0) * S3;
     if (slots >= (1ull << 31)) return TSDFL_OK;
@@ -379,7 +390,9 @@ int build_compact(tsdfl_ctx* ctx, tsdfl_map* m)
         skirt.push_back(layer0 ? 1 : 0);
         ++r;
     }
-    CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (slots ? slots : 1)));
+    CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (slots + kSentinels)));
+    CUDA_TRY(write_sentinels(m->dense, slots, ctx->stream));
+    m->dense_slots = slots;
     CUDA_TRY(cudaMalloc(&m->occ, sizeof(uint32_t) * occ.size()));
     m->bytes += sizeof(uint16_t) * slots + sizeof(uint32_t) * occ.size();
     CUDA_TRY(cudaMemcpy(m->occ, occ.data(), sizeof(uint32_t) * occ.size(), cudaMemcpyHostToDevice));
@@ -662,7 +675,8 @@ int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* 
     bool use_codes = !(flags & TSDFL_MAP_FORCE_F32);
     if (use_codes) {
         int32_t* fail = ctx->status + 2;
-        e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n ? n : 1));
+        e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n + kSentinels));
+        if (e == cudaSuccess) e = write_sentinels(m->codes, n, ctx->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(fail, 0, sizeof(int32_t), ctx->stream);
         if (e == cudaSuccess) {
             rc = launch_codes_from_floats(m->data, n, m->values, coef->init_value, m->codes, fail, ctx->stream);
@@ -709,9 +723,10 @@ int tsdfl_map_create_codes(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int
     rc = map_common(ctx, coef, grid_occ, sigma, m);
     if (rc) { destroy_map(m); return rc; }
     size_t n = coef->data_size;
-    cudaError_t e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n ? n : 1));
+    cudaError_t e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n + kSentinels));
     if (e == cudaSuccess && n)
         e = cudaMemcpyAsync(m->codes, codes, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = write_sentinels(m->codes, n, ctx->stream);
     if (e != cudaSuccess) {
         set_error("tsdfl_map_create_codes: %s", cudaGetErrorString(e));
         destroy_map(m);

@@ -400,37 +400,42 @@ struct FastIn {
 
 // Branch-free fast path: the slot code, kCodeMiss, or kCodeSlow when the exact
 // slow tiers must decide (offset outside [0, mmax + 1) -- on z outside
-// (-1, mmax + 1) -- or, dense layout, a sub-voxel index outside the brick).
+// (-1, mmax + 1) -- or, dense layout, a sub-voxel index outside the brick);
+// kCodeNone for a padding point (valid false).  `slow` is set for kCodeSlow.
+// The returned value is the gathered code itself: lookups that are not slots
+// read the array's sentinels, which saves the selects after the gather.
 // DENSE: one gather from the dense layout, the brick's occupancy bit from the
 // shared-memory bitmap `occ`; otherwise the brick table and the slot array.
 template <bool DENSE>
-__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const FastIn& in)
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const FastIn& in, bool valid,
+                                              bool& slow)
 {
     const uint32_t zb = __float_as_uint(in.oz);
     const uint32_t sgn = (uint32_t)((int32_t)zb >> 31);   // all ones when oz < 0
     const bool fast = __float_as_uint(in.ox) < m.lim_x && __float_as_uint(in.oy) < m.lim_y &&
                       (zb & 0x7fffffffu) < (sgn ? m.lim_zn : m.lim_z);
+    slow = valid && !fast;
+    const uint32_t alt = (valid ? (fast ? 0u : 1u) : 2u);   // sentinel: miss, later, none
     const uint32_t up = in.bmx + in.bmy * m.up_dim_x + in.bmz * m.up_dim_2 - m.up_bias;
     const uint32_t qz = ((in.bcz - kMagic) ^ sgn) - sgn;   // -q(|oz|) below the map
     const uint32_t sl = in.bcx + in.bcy * m.sub_dim - m.sl_bias_xy + qz * m.sub_dim_2;
     const bool inside = fast && up < m.grid_occ_size;
     if (DENSE) {   // the brick's rank from the shared-memory bitmap and prefix counts
         const uint32_t w = inside ? (up >> 5) : 0u;
-        const uint32_t word = occ[w], below = occ[m.occ_words + w];
+        const uint2 wb = reinterpret_cast<const uint2*>(occ)[w];
+        const uint32_t word = wb.x, below = wb.y;
         const uint32_t bit = 1u << (up & 31u);
         const bool alloc = (word & bit) != 0u;
         const uint32_t r = below + __popc(word & (bit - 1u));
         const uint32_t k = r + (up < m.up_dim_2 ? r + 1u : m.n0);   // bricks (and skirts) before this one
-        const bool ok = inside && alloc;
-        const uint32_t code = __ldg(m.dense + (ok ? k * m.sub_dim_3 + sl : 0u));
-        return ok ? code : fast ? (uint32_t)kCodeMiss : kCodeSlow;
+        const bool ok = valid && inside && alloc;
+        return __ldg(m.dense + (ok ? k * m.sub_dim_3 + sl : m.dense_sent + alt));
     } else {
         // slot indices below 0 wrap past 2^31 > data_size: a miss, as in getIndex's 64-bit sum
         const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
         const uint32_t idx = (uint32_t)base + sl;
-        const bool ok = inside && base >= 0 && idx < m.data_size;
-        const uint32_t code = __ldg(m.codes + (ok ? idx : 0u));
-        return ok ? code : fast ? (uint32_t)kCodeMiss : kCodeSlow;
+        const bool ok = valid && inside && base >= 0 && idx < m.data_size;
+        return __ldg(m.codes + (ok ? idx : m.codes_sent + alt));
     }
 }
 
@@ -566,20 +571,17 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
                 upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
                 upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
             }
-            uint32_t k0 = fast_code<DENSE>(m, occ, i0);
-            uint32_t k1 = fast_code<DENSE>(m, occ, i1);
-            if (partial) {
-                if (64 * blk + lane >= cn) k0 = kCodeNone;
-                if (64 * blk + 32 + lane >= cn) k1 = kCodeNone;
-            }
+            bool s0, s1;
+            const uint32_t k0 = fast_code<DENSE>(m, occ, i0, !partial || 64 * blk + lane < cn, s0);
+            const uint32_t k1 = fast_code<DENSE>(m, occ, i1, !partial || 64 * blk + 32 + lane < cn, s1);
             // lanes the fast path cannot decide are deferred to the warp's ring and
             // scored 32 at a time (kCodeLater contributes nothing here), so no warp
             // diverges into the slow tiers; at most 31 entries wait between steps,
             // so each append of <= 32 fits the ring
-            if (__any_sync(0xffffffffu, k0 == kCodeSlow || k1 == kCodeSlow)) {
+            if (__any_sync(0xffffffffu, s0 || s1)) {
                 float tx, ty, tz, u;
                 upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
-                defer(ring, head, tail, k0 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + lane, lane);
+                defer(ring, head, tail, s0, tx, ty, tz, c0 + 64 * blk + lane, lane);
                 if (tail - head >= 32) {
                     const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
                     acc += d.acc;
@@ -587,7 +589,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
                     head += 32;
                 }
                 upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
-                defer(ring, head, tail, k1 == kCodeSlow, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
+                defer(ring, head, tail, s1, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
                 if (tail - head >= 32) {
                     const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
                     acc += d.acc;

@@ -70,14 +70,21 @@ struct MapView {
     // index order, bricks of layer z = 0 each preceded by a "skirt" of sub_dim^3
     // slots holding what getIndex reads below them (the sub_dim^3 slots before
     // the brick in the reference's data order, kCodeMiss below slot 0).  occ is
-    // [occ_words bitmap words | occ_words prefix counts]: bit up of the bitmap
-    // is set when brick up is allocated, prefix[w] counts the set bits of words
-    // 0..w-1.  A brick of rank r starts at (2r + 1) S^3 in layer 0 (up < up_dim_2)
-    // and at (r + n0) S^3 above, n0 = allocated bricks in layer 0.
+    // occ_words pairs {bitmap word w, prefix[w]}: bit up of the bitmap is set
+    // when brick up is allocated, prefix[w] counts the set bits of words
+    // 0..w-1 (one 8-byte read gives both).  A brick of rank r starts at
+    // (2r + 1) S^3 in layer 0 (up < up_dim_2) and at (r + n0) S^3 above, n0 =
+    // allocated bricks in layer 0.
     const uint32_t* occ;
     uint32_t occ_words;            // a multiple of 4
     uint32_t n0;
+    // Both code arrays end in kSentinels extra entries {kCodeMiss, kCodeLater,
+    // kCodeNone, kCodeNone}: the fast path gathers a lookup that falls outside
+    // the allocated slots from there, so every gather yields the final code.
+    uint32_t codes_sent, dense_sent;   // index of the first sentinel in codes / dense
 };
+
+constexpr int kSentinels = 4;
 
 #ifdef __CUDACC__
 
