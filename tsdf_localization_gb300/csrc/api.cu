@@ -135,6 +135,7 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
     size_t npairs = 32 * ((nN + 63) / 64);
     size_t o_pxy = take(sizeof(float) * 4 * npairs);
     size_t o_pz = take(sizeof(float) * 2 * npairs);
+    size_t o_perm = take(sizeof(int32_t) * 2 * npairs);
     size_t o_lfx = take(sizeof(long long) * kNumCodes);
     size_t o_lf = take(sizeof(float) * kNumCodes);
     size_t o_cnt = take(sizeof(int32_t) * 16);
@@ -156,6 +157,7 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
         e->cs = reinterpret_cast<float*>(b + o_cs);
         e->pxy = reinterpret_cast<float4*>(b + o_pxy);
         e->pz = reinterpret_cast<float2*>(b + o_pz);
+        e->perm = reinterpret_cast<int32_t*>(b + o_perm);
         e->lut_fx = reinterpret_cast<long long*>(b + o_lfx);
         e->lut_f = reinterpret_cast<float*>(b + o_lf);
         e->counts = reinterpret_cast<int32_t*>(b + o_cnt);

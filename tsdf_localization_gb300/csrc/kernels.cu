@@ -125,13 +125,39 @@ struct PointParams {
     int shift;                 // fixed-point scale 2^shift
 };
 
+// Spatial order of the pair layout: the tiled kernels walk the scan in chunks
+// of consecutive points with every particle at once, so chunks whose points
+// lie close together in the sensor frame gather from a smaller part of the map
+// and hit L2 more often.  Bin = azimuth sector, then horizontal range band;
+// exact fixed-point sums make the result independent of the order.
+constexpr int kSortSectors = 16;
+constexpr int kSortBands = 128;
+constexpr float kSortBand = 0.5f;   // metres per range band
+constexpr int kSortBins = kSortSectors * kSortBands;
+constexpr int kPrepThreads = 1024;
+static_assert(kSortBins == 2 * kPrepThreads, "two bins per thread in the scan");
+
+__device__ __forceinline__ int spatial_bin(float x, float y)
+{
+    const float r2 = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
+    if (!(r2 < 1e30f)) return kSortBins - 1;   // NaN / huge: last
+    const float turn = __fadd_rn(__fdiv_rn(atan2f(y, x), 6.28318530717958647692f), 0.5f);   // [0, 1]
+    const int s = min(max((int)(turn * (float)kSortSectors), 0), kSortSectors - 1);
+    const int band = min((int)__fdiv_rn(sqrtf(r2), kSortBand), kSortBands - 1);
+    return s * kSortBands + band;
+}
+
 // Scan staging: AoS points -> SoA (padded with zeros to npad), the per-point
 // score constant of tsdf_evaluator.cpp:56-65 and the number of points inside
-// max_range; also the likelihood tables for this scan.  One block.
-__global__ void prepare_points_kernel(PointParams p, EvalBuffers b)
+// max_range; the pair layout of the tiled kernels in spatial order (a counting
+// sort by spatial_bin; perm records each position's scan index); also the
+// likelihood tables for this scan.  One block of kPrepThreads.
+__global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParams p, EvalBuffers b)
 {
     __shared__ int warp_counts[32];
+    __shared__ int bins[kSortBins];
     if (threadIdx.x == 0) *b.status = 0;
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
     int in = 0;
     for (int j = threadIdx.x; j < p.npad; j += blockDim.x) {
         float x = 0, y = 0, z = 0, c = 0;
@@ -149,16 +175,55 @@ __global__ void prepare_points_kernel(PointParams p, EvalBuffers b)
         ((float*)b.zs)[j] = z;
         ((float*)b.cs)[j] = c;
     }
-    // pair layout of the fast kernel: in every block of 64 points, lane l of a
-    // warp takes points 64*blk + l and 64*blk + 32 + l
-    for (int q = threadIdx.x; q < p.npairs; q += blockDim.x) {
-        int blk = q >> 5, l = q & 31;
-        int ja = 64 * blk + l, jb = ja + 32;
-        float xa = 0, ya = 0, za = 0, xb = 0, yb = 0, zb = 0;
-        if (ja < p.N) { xa = p.points[3 * ja]; ya = p.points[3 * ja + 1]; za = p.points[3 * ja + 2]; }
-        if (jb < p.N) { xb = p.points[3 * jb]; yb = p.points[3 * jb + 1]; zb = p.points[3 * jb + 2]; }
-        b.pxy[q] = make_float4(xa, xb, ya, yb);
-        b.pz[q] = make_float2(za, zb);
+    __syncthreads();   // bins cleared
+    for (int j = threadIdx.x; j < p.N; j += blockDim.x)
+        atomicAdd(&bins[spatial_bin(p.points[3 * j], p.points[3 * j + 1])], 1);
+    __syncthreads();
+    {   // exclusive scan of the bin counts, two bins per thread
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int c0 = bins[2 * threadIdx.x], c1 = bins[2 * threadIdx.x + 1];
+        int v = c0 + c1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += t;
+        }
+        if (lane == 31) warp_counts[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            int w = lane < (int)(blockDim.x >> 5) ? warp_counts[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += t;
+            }
+            warp_counts[lane] = w;   // inclusive over warps
+        }
+        __syncthreads();
+        const int before = (warp ? warp_counts[warp - 1] : 0) + v - c0 - c1;
+        bins[2 * threadIdx.x] = before;
+        bins[2 * threadIdx.x + 1] = before + c0;
+    }
+    __syncthreads();
+    // pair layout of the fast kernel: in every block of 64 positions, lane l of
+    // a warp takes positions 64*blk + l and 64*blk + 32 + l
+    for (int j = threadIdx.x; j < p.N; j += blockDim.x) {
+        const float x = p.points[3 * j], y = p.points[3 * j + 1], z = p.points[3 * j + 2];
+        const int q = atomicAdd(&bins[spatial_bin(x, y)], 1);
+        const int pair = (q >> 6) * 32 + (q & 31), half = (q >> 5) & 1;
+        float* xy = reinterpret_cast<float*>(b.pxy + pair);
+        xy[half] = x;
+        xy[2 + half] = y;
+        reinterpret_cast<float*>(b.pz + pair)[half] = z;
+        b.perm[q] = j;
+    }
+    for (int q = p.N + threadIdx.x; q < 2 * p.npairs; q += blockDim.x) {   // padding positions
+        const int pair = (q >> 6) * 32 + (q & 31), half = (q >> 5) & 1;
+        float* xy = reinterpret_cast<float*>(b.pxy + pair);
+        xy[half] = 0.0f;
+        xy[2 + half] = 0.0f;
+        reinterpret_cast<float*>(b.pz + pair)[half] = 0.0f;
+        b.perm[q] = 0;   // never read: padding lanes record no debug code
     }
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) {
         float v = p.code_values[c];
@@ -231,6 +296,7 @@ struct EvalParams {
     MapView m;
     const float4* pxy;
     const float2* pz;
+    const int32_t* perm;   // scan index of each pair-layout point (debug rows)
     const float* pose12;
     const float* xs;
     const float* ys;
@@ -465,7 +531,7 @@ struct Partial {
 // the exact second tier / 64-bit emulation.  The map view is read from a
 // shared-memory copy so that no kernel parameter's address escapes.
 __device__ __noinline__ Partial drain(const MapView* m, const long long* lut, const float4* ring, uint32_t head,
-                                      int count, int lane, uint32_t* dbg_row)
+                                      int count, int lane, uint32_t* dbg_row, const int32_t* perm)
 {
     Partial r{0, 0u};
     if (lane < count) {
@@ -473,7 +539,7 @@ __device__ __noinline__ Partial drain(const MapView* m, const long long* lut, co
         const uint32_t code = slow_code(*m, e.x, e.y, e.z);
         r.acc = lut[code];
         r.hits = code <= (uint32_t)kCodeInit ? 1u : 0u;
-        if (dbg_row) dbg_row[__float_as_int(e.w)] = code | kDbgSlow;
+        if (dbg_row) dbg_row[perm[__float_as_int(e.w)]] = code | kDbgSlow;
     }
     __syncwarp();
     return r;
@@ -527,7 +593,10 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
         const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
         long long acc = 0;
         uint32_t hits = 0;
-        uint32_t* dbg_row = DBG ? p.dbg + (size_t)pi * p.n_total + p.n0 : nullptr;
+        // debug rows are indexed by scan index: perm maps the pass's pair-layout
+        // positions back to it
+        uint32_t* dbg_row = DBG ? p.dbg + (size_t)pi * p.n_total : nullptr;
+        const int32_t* perm = DBG ? p.perm + p.n0 : nullptr;
         // one step: the two points of block blk held by this lane (the
         // chunk's partial last block masks its padding points)
         auto step = [&](int blk, bool partial) {
@@ -583,7 +652,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
                 upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
                 defer(ring, head, tail, s0, tx, ty, tz, c0 + 64 * blk + lane, lane);
                 if (tail - head >= 32) {
-                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
+                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row, perm);
                     acc += d.acc;
                     hits += d.hits;
                     head += 32;
@@ -591,7 +660,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
                 upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
                 defer(ring, head, tail, s1, tx, ty, tz, c0 + 64 * blk + 32 + lane, lane);
                 if (tail - head >= 32) {
-                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row);
+                    const Partial d = drain(s_map, lut, ring, head, 32, lane, dbg_row, perm);
                     acc += d.acc;
                     hits += d.hits;
                     head += 32;
@@ -599,8 +668,8 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
             }
             if (DBG) {
                 const int j = c0 + 64 * blk + lane;
-                if (k0 < (uint32_t)kCodeNone) dbg_row[j] = k0;
-                if (k1 < (uint32_t)kCodeNone) dbg_row[j + 32] = k1;
+                if (k0 < (uint32_t)kCodeNone) dbg_row[perm[j]] = k0;
+                if (k1 < (uint32_t)kCodeNone) dbg_row[perm[j + 32]] = k1;
             }
             acc += lut[k0] + lut[k1];
             hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
@@ -608,7 +677,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
         for (int blk = 0; blk < nfull; ++blk) step(blk, false);
         if (nfull < nblk) step(nfull, true);
         if (tail != head) {
-            const Partial d = drain(s_map, lut, ring, head, (int)(tail - head), lane, dbg_row);
+            const Partial d = drain(s_map, lut, ring, head, (int)(tail - head), lane, dbg_row, perm);
             acc += d.acc;
             hits += d.hits;
             head = tail;
@@ -1662,7 +1731,7 @@ int launch_prepare(const float* points, int N, int npad, float max_range_sq, flo
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
 {
     PointParams p{points, N, npad, 32 * ((N + 63) / 64), max_range_sq, c_in, c_out, code_values, shift};
-    prepare_points_kernel<<<1, 1024, 0, s>>>(p, b);
+    prepare_points_kernel<<<1, kPrepThreads, 0, s>>>(p, b);
     g_launches += 1;
     return check(cudaGetLastError());
 }
@@ -1706,7 +1775,7 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
     p.m = m;
     p.pose12 = b.pose12;
     p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
-    p.pxy = b.pxy; p.pz = b.pz;
+    p.pxy = b.pxy; p.pz = b.pz; p.perm = b.perm;
     p.lut_fx = b.lut_fx;
     p.lut_f = b.lut_f;
     p.sum_fx = b.sum_fx;
@@ -1791,7 +1860,7 @@ uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int gr
             p.m = sp.m;
             p.pose12 = b.pose12;
             p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
-            p.pxy = b.pxy; p.pz = b.pz;
+            p.pxy = b.pxy; p.pz = b.pz; p.perm = b.perm;
             p.lut_fx = b.lut_fx;
             p.lut_f = b.lut_f;
             p.sum_fx = b.sum_fx;

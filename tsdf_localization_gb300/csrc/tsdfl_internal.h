@@ -152,8 +152,9 @@ struct EvalBuffers {
     const float* ys;
     const float* zs;
     const float* cs;         // per-point score constant (a_range*inv_max_range or a_max)
-    float4* pxy;             // point pairs (x_a, x_b, y_a, y_b) per 64-point block
+    float4* pxy;             // point pairs (x_a, x_b, y_a, y_b) per 64-point block, spatial order
     float2* pz;              // point pairs (z_a, z_b)
+    int32_t* perm;           // scan index of each point of the pair layout
     float* pose12;           // P x 12 laser poses
     float* trig6;            // P x 6: sin/cos of roll, pitch, yaw
     long long* sum_fx;       // P: fixed-point likelihood sums
