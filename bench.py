@@ -756,7 +756,7 @@ def main():
     achieved = alg / (kmed / 1000.0) / 1e9
     # DRAM bytes of one scoring launch from an ncu capture of this exact workload
     # (dram__bytes_read.sum + dram__bytes_write.sum, single pass, full size)
-    measured_traffic = {("building", 100_000, 8192, "compact", "fast"): 5.05e9 + 0.108e9}
+    measured_traffic = {("building", 100_000, 8192, "compact", "fast"): 2.187e9 + 0.0576e9}
     traffic = measured_traffic.get((args.workload, P, Npts, args.layout, args.kernel))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "eval_tiled_kernel" if (args.kernel == "fast" and info["fast_index"])

@@ -135,15 +135,20 @@ constexpr int kSortBands = 128;
 constexpr float kSortBand = 0.5f;   // metres per range band
 constexpr int kSortBins = kSortSectors * kSortBands;
 constexpr int kPrepThreads = 1024;
+constexpr int kBinCache = 16384;    // points whose bin the staging keeps in shared memory
 static_assert(kSortBins == 2 * kPrepThreads, "two bins per thread in the scan");
 
+// Sector of the diamond angle (|y| / (|x| + |y|) per quadrant, counter-clockwise
+// from +x: monotone in the azimuth, no trigonometry), then the range band.
 __device__ __forceinline__ int spatial_bin(float x, float y)
 {
-    const float r2 = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
-    if (!(r2 < 1e30f)) return kSortBins - 1;   // NaN / huge: last
-    const float turn = __fadd_rn(__fdiv_rn(atan2f(y, x), 6.28318530717958647692f), 0.5f);   // [0, 1]
-    const int s = min(max((int)(turn * (float)kSortSectors), 0), kSortSectors - 1);
-    const int band = min((int)__fdiv_rn(sqrtf(r2), kSortBand), kSortBands - 1);
+    const float r1 = fabsf(x) + fabsf(y);
+    if (!(r1 < 1e30f)) return kSortBins - 1;   // NaN / huge: last
+    const float t = r1 > 0.0f ? __fdividef(fabsf(y), r1) : 0.0f;
+    const float a = x >= 0.0f ? (y >= 0.0f ? t : 4.0f - t) : (y >= 0.0f ? 2.0f - t : 2.0f + t);   // [0, 4]
+    const int s = min((int)(a * (0.25f * kSortSectors)), kSortSectors - 1);
+    const float r = sqrtf(x * x + y * y);
+    const int band = (int)fminf(r * (1.0f / kSortBand), (float)(kSortBands - 1));
     return s * kSortBands + band;
 }
 
@@ -156,29 +161,32 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
 {
     __shared__ int warp_counts[32];
     __shared__ int bins[kSortBins];
+    __shared__ uint16_t sbin[kBinCache];
     if (threadIdx.x == 0) *b.status = 0;
     for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
     int in = 0;
+#pragma unroll 4
     for (int j = threadIdx.x; j < p.npad; j += blockDim.x) {
         float x = 0, y = 0, z = 0, c = 0;
         if (j < p.N) {
-            x = p.points[3 * j];
-            y = p.points[3 * j + 1];
-            z = p.points[3 * j + 2];
+            x = __ldg(p.points + 3 * j);
+            y = __ldg(p.points + 3 * j + 1);
+            z = __ldg(p.points + 3 * j + 2);
             float sq = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
             bool inr = sq < p.max_range_sq;
             c = inr ? p.c_in : p.c_out;
             in += inr ? 1 : 0;
+            const int bin = spatial_bin(x, y);
+            atomicAdd(&bins[bin], 1);
+            if (j < kBinCache) sbin[j] = (uint16_t)bin;
         }
         ((float*)b.xs)[j] = x;
         ((float*)b.ys)[j] = y;
         ((float*)b.zs)[j] = z;
         ((float*)b.cs)[j] = c;
     }
-    __syncthreads();   // bins cleared
-    for (int j = threadIdx.x; j < p.N; j += blockDim.x)
-        atomicAdd(&bins[spatial_bin(p.points[3 * j], p.points[3 * j + 1])], 1);
-    __syncthreads();
+    __syncthreads();   // counts complete; this block's SoA stores visible to it
     {   // exclusive scan of the bin counts, two bins per thread
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const int c0 = bins[2 * threadIdx.x], c1 = bins[2 * threadIdx.x + 1];
@@ -208,8 +216,8 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
     // pair layout of the fast kernel: in every block of 64 positions, lane l of
     // a warp takes positions 64*blk + l and 64*blk + 32 + l
     for (int j = threadIdx.x; j < p.N; j += blockDim.x) {
-        const float x = p.points[3 * j], y = p.points[3 * j + 1], z = p.points[3 * j + 2];
-        const int q = atomicAdd(&bins[spatial_bin(x, y)], 1);
+        const float x = b.xs[j], y = b.ys[j], z = b.zs[j];
+        const int q = atomicAdd(&bins[j < kBinCache ? (int)sbin[j] : spatial_bin(x, y)], 1);
         const int pair = (q >> 6) * 32 + (q & 31), half = (q >> 5) & 1;
         float* xy = reinterpret_cast<float*>(b.pxy + pair);
         xy[half] = x;
