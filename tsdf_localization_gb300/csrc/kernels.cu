@@ -101,6 +101,19 @@ __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v)
     return v;
 }
 
+// Element-wise min (x, y) / max (z, w) over the warp; NaN entries are ignored.
+__device__ __forceinline__ float4 warp_extent(float4 e)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e.x = fminf(e.x, __shfl_xor_sync(0xffffffffu, e.x, o));
+        e.y = fminf(e.y, __shfl_xor_sync(0xffffffffu, e.y, o));
+        e.z = fmaxf(e.z, __shfl_xor_sync(0xffffffffu, e.z, o));
+        e.w = fmaxf(e.w, __shfl_xor_sync(0xffffffffu, e.w, o));
+    }
+    return e;
+}
+
 __device__ __forceinline__ double warp_sum_d(double v)
 {
 #pragma unroll
@@ -120,51 +133,81 @@ __device__ __forceinline__ uint32_t dense_code(const MapView& m, float x, float 
 struct PointParams {
     const float* points;  // N x 3
     int N, npad, npairs;
+    const float4* extent;  // the pose kernel's per-block cloud extents
+    int n_ext;
     float max_range_sq, c_in, c_out;
     const float* code_values;  // kNumCodes floats (device)
     int shift;                 // fixed-point scale 2^shift
 };
 
 // Spatial order of the pair layout: the tiled kernels walk the scan in chunks
-// of consecutive points with every particle at once, so chunks whose points
-// lie close together in the sensor frame gather from a smaller part of the map
-// and hit L2 more often.  Bin = azimuth sector, then horizontal range band;
-// exact fixed-point sums make the result independent of the order.
+// of consecutive points with every particle at once, so the order decides how
+// much of the map a chunk touches across the cloud; exact fixed-point sums make
+// the result independent of it.  A compact cloud (tracking) gathers least with
+// chunks that are compact in the sensor frame: azimuth sector, then range band
+// (0.5 m).  A cloud spread over the map (global localisation, any yaw) gathers
+// least with chunks of one height band (1 m), whose hits stay in one layer of
+// the map whatever the particle's position and yaw: height, sector, then range
+// band (2 m).  The cloud counts as spread when its x or y extent exceeds
+// kWideCloud.
 constexpr int kSortSectors = 16;
-constexpr int kSortBands = 128;
-constexpr float kSortBand = 0.5f;   // metres per range band
-constexpr int kSortBins = kSortSectors * kSortBands;
+constexpr int kSortBins = 2048;
+constexpr float kWideCloud = 10.0f;   // metres
 constexpr int kPrepThreads = 1024;
 constexpr int kBinCache = 16384;    // points whose bin the staging keeps in shared memory
 static_assert(kSortBins == 2 * kPrepThreads, "two bins per thread in the scan");
 
 // Sector of the diamond angle (|y| / (|x| + |y|) per quadrant, counter-clockwise
-// from +x: monotone in the azimuth, no trigonometry), then the range band.
-__device__ __forceinline__ int spatial_bin(float x, float y)
+// from +x: monotone in the azimuth, no trigonometry), with the range band and,
+// for a spread cloud, the height band.
+__device__ __forceinline__ int spatial_bin(float x, float y, float z, bool wide)
 {
     const float r1 = fabsf(x) + fabsf(y);
-    if (!(r1 < 1e30f)) return kSortBins - 1;   // NaN / huge: last
+    if (!(r1 < 1e30f) || !(fabsf(z) < 1e30f)) return kSortBins - 1;   // NaN / huge: last
     const float t = r1 > 0.0f ? __fdividef(fabsf(y), r1) : 0.0f;
     const float a = x >= 0.0f ? (y >= 0.0f ? t : 4.0f - t) : (y >= 0.0f ? 2.0f - t : 2.0f + t);   // [0, 4]
     const int s = min((int)(a * (0.25f * kSortSectors)), kSortSectors - 1);
     const float r = sqrtf(x * x + y * y);
-    const int band = (int)fminf(r * (1.0f / kSortBand), (float)(kSortBands - 1));
-    return s * kSortBands + band;
+    if (!wide) return s * 128 + (int)fminf(r * 2.0f, 127.0f);   // 16 sectors x 128 bands of 0.5 m
+    const int zb = (int)fminf(fmaxf(floorf(z) + 4.0f, 0.0f), 7.0f);   // [-4, 4) m in 1 m bands
+    return (zb * kSortSectors + s) * 16 + (int)fminf(r * 0.5f, 15.0f);   // x 16 bands of 2 m
 }
 
 // Scan staging: AoS points -> SoA (padded with zeros to npad), the per-point
 // score constant of tsdf_evaluator.cpp:56-65 and the number of points inside
 // max_range; the pair layout of the tiled kernels in spatial order (a counting
 // sort by spatial_bin; perm records each position's scan index); also the
-// likelihood tables for this scan.  One block of kPrepThreads.
+// likelihood tables for this scan.  One block of kPrepThreads, launched after
+// the pose kernel (it reads the cloud's extent).
 __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParams p, EvalBuffers b)
 {
     __shared__ int warp_counts[32];
     __shared__ int bins[kSortBins];
     __shared__ uint16_t sbin[kBinCache];
+    __shared__ float4 s_ext[32];
+    __shared__ int s_wide;
     if (threadIdx.x == 0) *b.status = 0;
+    {   // the cloud's x / y extent from the pose kernel's per-block partials
+        const float inf = __int_as_float(0x7f800000);
+        float4 e = make_float4(inf, inf, -inf, -inf);
+        for (int k = threadIdx.x; k < p.n_ext; k += blockDim.x) {
+            const float4 v = p.extent[k];
+            e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
+        }
+        e = warp_extent(e);
+        if ((threadIdx.x & 31) == 0) s_ext[threadIdx.x >> 5] = e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+                const float4 v = s_ext[w];
+                e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
+            }
+            s_wide = fmaxf(e.z - e.x, e.w - e.y) > kWideCloud ? 1 : 0;   // no particles: -inf
+        }
+    }
     for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
     __syncthreads();
+    const bool wide = s_wide != 0;
     int in = 0;
 #pragma unroll 4
     for (int j = threadIdx.x; j < p.npad; j += blockDim.x) {
@@ -177,7 +220,7 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
             bool inr = sq < p.max_range_sq;
             c = inr ? p.c_in : p.c_out;
             in += inr ? 1 : 0;
-            const int bin = spatial_bin(x, y);
+            const int bin = spatial_bin(x, y, z, wide);
             atomicAdd(&bins[bin], 1);
             if (j < kBinCache) sbin[j] = (uint16_t)bin;
         }
@@ -217,7 +260,7 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
     // a warp takes positions 64*blk + l and 64*blk + 32 + l
     for (int j = threadIdx.x; j < p.N; j += blockDim.x) {
         const float x = b.xs[j], y = b.ys[j], z = b.zs[j];
-        const int q = atomicAdd(&bins[j < kBinCache ? (int)sbin[j] : spatial_bin(x, y)], 1);
+        const int q = atomicAdd(&bins[j < kBinCache ? (int)sbin[j] : spatial_bin(x, y, z, wide)], 1);
         const int pair = (q >> 6) * 32 + (q & 31), half = (q >> 5) & 1;
         float* xy = reinterpret_cast<float*>(b.pxy + pair);
         xy[half] = x;
@@ -255,9 +298,30 @@ struct Tf16 {
 // Laser pose of every particle (tsdf_evaluator.cpp:102-147): trig in double,
 // rounded to float (the correctly rounded sin/cos), products and sums in the
 // reference's order without contraction.
-__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6)
+// Also: the x / y extent of the block's particles (min x, min y, max x, max y)
+// into extent[block], for the scan staging's choice of point order.
+__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6, float4* extent)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    {
+        __shared__ float4 s_ext[32];
+        const float inf = __int_as_float(0x7f800000);
+        float4 e = make_float4(inf, inf, -inf, -inf);
+        if (i < P) {
+            const float x = particles[7 * (size_t)i], y = particles[7 * (size_t)i + 1];
+            e = make_float4(x, y, x, y);
+        }
+        e = warp_extent(e);
+        if ((threadIdx.x & 31) == 0) s_ext[threadIdx.x >> 5] = e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+                const float4 v = s_ext[w];
+                e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
+            }
+            extent[blockIdx.x] = e;
+        }
+    }
     if (i >= P) return;
     const float* p = particles + 7 * (size_t)i;
     float px = p[0], py = p[1], pz = p[2];
@@ -1735,10 +1799,11 @@ int check(cudaError_t e)
 
 // ------------------------------------------------------------------ launchers
 
-int launch_prepare(const float* points, int N, int npad, float max_range_sq, float c_in, float c_out,
+int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
 {
-    PointParams p{points, N, npad, 32 * ((N + 63) / 64), max_range_sq, c_in, c_out, code_values, shift};
+    PointParams p{points, N, npad, 32 * ((N + 63) / 64), b.extent, P > 0 ? (P + 255) / 256 : 0,
+                  max_range_sq, c_in, c_out, code_values, shift};
     prepare_points_kernel<<<1, kPrepThreads, 0, s>>>(p, b);
     g_launches += 1;
     return check(cudaGetLastError());
@@ -1749,7 +1814,7 @@ int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_
     Tf16 t;
     for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
     if (P > 0) {
-        pose_kernel<<<(P + 255) / 256, 256, 0, s>>>(b.particles, P, t, b.pose12, b.trig6);
+        pose_kernel<<<(P + 255) / 256, 256, 0, s>>>(b.particles, P, t, b.pose12, b.trig6, b.extent);
         g_launches += 1;
     }
     return check(cudaGetLastError());

@@ -155,6 +155,7 @@ struct EvalBuffers {
     float4* pxy;             // point pairs (x_a, x_b, y_a, y_b) per 64-point block, spatial order
     float2* pz;              // point pairs (z_a, z_b)
     int32_t* perm;           // scan index of each point of the pair layout
+    float4* extent;          // per 256 particles: min x, min y, max x, max y
     float* pose12;           // P x 12 laser poses
     float* trig6;            // P x 6: sin/cos of roll, pitch, yaw
     long long* sum_fx;       // P: fixed-point likelihood sums
@@ -170,7 +171,8 @@ struct EvalBuffers {
     uint32_t* dbg_index;     // optional P x N
 };
 
-int launch_prepare(const float* points, int N, int npad, float max_range_sq, float c_in, float c_out,
+// Runs after launch_pose_kernel for the same buffers (reads the cloud's extent).
+int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s);
 int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
 size_t eval_smem_bytes(bool serial, int n);
