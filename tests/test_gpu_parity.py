@@ -202,6 +202,31 @@ def test_multi_pass_long_scan(ctx, room, room_oracle):
     assert np.allclose(d2["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
 
 
+@pytest.mark.parametrize("spread", ["compact", "wide"])
+def test_scan_order_independent_of_point_order(ctx, room, room_oracle, spread):
+    """The tiled kernels stage the scan in a spatial order chosen by the cloud's
+    extent (azimuth sector and range for a compact cloud, height band first for
+    one wider than 10 m): per-point codes still land at their scan index, the
+    weights equal the oracle's, and permuting the input points changes nothing."""
+    rng = np.random.default_rng(21)
+    parts = room.particles[:256].copy()
+    if spread == "wide":   # 16 m across in x and y, any yaw
+        parts[:, 0] += rng.uniform(-8.0, 8.0, 256).astype(np.float32)
+        parts[:, 1] += rng.uniform(-8.0, 8.0, 256).astype(np.float32)
+        parts[:, 5] = rng.uniform(-np.pi, np.pi, 256).astype(np.float32)
+    ref = _oracle_eval(room_oracle, room, particles=parts)
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=True)
+    ev = TSDFEvaluator(dmap)
+    d = ev.evaluate_debug(parts.copy(), room.points, room.tf, voxel_index=True)
+    assert np.array_equal(d["hits"], ref["hits"])
+    assert np.array_equal(d["voxel_index"] & 0xFFFF, _codes_of(ref["voxel_index"], room.codes, room.coef.data_size))
+    assert np.allclose(d["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+    perm = rng.permutation(room.points.shape[0])
+    e = ev.evaluate_debug(parts.copy(), room.points[perm], room.tf, voxel_index=True)
+    assert np.array_equal(e["raw"], d["raw"]) and np.array_equal(e["hits"], d["hits"])
+    assert np.array_equal(e["voxel_index"], d["voxel_index"][:, perm])
+
+
 def test_empty_scan_leaves_particles(ctx, room):
     dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes)
     p = room.particles.copy()
