@@ -83,6 +83,7 @@ __device__ bool stage_xyz(float* xs, float* ys, float* zs, const float* gx, cons
         bulk_g2s(zs, gz, bytes, bar);
     }
     bool ok = mbar_wait_bounded(bar, 0);
+    if (!ok) ok = mbar_wait_bounded(bar, 0);   // give copies in flight a second bound
     if (!ok && threadIdx.x == 0) atomicExch(status, TSDFL_ERR_TIMEOUT);
     return __syncthreads_and(ok ? 1 : 0) != 0;
 }
@@ -789,6 +790,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
         if (occ_words) bulk_g2s(occ, m.occ, occ_words * 4u, &bar);
     }
     bool staged = mbar_wait_bounded(&bar, 0);
+    if (!staged) staged = mbar_wait_bounded(&bar, 0);   // give copies in flight a second bound
     if (!staged && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
     if (__syncthreads_and(staged ? 1 : 0) == 0) return;
 
