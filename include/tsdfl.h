@@ -120,6 +120,17 @@ int tsdfl_map_get_info(const tsdfl_map* map, tsdfl_map_info* info);
 int tsdfl_build_map_codes(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
                           int voxel_mm, float sigma, tsdfl_map_coef* coef, int32_t** grid_occ,
                           uint16_t** codes, float** free_xyz, size_t* n_free);
+/* Reads a map file in the reference's HDF5 layout -- group "/map" with one
+ * dataset of edge^3 raw cells per chunk, named "<x>_<y>_<z>" (GlobalMap,
+ * global_map.cpp:12-170, written through HighFive; read by createTSDFMap,
+ * map_util.h:17-113) -- without the HDF5 library.  Outputs the chunks in the
+ * order createTSDFMap visits them (names in byte order) as tsdfl_build_map_codes
+ * takes them: chunk_pos (3 ints per chunk) and chunks (n_chunks x edge^3 raw
+ * cells), malloc'd (free with tsdfl_free).  Superblocks 0-3, object headers 1
+ * and 2, symbol-table and compact groups, contiguous and compact 4-byte integer
+ * datasets; other storage (dense groups, chunked or filtered datasets) gives
+ * TSDFL_ERR_UNSUPPORTED, a malformed file TSDFL_ERR_INVALID_ARG. */
+int tsdfl_read_map_h5(const char* path, int32_t** chunk_pos, uint32_t** chunks, size_t* n_chunks, int32_t* edge);
 /* The float value of every code for sigma (601 entries: codes 0..600). */
 int tsdfl_code_values(float sigma, float init_value, float* out601);
 void tsdfl_free(void* p);

@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -76,7 +77,39 @@ public:
     Map& operator=(const Map&) = delete;
     tsdfl_map* get() const { return h_; }
 
+    // createTSDFMap(h5_filename, free_map, sigma) (map_util.h:17-154) from a map
+    // file in the reference's HDF5 layout, read without the HDF5 library
+    // (tsdfl_read_map_h5): the device map, and the free-space cells (x, y, z
+    // per cell) when free_xyz is given.  voxel_mm is MAP_RESOLUTION (64).
+    static std::unique_ptr<Map> from_h5(Context& ctx, const char* path, int voxel_mm = 64, float sigma = 0.1f,
+                                        uint32_t flags = TSDFL_MAP_DENSE, std::vector<float>* free_xyz = nullptr)
+    {
+        int32_t* pos = nullptr;
+        uint32_t* raw = nullptr;
+        size_t n = 0;
+        int32_t edge = 0;
+        check(tsdfl_read_map_h5(path, &pos, &raw, &n, &edge));
+        tsdfl_map_coef coef{};
+        int32_t* grid_occ = nullptr;
+        uint16_t* codes = nullptr;
+        float* free_cells = nullptr;
+        size_t n_free = 0;
+        int rc = tsdfl_build_map_codes(pos, raw, n, edge, voxel_mm, sigma, &coef, &grid_occ, &codes,
+                                       free_xyz ? &free_cells : nullptr, free_xyz ? &n_free : nullptr);
+        tsdfl_free(pos);
+        tsdfl_free(raw);
+        std::unique_ptr<Map> m(new Map());
+        if (rc == TSDFL_OK) rc = tsdfl_map_create_codes(ctx.get(), &coef, grid_occ, codes, sigma, flags, &m->h_);
+        if (rc == TSDFL_OK && free_xyz) free_xyz->assign(free_cells, free_cells + 3 * n_free);
+        tsdfl_free(grid_occ);
+        tsdfl_free(codes);
+        tsdfl_free(free_cells);
+        check(rc);
+        return m;
+    }
+
 private:
+    Map() = default;
     tsdfl_map* h_ = nullptr;
 };
 

@@ -7,8 +7,10 @@ callers.  Build with `python -c "import __graft_entry__ as g; g.build()"`.
 from ._native import TsdflError
 from .evaluator import (Context, DeviceMap, FilterBatch, LocalizationServer, MetropolisResampler, MotionModel, Pose, RejectionResampler,
                         ResidualResampler, ResidualSystematicResampler, ScanReducer, SystematicResampler,
-                        TSDFEvaluator, WheelResampler, build_map_codes, code_values, pack_cloud, pose_array)
+                        TSDFEvaluator, WheelResampler, build_map_codes, code_values, load_map_h5, pack_cloud,
+                        pose_array, read_map_h5)
 
 __all__ = ["Context", "DeviceMap", "FilterBatch", "LocalizationServer", "MetropolisResampler", "MotionModel", "Pose", "RejectionResampler",
            "ResidualResampler", "ResidualSystematicResampler", "ScanReducer", "SystematicResampler", "TSDFEvaluator",
-           "TsdflError", "WheelResampler", "build_map_codes", "code_values", "pack_cloud", "pose_array"]
+           "TsdflError", "WheelResampler", "build_map_codes", "code_values", "load_map_h5", "pack_cloud", "pose_array",
+           "read_map_h5"]

@@ -57,7 +57,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     inc = ["-I", str(ROOT / "include"), "-I", str(CSRC)]
     headers = sorted(CSRC.glob("*.h")) + [ROOT / "include" / "tsdfl.h"]
     cu = sorted(CSRC.glob("*.cu"))
-    cpp_lib = [CSRC / "map_build.cpp", CSRC / "motion_model.cpp"]
+    cpp_lib = [CSRC / "map_build.cpp", CSRC / "motion_model.cpp", CSRC / "h5_map.cpp"]
     jobs = []
     objs = []
     for src in cu:

@@ -105,6 +105,7 @@ SIGNATURES = [
     ("tsdfl_build_map_codes", I, [P, P, SZ, I, I, F, C.POINTER(MapCoef), C.POINTER(P), C.POINTER(P),
                                   C.POINTER(P), C.POINTER(SZ)]),
     ("tsdfl_code_values", I, [F, F, P]),
+    ("tsdfl_read_map_h5", I, [C.c_char_p, C.POINTER(P), C.POINTER(P), C.POINTER(SZ), C.POINTER(C.c_int32)]),
     ("tsdfl_free", None, [P]),
     ("tsdfl_evaluate", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, C.c_uint32, P]),
     ("tsdfl_evaluate_debug", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, C.c_uint32, P, C.POINTER(EvalDebug)]),

@@ -617,3 +617,35 @@ def build_map_codes(chunk_pos: np.ndarray, chunks: np.ndarray, edge: int, voxel_
         if want_free:
             lib.tsdfl_free(fr)
     return coef, grid_occ, codes, free_xyz
+
+
+def read_map_h5(path) -> tuple[np.ndarray, np.ndarray, int]:
+    """The TSDF chunks of a map file in the reference's HDF5 layout (group
+    "/map", one dataset of edge^3 raw cells per chunk named "<x>_<y>_<z>";
+    global_map.cpp, map_util.h:17-113), read without the HDF5 library:
+    (chunk_pos (n, 3) int32, chunks (n, edge^3) uint32, edge), in the order
+    createTSDFMap visits them."""
+    lib = N.lib()
+    pos = C.c_void_p()
+    raw = C.c_void_p()
+    n = C.c_size_t()
+    edge = C.c_int32()
+    N.check(lib.tsdfl_read_map_h5(str(path).encode(), C.byref(pos), C.byref(raw), C.byref(n), C.byref(edge)))
+    try:
+        cells = edge.value ** 3
+        k = n.value
+        p = np.ctypeslib.as_array(C.cast(pos, C.POINTER(C.c_int32)), (max(k, 1) * 3,))[: 3 * k]
+        r = np.ctypeslib.as_array(C.cast(raw, C.POINTER(C.c_uint32)), (max(k * cells, 1),))[: k * cells]
+        return p.reshape(k, 3).copy(), r.reshape(k, cells).copy(), edge.value
+    finally:
+        lib.tsdfl_free(pos)
+        lib.tsdfl_free(raw)
+
+
+def load_map_h5(ctx: Context, path, voxel_mm: int = 64, sigma: float = 0.1, dense: bool = True):
+    """createTSDFMap (map_util.h:17-154) from a map file: the device map and the
+    free-space cell positions.  voxel_mm is the map's resolution in millimetres
+    (MAP_RESOLUTION, 64 in the reference)."""
+    chunk_pos, chunks, edge = read_map_h5(path)
+    coef, grid_occ, codes, free_xyz = build_map_codes(chunk_pos, chunks, edge, voxel_mm, sigma)
+    return DeviceMap(ctx, coef, grid_occ, codes=codes, sigma=sigma, dense=dense), free_xyz
