@@ -155,3 +155,25 @@ def test_empty_map_group(tmp_path):
     H.write(p, {})
     pos, raw, edge = read_map_h5(p)
     assert pos.shape == (0, 3) and raw.shape[0] == 0 and edge == 0
+
+
+@pytest.mark.parametrize("fmt", ["v0", "v2"])
+def test_corrupted_files_fail_cleanly(tmp_path, fmt):
+    """Random byte corruptions of a valid file: every read either succeeds or
+    raises TsdflError (never crashes, hangs or returns garbage shapes)."""
+    p = tmp_path / "x.h5"
+    H.write(p, _chunks(NAMES[:9], 2, 3), fmt=fmt, leaf_k=2, internal_k=2)
+    good = p.read_bytes()
+    rng = np.random.default_rng(17)
+    for trial in range(300):
+        data = bytearray(good)
+        for _ in range(int(rng.integers(1, 6))):
+            i = int(rng.integers(0, len(data)))
+            data[i] = int(rng.integers(0, 256)) if trial % 3 else data[i] ^ 0xFF
+        p.write_bytes(bytes(data))
+        try:
+            pos, raw, edge = read_map_h5(p)
+        except TsdflError as e:
+            assert e.code in (N.TSDFL_ERR_INVALID_ARG, N.TSDFL_ERR_UNSUPPORTED, N.TSDFL_ERR_OUT_OF_MEMORY)
+            continue
+        assert pos.shape == (raw.shape[0], 3) and (raw.shape[0] == 0 or raw.shape[1] == edge ** 3)

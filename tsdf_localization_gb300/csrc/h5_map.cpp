@@ -37,8 +37,10 @@ namespace tsdfl {
 namespace {
 
 constexpr uint64_t kUndef = ~0ull;
-constexpr int kMaxDepth = 64;            // B-tree levels / continuation chains followed
+constexpr int kMaxDepth = 64;            // B-tree levels followed
 constexpr size_t kMaxBlocks = 1u << 16;  // continuation blocks of one object header
+constexpr size_t kMaxNodes = 1u << 20;   // B-tree and symbol table nodes visited per group
+constexpr uint64_t kMaxCells = 1ull << 32;   // cells of one chunk that has no stored data
 
 struct H5Error {
     int code;
@@ -350,6 +352,8 @@ public:
             fail(TSDFL_ERR_INVALID_ARG, "dataset storage smaller than its dataspace");
         if (info.address != kUndef && (info.address > size_ || 4 * info.count > size_ - info.address))
             fail(TSDFL_ERR_INVALID_ARG, "dataset storage outside the file");
+        if (info.address == kUndef && info.compact.empty() && info.count > kMaxCells)
+            fail(TSDFL_ERR_INVALID_ARG, "dataset without storage larger than a chunk can be");
         return info;
     }
 
@@ -423,15 +427,18 @@ private:
         if (std::memcmp(h, "HEAP", 4) != 0) fail(TSDFL_ERR_INVALID_ARG, "bad local heap");
         const uint64_t dsize = len(h + 8);
         const uint64_t daddr = addr(h + 8 + 2 * sl_);
+        if (dsize > size_) fail(TSDFL_ERR_INVALID_ARG, "local heap larger than the file");
         std::vector<uint8_t> names((size_t)dsize);
         if (dsize) read(at(daddr), names.data(), names.size());
-        if (btree != kUndef) btree_node(btree, names, out, 0);
+        size_t visited = 0;
+        if (btree != kUndef) btree_node(btree, names, out, 0, visited);
     }
 
     void btree_node(uint64_t node, const std::vector<uint8_t>& names,
-                    std::vector<std::pair<std::string, uint64_t>>& out, int depth) const
+                    std::vector<std::pair<std::string, uint64_t>>& out, int depth, size_t& visited) const
     {
         if (depth > kMaxDepth) fail(TSDFL_ERR_INVALID_ARG, "B-tree too deep");
+        if (++visited > kMaxNodes) fail(TSDFL_ERR_INVALID_ARG, "B-tree with too many nodes");
         const uint64_t pos = at(node);
         const size_t hdr = 8 + 2 * (size_t)so_;
         uint8_t h[24];
@@ -445,8 +452,12 @@ private:
         read(pos + hdr, kc.data(), kc.size());
         for (size_t i = 0; i < entries; ++i) {
             const uint64_t c = addr(kc.data() + i * step + sl_);
-            if (level > 0) btree_node(c, names, out, depth + 1);
-            else symbol_node(c, names, out);
+            if (level > 0) {
+                btree_node(c, names, out, depth + 1, visited);
+            } else {
+                if (++visited > kMaxNodes) fail(TSDFL_ERR_INVALID_ARG, "B-tree with too many nodes");
+                symbol_node(c, names, out);
+            }
         }
     }
 
@@ -565,6 +576,8 @@ extern "C" int tsdfl_read_map_h5(const char* path, int32_t** chunk_pos, uint32_t
                 fail(TSDFL_ERR_INVALID_ARG, "chunks of " + std::to_string(count) + " cells are not cubes");
         }
         const size_t n = items.size();
+        if (n && (uint64_t)count > (uint64_t)(SIZE_MAX / sizeof(uint32_t)) / n)
+            fail(TSDFL_ERR_OUT_OF_MEMORY, "map larger than the address space");
         pos = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * 3 * (n ? n : 1)));
         raw = static_cast<uint32_t*>(std::malloc(sizeof(uint32_t) * (n ? n * (size_t)count : 1)));
         if (!pos || !raw) fail(TSDFL_ERR_OUT_OF_MEMORY, "out of host memory");
