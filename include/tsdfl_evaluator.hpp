@@ -16,6 +16,8 @@
  *   tsdf_localization::GpuWheelResampler, GpuResidualResampler,
  *       GpuMetropolisResampler, GpuRejectionResampler replace the other
  *       resamplers mcl_3d selects (mcl_3d.cpp:246-261)
+ *   tsdfl::Map::from_h5 replaces createTSDFMap's loading of the map file
+ *       (include/tsdf_localization/map/map_util.h:17-154) without HDF5
  *
  * Errors surface as std::runtime_error carrying libtsdfl's message, as the
  * reference's evaluators throw them ("No particle is valid!" for a zero
