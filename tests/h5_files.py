@@ -170,10 +170,13 @@ def _link_group(w: _Buf, children: dict[str, int], dense=False) -> int:
 
 
 def write(path, chunks: dict[str, Dataset], fmt: str = "v0", leaf_k: int = 4, internal_k: int = 16,
-          userblock: int = 0, extra_groups: bool = True, group_name: str = "map", dense_group: bool = False) -> None:
+          userblock: int = 0, extra_groups: bool = True, group_name: str = "map", dense_group: bool = False,
+          superblock: int | None = None) -> None:
     """A map file: group /<group_name> with one dataset per chunk name (in the
-    dict's order), and an unrelated /poses group."""
-    w = _Buf(96 if fmt == "v0" else 48)
+    dict's order), and an unrelated /poses group.  superblock: version 0 or 1
+    for fmt "v0", 2 or 3 for fmt "v2"."""
+    sbv = superblock if superblock is not None else (0 if fmt == "v0" else 2)
+    w = _Buf(100 if fmt == "v0" else 48)
     v2 = fmt == "v2"
     headers = {}
     for nm, ds in chunks.items():
@@ -188,7 +191,7 @@ def write(path, chunks: dict[str, Dataset], fmt: str = "v0", leaf_k: int = 4, in
             root_children["poses"] = _link_group(w, {"0": pose_hdr})
         root = _link_group(w, root_children)
         eof = len(w.b)
-        w.put(0, SIGNATURE + struct.pack("<BBBB", 2, 8, 8, 0) + struct.pack("<QQQQ", 0, UNDEF, eof, root) + b"\0" * 4)
+        w.put(0, SIGNATURE + struct.pack("<BBBB", sbv, 8, 8, 0) + struct.pack("<QQQQ", 0, UNDEF, eof, root) + b"\0" * 4)
     else:
         grp, _, _ = _symbol_group(w, headers, leaf_k, internal_k)
         root_children = {group_name: grp}
@@ -196,14 +199,16 @@ def write(path, chunks: dict[str, Dataset], fmt: str = "v0", leaf_k: int = 4, in
             root_children["poses"] = _symbol_group(w, {"0": pose_hdr}, leaf_k, internal_k)[0]
         root, rtree, rheap = _symbol_group(w, root_children, leaf_k, internal_k)
         eof = len(w.b)
-        sb = SIGNATURE + struct.pack("<8B", 0, 0, 0, 0, 0, 8, 8, 0) + struct.pack("<HHI", leaf_k, internal_k, 0)
+        sb = SIGNATURE + struct.pack("<8B", sbv, 0, 0, 0, 0, 8, 8, 0) + struct.pack("<HHI", leaf_k, internal_k, 0)
+        if sbv == 1:   # indexed storage internal node K, reserved
+            sb += struct.pack("<HH", 32, 0)
         sb += struct.pack("<QQQQ", 0, UNDEF, eof, UNDEF)
         sb += struct.pack("<QQII", 0, root, 1, 0) + struct.pack("<QQ", rtree, rheap)
         w.put(0, sb)
     data = bytes(w.b)
     if userblock:   # a user block before the superblock; addresses stay relative to it
         data = b"\0" * userblock + data
-        base_field = 24 if fmt == "v0" else 12
+        base_field = {0: 24, 1: 28}.get(sbv, 12)
         data = bytearray(data)
         data[userblock + base_field:userblock + base_field + 8] = struct.pack("<Q", userblock)
         data = bytes(data)

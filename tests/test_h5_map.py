@@ -32,13 +32,13 @@ NAMES = ["0_0_0", "1_0_0", "10_0_0", "2_0_0", "-1_0_2", "0_-3_1", "3_3_3", "0_1_
          "5_0_-1", "0_0_1", "4_4_0", "7_1_2", "0_2_2", "1_2_3", "6_6_6", "-1_-1_0", "2_2_0", "9_9_1"]
 
 
-@pytest.mark.parametrize("fmt", ["v0", "v2"])
+@pytest.mark.parametrize("fmt,superblock", [("v0", 0), ("v0", 1), ("v2", 2), ("v2", 3)])
 @pytest.mark.parametrize("userblock", [0, 512])
-def test_reads_chunks_in_listing_order(tmp_path, fmt, userblock):
+def test_reads_chunks_in_listing_order(tmp_path, fmt, superblock, userblock):
     chunks = _chunks(NAMES, 4, 1)
     path = tmp_path / f"map_{fmt}.h5"
     # small B-tree nodes (4 symbols per leaf, 4 children per node): a two-level tree
-    H.write(path, chunks, fmt=fmt, leaf_k=2, internal_k=2, userblock=userblock)
+    H.write(path, chunks, fmt=fmt, leaf_k=2, internal_k=2, userblock=userblock, superblock=superblock)
     pos, raw, edge = read_map_h5(path)
     epos, eraw = _expected(chunks)
     assert edge == 4
