@@ -69,8 +69,11 @@ def oracle() -> C.CDLL:
         L.orc_likelihood_value.argtypes = [C.c_int16, C.c_float]
         L.orc_likelihood_init.restype = C.c_float
         L.orc_likelihood_init.argtypes = [C.c_float]
-        L.orc_build_map_from_chunks.argtypes = [P, P, SZ, C.c_int, C.c_float, C.POINTER(Coef), C.POINTER(P),
-                                                C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
+        L.orc_build_map_from_chunks.argtypes = [P, P, SZ, C.c_int, C.c_int, C.c_float, C.POINTER(Coef),
+                                                C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(SZ)]
+        L.orc_chunk_tuples.restype = SZ
+        L.orc_chunk_tuples.argtypes = [P, P, SZ, C.c_int, C.c_int, C.c_float, P, P, P, C.POINTER(P), C.POINTER(P),
+                                       C.POINTER(SZ)]
         L.orc_resample_systematic.restype = SZ
         L.orc_resample_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
         L.orc_resample_wheel.restype = None
@@ -181,14 +184,17 @@ class OracleMap:
         return m
 
     @staticmethod
-    def from_chunks(chunk_pos: np.ndarray, chunks: np.ndarray, voxel_mm: int = 64, sigma: float = 0.1):
+    def from_chunks(chunk_pos: np.ndarray, chunks: np.ndarray, voxel_mm: int = 64, sigma: float = 0.1,
+                    edge: int = 64):
+        """createTSDFMap (map_util.h:17-154) on chunks of edge^3 cells (the
+        reference's CHUNK_SIZE is 64): (map, free-space cells)."""
         L = oracle()
         c = Coef()
         go, dp, fp = P(), P(), P()
         nf = SZ()
         pos = np.ascontiguousarray(chunk_pos, np.int32)
         raw = np.ascontiguousarray(chunks, np.uint32)
-        rc = L.orc_build_map_from_chunks(_ptr(pos), _ptr(raw), pos.shape[0], voxel_mm, sigma, C.byref(c),
+        rc = L.orc_build_map_from_chunks(_ptr(pos), _ptr(raw), pos.shape[0], edge, voxel_mm, sigma, C.byref(c),
                                          C.byref(go), C.byref(dp), C.byref(fp), C.byref(nf))
         if rc != 0:
             raise RuntimeError("Upper voxel index overflow!")
@@ -476,6 +482,32 @@ def ref_reduce_scan(xyz: np.ndarray, ring: np.ndarray, cell: float = 0.064) -> n
     out = np.zeros((max(x.shape[0], 1), 3), np.float32)
     n = reference().ref_reduce_scan(_ptr(x), _ptr(r), x.shape[0], np.float32(cell), _ptr(out), out.shape[0])
     return out[:n].copy()
+
+
+def chunk_tuples(chunk_pos: np.ndarray, chunks: np.ndarray, voxel_mm: int = 64, sigma: float = 0.1,
+                 edge: int = 64) -> dict:
+    """createTSDFMap up to its setData call (map_util.h:17-147): bounding box,
+    init value, the (x, y, z, value) tuples in push order, free-space cells."""
+    L = oracle()
+    pos = np.ascontiguousarray(chunk_pos, np.int32)
+    raw = np.ascontiguousarray(chunks, np.uint32)
+    mn = np.zeros(3, np.float32)
+    mx = np.zeros(3, np.float32)
+    init = np.zeros(1, np.float32)
+    tp, fp = P(), P()
+    nf = SZ()
+    n = L.orc_chunk_tuples(_ptr(pos), _ptr(raw), pos.shape[0], edge, voxel_mm, sigma, _ptr(mn), _ptr(mx),
+                           _ptr(init), C.byref(tp), C.byref(fp), C.byref(nf))
+    libc = C.CDLL(None)
+    try:
+        t = np.ctypeslib.as_array(C.cast(tp, C.POINTER(C.c_float)), (max(n, 1) * 4,))[: 4 * n].reshape(-1, 4).copy()
+        f = np.ctypeslib.as_array(C.cast(fp, C.POINTER(C.c_float)), (max(nf.value, 1) * 3,))[
+            : 3 * nf.value].reshape(-1, 3).copy()
+    finally:
+        for p in (tp, fp):
+            if p.value:
+                libc.free(p)
+    return {"min": mn, "max": mx, "init": float(init[0]), "tuples": t, "free": f}
 
 
 def likelihood_value(mm: int, sigma: float = 0.1) -> float:

@@ -276,13 +276,16 @@ static int cmp_tag(const void* a, const void* b)
     return strcmp(((const chunk_tag*)a)->name, ((const chunk_tag*)b)->name);
 }
 
-/* map_util.h:17-154 (HighFive lists "/map" members in increasing name order) */
-int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks,
-                              int voxel_mm, float sigma, orc_map_coef* c, int32_t** grid_occ_out,
-                              float** data_out, float** free_xyz_out, size_t* n_free_out)
+/* map_util.h:17-151 up to the setData call (HighFive lists "/map" members in
+ * increasing name order): the bounding box, the init value, the (x, y, z, value)
+ * tuples of touched cells with |tsdf| < 600 and the free-space cells, in the
+ * order the reference pushes them.  CH is the reference's CHUNK_SIZE. */
+static void chunk_tuples(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int CH,
+                         int voxel_mm, float sigma, float mn[3], float mx[3], float* init_out,
+                         float** tuples_out, size_t* n_out, float** free_out, size_t* nf_out)
 {
-    const int CH = 64;
-    float mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    mn[0] = mn[1] = mn[2] = 0.0f;
+    mx[0] = mx[1] = mx[2] = 0.0f;
     for (size_t k = 0; k < n_chunks; ++k)
         for (int a = 0; a < 3; ++a) {
             int coord = chunk_pos[3 * k + a];
@@ -293,8 +296,7 @@ int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, 
         mn[a] = (float)((double)(mn[a] * (float)CH * (float)voxel_mm) * 0.001);
         mx[a] = (float)((double)((mx[a] * (float)CH + (float)CH) * (float)voxel_mm) * 0.001);
     }
-    float init = orc_likelihood_init(sigma);
-    orc_map_coef_init(c, mn, mx, (float)(voxel_mm * 0.001), init);
+    *init_out = orc_likelihood_init(sigma);
 
     float lut[600];
     for (int v = 0; v < 600; ++v) lut[v] = orc_likelihood_value((int16_t)v, sigma);
@@ -312,7 +314,7 @@ int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, 
     float* freep = (float*)malloc(sizeof(float) * 3 * fcap);
     for (size_t t = 0; t < n_chunks; ++t) {
         size_t k = tags[t].index;
-        const uint32_t* raw = chunks + (size_t)k * CH * CH * CH;
+        const uint32_t* raw = chunks + (size_t)k * (size_t)(CH * CH * CH);
         const int32_t* cp = chunk_pos + 3 * k;
         for (int i = 0; i < CH; i++)
             for (int j = 0; j < CH; j++)
@@ -340,14 +342,40 @@ int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, 
                 }
     }
     free(tags);
+    *tuples_out = tuples;
+    *n_out = n;
+    *free_out = freep;
+    *nf_out = nf;
+}
+
+size_t orc_chunk_tuples(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
+                        int voxel_mm, float sigma, float mn[3], float mx[3], float* init_out,
+                        float** tuples_out, float** free_xyz_out, size_t* n_free_out)
+{
+    size_t n = 0;
+    chunk_tuples(chunk_pos, chunks, n_chunks, edge, voxel_mm, sigma, mn, mx, init_out, tuples_out, &n,
+                 free_xyz_out, n_free_out);
+    return n;
+}
+
+/* map_util.h:17-154: the tuples above, then the CudaSubVoxelMap ctor
+ * (map_util.h:73) and setData (:151). */
+int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
+                              int voxel_mm, float sigma, orc_map_coef* c, int32_t** grid_occ_out,
+                              float** data_out, float** free_xyz_out, size_t* n_free_out)
+{
+    float mn[3], mx[3], init;
+    float* tuples = NULL;
+    size_t n = 0;
+    chunk_tuples(chunk_pos, chunks, n_chunks, edge, voxel_mm, sigma, mn, mx, &init, &tuples, &n, free_xyz_out,
+                 n_free_out);
+    orc_map_coef_init(c, mn, mx, (float)(voxel_mm * 0.001), init);
     int32_t* grid_occ = (int32_t*)malloc(sizeof(int32_t) * (c->grid_occ_size ? c->grid_occ_size : 1));
     float* data = NULL;
     int rc = orc_map_set_data(c, grid_occ, tuples, n, &data, NULL);
     free(tuples);
     *grid_occ_out = grid_occ;
     *data_out = data;
-    *free_xyz_out = freep;
-    *n_free_out = nf;
     return rc;
 }
 

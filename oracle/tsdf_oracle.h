@@ -86,14 +86,24 @@ float orc_likelihood_value(int16_t tsdf_mm, float sigma);
 float orc_likelihood_init(float sigma);
 
 /* createTSDFMap (map_util.h:17-154) without HDF5.  chunk_pos: 3 ints per chunk
- * (chunk coordinates), chunks: n_chunks blocks of 64^3 uint32 raw TSDF values
+ * (chunk coordinates), chunks: n_chunks blocks of edge^3 uint32 raw TSDF values
  * (low int16 = value in mm, high int16 = weight, tsdf.h:11-33) in the order the
- * file lists them.  voxel_mm generalises the fixed 64 mm MAP_RESOLUTION.
+ * file lists them.  edge generalises the fixed CHUNK_SIZE (64, grid_map.h:18-19)
+ * and voxel_mm the fixed 64 mm MAP_RESOLUTION (grid_map.h:21-22).
  * Outputs the map coef, a malloc'd grid_occ, a malloc'd data array and the
  * free-space point list (malloc'd xyz triples). */
-int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks,
+int orc_build_map_from_chunks(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
                               int voxel_mm, float sigma, orc_map_coef* c, int32_t** grid_occ_out,
                               float** data_out, float** free_xyz_out, size_t* n_free_out);
+
+/* The part of createTSDFMap before the map is made (map_util.h:17-147): the
+ * bounding box mn/mx, the init value and the (x, y, z, value) tuples it hands
+ * to setData, in push order (malloc'd, 4 floats each; returned count), plus the
+ * free-space cells.  Feeding the tuples to the reference's own ctor + setData
+ * gives the reference's map for the same chunks. */
+size_t orc_chunk_tuples(const int32_t* chunk_pos, const uint32_t* chunks, size_t n_chunks, int edge,
+                        int voxel_mm, float sigma, float mn[3], float mx[3], float* init_out,
+                        float** tuples_out, float** free_xyz_out, size_t* n_free_out);
 
 /* SystematicResampler::resample (novel_resampling.h:41-72) with the uniform
  * draw U0 supplied.  Writes up to cap source indices, returns the number of
