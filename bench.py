@@ -22,6 +22,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -95,11 +96,12 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        fd, name = tempfile.mkstemp(prefix="tsdfl_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
@@ -172,6 +174,36 @@ def cpu_baseline(wl, target_s: float = 10.0) -> dict:
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{P_s} particles x {N} points, one update + resample, {dt:.2f} s"}, (P_s, kind, om,
                                                                                              rm if kind == "reference" else None)
+
+
+def accuracy_vs_fp64(om, wl, dmap, n: int = 4000) -> dict:
+    """Errors of the device's weights against FP64 on a particle sample (every
+    (P/n)-th particle of the step): the oracle scores the same particles with
+    per-particle sums in double; the reference's own float sums are reported
+    beside ours.  Also whether hit counts agree and the mean pose's distance
+    from the FP64 mean."""
+    from oracle import oracle_py as O
+    from tsdf_localization_gb300 import TSDFEvaluator
+    P = wl.particles.shape[0]
+    parts = np.ascontiguousarray(wl.particles[:: max(1, P // n)][:n])
+    ref = O.evaluate(om, parts.copy(), wl.points, wl.tf)
+    p = parts.copy()
+    d = TSDFEvaluator(dmap).evaluate_debug(p, wl.points, wl.tf)
+    f64 = ref["sum64"]
+    w64 = f64 / f64.sum()
+    rel = np.abs(d["raw"].astype(np.float64) - f64) / f64
+    rel_ref = np.abs(ref["raw"].astype(np.float64) - f64) / f64
+    rel_w = np.abs(p[:, 6].astype(np.float64) - w64) / w64
+    q = parts.astype(np.float64)
+    mean64 = np.concatenate([(q[:, :3] * w64[:, None]).sum(0),
+                             [np.arctan2((np.sin(q[:, k]) * w64).sum(), (np.cos(q[:, k]) * w64).sum())
+                              for k in (3, 4, 5)]])
+    return {"particles": int(parts.shape[0]), "points": int(wl.points.shape[0]),
+            "max_rel_raw_weight": float(rel.max()), "max_rel_normalised_weight": float(rel_w.max()),
+            "reference_float_sum_max_rel": float(rel_ref.max()),
+            "hits_equal_oracle": bool(np.array_equal(d["hits"], ref["hits"])),
+            "mean_pose_max_abs_err": float(np.abs(d["pose"].astype(np.float64) - mean64).max()),
+            "tolerance": 1e-5}
 
 
 def _reference_map(O, wl):
@@ -810,7 +842,9 @@ def main():
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
-        base, _ = cpu_baseline(wl)
+        base, (_, _, om, _) = cpu_baseline(wl)
+        base["error_vs_fp64"] = accuracy_vs_fp64(om, wl, dmap)
+        del om
     scan = motion = tracking = None
     if not args.no_scan:
         scan = scan_reduction_side(lib, ctx, stream, wl, f"cuda:{local}", rank == 0 and not args.no_cpu_baseline)

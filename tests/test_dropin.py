@@ -1,14 +1,14 @@
 """The C++ drop-in plug-ins (include/tsdfl_evaluator.hpp) compile against the
 reference's own Evaluator/Resampler headers and link with libtsdfl; without a
 GPU they report the failure as std::runtime_error, as the reference does."""
-import os
 import subprocess
 from pathlib import Path
 
 import pytest
 
+from tsdf_localization_gb300._build import REFERENCE
+
 ROOT = Path(__file__).resolve().parent.parent
-REFERENCE = Path(os.environ.get("TSDFL_REFERENCE_DIR", "/root/reference"))
 
 
 @pytest.mark.skipif(not (REFERENCE / "include" / "tsdf_localization").exists(),

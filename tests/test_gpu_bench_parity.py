@@ -1,0 +1,153 @@
+"""GPU parity on the workloads the bench reports, against the oracle.
+
+- the 100x100x10 m building at 0.05 m with 100,000 Gaussian particles x 8,192
+  points (compact layout, two-term sub-voxel multiplier, layer-0 skirts, the
+  compact-cloud scan order): a particle sample against the oracle, and all
+  100,000 particles across the two scoring kernels;
+- global localisation on the seed-3 building: 1,000,000 particles uniform over
+  free space (any yaw, the spread-cloud scan order) x 2,048 points, a sample
+  against the oracle; systematic resampling of the device's own normalised
+  weights at 1M bit for bit, and at 1M with weights below 2^-29 (the
+  binade-by-binade double sums).
+
+Bars (as in test_gpu_parity.py): slot codes and hit counts bit-exact; serial
+raw weights bit-exact; exact-mode weights within 1e-5 of the FP64 sums and no
+farther from them than the reference's float sums plus that bound; resampled
+indices bit-exact.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle_py as O
+from tsdf_localization_gb300 import Context, DeviceMap, SystematicResampler, TSDFEvaluator, synth
+
+pytestmark = pytest.mark.gpu
+
+WEIGHT_RTOL = 1e-5
+SAMPLE = 4000
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def building():
+    return synth.building_workload(seed=2, n_particles=100_000, n_points=8192)
+
+
+@pytest.fixture(scope="module")
+def global_wl():
+    return synth.global_workload(seed=3, n_particles=1_000_000, n_points=2048)
+
+
+def _codes_of(ref_idx, codes, data_size):
+    hit = ref_idx < data_size
+    return np.where(hit, codes[np.minimum(ref_idx, data_size - 1)], 601).astype(np.uint32)
+
+
+def _check_against_oracle(ctx, wl, parts, serial_n):
+    """Compact layout: tiled kernel (debug and production instantiations) and
+    serial kernel against the oracle on the given particles."""
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True)
+    info = dmap.info()
+    assert info["dense"] == 1 and info["fast_index"] in (1, 2)
+    om = O.OracleMap(O.coef_from(wl.coef), wl.grid_occ, wl.float_data())
+    p_ref = parts.copy()
+    ref = O.evaluate(om, p_ref, wl.points, wl.tf, want_idx=True)
+    assert ref["rc"] == 0
+    f64 = ref["sum64"]
+    ev = TSDFEvaluator(dmap)
+    p = parts.copy()
+    d = ev.evaluate_debug(p, wl.points, wl.tf, voxel_index=True)
+    assert np.array_equal(d["hits"], ref["hits"])
+    want_codes = _codes_of(ref["voxel_index"], wl.codes, wl.coef.data_size)
+    assert np.array_equal(d["voxel_index"] & 0xFFFF, want_codes)
+    err_gpu = np.abs(d["raw"].astype(np.float64) - f64)
+    err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
+    assert np.all(err_gpu <= WEIGHT_RTOL * f64)
+    assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
+    w64 = f64 / f64.sum()
+    assert np.all(np.abs(p[:, 6].astype(np.float64) - w64) <= WEIGHT_RTOL * w64)
+    # the production (debug-free) instantiation gives the same sums
+    p2 = parts.copy()
+    d2 = ev.evaluate_debug(p2, wl.points, wl.tf)
+    assert np.array_equal(d2["raw"], d["raw"]) and np.array_equal(d2["hits"], d["hits"])
+    assert np.array_equal(p2[:, 6], p[:, 6])
+    # serial mode: the reference's point-order float sums, bit for bit
+    sub = parts[:serial_n].copy()
+    ref_s = O.evaluate(om, sub.copy(), wl.points, wl.tf)
+    ds = TSDFEvaluator(dmap, serial_sums=True).evaluate_debug(sub, wl.points, wl.tf)
+    assert np.array_equal(ds["raw"], ref_s["raw"])
+    assert np.array_equal(ds["hits"], ref_s["hits"])
+    return {"max_rel": float((err_gpu / f64).max()), "ref_max_rel": float((err_ref / f64).max()),
+            "hits": d["hits"]}
+
+
+def test_building_sample_matches_oracle(ctx, building):
+    """C2's map, scan and particle cloud: every 25th of the 100,000 particles."""
+    parts = np.ascontiguousarray(building.particles[:: building.particles.shape[0] // SAMPLE][:SAMPLE])
+    ext = parts[:, :2].max(0) - parts[:, :2].min(0)
+    assert ext.max() < 10.0   # the compact-cloud scan order
+    r = _check_against_oracle(ctx, building, parts, serial_n=500)
+    assert r["max_rel"] <= 1e-6   # exact sums: far inside the bound
+    assert r["hits"].mean() > 0.5 * building.points.shape[0]
+
+
+def test_building_full_size_kernels_agree(ctx, building):
+    """All 100,000 x 8,192: the tiled kernel on the compact layout and the
+    generic kernel on the brick table give identical fixed-point sums (so
+    identical weights and hit counts), and the weights sum to 1."""
+    compact = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, dense=True)
+    brick = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, dense=False)
+    a = TSDFEvaluator(compact).evaluate_debug(building.particles.copy(), building.points, building.tf)
+    pb = building.particles.copy()
+    b = TSDFEvaluator(brick, generic=True).evaluate_debug(pb, building.points, building.tf)
+    assert np.array_equal(a["raw"], b["raw"]) and np.array_equal(a["hits"], b["hits"])
+    assert abs(float(pb[:, 6].astype(np.float64).sum()) - 1.0) < 1e-4
+
+
+def test_global_sample_matches_oracle(ctx, global_wl):
+    """C3: uniform particles over the whole building (the spread-cloud order)."""
+    parts = np.ascontiguousarray(global_wl.particles[:: global_wl.particles.shape[0] // SAMPLE][:SAMPLE])
+    ext = parts[:, :2].max(0) - parts[:, :2].min(0)
+    assert ext.max() > 10.0   # the spread-cloud scan order
+    _check_against_oracle(ctx, global_wl, parts, serial_n=500)
+
+
+def test_global_resample_of_device_weights(ctx, global_wl):
+    """C3's step: all 1,000,000 particles scored, then systematic resampling of
+    the device's normalised weights, bit for bit against the oracle."""
+    dmap = DeviceMap(ctx, global_wl.coef, global_wl.grid_occ, codes=global_wl.codes, dense=True)
+    p = global_wl.particles.copy()
+    TSDFEvaluator(dmap).evaluate(p, global_wl.points, global_wl.tf)
+    w = np.ascontiguousarray(p[:, 6])
+    rs = SystematicResampler(ctx, seed=5)
+    for u0 in (rs.draw(w.shape[0]), 0.0, float(np.float32(0.5e-6))):
+        got = rs.resample_indices(w, u0)
+        assert np.array_equal(got, O.resample_systematic(w, u0))
+
+
+@pytest.mark.parametrize("kind", ["c3", "mixed"])
+def test_resample_1m_tiny_weights(ctx, kind):
+    """1,000,000 weights, most of them below 2^-29: the serial double sums round,
+    and the device forms them binade by binade."""
+    m = 1_000_000
+    rng = np.random.default_rng(77 if kind == "c3" else 78)
+    if kind == "c3":   # 999,000 misses and 1,000 particles on the surface
+        w = np.ones(m)
+        w[rng.choice(m, 1000, replace=False)] = 1e6 * (1 + rng.random(1000))
+    else:
+        w = rng.random(m)
+        w[rng.random(m) < 0.6] *= 1e-5
+    w = (w / w.sum()).astype(np.float32)
+    assert (w < 2.0 ** -29).mean() > 0.5
+    rs = SystematicResampler(ctx, seed=m)
+    for u0 in (rs.draw(m), 0.0, float(np.nextafter(np.float32(1.0 / m), np.float32(0)))):
+        got = rs.resample_indices(w, u0)
+        exp = O.resample_systematic(w, u0)
+        assert got.shape == exp.shape
+        assert np.array_equal(got, exp)
