@@ -28,8 +28,18 @@ using namespace tsdfl;
 static uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 static float fof(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
-// Division-free sub-voxel index as the tiled kernel computes it: mode 2
-// floor of the exact product s * hi; mode 1 trunc(fl(fma(s, hi, fl(s * lo)))).
+// fl(x + m) rounded toward zero (add.rz), for x >= 0 (or any x with x + m > 0):
+// the exact sum in double, then truncated to float
+static float rz_add(float x, float m)
+{
+    const double d = (double)x + (double)m;
+    float f = (float)d;
+    if ((double)f > d) f = std::nextafter(f, 0.0f);
+    return f;
+}
+
+// Division-free sub-voxel index: mode 2 floor of the exact product s * hi;
+// mode 1 trunc(fl(fma(s, hi, fl(s * lo)))).
 static int64_t fast_sub_index(int mode, float s, float hi, float lo)
 {
     if (mode == 2) return (int64_t)std::floor((double)s * (double)hi);
@@ -95,6 +105,25 @@ int main(int argc, char** argv)
             v.up_dim_x64 = c.up_dim_x; v.up_dim_2_64 = c.up_dim_2; v.grid_occ_size64 = c.grid_occ_size;
             v.sub_dim64 = c.sub_dim; v.sub_dim_2_64 = c.sub_dim_2; v.data_size64 = c.data_size;
             v.sub_fast = sub_index_mult(res, c.sub_dim, &v.sub_inv, &v.sub_inv_lo);
+            // the tiled path's conditions and constants (fill_view): compact
+            // bitmap pairs {word, allocated bricks up to and including it}
+            const uint32_t v_lim_x = v.lim_x, v_lim_y = v.lim_y;
+            const float zhi = v.mmax_z < 0 ? 0.0f : (float)std::min<int64_t>((int64_t)v.mmax_z + 1, 4194304);
+            const float zlo = v.mmax_z < 0 ? 0.0f : -1.0f;
+            float below_one = fof(0x3F7FFFFFu);
+            const bool tiled = v.sub_fast != 0 && (uint64_t)S3 <= (1ull << 21) && c.grid_occ_size < (1ull << 22) &&
+                               f2u_x86_host(below_one / res) < c.sub_dim;
+            const uint64_t words = (c.grid_occ_size + 31) / 32;
+            uint64_t occ_bytes = 16;
+            while (occ_bytes < 8 * words) occ_bytes *= 2;
+            const uint32_t occ_mask = (uint32_t)(occ_bytes - 1) & ~7u;
+            std::vector<uint32_t> occ(occ_bytes / 4, 0u);
+            for (uint64_t u = 0; u < c.grid_occ_size; ++u)
+                if (go[u] >= 0) occ[2 * (u / 32)] |= 1u << (u % 32);
+            for (uint64_t w = 0, run = 0; w < words; ++w) {
+                run += (uint32_t)__builtin_popcount(occ[2 * w]);
+                occ[2 * w + 1] = (uint32_t)run;
+            }
             std::uniform_real_distribution<float> U(-3.5f, 25.0f);
             const float special[] = {-1.0f, -0.99999994f, -0.5f, -0.0f, 0.0f, 1e-30f, 0.99999994f, 1.0f, -2.0f, -1e-7f};
             for (long i = 0; i < n_points; ++i) {
@@ -118,30 +147,53 @@ int main(int argc, char** argv)
                     if (bad < 10) printf("tier2 mismatch res=%g o=(%.9g %.9g %.9g) got %u want %u\n", res, ox, oy, oz, t2, want);
                     ++bad;
                 }
-                // fast path emulation: offsets inside [0, mmax + 1) on x and y, and on
-                // z also (-1, 0) when lim_z > 0 (brick 0, negative sub-voxel index)
-                const bool zneg = std::signbit(oz) && std::fabs(oz) < 1.0f && v.lim_z != 0;
-                if (v.sub_fast && fbits(ox) < v.lim_x && fbits(oy) < v.lim_y && (fbits(oz) < v.lim_z || zneg)) {
+                // the tiled kernels' packed pipeline, operation by operation (float
+                // sums whose bits are the biased brick and sub-voxel offsets), for
+                // both layouts: the bitmap rank (compact) and the brick table
+                if (tiled) {
+                    const bool fast = fbits(ox) < v_lim_x && fbits(oy) < v_lim_y && oz > zlo && oz < zhi;
+                    if (!fast) goto next;
                     ++fast_n;
-                    float oo[3] = {ox, oy, std::fabs(oz)};
-                    int64_t mm[3], qq[3];
-                    for (int a = 0; a < 3; ++a) {
-                        mm[a] = (int64_t)oo[a];
-                        float s = oo[a] - (float)mm[a];
-                        qq[a] = fast_sub_index(v.sub_fast, s, v.sub_inv, v.sub_inv_lo);
-                    }
-                    if (std::signbit(oz)) qq[2] = -qq[2];
-                    uint64_t up = (uint64_t)(mm[0] + mm[1] * (int64_t)c.up_dim_x + mm[2] * (int64_t)c.up_dim_2);
-                    uint32_t got = kIdxMiss;
-                    if (up < c.grid_occ_size && go[up] >= 0) {
-                        uint64_t idx = (uint64_t)go[up] + qq[0] + qq[1] * c.sub_dim + qq[2] * c.sub_dim_2;
-                        if (idx < c.data_size) got = (uint32_t)idx;
-                    }
-                    if (got != want) {
-                        if (fast_bad < 10) printf("fast mismatch res=%g o=(%.9g %.9g %.9g) got %u want %u\n", res, ox, oy, oz, got, want);
-                        ++fast_bad;
+                    const float az = std::fabs(oz);
+                    const float MX = rz_add(ox, 8388608.0f), MY = rz_add(oy, 8388608.0f), MZ = rz_add(az, 8388608.0f);
+                    const float FY = MY - 8388608.0f, FZ = MZ - 8388608.0f;
+                    const float SX = ox - (MX - 8388608.0f), SY = oy - FY, SZ = az - FZ;
+                    auto cq = [&](float s_) {   // 1.5 2^23 + q(s)
+                        if (v.sub_fast == 2) return 12582912.0f + (float)std::floor((double)s_ * (double)v.sub_inv);
+                        return rz_add(std::fmaf(s_, v.sub_inv, s_ * v.sub_inv_lo), 12582912.0f);
+                    };
+                    const float CX = cq(SX), CY = cq(SY), CZ = cq(SZ);
+                    const float QY = CY - 12582912.0f, QZ = std::copysign(CZ - 12582912.0f, oz);
+                    const float SLB = std::fmaf(QZ, (float)c.sub_dim_2, std::fmaf(QY, (float)c.sub_dim, CX));
+                    const float UPB = std::fmaf(FZ, (float)c.up_dim_2, std::fmaf(FY, (float)c.up_dim_x, MX));
+                    const uint32_t upb = fbits(UPB), slb = fbits(SLB);
+                    const bool inside = upb < 0x4B000000u + (uint32_t)c.grid_occ_size;
+                    for (int layout = 0; layout < 2; ++layout) {
+                        uint32_t idx;
+                        bool ok;
+                        if (layout == 0) {   // compact: rank from the bitmap
+                            const uint32_t off = (upb >> 2) & occ_mask;
+                            const uint32_t word = occ[off / 4], incl = occ[off / 4 + 1];
+                            const uint32_t vv = word >> (upb & 31u);
+                            ok = inside && (vv & 1u);
+                            idx = (incl - (uint32_t)__builtin_popcount(vv)) * (uint32_t)S3 + slb;
+                        } else {             // brick table
+                            const int32_t base = go[inside ? upb - 0x4B000000u : 0u];
+                            ok = inside && base >= 0;
+                            idx = (uint32_t)base + slb;
+                        }
+                        // slot indices below 0 read the leading brick of misses
+                        const int64_t slot = (int64_t)idx - 0x4B400000ll;
+                        const uint32_t got = ok && slot >= 0 ? (uint32_t)slot : kIdxMiss;
+                        if (got != want) {
+                            if (fast_bad < 10)
+                                printf("fast mismatch layout=%d res=%g o=(%.9g %.9g %.9g) got %u want %u\n", layout, res,
+                                       ox, oy, oz, got, want);
+                            ++fast_bad;
+                        }
                     }
                 }
+            next:;
             }
         }
     printf("handled %ld slow %ld tier2_bad %ld fast %ld fast_bad %ld\n", handled, slow, bad, fast_n, fast_bad);

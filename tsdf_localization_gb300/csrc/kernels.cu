@@ -1,5 +1,6 @@
 // Sensor-update kernels for sm_103a: pose build, scan staging, per-particle
 // scoring, normalisation / mean pose, systematic resampling, map re-layout.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -8,6 +9,7 @@
 #include <vector>
 
 #include "index_math.h"
+#include "subsample.h"
 #include "tsdfl_internal.h"
 
 namespace tsdfl {
@@ -394,7 +396,7 @@ struct EvalParams {
 // lanes take neighbouring scan points, so their map gathers fall close
 // together).  Likelihood values are summed in 64-bit fixed point, which is
 // exact and independent of order; the weight is formed from the sum afterwards.
-template <bool DENSE, bool F32>
+template <bool DENSE, int ST>
 __global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -431,8 +433,11 @@ __global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
                 if (p.dbg) p.dbg[(size_t)pi * p.n_total + p.n0 + j] = code;
             } else {
                 uint32_t idx = slot_index(m, tx, ty, tz);
-                if (F32) {
+                if (ST == 1) {
                     float v = idx != kMissIndex ? __ldg(m.data + idx) : m.init_value;
+                    accd += (double)v;
+                } else if (ST == 2) {
+                    float v = idx != kMissIndex ? __half2float(__ushort_as_half(__ldg(m.h16 + idx))) : m.init_value;
                     accd += (double)v;
                 } else {
                     uint32_t code = idx != kMissIndex ? (uint32_t)__ldg(m.codes + idx) : (uint32_t)kCodeInit;
@@ -443,10 +448,10 @@ __global__ void __launch_bounds__(1024, 1) eval_exact_kernel(EvalParams p)
             }
         }
         h = warp_sum_u32(h);
-        if (F32) accd = warp_sum_d(accd);
+        if (ST != 0) accd = warp_sum_d(accd);
         else acc = warp_sum_ll(acc);
         if (lane == 0) {
-            if (F32) p.sum_f64[pi] = p.first_pass ? accd : p.sum_f64[pi] + accd;
+            if (ST != 0) p.sum_f64[pi] = p.first_pass ? accd : p.sum_f64[pi] + accd;
             else p.sum_fx[pi] = p.first_pass ? acc : p.sum_fx[pi] + acc;
             p.hits[pi] = p.first_pass ? h : p.hits[pi] + h;
         }
@@ -514,9 +519,15 @@ __device__ __forceinline__ f2_t fma2_rz(f2_t a, f2_t b, f2_t c)
     return r;
 }
 
-constexpr uint32_t kMagic = 0x4B000000u;          // bits of 2^23
-constexpr uint32_t kFastLimitBits = 0x4A800000u;  // bits of 2^22
-constexpr uint32_t kCodeSlow = (uint32_t)kCodeLater;   // fast path does not apply
+__device__ __forceinline__ f2_t or2(f2_t a, f2_t b)
+{
+    f2_t r;
+    asm("or.b64 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+constexpr uint32_t kMagic = 0x4B000000u;     // bits of 2^23
+constexpr uint32_t kMagic15 = 0x4B400000u;   // bits of 1.5 * 2^23
 
 // Code of a point the fast path does not cover: finite offsets go through the
 // signed second tier, NaN / infinite / huge ones through the 64-bit emulation.
@@ -528,57 +539,143 @@ __device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
 
-// Per-lookup inputs of the fast path, all from the packed pipeline: map
-// offsets o, bm = bits(2^23 + trunc(|o|)) and bc = bits(2^23 + q(s)) with q the
-// sub-voxel index of s = |o| - trunc(|o|) (x and y are fast only when o >= 0).
-struct FastIn {
-    float ox, oy, oz;
-    uint32_t bmx, bmy, bmz;
-    uint32_t bcx, bcy, bcz;
+// Likelihood table entry in shared memory: the fixed-point value and whether
+// the code is a slot (a hit); one 16-byte read per lookup gives both.
+struct __align__(16) LutEntry {
+    long long v;
+    uint32_t hit;
+    uint32_t pad;
 };
+constexpr int kLut16Bytes = kNumCodes * 16;
 
-// Branch-free fast path: the slot code, kCodeMiss, or kCodeSlow when the exact
-// slow tiers must decide (offset outside [0, mmax + 1) -- on z outside
-// (-1, mmax + 1) -- or, dense layout, a sub-voxel index outside the brick);
-// kCodeNone for a padding point (valid false).  `slow` is set for kCodeSlow.
-// The returned value is the gathered code itself: lookups that are not slots
-// read the array's sentinels, which saves the selects after the gather.
-// DENSE: one gather from the dense layout, the brick's occupancy bit from the
-// shared-memory bitmap `occ`; otherwise the brick table and the slot array.
+// Branch-free fast path of one lookup, from the packed pipeline's outputs: the
+// offsets' float bits (x, y) and value (z), upb = kMagic + brick index and
+// slb = kMagic15 + sub-voxel offset.  Returns the gathered code: the slot's, or
+// a sentinel's -- kCodeMiss (fast, but the brick is outside the grid or not
+// allocated), kCodeLater (the exact slow tiers decide: offset outside
+// [0, mmax + 1) on x or y, outside (-1, mmax + 1) on z; `slow` is set) or
+// kCodeNone (a padding point, valid false).
+// DENSE: the brick's rank from the shared-memory bitmap `occ`; otherwise the
+// brick table grid_occ.
 template <bool DENSE>
-__device__ __forceinline__ uint32_t fast_code(const MapView& m, const uint32_t* occ, const FastIn& in, bool valid,
+__device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned char* occ, uint32_t ox_b,
+                                              uint32_t oy_b, float oz, uint32_t upb, uint32_t slb, bool valid,
                                               bool& slow)
 {
-    const uint32_t zb = __float_as_uint(in.oz);
-    const uint32_t sgn = (uint32_t)((int32_t)zb >> 31);   // all ones when oz < 0
-    const bool fast = __float_as_uint(in.ox) < m.lim_x && __float_as_uint(in.oy) < m.lim_y &&
-                      (zb & 0x7fffffffu) < (sgn ? m.lim_zn : m.lim_z);
+    const bool fast = ox_b < m.lim_x && oy_b < m.lim_y && oz > m.zlo && oz < m.zhi;
     slow = valid && !fast;
-    const uint32_t alt = (valid ? (fast ? 0u : 1u) : 2u);   // sentinel: miss, later, none
-    const uint32_t up = in.bmx + in.bmy * m.up_dim_x + in.bmz * m.up_dim_2 - m.up_bias;
-    const uint32_t qz = ((in.bcz - kMagic) ^ sgn) - sgn;   // -q(|oz|) below the map
-    const uint32_t sl = in.bcx + in.bcy * m.sub_dim - m.sl_bias_xy + qz * m.sub_dim_2;
-    const bool inside = fast && up < m.grid_occ_size;
-    if (DENSE) {   // the brick's rank from the shared-memory bitmap and prefix counts
-        const uint32_t w = inside ? (up >> 5) : 0u;
-        const uint2 wb = reinterpret_cast<const uint2*>(occ)[w];
-        const uint32_t word = wb.x, below = wb.y;
-        const uint32_t bit = 1u << (up & 31u);
-        const bool alloc = (word & bit) != 0u;
-        const uint32_t r = below + __popc(word & (bit - 1u));
-        const uint32_t k = r + (up < m.up_dim_2 ? r + 1u : m.n0);   // bricks (and skirts) before this one
-        const bool ok = valid && inside && alloc;
-        return __ldg(m.dense + (ok ? k * m.sub_dim_3 + sl : m.dense_sent + alt));
+    const bool inside = valid && fast && upb < m.upb_lim;
+    uint32_t idx;
+    bool ok;
+    if (DENSE) {
+        // the masked offset stays inside the staged table whatever upb is
+        const uint2 wb = *reinterpret_cast<const uint2*>(occ + ((upb >> 2) & m.occ_mask));
+        const uint32_t v = __funnelshift_r(wb.x, 0u, upb);   // word >> (brick & 31)
+        ok = inside && (v & 1u) != 0u;
+        idx = (wb.y - (uint32_t)__popc(v)) * m.sub_dim_3 + slb;
     } else {
-        // slot indices below 0 wrap past 2^31 > data_size: a miss, as in getIndex's 64-bit sum
-        const int32_t base = __ldg(m.grid_occ + (inside ? up : 0u));
-        const uint32_t idx = (uint32_t)base + sl;
-        const bool ok = valid && inside && base >= 0 && idx < m.data_size;
-        return __ldg(m.codes + (ok ? idx : m.codes_sent + alt));
+        const int32_t base = __ldg(m.grid_occ + (inside ? upb - kMagic : 0u));
+        ok = inside && base >= 0;
+        idx = (uint32_t)base + slb;
     }
+    const uint32_t sent = valid ? (fast ? m.sent_miss : m.sent_later) : m.sent_none;
+    return __ldg(reinterpret_cast<const uint16_t*>(m.codes_b + 2ull * (ok ? idx : sent)));
 }
 
-constexpr int kTiledThreads = 768;
+// Constants of the packed index pipeline, each a pair of equal floats.
+struct PipeConsts {
+    f2_t NMX, NMY, NMZ;       // the map's min corner
+    f2_t MAG, MAG15;          // 2^23, 1.5 * 2^23
+    f2_t INV, INVLO;          // sub-voxel multiplier terms
+    f2_t UX, UXY, SD, SD2;    // up_dim_x, up_dim_x * up_dim_y, sub_dim, sub_dim^2
+    f2_t NZ;                  // -0
+};
+
+__device__ __forceinline__ PipeConsts pipe_consts(const MapView& m)
+{
+    PipeConsts c;
+    c.NMX = pk(m.min_x, m.min_x);
+    c.NMY = pk(m.min_y, m.min_y);
+    c.NMZ = pk(m.min_z, m.min_z);
+    c.MAG = pk(8388608.0f, 8388608.0f);
+    c.MAG15 = pk(12582912.0f, 12582912.0f);
+    c.INV = pk(m.sub_inv, m.sub_inv);
+    c.INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
+    c.UX = pk(m.up_dim_x_f, m.up_dim_x_f);
+    c.UXY = pk(m.up_dim_2_f, m.up_dim_2_f);
+    c.SD = pk(m.sub_dim_f, m.sub_dim_f);
+    c.SD2 = pk(m.sub_dim_2_f, m.sub_dim_2_f);
+    c.NZ = pk(m.neg_zero, m.neg_zero);
+    return c;
+}
+
+// A laser pose (3 x 4, row-major) as pairs: both halves of R[k] hold entry k
+// for a pose shared by the pair's two lookups, or entry k of two poses.
+struct PosePairs {
+    f2_t R[12];
+};
+
+__device__ __forceinline__ PosePairs pose_pairs(const float* pose12)
+{
+    const float4* src = reinterpret_cast<const float4*>(pose12);
+    const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+    PosePairs r;
+    r.R[0] = pk(a.x, a.x); r.R[1] = pk(a.y, a.y); r.R[2] = pk(a.z, a.z); r.R[3] = pk(a.w, a.w);
+    r.R[4] = pk(b.x, b.x); r.R[5] = pk(b.y, b.y); r.R[6] = pk(b.z, b.z); r.R[7] = pk(b.w, b.w);
+    r.R[8] = pk(c.x, c.x); r.R[9] = pk(c.y, c.y); r.R[10] = pk(c.z, c.z); r.R[11] = pk(c.w, c.w);
+    return r;
+}
+
+// Transform and fast-path lookup of two sensor-frame points (X, Y, Z pairs):
+// the gathered codes k0, k1, whether the exact slow tiers must decide them
+// (s0, s1), and the transformed points (for the deferral).  v0 / v1: the
+// lookup is a real point (false: padding, kCodeNone).
+template <bool DENSE, bool TWO, bool MIN0>
+__device__ __forceinline__ void pair_lookup(const MapView& m, const unsigned char* occ, const PosePairs& P,
+                                            const PipeConsts& K, f2_t X, f2_t Y, f2_t Z, bool v0, bool v1,
+                                            uint32_t& k0, uint32_t& k1, bool& s0, bool& s1, f2_t& TX, f2_t& TY,
+                                            f2_t& TZ)
+{
+    const f2_t ABS = 0x7fffffff7fffffffull, SGN = 0x8000000080000000ull;
+    // tsdf_evaluator.cpp:44-46: ((r0 x + r1 y) + r2 z) + r3, every product and
+    // sum rounded (products as FMAs with a -0 addend)
+    TX = add2(add2(add2(fma2_rn(P.R[0], X, K.NZ), fma2_rn(P.R[1], Y, K.NZ)), fma2_rn(P.R[2], Z, K.NZ)), P.R[3]);
+    TY = add2(add2(add2(fma2_rn(P.R[4], X, K.NZ), fma2_rn(P.R[5], Y, K.NZ)), fma2_rn(P.R[6], Z, K.NZ)), P.R[7]);
+    TZ = add2(add2(add2(fma2_rn(P.R[8], X, K.NZ), fma2_rn(P.R[9], Y, K.NZ)), fma2_rn(P.R[10], Z, K.NZ)), P.R[11]);
+    // offsets from the map's min corner (cuda_sub_voxel_map.tcc:52-54)
+    const f2_t OX = MIN0 ? TX : sub2(TX, K.NMX), OY = MIN0 ? TY : sub2(TY, K.NMY);
+    const f2_t OZ = MIN0 ? TZ : sub2(TZ, K.NMZ);
+    const f2_t AZ = and2(OZ, ABS);   // |oz|: below the map, brick 0 and a negative sub-voxel index
+    // 2^23 + trunc(o), trunc(o) and s = o - trunc(o), all exact
+    const f2_t MX = add2_rz(OX, K.MAG), MY = add2_rz(OY, K.MAG), MZ = add2_rz(AZ, K.MAG);
+    const f2_t FY = sub2(MY, K.MAG), FZ = sub2(MZ, K.MAG);
+    const f2_t SX = sub2(OX, sub2(MX, K.MAG)), SY = sub2(OY, FY), SZ = sub2(AZ, FZ);
+    f2_t CX, CY, CZ;   // 1.5 2^23 + sub-voxel index q
+    if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
+        CX = add2_rz(fma2_rn(SX, K.INV, mul2(SX, K.INVLO)), K.MAG15);
+        CY = add2_rz(fma2_rn(SY, K.INV, mul2(SY, K.INVLO)), K.MAG15);
+        CZ = add2_rz(fma2_rn(SZ, K.INV, mul2(SZ, K.INVLO)), K.MAG15);
+    } else {           // floor(s * inv), the product unrounded
+        CX = fma2_rz(SX, K.INV, K.MAG15);
+        CY = fma2_rz(SY, K.INV, K.MAG15);
+        CZ = fma2_rz(SZ, K.INV, K.MAG15);
+    }
+    // qz takes the sign of oz; slot and brick offsets as exact float sums
+    const f2_t QY = sub2(CY, K.MAG15), QZ = or2(sub2(CZ, K.MAG15), and2(OZ, SGN));
+    const f2_t SLB = fma2_rn(QZ, K.SD2, fma2_rn(QY, K.SD, CX));   // 1.5 2^23 + qx + qy S + qz S^2
+    const f2_t UPB = fma2_rn(FZ, K.UXY, fma2_rn(FY, K.UX, MX));   // 2^23 + mx + my Ux + mz Ux Uy
+    float ox0, ox1, oy0, oy1, oz0, oz1, u0, u1, l0, l1;
+    upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1); upk(UPB, u0, u1); upk(SLB, l0, l1);
+    k0 = fast_code<DENSE>(m, occ, __float_as_uint(ox0), __float_as_uint(oy0), oz0, __float_as_uint(u0),
+                          __float_as_uint(l0), v0, s0);
+    k1 = fast_code<DENSE>(m, occ, __float_as_uint(ox1), __float_as_uint(oy1), oz1, __float_as_uint(u1),
+                          __float_as_uint(l1), v1, s1);
+}
+
+#ifndef TSDFL_TILED_THREADS
+#define TSDFL_TILED_THREADS 768
+#endif
+constexpr int kTiledThreads = TSDFL_TILED_THREADS;
 constexpr int kTiledWarps = kTiledThreads / 32;
 constexpr int kRing = 64;   // deferred lookups per warp (transformed point + scan index)
 constexpr uint32_t kDbgSlow = 0x10000u;   // debug code flag: decided by the exact slow tiers
@@ -603,15 +700,15 @@ struct Partial {
 // Scores `count` (<= 32) deferred lookups from the ring, one per lane, through
 // the exact second tier / 64-bit emulation.  The map view is read from a
 // shared-memory copy so that no kernel parameter's address escapes.
-__device__ __noinline__ Partial drain(const MapView* m, const long long* lut, const float4* ring, uint32_t head,
+__device__ __noinline__ Partial drain(const MapView* m, const LutEntry* lut, const float4* ring, uint32_t head,
                                       int count, int lane, uint32_t* dbg_row, const int32_t* perm)
 {
     Partial r{0, 0u};
     if (lane < count) {
         const float4 e = ring[(head + (uint32_t)lane) & (kRing - 1)];
         const uint32_t code = slow_code(*m, e.x, e.y, e.z);
-        r.acc = lut[code];
-        r.hits = code <= (uint32_t)kCodeInit ? 1u : 0u;
+        r.acc = lut[code].v;
+        r.hits = lut[code].hit;
         if (dbg_row) dbg_row[perm[__float_as_int(e.w)]] = code | kDbgSlow;
     }
     __syncwarp();
@@ -634,26 +731,28 @@ struct TiledParams {
 // the (point chunk, particle group) work items in chunk-major order -- item k
 // belongs to warp k mod W of the W warps of the grid -- so all SMs score the
 // same part of the scan at a time and its map footprint stays in L2, with no
-// block-wide barrier after staging.  Each lane scores two points per step
-// (packed f32x2 arithmetic).  Likelihood codes are summed in 64-bit fixed point
-// and added to the particle's total with an integer atomic: exact and
-// independent of order, so results equal eval_exact_kernel's bit for bit.
-// TWO: the sub-voxel index needs the two-term multiplier (sub_fast 1);
-// DBG: per-point codes are written to the debug buffer.
+// block-wide barrier after staging.  Each lane scores two points per step:
+// every floating-point operation of the transform and of the index is one
+// packed f32x2 instruction for both points (products as FMAs with a -0 addend,
+// which round exactly like the reference's products), and the brick and
+// sub-voxel offsets are formed as exact float sums whose bits are the biased
+// integers, so the integer work per lookup is the rank, the address and the
+// bounds.  Likelihood codes are summed in 64-bit fixed point and added to the
+// particle's total with an integer atomic: exact and independent of order, so
+// results equal eval_exact_kernel's bit for bit.
 // One work item of the tiled scoring: the points [c0, c0 + chunk_pts) of the
 // staged pass (pair layout in sxy/spz) against the particles of group grp.
 // Sums go to p.sum_fx / p.hits with one integer atomic per particle.
-template <bool DENSE, bool TWO, bool DBG>
+// TWO: the sub-voxel index needs the two-term multiplier (sub_fast 1);
+// DBG: per-point codes are written to the debug buffer; MIN0: the map's min
+// corner is the origin, so offsets are the transformed coordinates.
+template <bool DENSE, bool TWO, bool DBG, bool MIN0>
 __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m, const MapView* s_map,
-                                           const uint32_t* occ, const float4* sxy, const float2* spz,
-                                           const long long* lut, float4* ring, int n, int chunk_pts, int group,
+                                           const unsigned char* occ, const float4* sxy, const float2* spz,
+                                           const LutEntry* lut, float4* ring, int n, int chunk_pts, int group,
                                            int chunk, int grp, int lane)
 {
-    const f2_t NMX = pk(m.min_x, m.min_x), NMY = pk(m.min_y, m.min_y), NMZ = pk(m.min_z, m.min_z);
-    const f2_t MAG = pk(8388608.0f, 8388608.0f);
-    const f2_t INV = pk(m.sub_inv, m.sub_inv);
-    const f2_t INVLO = pk(m.sub_inv_lo, m.sub_inv_lo);
-    const f2_t ABS = 0x7fffffff7fffffffull;
+    const PipeConsts K = pipe_consts(m);
     uint32_t head = 0, tail = 0;
     const int c0 = chunk * chunk_pts;
     const int cn = min(chunk_pts, n - c0);
@@ -661,9 +760,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
     for (int k = 0; k < group; ++k) {
         const int pi = grp * group + k;
         if (pi >= p.P) break;
-        const float4* src = reinterpret_cast<const float4*>(p.pose12 + 12 * (size_t)pi);
-        const float4 a = __ldg(src), b4 = __ldg(src + 1), c4 = __ldg(src + 2);
-        const f2_t R3 = pk(a.w, a.w), R7 = pk(b4.w, b4.w), R11 = pk(c4.w, c4.w);
+        const PosePairs R = pose_pairs(p.pose12 + 12 * (size_t)pi);
         long long acc = 0;
         uint32_t hits = 0;
         // debug rows are indexed by scan index: perm maps the pass's pair-layout
@@ -675,47 +772,12 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
         auto step = [&](int blk, bool partial) {
             const float4 xy = sxy[(b0 + blk) * 32 + lane];
             const float2 zz = spz[(b0 + blk) * 32 + lane];
-            // tsdf_evaluator.cpp:44-46 for two points: ((r0 x + r1 y) + r2 z) + r3
-            const f2_t TX = add2(add2(add2(pk(__fmul_rn(a.x, xy.x), __fmul_rn(a.x, xy.y)),
-                                           pk(__fmul_rn(a.y, xy.z), __fmul_rn(a.y, xy.w))),
-                                      pk(__fmul_rn(a.z, zz.x), __fmul_rn(a.z, zz.y))),
-                                 R3);
-            const f2_t TY = add2(add2(add2(pk(__fmul_rn(b4.x, xy.x), __fmul_rn(b4.x, xy.y)),
-                                           pk(__fmul_rn(b4.y, xy.z), __fmul_rn(b4.y, xy.w))),
-                                      pk(__fmul_rn(b4.z, zz.x), __fmul_rn(b4.z, zz.y))),
-                                 R7);
-            const f2_t TZ = add2(add2(add2(pk(__fmul_rn(c4.x, xy.x), __fmul_rn(c4.x, xy.y)),
-                                           pk(__fmul_rn(c4.y, xy.z), __fmul_rn(c4.y, xy.w))),
-                                      pk(__fmul_rn(c4.z, zz.x), __fmul_rn(c4.z, zz.y))),
-                                 R11);
-            const f2_t OX = sub2(TX, NMX), OY = sub2(TY, NMY), OZ = sub2(TZ, NMZ);
-            const f2_t AZ = and2(OZ, ABS);   // |oz|
-            const f2_t MX = add2_rz(OX, MAG), MY = add2_rz(OY, MAG), MZ = add2_rz(AZ, MAG);  // 2^23 + trunc
-            const f2_t SX = sub2(OX, sub2(MX, MAG)), SY = sub2(OY, sub2(MY, MAG)), SZ = sub2(AZ, sub2(MZ, MAG));
-            f2_t CX, CY, CZ;   // 2^23 + sub-voxel index
-            if (TWO) {         // trunc(fl(s * hi + fl(s * lo)))
-                CX = add2_rz(fma2_rn(SX, INV, mul2(SX, INVLO)), MAG);
-                CY = add2_rz(fma2_rn(SY, INV, mul2(SY, INVLO)), MAG);
-                CZ = add2_rz(fma2_rn(SZ, INV, mul2(SZ, INVLO)), MAG);
-            } else {           // floor(s * inv), the product unrounded
-                CX = fma2_rz(SX, INV, MAG);
-                CY = fma2_rz(SY, INV, MAG);
-                CZ = fma2_rz(SZ, INV, MAG);
-            }
-            FastIn i0, i1;
-            upk(OX, i0.ox, i1.ox); upk(OY, i0.oy, i1.oy); upk(OZ, i0.oz, i1.oz);
-            {
-                float a0, a1;
-                upk(MX, a0, a1); i0.bmx = __float_as_uint(a0); i1.bmx = __float_as_uint(a1);
-                upk(MY, a0, a1); i0.bmy = __float_as_uint(a0); i1.bmy = __float_as_uint(a1);
-                upk(MZ, a0, a1); i0.bmz = __float_as_uint(a0); i1.bmz = __float_as_uint(a1);
-                upk(CX, a0, a1); i0.bcx = __float_as_uint(a0); i1.bcx = __float_as_uint(a1);
-                upk(CY, a0, a1); i0.bcy = __float_as_uint(a0); i1.bcy = __float_as_uint(a1);
-                upk(CZ, a0, a1); i0.bcz = __float_as_uint(a0); i1.bcz = __float_as_uint(a1);
-            }
+            uint32_t k0, k1;
             bool s0, s1;
-            const uint32_t k0 = fast_code<DENSE>(m, occ, i0, !partial || 64 * blk + lane < cn, s0);
-            const uint32_t k1 = fast_code<DENSE>(m, occ, i1, !partial || 64 * blk + 32 + lane < cn, s1);
+            f2_t TX, TY, TZ;
+            pair_lookup<DENSE, TWO, MIN0>(m, occ, R, K, pk(xy.x, xy.y), pk(xy.z, xy.w), pk(zz.x, zz.y),
+                                          !partial || 64 * blk + lane < cn, !partial || 64 * blk + 32 + lane < cn,
+                                          k0, k1, s0, s1, TX, TY, TZ);
             // lanes the fast path cannot decide are deferred to the warp's ring and
             // scored 32 at a time (kCodeLater contributes nothing here), so no warp
             // diverges into the slow tiers; at most 31 entries wait between steps,
@@ -744,8 +806,9 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
                 if (k0 < (uint32_t)kCodeNone) dbg_row[perm[j]] = k0;
                 if (k1 < (uint32_t)kCodeNone) dbg_row[perm[j + 32]] = k1;
             }
-            acc += lut[k0] + lut[k1];
-            hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
+            const LutEntry e0 = lut[k0], e1 = lut[k1];
+            acc += e0.v + e1.v;
+            hits += e0.hit + e1.hit;
         };
         for (int blk = 0; blk < nfull; ++blk) step(blk, false);
         if (nfull < nblk) step(nfull, true);
@@ -764,7 +827,20 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
     }
 }
 
-template <bool DENSE, bool TWO, bool DBG>
+// Shared memory of the tiled kernels: the 16-byte likelihood table, the brick
+// bitmap (compact layout), then the staged pass and the deferral rings.
+__device__ __forceinline__ void fill_lut16(LutEntry* lut, const long long* lut_fx)
+{
+    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) {
+        LutEntry e;
+        e.v = lut_fx[c];
+        e.hit = c <= kCodeInit ? 1u : 0u;
+        e.pad = 0u;
+        lut[c] = e;
+    }
+}
+
+template <bool DENSE, bool TWO, bool DBG, bool MIN0>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -772,22 +848,22 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     __shared__ MapView s_map;   // the map view the slow tiers read
     const EvalParams& p = tp.e;
     const MapView& m = p.m;
-    long long* lut = reinterpret_cast<long long*>(smem);
+    LutEntry* lut = reinterpret_cast<LutEntry*>(smem);
     const int n = p.n1 - p.n0;
     const int npairs = ((n + 63) >> 6) * 32;
     if (threadIdx.x == 0) s_map = m;
-    const uint32_t occ_words = DENSE ? 2u * m.occ_words : 0u;   // bitmap + prefix counts
-    uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
-    float4* sxy = reinterpret_cast<float4*>(occ + occ_words);
+    const uint32_t occ_bytes = DENSE ? m.occ_bytes : 0u;
+    unsigned char* occ = smem + kLut16Bytes;
+    float4* sxy = reinterpret_cast<float4*>(occ + occ_bytes);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
-    for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
+    fill_lut16(lut, p.lut_fx);
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_words * 4u);
+        mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_bytes);
         bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
         bulk_g2s(spz, p.pz + p.n0 / 2, (uint32_t)npairs * 8u, &bar);
-        if (occ_words) bulk_g2s(occ, m.occ, occ_words * 4u, &bar);
+        if (occ_bytes) bulk_g2s(occ, m.occ, occ_bytes, &bar);
     }
     bool staged = mbar_wait_bounded(&bar, 0);
     if (!staged) staged = mbar_wait_bounded(&bar, 0);   // give copies in flight a second bound
@@ -800,7 +876,113 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const int nwarps = gridDim.x * kTiledWarps;
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
-        tiled_item<DENSE, TWO, DBG>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp, lane);
+        tiled_item<DENSE, TWO, DBG, MIN0>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp,
+                                          lane);
+    }
+}
+
+// Seeded per-particle scan subsampling (subsample.h): one warp per particle
+// scores the particle's K kept points, two per lane per step, through the same
+// packed pipeline as the tiled kernel, reading the scan from the SoA arrays the
+// staging kernel wrote (scan order, L1-resident for scans of a few thousand
+// points).  Per particle: the fixed-point likelihood sum, the hits and the
+// number of kept points within max_range (its weight's range term), written
+// directly (one warp owns the particle).
+struct SubParams {
+    EvalParams e;
+    int K;
+    unsigned long long seed;
+    uint32_t* nin;
+    float c_in;
+};
+
+template <bool DENSE, bool TWO, bool MIN0>
+__global__ void __launch_bounds__(kTiledThreads, 1) eval_subsample_kernel(SubParams sp)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ MapView s_map;   // the map view the slow tiers read
+    const EvalParams& p = sp.e;
+    const MapView& m = p.m;
+    LutEntry* lut = reinterpret_cast<LutEntry*>(smem);
+    const uint32_t occ_bytes = DENSE ? m.occ_bytes : 0u;
+    unsigned char* occ = smem + kLut16Bytes;
+    float4* rings = reinterpret_cast<float4*>(occ + occ_bytes);
+    if (threadIdx.x == 0) s_map = m;
+    fill_lut16(lut, p.lut_fx);
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    bool staged = true;
+    if (occ_bytes) {
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bar, occ_bytes);
+            bulk_g2s(occ, m.occ, occ_bytes, &bar);
+        }
+        staged = mbar_wait_bounded(&bar, 0);
+        if (!staged) staged = mbar_wait_bounded(&bar, 0);   // give the copy in flight a second bound
+    }
+    if (!staged && threadIdx.x == 0) atomicExch(p.status, TSDFL_ERR_TIMEOUT);
+    if (__syncthreads_and(staged ? 1 : 0) == 0) return;
+
+    const int lane = threadIdx.x & 31;
+    float4* ring = rings + (threadIdx.x >> 5) * kRing;
+    const PipeConsts K = pipe_consts(m);
+    const uint32_t N = (uint32_t)p.n_total, Ks = (uint32_t)sp.K;
+    const int gwarp = blockIdx.x * kTiledWarps + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * kTiledWarps;
+    for (int pi = gwarp; pi < p.P; pi += nwarps) {
+        const PosePairs R = pose_pairs(p.pose12 + 12 * (size_t)pi);
+        const uint64_t st = sub_particle_state(sp.seed, (uint64_t)pi);
+        long long acc = 0;
+        uint32_t hits = 0, nin = 0, head = 0, tail = 0;
+        for (uint32_t base = 0; base < Ks; base += 64) {   // the same trip count on every lane
+            const uint32_t ka = base + (uint32_t)lane, kb = ka + 32u;
+            const bool va = ka < Ks, vb = kb < Ks;
+            const uint32_t ja = sub_point(st, N, Ks, va ? ka : 0u), jb = sub_point(st, N, Ks, vb ? kb : 0u);
+            const float xa = __ldg(p.xs + ja), ya = __ldg(p.ys + ja), za = __ldg(p.zs + ja);
+            const float xb = __ldg(p.xs + jb), yb = __ldg(p.ys + jb), zb = __ldg(p.zs + jb);
+            nin += (va && __ldg(p.cs + ja) == sp.c_in ? 1u : 0u) + (vb && __ldg(p.cs + jb) == sp.c_in ? 1u : 0u);
+            uint32_t k0, k1;
+            bool s0, s1;
+            f2_t TX, TY, TZ;
+            pair_lookup<DENSE, TWO, MIN0>(m, occ, R, K, pk(xa, xb), pk(ya, yb), pk(za, zb), va, vb, k0, k1, s0, s1,
+                                          TX, TY, TZ);
+            if (__any_sync(0xffffffffu, s0 || s1)) {
+                float tx, ty, tz, u;
+                upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
+                defer(ring, head, tail, s0, tx, ty, tz, (int)ja, lane);
+                if (tail - head >= 32) {
+                    const Partial d = drain(&s_map, lut, ring, head, 32, lane, nullptr, nullptr);
+                    acc += d.acc;
+                    hits += d.hits;
+                    head += 32;
+                }
+                upk(TX, u, tx); upk(TY, u, ty); upk(TZ, u, tz);
+                defer(ring, head, tail, s1, tx, ty, tz, (int)jb, lane);
+                if (tail - head >= 32) {
+                    const Partial d = drain(&s_map, lut, ring, head, 32, lane, nullptr, nullptr);
+                    acc += d.acc;
+                    hits += d.hits;
+                    head += 32;
+                }
+            }
+            const LutEntry e0 = lut[k0], e1 = lut[k1];
+            acc += e0.v + e1.v;
+            hits += e0.hit + e1.hit;
+        }
+        if (tail != head) {
+            const Partial d = drain(&s_map, lut, ring, head, (int)(tail - head), lane, nullptr, nullptr);
+            acc += d.acc;
+            hits += d.hits;
+        }
+        acc = warp_sum_ll(acc);
+        hits = warp_sum_u32(hits);
+        nin = warp_sum_u32(nin);
+        if (lane == 0) {
+            p.sum_fx[pi] = acc;
+            p.hits[pi] = hits;
+            sp.nin[pi] = nin;
+        }
     }
 }
 
@@ -839,8 +1021,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
     __shared__ uint32_t s_batch;
     __shared__ uint32_t s_next;
     __shared__ int s_segi;
-    long long* lut = reinterpret_cast<long long*>(smem);
-    uint32_t* occ = reinterpret_cast<uint32_t*>(smem + kLutBytes);
+    LutEntry* lut = reinterpret_cast<LutEntry*>(smem);
+    unsigned char* occ = smem + kLut16Bytes;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
@@ -873,16 +1055,16 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             const EvalParams& p = s_seg.e;
             n = p.n1 - p.n0;
             const int npairs = ((n + 63) >> 6) * 32;
-            const uint32_t occ_words = DENSE ? 2u * p.m.occ_words : 0u;
-            sxy = reinterpret_cast<float4*>(occ + occ_words);
+            const uint32_t occ_bytes = DENSE ? p.m.occ_bytes : 0u;
+            sxy = reinterpret_cast<float4*>(occ + occ_bytes);
             spz = reinterpret_cast<float2*>(sxy + npairs);
             ring = reinterpret_cast<float4*>(spz + npairs) + warp * kRing;
-            for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) lut[c] = p.lut_fx[c];
+            fill_lut16(lut, p.lut_fx);
             if (threadIdx.x == 0) {
-                mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_words * 4u);
+                mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_bytes);
                 bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
                 bulk_g2s(spz, p.pz + p.n0 / 2, (uint32_t)npairs * 8u, &bar);
-                if (occ_words) bulk_g2s(occ, p.m.occ, occ_words * 4u, &bar);
+                if (occ_bytes) bulk_g2s(occ, p.m.occ, occ_bytes, &bar);
             }
             bool staged = mbar_wait_bounded(&bar, phase);
             if (!staged) staged = mbar_wait_bounded(&bar, phase);   // give copies in flight a second bound
@@ -900,8 +1082,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             if (j >= (uint32_t)kBatchItems || item >= s_seg.items) break;
             const EvalParams& p = s_seg.e;
             const int chunk = item / s_seg.groups, grp = item - chunk * s_seg.groups;
-            tiled_item<DENSE, TWO, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group, chunk,
-                                          grp, lane);
+            tiled_item<DENSE, TWO, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group,
+                                                 chunk, grp, lane);
         }
         __syncthreads();   // every warp is done with s_batch and the staged segment
     }
@@ -957,7 +1139,8 @@ struct NormParams {
     int mode;            // 0 fixed point, 1 double sums, 2 serial raw
     int shift;
     double a_hit, c_in, c_out;
-    int n_points;
+    int n_points;        // points every particle scored
+    const uint32_t* nin; // per-particle points within max_range (subsampled scans), else null
 };
 
 // Forms each particle's un-normalised weight from its likelihood sum and
@@ -967,10 +1150,11 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
 {
     double acc[kNormSums];
     for (int k = 0; k < kNormSums; ++k) acc[k] = 0.0;
-    const double n_in = (double)b.counts[0];
-    const double n_out = (double)q.n_points - n_in;
+    const double n_in_all = (double)b.counts[0];
     const double scale = ldexp(1.0, -q.shift);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < q.P; i += gridDim.x * blockDim.x) {
+        const double n_in = q.nin ? (double)q.nin[i] : n_in_all;
+        const double n_out = (double)q.n_points - n_in;
         float raw;
         if (q.mode == 2) {
             raw = b.raw[i];
@@ -1053,6 +1237,63 @@ __global__ void normalize_kernel(int P, EvalBuffers b, float* particles_out)
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
     particles_out[7 * (size_t)i + 6] = __fdiv_rn(b.raw[i], b.weight_sum_f[0]);
+}
+
+// Log-domain normalisation (TSDFL_NORM_LOG), after norm_partial/final have
+// formed the raw weights: the largest raw weight (positive floats order like
+// their bits: one atomicMax), then sum_i exp(ln raw_i - ln max) in double
+// (block partials in a fixed order), LSE, and w_i = exp(ln raw_i - LSE).
+__global__ void log_max_kernel(int P, EvalBuffers b)
+{
+    uint32_t mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        const float r = b.raw[i];
+        if (r > 0.0f) mx = max(mx, __float_as_uint(r));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(reinterpret_cast<unsigned int*>(b.counts + 1), mx);
+}
+
+__global__ void log_sum_kernel(int P, EvalBuffers b)
+{
+    const double lm = log((double)__uint_as_float((uint32_t)b.counts[1]));
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        const float r = b.raw[i];
+        if (r > 0.0f) acc += exp(log((double)r) - lm);
+    }
+    __shared__ double red[kNormThreads / 32];
+    acc = warp_sum_d(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < kNormThreads / 32; ++w) v += red[w];
+        b.partials[blockIdx.x] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kNormBlocks) log_final_kernel(EvalBuffers b)
+{
+    __shared__ double red[kNormBlocks / 32];
+    const double v = warp_sum_d(b.partials[threadIdx.x]);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kNormBlocks / 32; ++w) s += red[w];
+        b.sums[10] = log((double)__uint_as_float((uint32_t)b.counts[1])) + log(s);   // LSE
+    }
+}
+
+__global__ void normalize_log_kernel(int P, EvalBuffers b, float* particles_out)
+{
+    if (*b.status == TSDFL_ERR_DEGENERATE) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const float r = b.raw[i];
+    particles_out[7 * (size_t)i + 6] = r > 0.0f ? (float)exp(log((double)r) - b.sums[10]) : 0.0f;
 }
 
 // ---------------------------------------------------------------- resampling
@@ -1747,6 +1988,15 @@ __global__ void fold_status_kernel(int32_t* ev, int32_t* sticky)
 
 // ------------------------------------------------------------- map layouts
 
+__global__ void halves_kernel(const uint16_t* codes, const float* values, const float* data, size_t n,
+                              uint16_t* h16)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = codes ? values[codes[i]] : data[i];
+        h16[i] = __half_as_ushort(__float2half_rn(v));
+    }
+}
+
 __global__ void codes_from_floats_kernel(const float* data, size_t n, const float* values, float init_value,
                                          uint16_t* codes, int32_t* fail)
 {
@@ -1775,22 +2025,6 @@ __global__ void codes_from_floats_kernel(const float* data, size_t n, const floa
     }
 }
 
-// Compact layout: one CTA per allocated brick copies its sub3 slot codes (and,
-// for bricks of layer z = 0, the sub3 slots before it in the reference's data
-// order into the skirt in front of it).
-__global__ void compact_fill_kernel(const uint16_t* codes, const int64_t* src, const int64_t* dst,
-                                    const uint8_t* skirt, uint32_t n, uint32_t sub3, uint16_t* dense)
-{
-    for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
-        const int64_t s0 = src[b], d0 = dst[b];
-        for (uint32_t i = threadIdx.x; i < sub3; i += blockDim.x) dense[d0 + i] = codes[s0 + i];
-        if (skirt[b])
-            for (uint32_t i = threadIdx.x; i < sub3; i += blockDim.x) {
-                const int64_t from = s0 - (int64_t)sub3 + i;
-                dense[d0 - (int64_t)sub3 + i] = from >= 0 ? codes[from] : (uint16_t)kCodeMiss;
-            }
-    }
-}
 
 int check(cudaError_t e)
 {
@@ -1828,9 +2062,24 @@ size_t eval_smem_bytes(bool serial, int n)
     return serial ? (size_t)kLutFBytes + 4ull * npad * 4 : (size_t)kLutBytes + 3ull * npad * 4;
 }
 
+using TiledKernel = void (*)(TiledParams);
+
+template <bool DENSE, bool TWO>
+TiledKernel pick_tiled_2(bool dbg, bool min0)
+{
+    return dbg ? (min0 ? eval_tiled_kernel<DENSE, TWO, true, true> : eval_tiled_kernel<DENSE, TWO, true, false>)
+               : (min0 ? eval_tiled_kernel<DENSE, TWO, false, true> : eval_tiled_kernel<DENSE, TWO, false, false>);
+}
+
+TiledKernel pick_tiled(bool dense, bool two, bool dbg, bool min0)
+{
+    return dense ? (two ? pick_tiled_2<true, true>(dbg, min0) : pick_tiled_2<true, false>(dbg, min0))
+                 : (two ? pick_tiled_2<false, true>(dbg, min0) : pick_tiled_2<false, false>(dbg, min0));
+}
+
 size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
 {
-    return (size_t)kLutBytes + (dense ? (size_t)m.occ_words * 8 : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
+    return (size_t)kLut16Bytes + (dense ? (size_t)m.occ_bytes : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
            sizeof(float4) * kRing * kTiledWarps;
 }
 
@@ -1862,13 +2111,13 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
     p.P = P; p.n0 = n0; p.n1 = n1; p.n_total = n_total; p.first_pass = first ? 1 : 0;
     p.a_hit = a_hit;
     size_t smem = eval_smem_bytes(serial, n1 - n0);
-    const bool f32 = m.storage == 1;
+    const bool f32 = m.storage != 0;   // value slots (float or half) rather than codes
     if (serial) {
         auto k = f32 ? eval_serial_kernel<true> : eval_serial_kernel<false>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k<<<(P + 255) / 256, 256, smem, s>>>(p);
         g_launches += 1;
-    } else if (!f32 && m.sub_fast && !generic) {
+    } else if (!f32 && m.tiled && !generic) {
         // one launch covers the whole scan; sums are accumulated with atomics
         TiledParams tp;
         tp.e = p;
@@ -1878,10 +2127,7 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
         // sub_fast 2: floor(s * sub_inv) is the sub-voxel index; 1: the two-term multiplier
         const bool two = m.sub_fast == 1, dbg = p.dbg != nullptr;
-        auto k = dense ? (two ? (dbg ? eval_tiled_kernel<true, true, true> : eval_tiled_kernel<true, true, false>)
-                              : (dbg ? eval_tiled_kernel<true, false, true> : eval_tiled_kernel<true, false, false>))
-                       : (two ? (dbg ? eval_tiled_kernel<false, true, true> : eval_tiled_kernel<false, true, false>)
-                              : (dbg ? eval_tiled_kernel<false, false, true> : eval_tiled_kernel<false, false, false>));
+        auto k = pick_tiled(dense, two, dbg, m.min0 != 0);
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (first) {
@@ -1894,8 +2140,9 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         k<<<blocks, kTiledThreads, tsmem, s>>>(tp);
         g_launches += 1;
     } else {
-        auto k = dense && !f32 ? eval_exact_kernel<true, false>
-                               : (f32 ? eval_exact_kernel<false, true> : eval_exact_kernel<false, false>);
+        auto k = dense && !f32 ? eval_exact_kernel<true, 0>
+                               : (m.storage == 2 ? eval_exact_kernel<false, 2>
+                                                 : (f32 ? eval_exact_kernel<false, 1> : eval_exact_kernel<false, 0>));
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int blocks = sm_count;
         int need = (P + 31) / 32;
@@ -1903,6 +2150,45 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         k<<<blocks, 1024, smem, s>>>(p);
         g_launches += 1;
     }
+    return check(cudaGetLastError());
+}
+
+template <bool DENSE, bool TWO>
+void (*pick_sub_2(bool min0))(SubParams)
+{
+    return min0 ? eval_subsample_kernel<DENSE, TWO, true> : eval_subsample_kernel<DENSE, TWO, false>;
+}
+
+int launch_eval_subsample(const MapView& m, float a_hit, int P, int N, int K, unsigned long long seed, float c_in,
+                          const EvalBuffers& b, int sm_count, cudaStream_t s)
+{
+    if (!m.tiled || m.storage != 0) return TSDFL_ERR_UNSUPPORTED;
+    SubParams sp;
+    EvalParams& p = sp.e;
+    p = EvalParams{};
+    p.m = m;
+    p.pose12 = b.pose12;
+    p.xs = b.xs; p.ys = b.ys; p.zs = b.zs; p.cs = b.cs;
+    p.lut_fx = b.lut_fx;
+    p.sum_fx = b.sum_fx;
+    p.hits = b.hits;
+    p.status = b.status;
+    p.P = P; p.n0 = 0; p.n1 = N; p.n_total = N; p.first_pass = 1;
+    p.a_hit = a_hit;
+    sp.K = K;
+    sp.seed = seed;
+    sp.nin = b.nin;
+    sp.c_in = c_in;
+    const bool dense = m.occ_bytes != 0, two = m.sub_fast == 1;
+    auto k = dense ? (two ? pick_sub_2<true, true>(m.min0 != 0) : pick_sub_2<true, false>(m.min0 != 0))
+                   : (two ? pick_sub_2<false, true>(m.min0 != 0) : pick_sub_2<false, false>(m.min0 != 0));
+    const size_t smem = (size_t)kLut16Bytes + (dense ? (size_t)m.occ_bytes : 0) + sizeof(float4) * kRing * kTiledWarps;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int blocks = sm_count;
+    const int need = (P + kTiledWarps - 1) / kTiledWarps;
+    if (need < blocks) blocks = need > 0 ? need : 1;
+    k<<<blocks, kTiledThreads, smem, s>>>(sp);
+    g_launches += 1;
     return check(cudaGetLastError());
 }
 
@@ -1984,13 +2270,21 @@ int launch_eval_batch(const void* d_segs, const BatchKinds& kinds, uint32_t* cou
 }
 
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
-                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s)
+                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s,
+                const uint32_t* nin, bool log_domain)
 {
-    NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points};
+    NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points, nin};
     norm_partial_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(q, b, sum_f64);
     norm_final_kernel<<<1, kNormBlocks, 0, s>>>(b, pose_out);
     g_launches += 2;
-    if (P > 0) {
+    if (P > 0 && log_domain) {
+        cudaMemsetAsync(b.counts + 1, 0, sizeof(int32_t), s);
+        log_max_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(P, b);
+        log_sum_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(P, b);
+        log_final_kernel<<<1, kNormBlocks, 0, s>>>(b);
+        normalize_log_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
+        g_launches += 4;
+    } else if (P > 0) {
         normalize_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
         g_launches += 1;
     }
@@ -2089,11 +2383,12 @@ int launch_codes_from_floats(const float* data, size_t n, const float* code_valu
     return check(cudaGetLastError());
 }
 
-int launch_compact_fill(const uint16_t* codes, const int64_t* src, const int64_t* dst, const uint8_t* skirt,
-                        uint32_t n, uint32_t sub3, uint16_t* dense, cudaStream_t s)
+int launch_halves(const uint16_t* codes, const float* code_values, const float* data, size_t n, uint16_t* h16,
+                  cudaStream_t s)
 {
-    if (n) compact_fill_kernel<<<n < 65535u ? n : 65535u, 256, 0, s>>>(codes, src, dst, skirt, n, sub3, dense);
+    if (n) halves_kernel<<<1024, 256, 0, s>>>(codes, code_values, data, n, h16);
     return check(cudaGetLastError());
 }
+
 
 }  // namespace tsdfl

@@ -46,8 +46,9 @@ struct MapView {
     const int32_t* grid_occ;
     const uint16_t* codes;    // 16-bit slot codes (storage 0)
     const float* data;        // float slots (storage 1)
-    const uint16_t* dense;    // compact rank-ordered layout (may be null; see occ)
-    int32_t storage;          // 0 = codes, 1 = float
+    const uint16_t* h16;      // half-precision slot values, IEEE bits (storage 2)
+    const uint16_t* dense;    // non-null when the compact layout (occ) is built; equals codes
+    int32_t storage;          // 0 = codes, 1 = float, 2 = half
     // Division-free sub-voxel index q = trunc(fl(s / res)) for s in [0, 1),
     // verified on the host (every threshold of q; monotone in s):
     // sub_fast = 2: q == floor(s * sub_inv) (exact product);
@@ -56,32 +57,41 @@ struct MapView {
     int32_t sub_fast;
     float sub_inv, sub_inv_lo;
     uint32_t lim_x, lim_y, lim_z;  // float bits of min(mmax + 1, 2^22) per axis
-    // Fast path on float bits: with bm = bits(2^23 + trunc(offset)) and
-    // bc = bits(2^23 + floor(s * sub_inv)) per axis,
-    //   brick = bm_x + bm_y * up_dim_x + bm_z * up_dim_2 - up_bias   (mod 2^32)
-    //   slot  = bc_x + bc_y * sub_dim + bc_z * sub_dim_2 - sl_bias    (mod 2^32)
-    uint32_t up_bias, sl_bias;
-    // Negative z offsets in (-1, 0) (points just below the map) also take the
-    // fast path: brick z 0 and sub-voxel index -q(|oz|), as getIndex gives them.
-    // lim_zn: float bits bounding |oz| there (1.0, or 0 when lim_z is 0);
-    // sl_bias_xy = bits(2^23) * (1 + sub_dim).
-    uint32_t lim_zn, sl_bias_xy;
-    // Compact layout (TSDFL_MAP_DENSE): the allocated bricks' slots in brick
-    // index order, bricks of layer z = 0 each preceded by a "skirt" of sub_dim^3
-    // slots holding what getIndex reads below them (the sub_dim^3 slots before
-    // the brick in the reference's data order, kCodeMiss below slot 0).  occ is
-    // occ_words pairs {bitmap word w, prefix[w]}: bit up of the bitmap is set
-    // when brick up is allocated, prefix[w] counts the set bits of words
-    // 0..w-1 (one 8-byte read gives both).  A brick of rank r starts at
-    // (2r + 1) S^3 in layer 0 (up < up_dim_2) and at (r + n0) S^3 above, n0 =
-    // allocated bricks in layer 0.
+    // Code arrays: the reference's slots in its data order (bricks in linear
+    // brick order, sub_dim^3 slots each, x fastest), preceded by one brick of
+    // kCodeMiss -- what getIndex's wrapped 64-bit sum reads below slot 0 is a
+    // miss -- and followed by kSentinels codes.  A brick of rank r (r allocated
+    // bricks before it) starts at r * sub_dim^3, so a slot index is
+    // r * sub_dim^3 + sub with sub in [-sub_dim^3, sub_dim^3).
+    // Compact layout (TSDFL_MAP_DENSE): the brick's rank comes from a bitmap of
+    // the brick grid staged in shared memory instead of a grid_occ gather.  occ
+    // holds pairs {word w, allocated bricks in words 0..w}; bit (up & 31) of
+    // word up >> 5 is set when brick up is allocated; the pairs are zero-padded
+    // to occ_bytes (a power of two), so any index masked by occ_mask reads
+    // inside the staged table.  rank = incl[w] - popc(word >> (up & 31)) for an
+    // allocated brick.
     const uint32_t* occ;
-    uint32_t occ_words;            // a multiple of 4
-    uint32_t n0;
+    uint32_t occ_bytes;            // staged bytes (power of two), 0 without the compact layout
+    uint32_t occ_mask;             // (occ_bytes - 1) & ~7
     // Both code arrays end in kSentinels extra entries {kCodeMiss, kCodeLater,
     // kCodeNone, kCodeNone}: the fast path gathers a lookup that falls outside
     // the allocated slots from there, so every gather yields the final code.
-    uint32_t codes_sent, dense_sent;   // index of the first sentinel in codes / dense
+    uint32_t codes_sent;           // index of the first sentinel in codes
+    // Tiled fast path (eval_tiled_kernel, eval_batch_kernel), verified on the
+    // host: brick indices below 2^23 and sub-voxel indices below sub_dim, so
+    // that with float offsets o the packed pipeline forms
+    //   bits(2^23 + trunc(ox) + trunc(oy) up_dim_x + trunc(|oz|) up_dim_2) = kMagic + brick
+    //   bits(1.5 2^23 + qx + qy sub_dim +- qz sub_dim^2)                    = kMagic15 + sub
+    // exactly (every term an integer below 2^22).  Gathers address
+    // codes_b + 2 (r sub_dim^3 + bits(...)), codes_b = codes - 2 kMagic15 (bytes).
+    int32_t tiled;                 // 1 when the conditions hold
+    int32_t min0;                  // the map's min corner is (0, 0, 0): offsets are the coordinates
+    float up_dim_x_f, up_dim_2_f, sub_dim_f, sub_dim_2_f;
+    float zlo, zhi;                // fast z offsets: zlo < oz < zhi
+    float neg_zero;                // -0.0f: the addend of exact products formed by FMA
+    uint32_t upb_lim;              // kMagic + grid_occ_size
+    uint32_t sent_miss, sent_later, sent_none;   // sentinels in the biased index
+    unsigned long long codes_b;
 };
 
 constexpr int kSentinels = 4;
@@ -161,6 +171,7 @@ struct EvalBuffers {
     long long* sum_fx;       // P: fixed-point likelihood sums
     float* raw;              // P: un-normalised weights
     uint32_t* hits;          // P
+    uint32_t* nin;           // P: kept points within max_range (subsampled scans)
     long long* lut_fx;       // kNumCodes fixed-point likelihoods
     float* lut_f;            // kNumCodes float likelihoods
     int32_t* counts;         // [0] = points in range
@@ -181,8 +192,17 @@ size_t eval_smem_bytes(bool serial, int n);
 int tiled_pass_points(const MapView& m, bool dense);
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
                      bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
+// nin: per-particle points within max_range when the particles scored
+// different point subsets (n_points each), else null (the scan's count).
+// log_domain: weights from ln raw - LSE in double (TSDFL_NORM_LOG).
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
-                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s);
+                const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s,
+                const uint32_t* nin = nullptr, bool log_domain = false);
+// Seeded per-particle subsampling (subsample.h): K of the N staged points per
+// particle, exact fixed-point sums, hits and in-range counts into b.sum_fx,
+// b.hits, b.nin.  Needs a map on the tiled path (TSDFL_ERR_UNSUPPORTED else).
+int launch_eval_subsample(const MapView& m, float a_hit, int P, int N, int K, unsigned long long seed, float c_in,
+                          const EvalBuffers& b, int sm_count, cudaStream_t s);
 int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s);
 
 // Many filters' scoring in one persistent launch (eval_batch_kernel).  One
@@ -221,11 +241,10 @@ int launch_best_particle(const float* particles, size_t M, unsigned long long* k
                          cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
-// Fills the compact layout: brick b (of n) copies sub3 codes from codes[src[b]]
-// to dense[dst[b]]; skirt[b] != 0 also fills the sub3 slots before dst[b] from
-// the sub3 before src[b] (kCodeMiss below 0).
-int launch_compact_fill(const uint16_t* codes, const int64_t* src, const int64_t* dst, const uint8_t* skirt,
-                        uint32_t n, uint32_t sub3, uint16_t* dense, cudaStream_t s);
+// Half-precision slot values (round to nearest): from codes through the
+// code -> value table, or from float slots when codes is null.
+int launch_halves(const uint16_t* codes, const float* code_values, const float* data, size_t n, uint16_t* h16,
+                  cudaStream_t s);
 
 // Scan reduction of a PointCloud2 (scan.cu); workspace: scan_workspace_bytes(n).
 size_t scan_workspace_bytes(size_t n);
