@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-scan", action="store_true", help="skip the scan-reduction and motion side measurements")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the global-localisation, batched and served measurements of the default run")
+    ap.add_argument("--batch-steps", type=int, default=20, help="graph replays timed by the batched measurement")
+    ap.add_argument("--served-seconds", type=float, default=2.0, help="arrival window of the served measurement")
     return ap.parse_args()
 
 
@@ -198,12 +202,27 @@ def accuracy_vs_fp64(om, wl, dmap, n: int = 4000) -> dict:
     mean64 = np.concatenate([(q[:, :3] * w64[:, None]).sum(0),
                              [np.arctan2((np.sin(q[:, k]) * w64).sum(), (np.cos(q[:, k]) * w64).sum())
                               for k in (3, 4, 5)]])
-    return {"particles": int(parts.shape[0]), "points": int(wl.points.shape[0]),
-            "max_rel_raw_weight": float(rel.max()), "max_rel_normalised_weight": float(rel_w.max()),
-            "reference_float_sum_max_rel": float(rel_ref.max()),
-            "hits_equal_oracle": bool(np.array_equal(d["hits"], ref["hits"])),
-            "mean_pose_max_abs_err": float(np.abs(d["pose"].astype(np.float64) - mean64).max()),
-            "tolerance": 1e-5}
+    out = {"particles": int(parts.shape[0]), "points": int(wl.points.shape[0]),
+           "max_rel_raw_weight": float(rel.max()), "max_rel_normalised_weight": float(rel_w.max()),
+           "reference_float_sum_max_rel": float(rel_ref.max()),
+           "hits_equal_oracle": bool(np.array_equal(d["hits"], ref["hits"])),
+           "mean_pose_max_abs_err": float(np.abs(d["pose"].astype(np.float64) - mean64).max()),
+           "tolerance": 1e-5}
+    # the half-precision storage variant on the same sample (an accuracy line)
+    from tsdf_localization_gb300 import DeviceMap
+    hmap = DeviceMap(dmap.ctx, wl.coef, wl.grid_occ, codes=wl.codes, f16=True)
+    ph = parts.copy()
+    dh = TSDFEvaluator(hmap).evaluate_debug(ph, wl.points, wl.tf)
+    hmap.close()
+    pl = parts.copy()
+    TSDFEvaluator(dmap, log_normalise=True).evaluate(pl, wl.points, wl.tf)
+    out["log_domain_normaliser"] = {"max_rel_normalised_weight":
+                                    float((np.abs(pl[:, 6].astype(np.float64) - w64) / w64).max())}
+    out["f16_storage"] = {"max_rel_raw_weight": float((np.abs(dh["raw"].astype(np.float64) - f64) / f64).max()),
+                          "max_rel_normalised_weight":
+                              float((np.abs(ph[:, 6].astype(np.float64) - w64) / w64).max()),
+                          "hits_equal_oracle": bool(np.array_equal(dh["hits"], ref["hits"]))}
+    return out
 
 
 def _reference_map(O, wl):
@@ -436,25 +455,16 @@ def plain_rate(ctx, stream, dev: str, flush) -> float:
     return 100_000 * 8192 / (float(np.median(pt)) / 1000.0)
 
 
-def run_served(args, rank: int, world: int, local: int) -> None:
+def served_measure(args, local: int, worlds, ctx, stream, maps, seconds: float) -> dict:
     """Served localization: robots over the four maps submit scans as Poisson
     arrivals (10-20 Hz each) to the native request loop for a fixed window;
     particle counts log-uniform in [5k, 500k] (2 % of the robots at 1M), scans
-    uniform in [2k, 16k] points.  Reports the served aggregate rate, p50/p99
+    uniform in [2k, 16k] points.  Returns the served aggregate rate, p50/p99
     latency of the published updates (submission to publication, host clock),
     and what admission refused."""
-    import torch
-
-    from tsdf_localization_gb300 import Context, DeviceMap, LocalizationServer
+    from tsdf_localization_gb300 import LocalizationServer
     from tsdf_localization_gb300 import synth
-    dev = f"cuda:{local}"
-    torch.cuda.set_device(local)
-    worlds, _ = batch_workload(1)
-    ctx = Context(local)
-    stream = torch.cuda.Stream()
-    ctx.set_stream(stream.cuda_stream)
-    maps = [DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True) for wl in worlds]
-    rng = np.random.default_rng(17 + rank)
+    rng = np.random.default_rng(17 + local)
     srv = LocalizationServer(ctx, hbm_budget=150 << 30, max_sessions=args.sessions, max_points=16000,
                              max_wait_ms=args.max_wait_ms, max_queue=2)
     robots = []
@@ -491,7 +501,7 @@ def run_served(args, rank: int, world: int, local: int) -> None:
     with ClockSampler(local) as clk:
         while True:
             now = time.perf_counter() - t0
-            if now >= args.seconds:
+            if now >= seconds:
                 break
             for r in robots:
                 while r["next"] <= now:
@@ -518,46 +528,65 @@ def run_served(args, rank: int, world: int, local: int) -> None:
                 lat.append(res[1])
                 tickets.pop(t)
     st = srv.stats()
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    plain = plain_rate(ctx, stream, dev, flush)
-    value = served_pp / window
-    if rank == 0:
-        Pv = np.array([r["P"] for r in robots])
-        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": int(len(lat)),
-               "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": {"workload": f"{args.sessions} served robots over room/building/warehouse/tunnel maps",
-                          "sessions_open": len(robots), "sessions_refused": refused_open,
-                          "particles_range": [int(Pv.min()), int(Pv.max())], "bursts_1M": int((Pv >= 1_000_000).sum()),
-                          "arrivals": "Poisson 10-20 Hz per robot", "window_s": window,
-                          "hbm_budget_gb": 150, "max_wait_ms": args.max_wait_ms, "form": "served: native request loop, "
-                          "continuous batching over two dispatch slots", "parallelism": f"replicas x{world}"},
-               "served": {"offered_pp_per_s": offered_pp / window, "served_pp_per_s": value,
-                          "submitted": st["accepted"] - base["accepted"] + st["refused"] - base["refused"],
-                          "refused": st["refused"] - base["refused"], "published": len(lat),
-                          "batches": st["batches"] - base["batches"]},
-               "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
-                              "p99": float(np.percentile(lat, 99)) if lat else None},
-               "vs_plain": value / plain, "plain_value": plain,
-               "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": clocks}
-        print(json.dumps(out), flush=True)
+    srv.close()
+    Pv = np.array([r["P"] for r in robots])
+    return {"workload": f"{args.sessions} served robots over room/building/warehouse/tunnel maps",
+            "sessions_open": len(robots), "sessions_refused": refused_open,
+            "particles_range": [int(Pv.min()), int(Pv.max())], "bursts_1M": int((Pv >= 1_000_000).sum()),
+            "arrivals": "Poisson 10-20 Hz per robot", "window_s": window, "hbm_budget_gb": 150,
+            "max_wait_ms": args.max_wait_ms,
+            "form": "served: native request loop, continuous batching over two dispatch slots",
+            "value": served_pp / window, "unit": UNIT,
+            "offered_pp_per_s": offered_pp / window,
+            "submitted": st["accepted"] - base["accepted"] + st["refused"] - base["refused"],
+            "refused": st["refused"] - base["refused"], "published": len(lat),
+            "batches": st["batches"] - base["batches"],
+            "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
+                           "p99": float(np.percentile(lat, 99)) if lat else None},
+            "clocks": clocks}
 
 
-def run_batch(args, rank: int, world: int, local: int) -> None:
-    """Batched uneven filters: one update of every filter per step (graph
-    replay of prepare, the persistent scoring launch, normalise, resample),
-    with new resampling draws written before each step."""
+def run_served(args, rank: int, world: int, local: int) -> None:
+    """--workload served: the served measurement as the bench's line, with the
+    plain single-filter rate beside it."""
     import torch
 
-    from tsdf_localization_gb300 import Context, DeviceMap, FilterBatch
-    from tsdf_localization_gb300 import _native as N
+    from tsdf_localization_gb300 import Context, DeviceMap
     dev = f"cuda:{local}"
     torch.cuda.set_device(local)
-    worlds, specs = batch_workload(args.filters)
+    worlds, _ = batch_workload(1)
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     maps = [DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True) for wl in worlds]
+    sv = served_measure(args, local, worlds, ctx, stream, maps, args.seconds)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    plain = plain_rate(ctx, stream, dev, flush)
+    if rank == 0:
+        out = {"metric": METRIC, "value": sv["value"], "unit": UNIT, "n_gpus": world, "steps": sv["published"],
+               "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {k: sv[k] for k in ("workload", "sessions_open", "sessions_refused", "particles_range",
+                                             "bursts_1M", "arrivals", "window_s", "hbm_budget_gb", "max_wait_ms",
+                                             "form")} | {"parallelism": f"replicas x{world}"},
+               "served": {"offered_pp_per_s": sv["offered_pp_per_s"], "served_pp_per_s": sv["value"],
+                          "submitted": sv["submitted"], "refused": sv["refused"], "published": sv["published"],
+                          "batches": sv["batches"]},
+               "latency_ms": sv["latency_ms"], "vs_plain": sv["value"] / plain, "plain_value": plain,
+               "roofline": None, "cpu_baseline": None, "e2e": None, "gpu_launches": None, "clocks": sv["clocks"]}
+        print(json.dumps(out), flush=True)
+
+
+def batch_measure(args, local: int, worlds, specs, ctx, stream, maps, flush) -> dict:
+    """Batched uneven filters: one update of every filter per step (graph
+    replay of prepare, the persistent scoring launch, normalise, resample),
+    with new resampling draws written before each step.  Returns the rate, the
+    step latencies, the autotuned tiles and the scoring launch's roofline."""
+    import torch
+
+    from tsdf_localization_gb300 import FilterBatch
+    from tsdf_localization_gb300 import _native as N
+    dev = f"cuda:{local}"
     keep, fs = [], []
     total_pp = 0
     for mi, parts, pts in specs:
@@ -577,7 +606,7 @@ def run_batch(args, rank: int, world: int, local: int) -> None:
     batch = FilterBatch(ctx, fs)
     info = batch.info()
     lib = N.lib()
-    rng = np.random.default_rng(5 + rank)
+    rng = np.random.default_rng(5 + local)
     u0_all = torch.zeros(len(fs), dtype=torch.float32).pin_memory()
     d_u0s = [k[3] for k in keep]
     Ps = np.array([f["P"] for f in fs], np.float64)
@@ -587,7 +616,6 @@ def run_batch(args, rank: int, world: int, local: int) -> None:
         for i, d in enumerate(d_u0s):
             d.copy_(u0_all[i:i + 1], non_blocking=True)
 
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     with torch.cuda.stream(stream):
         new_draws()
         batch.run()
@@ -600,10 +628,11 @@ def run_batch(args, rank: int, world: int, local: int) -> None:
         ctx.sync()
         torch.cuda.synchronize()
         l0 = lib.tsdfl_launch_count()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        steps = args.batch_steps
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         with ClockSampler(local) as clk:
-            for i in range(args.steps):
+            for i in range(steps):
                 flush.zero_()
                 starts[i].record(stream)
                 new_draws()
@@ -614,35 +643,151 @@ def run_batch(args, rank: int, world: int, local: int) -> None:
             torch.cuda.synchronize()
         launches = lib.tsdfl_launch_count() - l0
         clocks = clk.summary()
+    batch.close()
+    del keep
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    total_ms = max_over_ranks(float(np.sum(step_ms)), device=dev)
-    value = total_pp * args.steps * world / (total_ms / 1000.0)
-    plain = plain_rate(ctx, stream, dev, flush)
+    total_ms = float(np.sum(step_ms))
     peak, peak_src = measured_peaks()
     alg = 2.0 * total_pp + sum(56.0 * f["P"] + 12.0 * f["N"] for f in fs)
     achieved = alg / (score_ms / 1000.0) / 1e9
+    Pv = np.array([f["P"] for f in fs])
+    Nv = np.array([f["N"] for f in fs])
+    return {"workload": f"{len(fs)} batched filters over room/building/warehouse/tunnel maps",
+            "filters": len(fs), "particles_total": int(Pv.sum()), "particles_range": [int(Pv.min()), int(Pv.max())],
+            "points_range": [int(Nv.min()), int(Nv.max())], "particle_points_per_step": int(total_pp),
+            "layout": "compact", "tiles": [chunk, group], "segments": info["segments"],
+            "work_batches": info["batches"],
+            "form": "batched: one persistent scoring launch, graph-replayed update",
+            "l2": "flushed (512 MB write) before every timed step",
+            "steps": steps, "value": total_pp * steps / (total_ms / 1000.0), "unit": UNIT,
+            "ms_per_step": total_ms / steps, "gpu_launches": int(launches),
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "eval_batch_kernel",
+                         "kernel_ms": score_ms, "peak_source": peak_src, "algorithmic_bytes": alg},
+            "clocks": clocks}
+
+
+def run_batch(args, rank: int, world: int, local: int) -> None:
+    """--workload batch: the batched measurement as the bench's line, with the
+    plain single-filter rate beside it."""
+    import torch
+
+    from tsdf_localization_gb300 import Context, DeviceMap
+    dev = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    worlds, specs = batch_workload(args.filters)
+    ctx = Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    maps = [DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True) for wl in worlds]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    args.batch_steps = args.steps
+    bm = batch_measure(args, local, worlds, specs, ctx, stream, maps, flush)
+    total_ms = max_over_ranks(bm["ms_per_step"] * args.steps, device=dev)
+    value = bm["particle_points_per_step"] * args.steps * world / (total_ms / 1000.0)
+    plain = plain_rate(ctx, stream, dev, flush)
     if rank == 0:
-        Pv = np.array([f["P"] for f in fs])
-        Nv = np.array([f["N"] for f in fs])
+        cfg = {k: bm[k] for k in ("workload", "filters", "particles_total", "particles_range", "points_range",
+                                  "particle_points_per_step", "layout", "tiles", "segments", "work_batches", "form",
+                                  "l2")}
+        cfg["parallelism"] = f"replicas x{world}"
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": {"workload": f"{len(fs)} batched filters over room/building/warehouse/tunnel maps",
-                          "filters": len(fs), "particles_total": int(Pv.sum()), "particles_range": [int(Pv.min()),
-                                                                                                    int(Pv.max())],
-                          "points_range": [int(Nv.min()), int(Nv.max())], "particle_points_per_step": int(total_pp),
-                          "layout": "compact", "tiles": [chunk, group], "segments": info["segments"],
-                          "work_batches": info["batches"], "form": "batched: one persistent scoring launch, "
-                                                                   "graph-replayed update",
-                          "l2": "flushed (512 MB write) before every timed step", "parallelism": f"replicas x{world}"},
-               "vs_plain": value / plain, "plain_value": plain,
-               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None, "kernel": "eval_batch_kernel",
-                            "kernel_ms": score_ms, "peak_source": peak_src, "algorithmic_bytes": alg},
-               "cpu_baseline": None, "e2e": None, "gpu_launches": int(launches),
-               "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
-               "clocks": clocks}
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+               "vs_plain": value / plain, "plain_value": plain, "roofline": bm["roofline"],
+               "cpu_baseline": None, "e2e": None, "gpu_launches": bm["gpu_launches"],
+               "latency_ms": bm["latency_ms"], "clocks": bm["clocks"]}
         print(json.dumps(out), flush=True)
+
+
+def global_measure(args, local: int, ctx, stream, flush, steps: int = 5, warmup: int = 3) -> dict:
+    """Global localisation (1,000,000 particles uniform over the seed-3
+    building's free space, any yaw, 2,048 points): update plus systematic
+    resampling on the device, L2 flushed before every step; the scoring
+    kernel's time and roofline."""
+    import torch
+
+    from tsdf_localization_gb300 import DeviceMap
+    from tsdf_localization_gb300 import _native as N
+    from tsdf_localization_gb300 import synth
+    dev = f"cuda:{local}"
+    lib = N.lib()
+    wl = synth.global_workload(seed=3, n_particles=1_000_000, n_points=2048)
+    P, Npts = int(wl.particles.shape[0]), int(wl.points.shape[0])
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True)
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    tfp = np.ascontiguousarray(wl.tf, np.float32)
+    d_part = torch.from_numpy(wl.particles).to(dev)
+    d_pts = torch.from_numpy(wl.points).to(dev)
+    cap = 2 * P + 16
+    d_out = torch.empty((cap, 7), dtype=torch.float32, device=dev)
+    d_cnt = torch.zeros(4, dtype=torch.int32, device=dev)
+    d_pose = torch.zeros(8, dtype=torch.float32, device=dev)
+    rng = np.random.default_rng(4321)
+    vp = C.c_void_p
+    ctx.reserve(P, Npts)
+
+    def step():
+        N.check(lib.tsdfl_evaluate_device(ctx.handle, dmap.handle, C.byref(model), vp(d_part.data_ptr()), P,
+                                          vp(d_pts.data_ptr()), Npts, tfp.ctypes.data_as(vp), 0,
+                                          vp(d_pose.data_ptr())))
+        N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(d_part.data_ptr()), P,
+                                                     float(np.float32(rng.random() / P)), vp(d_out.data_ptr()), cap,
+                                                     vp(d_cnt.data_ptr())))
+
+    lib.tsdfl_ctx_set_timing(ctx.handle, 1)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+        ctx.sync()
+        ms, kms = [], []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            k = C.c_float()
+            N.check(lib.tsdfl_ctx_last_timing(ctx.handle, C.byref(k)))
+            kms.append(k.value)
+        ctx.sync()
+    lib.tsdfl_ctx_set_timing(ctx.handle, 0)
+    peak, peak_src = measured_peaks()
+    kmed = float(np.median(kms))
+    alg = roofline_bytes(P, Npts, "compact")
+    dmap.close()
+    return {"workload": wl.name, "particles": P, "points": Npts, "steps": steps,
+            "step": "sensor update + normalise + mean pose + systematic resample (FP64 CDF)",
+            "value": P * Npts * steps / (float(np.sum(ms)) / 1000.0), "unit": UNIT,
+            "ms_per_step": float(np.mean(ms)),
+            "roofline": {"bound": "hbm", "achieved": alg / (kmed / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (kmed / 1000.0) / 1e9 / peak, "traffic": None, "kernel": "eval_tiled_kernel",
+                         "kernel_ms": kmed, "peak_source": peak_src, "algorithmic_bytes": alg}}
+
+
+def sub_measurements(args, local: int, ctx, stream, flush, plain_value: float) -> dict:
+    """The default run's side lines: global localisation, the batched filters
+    and the served sessions, each with its rate against the plain line."""
+    from tsdf_localization_gb300 import DeviceMap
+    out = {}
+    g = global_measure(args, local, ctx, stream, flush)
+    g["vs_plain"] = g["value"] / plain_value
+    out["global"] = g
+    worlds, specs = batch_workload(args.filters)
+    maps = [DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True) for wl in worlds]
+    b = batch_measure(args, local, worlds, specs, ctx, stream, maps, flush)
+    b["vs_plain"] = b["value"] / plain_value
+    out["batch"] = b
+    sv = served_measure(args, local, worlds, ctx, stream, maps, args.served_seconds)
+    sv["vs_plain"] = sv["value"] / plain_value
+    out["served"] = sv
+    for m in maps:
+        m.close()
+    return out
 
 
 def max_over_ranks(x: float, device=None) -> float:
@@ -787,8 +932,9 @@ def main():
     peak, peak_src = measured_peaks()
     achieved = alg / (kmed / 1000.0) / 1e9
     # DRAM bytes of one scoring launch from an ncu capture of this exact workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum, single pass, full size)
-    measured_traffic = {("building", 100_000, 8192, "compact", "fast"): 2.187e9 + 0.0576e9}
+    # (dram__bytes_read.sum + dram__bytes_write.sum, single pass, full size;
+    # profiles/eval_tiled_kernel_building_100k_x_8192.md)
+    measured_traffic = {("building", 100_000, 8192, "compact", "fast"): 1.326252e9 + 0.054576e9}
     traffic = measured_traffic.get((args.workload, P, Npts, args.layout, args.kernel))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "eval_tiled_kernel" if (args.kernel == "fast" and info["fast_index"])
@@ -852,6 +998,9 @@ def main():
         if args.workload in ("building", "global"):
             tracking = tracking_side(lib, ctx, stream, wl, dmap, f"cuda:{local}",
                                      100 if args.workload == "building" else 50)
+    subs = {}
+    if world == 1 and args.workload == "building" and not args.no_sub:
+        subs = sub_measurements(args, local, ctx, stream, flush, value)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -865,7 +1014,7 @@ def main():
                           "form": "plain single filter", "parallelism": f"replicas x{world}"},
                "roofline": roof, "cpu_baseline": base, "e2e": e2e, "gpu_launches": int(launches),
                "latency_ms": latency, "clocks": clocks, "scan_reduction": scan,
-               "motion_update": motion, "tracking": tracking}
+               "motion_update": motion, "tracking": tracking, **subs}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()

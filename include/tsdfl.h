@@ -78,6 +78,9 @@ int tsdfl_ctx_reserve(tsdfl_ctx* ctx, size_t P, size_t N);
 int tsdfl_ctx_set_timing(tsdfl_ctx* ctx, int enable);
 int tsdfl_ctx_last_timing(tsdfl_ctx* ctx, float* eval_kernel_ms);
 uint64_t tsdfl_launch_count(void);
+/* Device bytes the context holds for evaluations and for resampling (each
+ * grows on demand; either may be NULL). */
+int tsdfl_ctx_workspace_bytes(const tsdfl_ctx* ctx, size_t* eval_bytes, size_t* resample_bytes);
 
 /* ---- map ----
  * Uploads a built CudaSubVoxelMap<float,float> (coef(), rawGridOcc(),
@@ -85,13 +88,18 @@ uint64_t tsdfl_launch_count(void);
  * cuda_evaluator.cu:21-59).  When every slot equals one of the likelihood
  * values of createTSDFMap for `sigma` (map_util.h:68-71,124-127), slots are
  * stored as 16-bit codes, losslessly; otherwise as float.  flags: TSDFL_MAP_*. */
-/* TSDFL_MAP_DENSE: also build the compact layout -- the allocated bricks in
- * brick-index order, a skirt of slots below layer z = 0, brick ranks from a
- * bitmap held in shared memory -- so the tiled kernel makes one map gather per
- * lookup instead of two.  Skipped (brick layout only) when a sub-voxel index
- * can reach sub_dim or the slots exceed 2^31. */
+/* TSDFL_MAP_DENSE: also build the compact layout -- brick ranks from a bitmap
+ * of the brick grid held in shared memory, read beside the slot codes (which
+ * stay in the reference's data order) -- so the tiled kernel makes one map
+ * gather per lookup instead of two.  Skipped (brick layout only) when a
+ * sub-voxel index can reach sub_dim or the bitmap exceeds 128 KB.
+ * TSDFL_MAP_F16: store every slot's likelihood value as an IEEE half instead
+ * of a 16-bit code (the same 2 bytes a slot): values round to 11 significant
+ * bits, so weights move by up to about 5e-4 relative -- an accuracy variant
+ * scored by the generic kernel, not bit-exact with the reference. */
 #define TSDFL_MAP_DENSE 1u
 #define TSDFL_MAP_FORCE_F32 2u    /* keep float slots */
+#define TSDFL_MAP_F16 4u
 int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
                      float sigma, uint32_t flags, tsdfl_map** out);
 /* Same map from 16-bit slot codes (code c < 600: likelihood of |tsdf| = c mm;
@@ -150,6 +158,12 @@ void tsdfl_free(void* p);
 #define TSDFL_SUM_EXACT 0u    /* order-independent fixed-point likelihood sums (default) */
 #define TSDFL_SUM_SERIAL 1u   /* reference order float sums: raw weights bit-identical */
 #define TSDFL_EVAL_GENERIC 4u /* exact sums with the generic (division-based) scoring kernel */
+/* Normalise in the log domain: w_i = exp(ln raw_i - LSE), LSE = ln max_j raw_j
+ * + ln sum_j exp(ln raw_j - ln max_j raw_j), all in double, instead of
+ * raw_i / sum_j raw_j.  The same weights up to the final rounding for this
+ * sensor model (raw weights are sums of bounded scores); for callers that
+ * keep the reference's linear normalisation optional. */
+#define TSDFL_NORM_LOG 8u
 int tsdfl_evaluate(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles, size_t P,
                    const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6]);
 
@@ -425,14 +439,37 @@ int tsdfl_motion_apply(tsdfl_ctx* ctx, float* particles, size_t P, const double*
 int tsdfl_pose_array_device(tsdfl_ctx* ctx, const float* d_particles, size_t P, double* d_poses);
 int tsdfl_pose_array(tsdfl_ctx* ctx, const float* particles, size_t P, double* poses);
 
+/* ---- seeded per-particle scan subsampling ----
+ * No counterpart in the reference (its evaluator scores every reduced point
+ * for every particle).  The sensor update of tsdfl_evaluate_device with each
+ * particle scoring K of the N points: particle i keeps one point from each of
+ * K strata of consecutive scan indices, [floor(k N / K), floor((k+1) N / K)),
+ * chosen by a SplitMix64 stream seeded from (seed, i) -- tsdfl_subsample_index
+ * gives the k-th kept scan index.  Weights, normalisation and mean pose as in
+ * tsdfl_evaluate_device, each particle's range term counting its own kept
+ * points.  Needs a code map on the tiled path (TSDFL_ERR_UNSUPPORTED
+ * otherwise); 0 < K <= N.  The host form optionally returns the un-normalised
+ * weights and hit counts. */
+int tsdfl_evaluate_subsampled_device(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model,
+                                     float* d_particles, size_t P, const float* d_points, size_t N, const float tf[16],
+                                     size_t K, uint64_t seed, float* d_pose_out);
+int tsdfl_evaluate_subsampled(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_model* model, float* particles,
+                              size_t P, const float* points, size_t N, const float tf[16], size_t K, uint64_t seed,
+                              float pose_out[6], float* raw_out, uint32_t* hits_out);
+/* Scan index of the k-th point particle `particle` keeps (0xffffffff for
+ * arguments outside 0 <= k < K <= N). */
+uint32_t tsdfl_subsample_index(uint64_t seed, uint64_t particle, uint32_t N, uint32_t K, uint32_t k);
+
 /* No counterpart in the reference.  tsdfl_resample_systematic_device for
  * callers that must not allocate device memory while their filter runs: the
  * scratch is a fixed area compiled into the library (one per device, about
  * 2.2 MB) instead of the context's growable workspace, so M is limited to
  * 262144 particles (larger M: TSDFL_ERR_UNSUPPORTED, nothing launched).
  * Same arguments, results and error reporting as the device form.  The first
- * call on a device looks the scratch up (cudaGetSymbolAddress): make it before
- * any stream capture.  Nothing in the scratch has to start at zero.  Calls
+ * call on a device looks the scratch up (cudaGetSymbolAddress), and so does
+ * the first call after the device's context changed (cudaDeviceReset): make
+ * those calls before any stream capture.  Nothing in the scratch has to start
+ * at zero.  Calls
  * whose work overlaps on one device (different streams or host threads with
  * no ordering between them) share the scratch and race: order them. */
 int tsdfl_resample_systematic_static(tsdfl_ctx* ctx, const float* d_particles, size_t M, float u0,

@@ -90,6 +90,8 @@ def oracle() -> C.CDLL:
         L.orc_motion_apply.argtypes = [P, SZ, P]
         L.orc_reduce_scan.restype = SZ
         L.orc_reduce_scan.argtypes = [P, P, SZ, C.c_float, C.c_int, P, SZ]
+        L.orc_subsample_indices.restype = None
+        L.orc_subsample_indices.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, P]
         L.orc_resample_residual_systematic.restype = SZ
         L.orc_resample_residual_systematic.argtypes = [P, SZ, C.c_float, P, SZ]
         _orc = L
@@ -236,6 +238,31 @@ def evaluate(m: OracleMap, particles: np.ndarray, points: np.ndarray, tf, model=
     rc = L.orc_evaluate(C.byref(m.coef), _ptr(m.grid_occ), _ptr(d), C.byref(mdl), _ptr(particles), Pn, _ptr(pts),
                         Nn, _ptr(tfa), _ptr(raw), _ptr(hits), _ptr(idx), _ptr(s64), _ptr(pose), threads)
     return {"rc": rc, "raw": raw, "hits": hits, "sum64": s64, "voxel_index": idx, "pose": pose}
+
+
+def subsample_indices(seed: int, i: int, N: int, K: int) -> np.ndarray:
+    """The K scan indices particle i keeps under the library's seeded
+    subsampling rule."""
+    out = np.zeros(max(K, 1), np.uint32)
+    oracle().orc_subsample_indices(seed, i, N, K, _ptr(out))
+    return out[:K]
+
+
+def evaluate_subsampled(m: OracleMap, particles: np.ndarray, points: np.ndarray, tf, K: int, seed: int,
+                        model=(0.9, 0.1, 0.0, 100.0)) -> dict:
+    """Every particle scored on its own K kept points (evaluatePose's loop per
+    particle): raw float sums, hits and FP64 sums; weights normalised over the
+    particles as TSDFEvaluator::evaluate does."""
+    P, N = particles.shape[0], points.shape[0]
+    raw = np.zeros(P, np.float32)
+    hits = np.zeros(P, np.uint32)
+    s64 = np.zeros(P, np.float64)
+    pts = np.ascontiguousarray(points, np.float32)
+    for i in range(P):
+        idx = subsample_indices(seed, i, N, K)
+        r = evaluate(m, np.ascontiguousarray(particles[i:i + 1]).copy(), pts[idx], tf, model, threads=1)
+        raw[i], hits[i], s64[i] = r["raw"][0], r["hits"][0], r["sum64"][0]
+    return {"raw": raw, "hits": hits, "sum64": s64}
 
 
 def particle_pose(particle7, tf) -> np.ndarray:

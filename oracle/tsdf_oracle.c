@@ -674,3 +674,25 @@ void orc_pose_array(const float* particles, size_t P, double* poses)
         o[6] = cr * cp * cy + sr * sp * sy;
     }
 }
+
+/* Seeded per-particle subsampling (the library's own feature; the reference
+ * scores every point): one point from each stratum [floor(k N / K),
+ * floor((k+1) N / K)), picked by the upper 32 bits of the k-th output of a
+ * SplitMix64 stream (Steele, Lea and Flood 2014) started at
+ * mix(seed ^ mix(i)), scaled to the stratum by a 32x32 -> 64-bit product. */
+static uint64_t orc_mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void orc_subsample_indices(uint64_t seed, uint64_t i, uint32_t N, uint32_t K, uint32_t* out)
+{
+    const uint64_t state = orc_mix64(seed ^ orc_mix64(i));
+    for (uint32_t k = 0; k < K; ++k) {
+        const uint64_t lo = (uint64_t)k * N / K, hi = (uint64_t)(k + 1) * N / K;
+        const uint64_t u = orc_mix64(state + (uint64_t)(k + 1) * 0x9E3779B97F4A7C15ull) >> 32;
+        out[k] = (uint32_t)(lo + ((u * (hi - lo)) >> 32));
+    }
+}

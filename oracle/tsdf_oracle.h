@@ -167,6 +167,10 @@ void orc_philox4x64_10(uint64_t c[4], uint64_t k0, uint64_t k1);
 float orc_philox_u(void* src, size_t i, uint32_t t);
 uint32_t orc_philox_j(void* src, size_t i, uint32_t t);
 
+/* The library's seeded per-particle subsampling rule (no counterpart in the
+ * reference): the K kept scan indices of particle i, out[K]. */
+void orc_subsample_indices(uint64_t seed, uint64_t i, uint32_t N, uint32_t K, uint32_t* out);
+
 #ifdef __cplusplus
 }
 #endif

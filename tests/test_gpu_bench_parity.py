@@ -1,14 +1,15 @@
 """GPU parity on the workloads the bench reports, against the oracle.
 
 - the 100x100x10 m building at 0.05 m with 100,000 Gaussian particles x 8,192
-  points (compact layout, two-term sub-voxel multiplier, layer-0 skirts, the
-  compact-cloud scan order): a particle sample against the oracle, and all
-  100,000 particles across the two scoring kernels;
+  points (compact layout, two-term sub-voxel multiplier, points below the
+  map's floor, the compact-cloud scan order): a particle sample against the
+  oracle, and all 100,000 particles across the two scoring kernels;
 - global localisation on the seed-3 building: 1,000,000 particles uniform over
   free space (any yaw, the spread-cloud scan order) x 2,048 points, a sample
   against the oracle; systematic resampling of the device's own normalised
   weights at 1M bit for bit, and at 1M with weights below 2^-29 (the
-  binade-by-binade double sums).
+  binade-by-binade double sums); the variant where every particle scores 256
+  of the points, chosen per particle and seed.
 
 Bars (as in test_gpu_parity.py): slot codes and hit counts bit-exact; serial
 raw weights bit-exact; exact-mode weights within 1e-5 of the FP64 sums and no
@@ -151,3 +152,83 @@ def test_resample_1m_tiny_weights(ctx, kind):
         exp = O.resample_systematic(w, u0)
         assert got.shape == exp.shape
         assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("k", [256, 2048])
+def test_global_subsampled_matches_oracle(ctx, global_wl, k):
+    """C3's variant: every particle scores 256 of the 2,048 points, chosen per
+    particle and seed (k = 2048 keeps every point: the full update's sums);
+    hit counts bit-exact, weights within 1e-5 of FP64 and never farther from
+    it than the reference-order float sums."""
+    n = 2000
+    parts = np.ascontiguousarray(global_wl.particles[:: global_wl.particles.shape[0] // n][:n])
+    dmap = DeviceMap(ctx, global_wl.coef, global_wl.grid_occ, codes=global_wl.codes, dense=True)
+    om = O.OracleMap(O.coef_from(global_wl.coef), global_wl.grid_occ, global_wl.float_data())
+    seed = 20250
+    ref = O.evaluate_subsampled(om, parts, global_wl.points, global_wl.tf, k, seed)
+    p = parts.copy()
+    pose, raw, hits = TSDFEvaluator(dmap).evaluate_subsampled(p, global_wl.points, global_wl.tf, k, seed, debug=True)
+    assert np.array_equal(hits, ref["hits"])
+    f64 = ref["sum64"]
+    err_gpu = np.abs(raw.astype(np.float64) - f64)
+    err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
+    assert np.all(err_gpu <= WEIGHT_RTOL * f64)
+    assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
+    w64 = f64 / f64.sum()
+    assert np.all(np.abs(p[:, 6].astype(np.float64) - w64) <= WEIGHT_RTOL * w64)
+    if k == global_wl.points.shape[0]:   # every point kept: the full update's sums
+        d = TSDFEvaluator(dmap).evaluate_debug(parts.copy(), global_wl.points, global_wl.tf)
+        assert np.array_equal(d["raw"], raw) and np.array_equal(d["hits"], hits)
+    # the device form gives the same weights
+    import torch
+    dp = torch.from_numpy(parts.copy()).cuda()
+    dpts = torch.from_numpy(global_wl.points).cuda()
+    dpose = torch.zeros(8, dtype=torch.float32, device="cuda")
+    import ctypes as C
+    from tsdf_localization_gb300 import _native as N
+    tf = np.ascontiguousarray(global_wl.tf, np.float32)
+    model = N.Model(0.9, 0.1, 0.0, 100.0)
+    torch.cuda.synchronize()
+    N.check(N.lib().tsdfl_evaluate_subsampled_device(ctx.handle, dmap.handle, C.byref(model),
+                                                     C.c_void_p(dp.data_ptr()), n, C.c_void_p(dpts.data_ptr()),
+                                                     global_wl.points.shape[0], tf.ctypes.data_as(C.c_void_p), k,
+                                                     seed, C.c_void_p(dpose.data_ptr())))
+    ctx.sync()
+    assert np.array_equal(dp.cpu().numpy()[:, 6], p[:, 6])
+    assert np.array_equal(dpose.cpu().numpy()[:6], pose)
+
+
+def test_building_f16_storage_accuracy(ctx, building):
+    """The half-precision storage variant on C2's map: the same slots are hit
+    (indices do not depend on storage), and the weights stay within the
+    half-precision bound of FP64 -- an accuracy line, not the 1e-5 bar."""
+    parts = np.ascontiguousarray(building.particles[:: building.particles.shape[0] // 1000][:1000])
+    dmap = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, f16=True)
+    assert dmap.info()["storage"] == 2
+    om = O.OracleMap(O.coef_from(building.coef), building.grid_occ, building.float_data())
+    ref = O.evaluate(om, parts.copy(), building.points, building.tf)
+    p = parts.copy()
+    d = TSDFEvaluator(dmap).evaluate_debug(p, building.points, building.tf)
+    assert np.array_equal(d["hits"], ref["hits"])
+    rel = np.abs(d["raw"].astype(np.float64) - ref["sum64"]) / ref["sum64"]
+    assert rel.max() <= 2.0 ** -10
+    assert rel.max() > 1e-7   # the rounding is visible: it is a different storage
+    with pytest.raises(Exception):   # serial sums need exact slot values
+        TSDFEvaluator(dmap, serial_sums=True).evaluate(parts.copy(), building.points, building.tf)
+
+
+def test_building_log_domain_normaliser(ctx, building):
+    """TSDFL_NORM_LOG on C2's sample: the log-sum-exp weights are the linear
+    ones up to the final float rounding, and within 1e-5 of FP64."""
+    parts = np.ascontiguousarray(building.particles[:: building.particles.shape[0] // 2000][:2000])
+    dmap = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, dense=True)
+    om = O.OracleMap(O.coef_from(building.coef), building.grid_occ, building.float_data())
+    ref = O.evaluate(om, parts.copy(), building.points, building.tf)
+    w64 = ref["sum64"] / ref["sum64"].sum()
+    p_lin, p_log = parts.copy(), parts.copy()
+    TSDFEvaluator(dmap).evaluate(p_lin, building.points, building.tf)
+    pose = TSDFEvaluator(dmap, log_normalise=True).evaluate(p_log, building.points, building.tf)
+    assert pose is not None
+    assert np.all(np.abs(p_log[:, 6].astype(np.float64) - w64) <= WEIGHT_RTOL * w64)
+    rel = np.abs(p_log[:, 6].astype(np.float64) - p_lin[:, 6]) / p_lin[:, 6]
+    assert rel.max() <= 4 * 2.0 ** -24

@@ -122,3 +122,39 @@ def test_gpu_server_admission(ctx, worlds):
     sid = srv.open(dm, parts[:1000], wl.tf)
     assert srv.submit(sid, pts) is None   # any work would wait longer than the bound
     srv.close()
+
+
+def test_gpu_server_long_scans_and_failed_update(ctx, worlds):
+    """Scans of several shared-memory passes from every session in one batch,
+    and one session whose update fails (all scores zero: "No particle is
+    valid!"): that update is published with its error and the session keeps
+    its particles; every other update equals the single-filter calls, and the
+    server keeps serving all sessions afterwards."""
+    rng = np.random.default_rng(9)
+    srv = LocalizationServer(ctx, hbm_budget=8 << 30, max_sessions=6, max_points=40000, max_queue=2)
+    sessions = []
+    for i, P in enumerate([2000, 700, 5000, 1200, 3000]):
+        wl, dm = worlds[i % 2]
+        parts = synth.particles_gaussian(wl.true_pose, 0.3, np.deg2rad(5.0), P, 80 + i)
+        sessions.append({"sid": srv.open(dm, parts, wl.tf, seed=70 + i), "dm": dm, "wl": wl, "parts": parts,
+                         "seed": 70 + i})
+    wl, dm = worlds[0]
+    bad_parts = synth.particles_gaussian(wl.true_pose, 0.3, 0.1, 900, 99)
+    bad = srv.open(dm, bad_parts, wl.tf, model=(0.0, 0.0, 0.0, 100.0), seed=5)
+    for rnd in range(2):
+        tickets = {}
+        for s in sessions:
+            pts = rng.normal(0, 4, (int(rng.integers(20000, 40001)), 3)).astype(np.float32)
+            tickets[srv.submit(s["sid"], pts)] = (s, pts)
+        tb = srv.submit(bad, rng.normal(0, 4, (25000, 3)).astype(np.float32))
+        res = drain(srv, set(tickets) | {tb})
+        assert res[tb][2] == N.TSDFL_ERR_DEGENERATE
+        for t, (s, pts) in tickets.items():
+            u0 = LocalizationServer.draw(s["seed"], rnd, s["parts"].shape[0])
+            pose, s["parts"] = single_update(ctx, s["dm"], s["parts"], pts, s["wl"].tf, u0)
+            got_pose, _, st = res[t]
+            assert st == 0 and np.array_equal(got_pose, pose)
+    for s in sessions:
+        assert np.array_equal(srv.particles(s["sid"]), s["parts"])
+    assert np.array_equal(srv.particles(bad), bad_parts)
+    srv.close()

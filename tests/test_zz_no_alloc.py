@@ -71,3 +71,48 @@ def test_static_scratch_rejects_oversize():
             N.check(rc)
     finally:
         ctx.close()
+
+
+def _resample_ws(lib, ctx):
+    rs = C.c_size_t()
+    N.check(lib.tsdfl_ctx_workspace_bytes(ctx.handle, None, C.byref(rs)))
+    return rs.value
+
+
+def test_static_scratch_allocates_nothing():
+    """On a fresh context, with every buffer allocated beforehand: the static
+    form runs first (its first call only loads kernels and looks the scratch
+    up); the context's resampling workspace stays at zero bytes through both
+    static calls, and the second leaves the device's free memory exactly where
+    it was.  The device form called afterwards grows that workspace, which
+    shows the check would see it."""
+    torch = pytest.importorskip("torch")
+    lib = N.lib()
+    ctx = Context(0)
+    try:
+        m = 200_000
+        p1, p2 = _particles(m, 5), _particles(m, 6)
+        d1, d2 = torch.from_numpy(p1).cuda(), torch.from_numpy(p2).cuda()
+        cap = 2 * m + 16
+        out = torch.zeros((cap, 7), dtype=torch.float32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+
+        def call(fn, d_in, u0):
+            N.check(fn(ctx.handle, C.c_void_p(d_in.data_ptr()), m, np.float32(u0), C.c_void_p(out.data_ptr()), cap,
+                       C.c_void_p(cnt.data_ptr())))
+            ctx.sync()
+
+        assert _resample_ws(lib, ctx) == 0
+        call(lib.tsdfl_resample_systematic_static, d1, 1.0e-6)
+        free0 = torch.cuda.mem_get_info()[0]
+        call(lib.tsdfl_resample_systematic_static, d2, 2.0e-6)
+        assert torch.cuda.mem_get_info()[0] == free0
+        assert _resample_ws(lib, ctx) == 0
+        n_static = int(cnt.item())
+        got = out[:n_static].cpu().numpy()
+        call(lib.tsdfl_resample_systematic_device, d2, 2.0e-6)
+        assert _resample_ws(lib, ctx) > 0
+        assert int(cnt.item()) == n_static and np.array_equal(out[:n_static].cpu().numpy(), got)
+    finally:
+        ctx.close()

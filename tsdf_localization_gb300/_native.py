@@ -21,9 +21,11 @@ TSDFL_ERR_UNSUPPORTED = 7
 
 TSDFL_MAP_DENSE = 1
 TSDFL_MAP_FORCE_F32 = 2
+TSDFL_MAP_F16 = 4
 TSDFL_SUM_EXACT = 0
 TSDFL_SUM_SERIAL = 1
 TSDFL_EVAL_GENERIC = 4
+TSDFL_NORM_LOG = 8
 TSDFL_SCAN_OWN_RING = 1
 TSDFL_MOTION_ODOM, TSDFL_MOTION_IMU, TSDFL_MOTION_SCALE, TSDFL_MOTION_SCALE_IMU, TSDFL_MOTION_DELTA = range(5)
 
@@ -98,6 +100,7 @@ SIGNATURES = [
     ("tsdfl_ctx_set_timing", I, [P, I]),
     ("tsdfl_ctx_last_timing", I, [P, C.POINTER(F)]),
     ("tsdfl_launch_count", C.c_uint64, []),
+    ("tsdfl_ctx_workspace_bytes", I, [P, C.POINTER(SZ), C.POINTER(SZ)]),
     ("tsdfl_map_create", I, [P, C.POINTER(MapCoef), P, P, F, C.c_uint32, C.POINTER(P)]),
     ("tsdfl_map_create_codes", I, [P, C.POINTER(MapCoef), P, P, F, C.c_uint32, C.POINTER(P)]),
     ("tsdfl_map_destroy", I, [P]),
@@ -154,6 +157,9 @@ SIGNATURES = [
     ("tsdfl_motion_apply", I, [P, P, SZ, P]),
     ("tsdfl_evaluate_cloud", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, U32, U32, U32, F, U32, P, U32, P,
                                  C.POINTER(SZ)]),
+    ("tsdfl_evaluate_subsampled_device", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, SZ, C.c_uint64, P]),
+    ("tsdfl_evaluate_subsampled", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, SZ, C.c_uint64, P, P, P]),
+    ("tsdfl_subsample_index", U32, [C.c_uint64, C.c_uint64, U32, U32, U32]),
 ]
 
 SYNTH_SIGNATURES = [

@@ -18,6 +18,7 @@
 #include "map_host.h"
 #include "tsdfl.h"
 #include "tsdfl_internal.h"
+#include "subsample.h"
 
 namespace tsdfl {
 
@@ -88,13 +89,13 @@ struct tsdfl_map {
     tsdfl_map_coef coef{};
     MapView view{};
     int32_t* grid_occ = nullptr;
-    uint16_t* codes = nullptr;
+    uint16_t* codes = nullptr;    // the reference's slots (codes_base + miss brick)
+    uint16_t* codes_base = nullptr;   // the allocation: one brick of kCodeMiss, the slots, the sentinels
+    uint64_t codes_pre = 0;       // codes in front of the slots (sub_dim^3, or 0 for huge bricks)
     float* data = nullptr;
-    uint16_t* dense = nullptr;    // compact layout (TSDFL_MAP_DENSE)
-    uint64_t dense_slots = 0;     // its slots before the sentinels
-    uint32_t* occ = nullptr;      // its bitmap and prefix counts
-    uint32_t occ_words = 0;
-    uint32_t n0 = 0;
+    uint16_t* h16 = nullptr;      // TSDFL_MAP_F16: half-precision slot values
+    uint32_t* occ = nullptr;      // compact layout (TSDFL_MAP_DENSE): brick bitmap and prefix counts
+    uint32_t occ_bytes = 0;
     float* values = nullptr;      // kNumCodes likelihood values (device)
     float max_value = 0;
     uint64_t bricks = 0;
@@ -128,6 +129,7 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
     size_t o_f64 = take(sizeof(double) * nP);
     size_t o_raw = take(sizeof(float) * nP);
     size_t o_hits = take(sizeof(uint32_t) * nP);
+    size_t o_nin = take(sizeof(uint32_t) * nP);
     size_t o_xs = take(sizeof(float) * npad);
     size_t o_ys = take(sizeof(float) * npad);
     size_t o_zs = take(sizeof(float) * npad);
@@ -152,6 +154,7 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
         *sum_f64 = reinterpret_cast<double*>(b + o_f64);
         e->raw = reinterpret_cast<float*>(b + o_raw);
         e->hits = reinterpret_cast<uint32_t*>(b + o_hits);
+        e->nin = reinterpret_cast<uint32_t*>(b + o_nin);
         e->xs = reinterpret_cast<float*>(b + o_xs);
         e->ys = reinterpret_cast<float*>(b + o_ys);
         e->zs = reinterpret_cast<float*>(b + o_zs);
@@ -286,6 +289,53 @@ int validate_coef(const tsdfl_map_coef* c)
     return TSDFL_OK;
 }
 
+// The kSentinels codes after the last slot of a code array (MapView::codes_sent).
+cudaError_t write_sentinels(uint16_t* arr, size_t at, cudaStream_t s)
+{
+    static const uint16_t kSent[kSentinels] = {(uint16_t)kCodeMiss, (uint16_t)kCodeLater, (uint16_t)kCodeNone,
+                                               (uint16_t)kCodeNone};
+    return cudaMemcpyAsync(arr + at, kSent, sizeof(kSent), cudaMemcpyHostToDevice, s);
+}
+
+// The code array of a map: one brick of kCodeMiss in front of the n slots (what
+// a slot index below 0 reads: getIndex's wrapped 64-bit sum is a miss there),
+// the sentinels behind them.  Sets m->codes_base, m->codes_pre and m->codes.
+cudaError_t alloc_codes(tsdfl_map* m, size_t n, cudaStream_t s)
+{
+    const uint64_t S3 = m->coef.sub_dim * m->coef.sub_dim_2;
+    const uint64_t pre = S3 <= (1ull << 21) ? S3 : 0;
+    cudaError_t e = cudaMalloc(&m->codes_base, sizeof(uint16_t) * (pre + n + kSentinels));
+    if (e != cudaSuccess) {
+        m->codes_base = nullptr;
+        return e;
+    }
+    m->codes_pre = pre;
+    m->codes = m->codes_base + pre;
+    if (pre) {
+        std::vector<uint16_t> miss(pre, (uint16_t)kCodeMiss);
+        e = cudaMemcpy(m->codes_base, miss.data(), sizeof(uint16_t) * pre, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = write_sentinels(m->codes, n, s);
+    return e;
+}
+
+void free_codes(tsdfl_map* m)
+{
+    cudaFree(m->codes_base);
+    m->codes_base = nullptr;
+    m->codes = nullptr;
+    m->codes_pre = 0;
+}
+
+// Largest sub-voxel index trunc(fl(s / res)) over floats s in [0, 1).
+uint64_t max_sub_index(float res)
+{
+    float below_one;
+    const uint32_t b = 0x3F7FFFFFu;
+    std::memcpy(&below_one, &b, 4);
+    return f2u_x86_host(below_one / res);
+}
+
 void fill_view(tsdfl_map* m)
 {
     const tsdfl_map_coef& c = m->coef;
@@ -313,8 +363,9 @@ void fill_view(tsdfl_map* m)
     v.grid_occ = m->grid_occ;
     v.codes = m->codes;
     v.data = m->data;
-    v.dense = m->dense;
-    v.storage = m->codes ? 0 : 1;
+    v.h16 = m->h16;
+    v.dense = m->occ ? m->codes : nullptr;
+    v.storage = m->h16 ? 2 : (m->codes ? 0 : 1);
     v.sub_fast = sub_index_mult(c.resolution, c.sub_dim, &v.sub_inv, &v.sub_inv_lo);
     auto lim = [](int32_t mmax) {
         float f = (float)std::min<int64_t>((int64_t)mmax + 1, 4194304);
@@ -326,109 +377,89 @@ void fill_view(tsdfl_map* m)
     v.lim_x = lim(v.mmax_x);
     v.lim_y = lim(v.mmax_y);
     v.lim_z = lim(v.mmax_z);
-    const uint32_t K = 0x4B000000u;
-    v.up_bias = K * (1u + v.up_dim_x + v.up_dim_2);
-    v.sl_bias = K * (1u + v.sub_dim + v.sub_dim_2);
-    v.lim_zn = v.lim_z ? 0x3F800000u : 0u;
-    v.sl_bias_xy = K * (1u + v.sub_dim);
     v.occ = m->occ;
-    v.occ_words = m->occ_words;
-    v.n0 = m->n0;
+    v.occ_bytes = m->occ_bytes;
+    v.occ_mask = m->occ_bytes ? (m->occ_bytes - 1u) & ~7u : 0u;
     v.codes_sent = (uint32_t)c.data_size;
-    v.dense_sent = (uint32_t)m->dense_slots;
+    // tiled fast path: the packed pipeline's float sums are exact integers
+    // (largest brick index a fast lookup forms below 2^23, sub-voxel offsets
+    // within +-sub_dim^3 <= 2^21) and every sub-voxel index stays inside its
+    // brick, so slot indices land in [r S^3 - S^3, r S^3 + S^3)
+    const uint64_t S3 = c.sub_dim * c.sub_dim_2;
+    auto fmax_trunc = [&](int32_t mmax) { return mmax < 0 ? 0ull : (uint64_t)std::min<int64_t>(mmax, 4194303); };
+    const uint64_t up_max = fmax_trunc(v.mmax_x) + fmax_trunc(v.mmax_y) * c.up_dim_x + fmax_trunc(v.mmax_z) * c.up_dim_2;
+    v.tiled = v.sub_fast != 0 && m->codes != nullptr && m->codes_pre == S3 && S3 <= (1ull << 21) && up_max < (1ull << 23) &&
+              c.grid_occ_size < (1ull << 23) && max_sub_index(c.resolution) < c.sub_dim ? 1 : 0;
+    v.min0 = c.min_x == 0.0f && c.min_y == 0.0f && c.min_z == 0.0f && !std::signbit(c.min_x) &&
+             !std::signbit(c.min_y) && !std::signbit(c.min_z) ? 1 : 0;
+    v.up_dim_x_f = (float)c.up_dim_x;
+    v.up_dim_2_f = (float)c.up_dim_2;
+    v.sub_dim_f = (float)c.sub_dim;
+    v.sub_dim_2_f = (float)c.sub_dim_2;
+    // -1 < oz < mmax_z + 1: points just below the map take brick layer 0 and a
+    // negative sub-voxel index (an empty range when not even layer 0 passes)
+    v.zhi = v.mmax_z < 0 ? 0.0f : (float)std::min<int64_t>((int64_t)v.mmax_z + 1, 4194304);
+    v.zlo = v.mmax_z < 0 ? 0.0f : -1.0f;
+    v.neg_zero = -0.0f;
+    const uint32_t kMag = 0x4B000000u, kMag15 = 0x4B400000u;
+    v.upb_lim = kMag + (uint32_t)std::min<uint64_t>(c.grid_occ_size, 1ull << 23);
+    v.sent_miss = (uint32_t)c.data_size + kMag15;
+    v.sent_later = v.sent_miss + 1u;
+    v.sent_none = v.sent_miss + 2u;
+    v.codes_b = (unsigned long long)(uintptr_t)m->codes - 2ull * kMag15;
 }
 
-// The kSentinels codes after the last slot of a code array (MapView::codes_sent).
-cudaError_t write_sentinels(uint16_t* arr, size_t at, cudaStream_t s)
-{
-    static const uint16_t kSent[kSentinels] = {(uint16_t)kCodeMiss, (uint16_t)kCodeLater, (uint16_t)kCodeNone,
-                                               (uint16_t)kCodeNone};
-    return cudaMemcpyAsync(arr + at, kSent, sizeof(kSent), cudaMemcpyHostToDevice, s);
-}
 
-// Largest sub-voxel index trunc(fl(s / res)) over floats s in [0, 1).
-uint64_t max_sub_index(float res)
-{
-    float below_one;
-    const uint32_t b = 0x3F7FFFFFu;
-    std::memcpy(&below_one, &b, 4);
-    return f2u_x86_host(below_one / res);
-}
 
-// Compact layout (MapView::dense): needs every fast-path slot inside its brick
-// (sub-voxel indices below sub_dim) and 32-bit slot offsets.
-int build_compact(tsdfl_ctx* ctx, tsdfl_map* m)
+// Compact layout (TSDFL_MAP_DENSE): the code array itself, with the brick's
+// rank read from a bitmap of the brick grid staged in shared memory instead of
+// a grid_occ gather.  Built when every sub-voxel index stays inside its brick
+// and the bitmap (pairs {word, allocated bricks up to and including it},
+// zero-padded to a power of two) fits the tiled kernels' staging.
+int build_compact(tsdfl_map* m, const int32_t* go)
 {
     const tsdfl_map_coef& c = m->coef;
-    const uint64_t S3 = c.sub_dim * c.sub_dim_2, gos = c.grid_occ_size;
-    if (max_sub_index(c.resolution) >= c.sub_dim) return TSDFL_OK;   // keep the brick layout only
-    std::vector<int32_t> go(gos ? gos : 1);
-    if (gos) CUDA_TRY(cudaMemcpy(go.data(), m->grid_occ, sizeof(int32_t) * gos, cudaMemcpyDeviceToHost));
-    const uint32_t words = (uint32_t)(((gos + 31) / 32 + 3) / 4 * 4);
-    std::vector<uint32_t> occ(2 * (size_t)words, 0u);
-    uint64_t nb = 0, n0 = 0;
-    for (uint64_t up = 0; up < gos; ++up) {
-        if (go[up] < 0) continue;
-        occ[2 * (up / 32)] |= 1u << (up % 32);
-        ++nb;
-        if (up < c.up_dim_2) ++n0;
-    }
+    const uint64_t gos = c.grid_occ_size;
+    if (max_sub_index(c.resolution) >= c.sub_dim || !m->codes || m->codes_pre != c.sub_dim * c.sub_dim_2)
+        return TSDFL_OK;   // brick table only
+    const uint64_t words = (gos + 31) / 32;
+    uint64_t bytes = 16;
+    while (bytes < 8 * words) bytes *= 2;
+    if (bytes > (1u << 17)) return TSDFL_OK;
+    std::vector<uint32_t> occ(bytes / 4, 0u);
+    for (uint64_t up = 0; up < gos; ++up)
+        if (go[up] >= 0) occ[2 * (up / 32)] |= 1u << (up % 32);
     uint32_t run = 0;
-    for (uint32_t w = 0; w < words; ++w) {
-        occ[2 * w + 1] = run;
+    for (uint64_t w = 0; w < words; ++w) {
         run += (uint32_t)__builtin_popcount(occ[2 * w]);
+        occ[2 * w + 1] = run;
     }
-    const uint64_t slots = (nb + n0) * S3;
-    if (slots >= (1ull << 31)) return TSDFL_OK;
-    std::vector<int64_t> src, dst;
-    std::vector<uint8_t> skirt;
-    src.reserve(nb);
-    dst.reserve(nb);
-    skirt.reserve(nb);
-    uint64_t r = 0;
-    for (uint64_t up = 0; up < gos; ++up) {
-        if (go[up] < 0) continue;
-        const bool layer0 = up < c.up_dim_2;
-        src.push_back(go[up]);
-        dst.push_back((int64_t)((layer0 ? 2 * r + 1 : r + n0) * S3));
-        skirt.push_back(layer0 ? 1 : 0);
-        ++r;
-    }
-    CUDA_TRY(cudaMalloc(&m->dense, sizeof(uint16_t) * (slots + kSentinels)));
-    CUDA_TRY(write_sentinels(m->dense, slots, ctx->stream));
-    m->dense_slots = slots;
-    CUDA_TRY(cudaMalloc(&m->occ, sizeof(uint32_t) * occ.size()));
-    m->bytes += sizeof(uint16_t) * slots + sizeof(uint32_t) * occ.size();
-    CUDA_TRY(cudaMemcpy(m->occ, occ.data(), sizeof(uint32_t) * occ.size(), cudaMemcpyHostToDevice));
-    m->occ_words = words;
-    m->n0 = (uint32_t)n0;
-    if (nb) {
-        void* tmp = nullptr;
-        const size_t nbytes = nb * (2 * sizeof(int64_t) + 1);
-        CUDA_TRY(cudaMalloc(&tmp, nbytes));
-        int64_t* d_src = static_cast<int64_t*>(tmp);
-        int64_t* d_dst = d_src + nb;
-        uint8_t* d_sk = reinterpret_cast<uint8_t*>(d_dst + nb);
-        cudaError_t e = cudaMemcpy(d_src, src.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(d_dst, dst.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMemcpy(d_sk, skirt.data(), nb, cudaMemcpyHostToDevice);
-        int rc = e == cudaSuccess ? launch_compact_fill(m->codes, d_src, d_dst, d_sk, (uint32_t)nb, (uint32_t)S3,
-                                                        m->dense, ctx->stream)
-                                  : TSDFL_ERR_DEVICE;
-        if (rc == TSDFL_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = TSDFL_ERR_DEVICE;
-        cudaFree(tmp);
-        if (rc) {
-            set_error("map: building the compact layout failed");
-            return rc;
-        }
-    }
+    CUDA_TRY(cudaMalloc(&m->occ, bytes));
+    CUDA_TRY(cudaMemcpy(m->occ, occ.data(), bytes, cudaMemcpyHostToDevice));
+    m->occ_bytes = (uint32_t)bytes;
+    m->bytes += bytes;
     return TSDFL_OK;
 }
 
-int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, uint32_t flags)
+// grid_occ: the caller's brick table (host)
+int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, const int32_t* grid_occ, uint32_t flags)
 {
+    if (flags & TSDFL_MAP_F16) {   // half-precision values replace the codes or float slots
+        const size_t n = m->coef.data_size;
+        CUDA_TRY(cudaMalloc(&m->h16, sizeof(uint16_t) * (n ? n : 1)));
+        int rc = launch_halves(m->codes, m->values, m->data, n, m->h16, ctx->stream);
+        if (rc) return rc;
+        CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        m->bytes -= m->codes ? sizeof(uint16_t) * (m->codes_pre + n) : sizeof(float) * n;
+        m->bytes += sizeof(uint16_t) * n;
+        free_codes(m);
+        cudaFree(m->data);
+        m->data = nullptr;
+        fill_view(m);
+        return TSDFL_OK;
+    }
     if ((flags & TSDFL_MAP_DENSE) && m->codes) {
-        int rc = build_compact(ctx, m);
+        int rc = build_compact(m, grid_occ);
         if (rc) return rc;
     }
     fill_view(m);
@@ -441,9 +472,9 @@ void destroy_map(tsdfl_map* m)
     if (!m) return;
     cudaSetDevice(m->device);
     cudaFree(m->grid_occ);
-    cudaFree(m->codes);
+    cudaFree(m->codes_base);
     cudaFree(m->data);
-    cudaFree(m->dense);
+    cudaFree(m->h16);
     cudaFree(m->occ);
     cudaFree(m->values);
     delete m;
@@ -480,6 +511,10 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     b.particles = d_particles;
     b.dbg_index = d_dbg;
     const bool serial = (flags & TSDFL_SUM_SERIAL) != 0;
+    if (serial && map->view.storage == 2) {
+        set_error("evaluate: serial sums need code or float slots (the map holds half-precision values)");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
     const float inv_max_range = (float)(1.0 / (double)mdl->max_range);
     const float max_range_sq = mdl->max_range * mdl->max_range;
     const float c_in = mdl->a_range * inv_max_range;
@@ -497,8 +532,8 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     if (rc) return rc;
     rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
     if (rc) return rc;
-    bool dense = map->dense != nullptr;
-    const bool tiled = !serial && map->view.storage == 0 && map->view.sub_fast && !(flags & TSDFL_EVAL_GENERIC);
+    bool dense = map->occ != nullptr;
+    const bool tiled = !serial && map->view.storage == 0 && map->view.tiled && !(flags & TSDFL_EVAL_GENERIC);
     size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
     if (tiled) {
         int tp = tiled_pass_points(map->view, dense);
@@ -519,11 +554,68 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
         CUDA_TRY(cudaEventRecord(c->ev1, s));
         c->timed = true;
     }
-    const int mode = serial ? 2 : (map->view.storage == 1 ? 1 : 0);
+    const int mode = serial ? 2 : (map->view.storage != 0 ? 1 : 0);
     rc = launch_norm((int)P, mode, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)N, c->sum_f64,
-                     d_particles, d_pose, b, s);
+                     d_particles, d_pose, b, s, nullptr, (flags & TSDFL_NORM_LOG) != 0);
     if (rc) return rc;
     return launch_fold_status(c->status + 1, c->status, s);
+}
+
+// Seeded per-particle subsampling: K of the N points per particle
+// (subsample.h), exact fixed-point sums, per-particle range terms.
+int run_eval_sub(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* d_particles, size_t P,
+                 const float* d_points, size_t N, const float tf[16], size_t K, uint64_t seed, float* d_pose)
+{
+    if (!map->view.tiled || map->view.storage != 0) {
+        set_error("tsdfl_evaluate_subsampled: the map has no tiled fast path (float slots or an unsupported "
+                  "resolution)");
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    int rc = ensure_workspace(c, P, N);
+    if (rc) return rc;
+    EvalBuffers b = c->buf;
+    b.particles = d_particles;
+    b.dbg_index = nullptr;
+    const float inv_max_range = (float)(1.0 / (double)mdl->max_range);
+    const float max_range_sq = mdl->max_range * mdl->max_range;
+    const float c_in = mdl->a_range * inv_max_range;
+    const float c_out = mdl->a_max;
+    int shift = 40;
+    {
+        double bound = std::fmax((double)map->max_value, 1e-30) * (double)(K + 1);
+        int need = (int)std::ceil(std::log2(bound));
+        if (62 - need < shift) shift = 62 - need;
+    }
+    const int npad = (int)align_up(N, 4);
+    cudaStream_t s = c->stream;
+    rc = launch_pose_kernel(tf, (int)P, b, s);
+    if (rc) return rc;
+    rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
+    if (rc) return rc;
+    if (c->timing) CUDA_TRY(cudaEventRecord(c->ev0, s));
+    rc = launch_eval_subsample(map->view, mdl->a_hit, (int)P, (int)N, (int)K, seed, c_in, b, c->sm_count, s);
+    if (rc) return rc;
+    if (c->timing) {
+        CUDA_TRY(cudaEventRecord(c->ev1, s));
+        c->timed = true;
+    }
+    rc = launch_norm((int)P, 0, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)K, c->sum_f64,
+                     d_particles, d_pose, b, s, b.nin);
+    if (rc) return rc;
+    return launch_fold_status(c->status + 1, c->status, s);
+}
+
+int check_sub_args(const char* fn, size_t P, size_t N, size_t K)
+{
+    if (K == 0 || K > N) {
+        set_error("%s: need 0 < K <= N (K = %zu, N = %zu)", fn, K, N);
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    if (P >= (1ull << 31) || N >= (1ull << 31)) {
+        set_error("%s: too many particles or points", fn);
+        return TSDFL_ERR_UNSUPPORTED;
+    }
+    return TSDFL_OK;
 }
 
 int check_model(const tsdfl_model* mdl)
@@ -626,6 +718,14 @@ int tsdfl_ctx_last_timing(tsdfl_ctx* c, float* eval_kernel_ms)
 
 uint64_t tsdfl_launch_count(void) { return (uint64_t)g_launches.load(); }
 
+int tsdfl_ctx_workspace_bytes(const tsdfl_ctx* c, size_t* eval_bytes, size_t* resample_bytes)
+{
+    if (!c) return TSDFL_ERR_INVALID_ARG;
+    if (eval_bytes) *eval_bytes = c->ws_bytes;
+    if (resample_bytes) *resample_bytes = c->rs_bytes;
+    return TSDFL_OK;
+}
+
 int tsdfl_ctx_sync(tsdfl_ctx* c)
 {
     if (!c) return TSDFL_ERR_INVALID_ARG;
@@ -679,8 +779,7 @@ int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* 
     bool use_codes = !(flags & TSDFL_MAP_FORCE_F32);
     if (use_codes) {
         int32_t* fail = ctx->status + 2;
-        e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n + kSentinels));
-        if (e == cudaSuccess) e = write_sentinels(m->codes, n, ctx->stream);
+        e = alloc_codes(m, n, ctx->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(fail, 0, sizeof(int32_t), ctx->stream);
         if (e == cudaSuccess) {
             rc = launch_codes_from_floats(m->data, n, m->values, coef->init_value, m->codes, fail, ctx->stream);
@@ -693,19 +792,16 @@ int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* 
             destroy_map(m);
             return TSDFL_ERR_DEVICE;
         }
-        if (ctx->h_status[2]) {   // some slot is not a likelihood value of this sigma: keep floats
-            cudaFree(m->codes);
-            m->codes = nullptr;
-        }
+        if (ctx->h_status[2]) free_codes(m);   // some slot is not a likelihood value of this sigma: keep floats
     }
     if (m->codes) {
         cudaFree(m->data);
         m->data = nullptr;
-        m->bytes += sizeof(uint16_t) * n;
+        m->bytes += sizeof(uint16_t) * (m->codes_pre + n);
     } else {
         m->bytes += sizeof(float) * n;
     }
-    rc = finish_map(ctx, m, flags);
+    rc = finish_map(ctx, m, grid_occ, flags);
     if (rc) { destroy_map(m); return rc; }
     *out = m;
     return TSDFL_OK;
@@ -727,17 +823,16 @@ int tsdfl_map_create_codes(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int
     rc = map_common(ctx, coef, grid_occ, sigma, m);
     if (rc) { destroy_map(m); return rc; }
     size_t n = coef->data_size;
-    cudaError_t e = cudaMalloc(&m->codes, sizeof(uint16_t) * (n + kSentinels));
+    cudaError_t e = alloc_codes(m, n, ctx->stream);
     if (e == cudaSuccess && n)
         e = cudaMemcpyAsync(m->codes, codes, sizeof(uint16_t) * n, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = write_sentinels(m->codes, n, ctx->stream);
     if (e != cudaSuccess) {
         set_error("tsdfl_map_create_codes: %s", cudaGetErrorString(e));
         destroy_map(m);
         return e == cudaErrorMemoryAllocation ? TSDFL_ERR_OUT_OF_MEMORY : TSDFL_ERR_DEVICE;
     }
-    m->bytes += sizeof(uint16_t) * n;
-    rc = finish_map(ctx, m, flags);
+    m->bytes += sizeof(uint16_t) * (m->codes_pre + n);
+    rc = finish_map(ctx, m, grid_occ, flags);
     if (rc) { destroy_map(m); return rc; }
     *out = m;
     return TSDFL_OK;
@@ -756,9 +851,9 @@ int tsdfl_map_get_info(const tsdfl_map* m, tsdfl_map_info* info)
     info->data_size = m->coef.data_size;
     info->bricks = m->bricks;
     info->device_bytes = m->bytes;
-    info->storage = m->codes ? 0 : 1;
-    info->dense = m->dense ? 1 : 0;
-    info->fast_index = m->view.sub_fast;
+    info->storage = m->h16 ? 2 : (m->codes ? 0 : 1);
+    info->dense = m->occ ? 1 : 0;
+    info->fast_index = m->view.tiled ? m->view.sub_fast : 0;
     info->reserved = 0;
     return TSDFL_OK;
 }
@@ -847,6 +942,76 @@ int tsdfl_evaluate(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, f
                    const float* points, size_t N, const float tf[16], uint32_t flags, float pose_out[6])
 {
     return tsdfl_evaluate_debug(c, map, mdl, particles, P, points, N, tf, flags, pose_out, nullptr);
+}
+
+int tsdfl_evaluate_subsampled_device(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* d_particles,
+                                     size_t P, const float* d_points, size_t N, const float tf[16], size_t K,
+                                     uint64_t seed, float* d_pose_out)
+{
+    if (!c || !map || !tf || (P && !d_particles) || (N && !d_points)) {
+        set_error("tsdfl_evaluate_subsampled_device: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(mdl);
+    if (rc) return rc;
+    if (N == 0) return TSDFL_OK;
+    if (P == 0) {
+        set_error("No particle is valid!");
+        return TSDFL_ERR_DEGENERATE;
+    }
+    rc = check_sub_args("tsdfl_evaluate_subsampled_device", P, N, K);
+    if (rc) return rc;
+    rc = set_device(c->device);
+    if (rc) return rc;
+    return run_eval_sub(c, map, mdl, d_particles, P, d_points, N, tf, K, seed, d_pose_out);
+}
+
+int tsdfl_evaluate_subsampled(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* particles, size_t P,
+                              const float* points, size_t N, const float tf[16], size_t K, uint64_t seed,
+                              float pose_out[6], float* raw_out, uint32_t* hits_out)
+{
+    if (!c || !map || !tf || (P && !particles) || (N && !points)) {
+        set_error("tsdfl_evaluate_subsampled: invalid argument");
+        return TSDFL_ERR_INVALID_ARG;
+    }
+    int rc = check_model(mdl);
+    if (rc) return rc;
+    if (N == 0) return TSDFL_OK;
+    if (P == 0) {
+        set_error("No particle is valid!");
+        return TSDFL_ERR_DEGENERATE;
+    }
+    rc = check_sub_args("tsdfl_evaluate_subsampled", P, N, K);
+    if (rc) return rc;
+    rc = set_device(c->device);
+    if (rc) return rc;
+    size_t part_b = align_up(sizeof(float) * 7 * P, 256);
+    size_t pts_b = align_up(sizeof(float) * 3 * N, 256);
+    rc = ensure_io(c, part_b + pts_b + 256);
+    if (rc) return rc;
+    char* io = static_cast<char*>(c->io);
+    float* d_part = reinterpret_cast<float*>(io);
+    float* d_pts = reinterpret_cast<float*>(io + part_b);
+    float* d_pose = reinterpret_cast<float*>(io + part_b + pts_b);
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(d_part, particles, sizeof(float) * 7 * P, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(d_pts, points, sizeof(float) * 3 * N, cudaMemcpyHostToDevice, s));
+    rc = run_eval_sub(c, map, mdl, d_part, P, d_pts, N, tf, K, seed, d_pose);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(particles, d_part, sizeof(float) * 7 * P, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(c->h_pose, d_pose, sizeof(float) * 6, cudaMemcpyDeviceToHost, s));
+    if (raw_out) CUDA_TRY(cudaMemcpyAsync(raw_out, c->buf.raw, sizeof(float) * P, cudaMemcpyDeviceToHost, s));
+    if (hits_out) CUDA_TRY(cudaMemcpyAsync(hits_out, c->buf.hits, sizeof(uint32_t) * P, cudaMemcpyDeviceToHost, s));
+    int st = tsdfl_ctx_sync(c);
+    if (st) return st;
+    if (pose_out) std::memcpy(pose_out, c->h_pose, sizeof(float) * 6);
+    return TSDFL_OK;
+}
+
+uint32_t tsdfl_subsample_index(uint64_t seed, uint64_t particle, uint32_t N, uint32_t K, uint32_t k)
+{
+    if (K == 0 || K > N || k >= K) return 0xffffffffu;
+    return sub_point(sub_particle_state(seed, particle), N, K, k);
 }
 
 int tsdfl_resample_systematic(tsdfl_ctx* c, const float* weights, size_t M, float u0, uint32_t* idx_out, size_t cap,
@@ -1157,8 +1322,8 @@ void per_configure(tsdfl_batch::Per& q, const tsdfl_filter& F)
     int need = (int)std::ceil(std::log2(bound));
     q.shift = 62 - need < 40 ? 62 - need : 40;
     const MapView& m = F.map->view;
-    q.dense = F.map->dense != nullptr;
-    q.tiled = m.storage == 0 && m.sub_fast != 0;
+    q.dense = F.map->occ != nullptr;
+    q.tiled = m.storage == 0 && m.tiled != 0;
     if (q.tiled) {
         int tp = tiled_pass_points(m, q.dense);
         if (tp < 1024 && q.dense) {
@@ -1242,7 +1407,7 @@ int batch_record(tsdfl_batch* B)
         if (F.N == 0) continue;
         const float inv_max_range = (float)(1.0 / (double)F.model.max_range);
         const float c_in = F.model.a_range * inv_max_range;
-        const int mode = F.map->view.storage == 1 ? 1 : 0;
+        const int mode = F.map->view.storage != 0 ? 1 : 0;
         rc = launch_norm((int)F.P, mode, q.shift, (double)F.model.a_hit, (double)c_in, (double)F.model.a_max,
                          (int)F.N, q.sum_f64, F.d_particles, F.d_pose_out, q.b, s);
         if (rc) return rc;
@@ -1579,26 +1744,50 @@ size_t session_bytes(size_t cap, size_t max_points)
            align_up(resample_workspace_bytes(cap), 256) + 256;
 }
 
-// Returns the slot's requests to the front of their sessions' queues (a
-// dispatch that could not be launched).
-void server_requeue(tsdfl_server* S, tsdfl_server::Slot& sl)
+// Returns requests [from, end) of the slot to the front of their sessions'
+// queues, in order (updates that were not launched).
+void server_requeue(tsdfl_server* S, tsdfl_server::Slot& sl, size_t from = 0)
 {
-    for (size_t r = sl.reqs.size(); r-- > 0;) {
+    for (size_t r = sl.reqs.size(); r-- > from;) {
         tsdfl_server::Session& se = S->sessions[sl.reqs[r].session];
         se.busy = false;
         se.queue.push_front(std::move(sl.reqs[r]));
+    }
+    sl.reqs.resize(from);
+}
+
+// Publishes the slot's requests as failed with `status` (updates that cannot
+// be launched however often they are tried); the sessions stay as they were.
+void server_fail(tsdfl_server* S, tsdfl_server::Slot& sl, int status)
+{
+    const auto now = std::chrono::steady_clock::now();
+    for (auto& q : sl.reqs) {
+        tsdfl_server::Session& se = S->sessions[q.session];
+        se.busy = false;
+        tsdfl_server::Result res{};
+        res.status = status;
+        res.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_submit).count();
+        S->results[q.ticket] = res;
+        S->queued_pp -= q.pp;
+        S->published += 1;
     }
     sl.reqs.clear();
 }
 
 int server_launch(tsdfl_server* S, int k);
 
-// Launches every queued update of an idle session as one batch on slot k; on
-// failure the updates go back to their queues.
+// Launches every queued update of an idle session as one batch on slot k.  A
+// launch that failed for want of device memory goes back to the queues (the
+// memory may free up); any other failure would repeat on every attempt, so its
+// updates are published with the error status and the server moves on.
 int server_dispatch(tsdfl_server* S, int k)
 {
+    tsdfl_server::Slot& sl = S->slots[k];
     const int rc = server_launch(S, k);
-    if (rc && !S->slots[k].busy) server_requeue(S, S->slots[k]);
+    if (rc && !sl.busy) {
+        if (rc == TSDFL_ERR_OUT_OF_MEMORY) server_requeue(S, sl);
+        else server_fail(S, sl, rc);
+    }
     return rc;
 }
 
@@ -1618,7 +1807,7 @@ int server_launch(tsdfl_server* S, int k)
     B.f.clear();
     B.per.clear();
     B.specs.clear();
-    const size_t n = sl.reqs.size();
+    size_t n = sl.reqs.size();
     sl.pp = 0;
     for (size_t r = 0; r < n; ++r) {
         const tsdfl_server::Request& q = sl.reqs[r];
@@ -1644,12 +1833,25 @@ int server_launch(tsdfl_server* S, int k)
         per_configure(pq, F);
         pq.sticky = sl.d_status + r;
         B.per.push_back(pq);
+        const size_t before = B.specs.size();
         append_specs(&B, r);
+        if (B.specs.size() > sl.seg_cap) {
+            // more scan passes than the slot's tables hold (the tables are sized
+            // for max_sessions scans of max_points, so this is a safeguard):
+            // this and the later updates wait for the next batch
+            B.specs.resize(before);
+            B.f.pop_back();
+            B.per.pop_back();
+            if (r == 0) {   // this update alone does not fit: it fails, the others wait
+                server_requeue(S, sl, 1);
+                set_error("tsdfl_server_poll: one scan has more passes than a batch holds");
+                return TSDFL_ERR_UNSUPPORTED;
+            }
+            server_requeue(S, sl, r);
+            n = r;
+            break;
+        }
         sl.pp += (uint64_t)se.P * N;
-    }
-    if (B.specs.size() > sl.seg_cap) {   // more passes than the slot's tables hold
-        set_error("tsdfl_server_poll: too many scan passes in one batch");
-        return TSDFL_ERR_UNSUPPORTED;
     }
     cudaStream_t s = sl.stream;
     CUDA_TRY(cudaMemsetAsync(sl.d_status, 0, sizeof(int32_t) * n, s));
@@ -1728,8 +1930,12 @@ int tsdfl_server_create(tsdfl_ctx* c, const tsdfl_server_config* cfg, tsdfl_serv
     S->cfg = *cfg;
     if (S->cfg.max_queue == 0) S->cfg.max_queue = 4;
     const size_t ns = cfg->max_sessions, np = cfg->max_points;
+    // a scan of max_points needs at most ceil(max_points / 1024) + 1 passes
+    // (every tiled pass holds at least 1,024 points), so a batch of
+    // max_sessions scans always fits the segment tables
+    const size_t passes = (np + 1023) / 1024 + 1;
     for (auto& sl : S->slots) {
-        sl.seg_cap = 4 * ns + 8;
+        sl.seg_cap = ns * passes + 8;
         const size_t pts_b = align_up(sizeof(float) * 3 * np * ns, 256);
         const size_t u0_b = align_up(sizeof(float) * ns, 256), pose_b = align_up(sizeof(float) * 8 * ns, 256);
         const size_t cnt_b = align_up(sizeof(uint32_t) * ns, 256), st_b = align_up(sizeof(int32_t) * ns, 256);
@@ -1912,12 +2118,13 @@ int tsdfl_server_poll(tsdfl_server* S, size_t* completed)
     int rc = set_device(S->ctx->device);
     if (rc) return rc;
     for (int k = 0; k < 2; ++k) server_collect(S, k, completed);
-    for (int k = 0; k < 2; ++k) {
+    int first = TSDFL_OK;
+    for (int k = 0; k < 2; ++k) {   // a failed dispatch on one slot does not hold up the other
         if (S->slots[k].busy) continue;
         rc = server_dispatch(S, k);
-        if (rc) return rc;
+        if (rc && first == TSDFL_OK) first = rc;
     }
-    return TSDFL_OK;
+    return first;
 }
 
 int tsdfl_server_result(tsdfl_server* S, uint64_t ticket, float pose[6], double* latency_ms, int* status)
@@ -2295,9 +2502,38 @@ static __device__ __align__(256) unsigned char g_resample_scratch[kStaticResampl
 
 std::mutex g_static_mu;
 void* g_static_ptr[kStaticMaxDevices] = {};
+unsigned long long g_static_ctx[kStaticMaxDevices] = {};   // context id the address belongs to
 
-// Device address of this device's copy of g_resample_scratch, looked up once
-// per device with that device current (the caller has made it current).
+// Unique id of the current context (cuCtxGetId through the runtime's driver
+// entry points; ids are never reused within a process), 0 when unavailable.
+unsigned long long current_context_id()
+{
+    typedef int (*GetCurrent)(void**);
+    typedef int (*GetId)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of this device's copy of g_resample_scratch, looked up with
+// that device current (the caller has made it current) on the first call and
+// again whenever the device's context has changed since (a cudaDeviceReset
+// loads the module into a new context, where the array may sit elsewhere).
 int static_scratch(int dev, void** out)
 {
     if (dev < 0 || dev >= kStaticMaxDevices) {
@@ -2306,7 +2542,8 @@ int static_scratch(int dev, void** out)
         return TSDFL_ERR_UNSUPPORTED;
     }
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[dev]) {
+    const unsigned long long ctx_id = current_context_id();
+    if (!g_static_ptr[dev] || ctx_id != g_static_ctx[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_resample_scratch);
         if (e != cudaSuccess || !p) {
@@ -2315,6 +2552,7 @@ int static_scratch(int dev, void** out)
             return TSDFL_ERR_DEVICE;
         }
         g_static_ptr[dev] = p;
+        g_static_ctx[dev] = ctx_id;
     }
     *out = g_static_ptr[dev];
     return TSDFL_OK;

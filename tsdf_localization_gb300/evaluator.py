@@ -64,15 +64,19 @@ class Context:
 
 class DeviceMap:
     """A likelihood map resident on the device (tsdfl_map).  dense=True also
-    builds the compact layout (TSDFL_MAP_DENSE): one map gather per lookup."""
+    builds the compact layout (TSDFL_MAP_DENSE): one map gather per lookup.
+    f16=True stores half-precision likelihood values instead (TSDFL_MAP_F16,
+    an accuracy variant)."""
 
     def __init__(self, ctx: Context, coef: N.MapCoef, grid_occ: np.ndarray, data: np.ndarray | None = None,
-                 codes: np.ndarray | None = None, sigma: float = 0.1, dense: bool = False, force_f32: bool = False):
+                 codes: np.ndarray | None = None, sigma: float = 0.1, dense: bool = False, force_f32: bool = False,
+                 f16: bool = False):
         self.ctx = ctx
         self.coef = coef
         lib = N.lib()
         go = np.ascontiguousarray(grid_occ, dtype=np.int32)
-        flags = (N.TSDFL_MAP_DENSE if dense else 0) | (N.TSDFL_MAP_FORCE_F32 if force_f32 else 0)
+        flags = ((N.TSDFL_MAP_DENSE if dense else 0) | (N.TSDFL_MAP_FORCE_F32 if force_f32 else 0) |
+                 (N.TSDFL_MAP_F16 if f16 else 0))
         h = C.c_void_p()
         if codes is not None:
             cd = np.ascontiguousarray(codes, dtype=np.uint16)
@@ -125,13 +129,14 @@ class TSDFEvaluator:
     """
 
     def __init__(self, device_map: DeviceMap, per_point: bool = False, a_hit: float = 0.9, a_range: float = 0.1,
-                 a_max: float = 0.0, max_range: float = 100.0, serial_sums: bool = False, generic: bool = False):
+                 a_max: float = 0.0, max_range: float = 100.0, serial_sums: bool = False, generic: bool = False,
+                 log_normalise: bool = False):
         self.map = device_map
         self.ctx = device_map.ctx
         self.per_point = per_point
         self.model = N.Model(a_hit, a_range, a_max, max_range)
-        self.flags = (N.TSDFL_SUM_SERIAL if serial_sums else N.TSDFL_SUM_EXACT) | (N.TSDFL_EVAL_GENERIC if generic
-                                                                                    else 0)
+        self.flags = ((N.TSDFL_SUM_SERIAL if serial_sums else N.TSDFL_SUM_EXACT) |
+                      (N.TSDFL_EVAL_GENERIC if generic else 0) | (N.TSDFL_NORM_LOG if log_normalise else 0))
 
     def evaluate(self, particles: np.ndarray, points: np.ndarray, tf_matrix) -> Pose | None:
         """Writes normalised weights into particles[:, 6]; returns the mean pose,
@@ -172,6 +177,27 @@ class TSDFEvaluator:
         if nred.value == 0:
             return None, 0
         return Pose(*[float(v) for v in pose]), nred.value
+
+    def evaluate_subsampled(self, particles: np.ndarray, points: np.ndarray, tf_matrix, k: int, seed: int,
+                            debug: bool = False):
+        """evaluate() with every particle scoring k of the points, chosen per
+        particle and seed (tsdfl_evaluate_subsampled): the mean pose, or with
+        debug (pose, raw weights, hit counts)."""
+        if not (isinstance(particles, np.ndarray) and particles.dtype == np.float32 and particles.flags.c_contiguous
+                and particles.ndim == 2 and particles.shape[1] == 7):
+            raise ValueError("particles must be a C-contiguous (P, 7) float32 array")
+        pts = _f32(points, 3)
+        tf = np.ascontiguousarray(np.asarray(tf_matrix, dtype=np.float32).reshape(16))
+        P = particles.shape[0]
+        pose = np.zeros(6, dtype=np.float32)
+        raw = np.zeros(max(P, 1), np.float32)
+        hits = np.zeros(max(P, 1), np.uint32)
+        N.check(N.lib().tsdfl_evaluate_subsampled(self.ctx.handle, self.map.handle, C.byref(self.model),
+                                                  _ptr(particles), P, _ptr(pts), pts.shape[0], _ptr(tf), int(k),
+                                                  int(seed), _ptr(pose), _ptr(raw), _ptr(hits)))
+        if debug:
+            return pose, raw[:P], hits[:P]
+        return Pose(*[float(v) for v in pose])
 
     def evaluate_debug(self, particles: np.ndarray, points: np.ndarray, tf_matrix, voxel_index: bool = False):
         """evaluate() plus per-particle raw weights, hit counts, laser poses and,
