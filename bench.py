@@ -71,6 +71,14 @@ def make_workload(args):
     return wl
 
 
+# DRAM bytes of one scoring launch from ncu captures of these exact workloads
+# (dram__bytes_read.sum + dram__bytes_write.sum, single pass, full size;
+# profiles/eval_tiled_kernel_building_20k_x_8192.md and
+# profiles/eval_tiled_kernel_global_1m_x_2048.md)
+MEASURED_TRAFFIC = {("building", 100_000, 8192, "compact", "fast"): 1.326252e9 + 0.054576e9,
+                    ("global", 1_000_000, 2048, "compact", "fast"): 121.801142e9 + 0.565432e9}
+
+
 def roofline_bytes(P: int, N: int, layout: str) -> float:
     """Algorithmic bytes of one scoring launch: per particle*point the map
     reads (brick layout: 4 B brick-table entry + 2 B slot code; compact layout:
@@ -385,27 +393,28 @@ def motion_side(lib, ctx, stream, wl, device: str, with_cpu: bool, reps: int = 2
     return res
 
 
-def batch_workload(n_filters: int, seed: int = 11):
+def batch_workload(n_filters: int, seed: int = 11, worlds=None, p_range=(1000, 200_000)):
     """64 independent filters over 4 seeded maps (room 20x20x4 m @0.05, the
     building @0.05, warehouse 200x80x15 m @0.1, tunnel 500x8x6 m @0.1);
-    particle counts log-uniform in [1k, 200k], scan sizes uniform in [1k, 16k]
-    drawn from each map's reduced 64x2048 ray-cast scan, particles Gaussian
-    (0.3 m, 5 deg) around each map's true pose."""
+    particle counts log-uniform in p_range ([1k, 200k]), scan sizes uniform in
+    [1k, 16k] drawn from each map's reduced 64x2048 ray-cast scan, particles
+    Gaussian (0.3 m, 5 deg) around each map's true pose."""
     from tsdf_localization_gb300 import synth
-    worlds = [
-        synth.make_workload(synth.ROOM, 21, 50, 16000, 1, 64, 2048, dropout=0.01, edge=8, reduce_cell=0.05,
-                            name="room20x20x4@0.05"),
-        synth.building_workload(seed=2, n_particles=1, n_points=16000),
-        synth.make_workload(synth.WAREHOUSE, 23, 100, 16000, 1, 64, 2048, dropout=0.01, edge=16, reduce_cell=0.1,
-                            name="warehouse200x80x15@0.1"),
-        synth.make_workload(synth.TUNNEL, 24, 100, 16000, 1, 64, 2048, dropout=0.01, edge=16, reduce_cell=0.1,
-                            name="tunnel500x8x6@0.1"),
-    ]
+    if worlds is None:
+        worlds = [
+            synth.make_workload(synth.ROOM, 21, 50, 16000, 1, 64, 2048, dropout=0.01, edge=8, reduce_cell=0.05,
+                                name="room20x20x4@0.05"),
+            synth.building_workload(seed=2, n_particles=1, n_points=16000),
+            synth.make_workload(synth.WAREHOUSE, 23, 100, 16000, 1, 64, 2048, dropout=0.01, edge=16,
+                                reduce_cell=0.1, name="warehouse200x80x15@0.1"),
+            synth.make_workload(synth.TUNNEL, 24, 100, 16000, 1, 64, 2048, dropout=0.01, edge=16, reduce_cell=0.1,
+                                name="tunnel500x8x6@0.1"),
+        ]
     rng = np.random.default_rng(seed)
     filters = []
     for i in range(n_filters):
         wl = worlds[i % 4]
-        P = int(round(np.exp(rng.uniform(np.log(1000), np.log(200_000)))))
+        P = int(round(np.exp(rng.uniform(np.log(p_range[0]), np.log(p_range[1])))))
         N = int(rng.integers(1000, 16001))
         N = min(N, wl.points.shape[0])
         pts = wl.points[np.sort(rng.permutation(wl.points.shape[0])[:N])]
@@ -643,6 +652,33 @@ def batch_measure(args, local: int, worlds, specs, ctx, stream, maps, flush) -> 
             torch.cuda.synchronize()
         launches = lib.tsdfl_launch_count() - l0
         clocks = clk.summary()
+        # the same updates as one single-filter call pair per filter, one after
+        # another on the stream (what the batch replaces)
+        model = N.Model(0.9, 0.1, 0.0, 100.0)
+        vp = C.c_void_p
+        tfs = [np.ascontiguousarray(worlds[mi].tf, np.float32) for mi, _, _ in specs]
+
+        def sequential():
+            for f, t in zip(fs, tfs):
+                N.check(lib.tsdfl_evaluate_device(ctx.handle, f["map"].handle, C.byref(model), vp(f["particles"]),
+                                                  f["P"], vp(f["points"]), f["N"], t.ctypes.data_as(vp), 0,
+                                                  vp(f["pose_out"])))
+                N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(f["particles"]), f["P"],
+                                                             float(np.float32(0.5 / f["P"])), vp(f["resampled"]),
+                                                             f["cap"], vp(f["count"])))
+
+        sequential()
+        ctx.sync()
+        seq_ms = []
+        for i in range(3):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sequential()
+            e1.record(stream)
+            e1.synchronize()
+            seq_ms.append(e0.elapsed_time(e1))
+        ctx.sync()
     batch.close()
     del keep
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
@@ -661,6 +697,8 @@ def batch_measure(args, local: int, worlds, specs, ctx, stream, maps, flush) -> 
             "l2": "flushed (512 MB write) before every timed step",
             "steps": steps, "value": total_pp * steps / (total_ms / 1000.0), "unit": UNIT,
             "ms_per_step": total_ms / steps, "gpu_launches": int(launches),
+            "sequential_single_filter_ms": float(np.median(seq_ms)),
+            "vs_sequential": float(np.median(seq_ms)) / (total_ms / steps),
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "kernel": "eval_batch_kernel",
@@ -755,18 +793,46 @@ def global_measure(args, local: int, ctx, stream, flush, steps: int = 5, warmup:
             N.check(lib.tsdfl_ctx_last_timing(ctx.handle, C.byref(k)))
             kms.append(k.value)
         ctx.sync()
+        # the variant where every particle scores 256 of the points, chosen per
+        # particle and seed (tsdfl_evaluate_subsampled_device)
+        K = 256
+        ms_sub, kms_sub = [], []
+        for i in range(warmup + steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            N.check(lib.tsdfl_evaluate_subsampled_device(ctx.handle, dmap.handle, C.byref(model),
+                                                         vp(d_part.data_ptr()), P, vp(d_pts.data_ptr()), Npts,
+                                                         tfp.ctypes.data_as(vp), K, 1000 + i, vp(d_pose.data_ptr())))
+            N.check(lib.tsdfl_resample_systematic_device(ctx.handle, vp(d_part.data_ptr()), P,
+                                                         float(np.float32(rng.random() / P)), vp(d_out.data_ptr()),
+                                                         cap, vp(d_cnt.data_ptr())))
+            e1.record(stream)
+            e1.synchronize()
+            if i >= warmup:
+                ms_sub.append(e0.elapsed_time(e1))
+                k = C.c_float()
+                N.check(lib.tsdfl_ctx_last_timing(ctx.handle, C.byref(k)))
+                kms_sub.append(k.value)
+        ctx.sync()
     lib.tsdfl_ctx_set_timing(ctx.handle, 0)
     peak, peak_src = measured_peaks()
     kmed = float(np.median(kms))
     alg = roofline_bytes(P, Npts, "compact")
     dmap.close()
-    return {"workload": wl.name, "particles": P, "points": Npts, "steps": steps,
+    sub = {"points_per_particle": K, "selection": "one point per stratum of N/K consecutive scan indices, "
+                                                  "SplitMix64 per (seed, particle)",
+           "value": P * K * steps / (float(np.sum(ms_sub)) / 1000.0), "unit": UNIT,
+           "ms_per_step": float(np.mean(ms_sub)), "kernel_ms": float(np.median(kms_sub))}
+    return {"workload": wl.name, "particles": P, "points": Npts, "steps": steps, "subsampled": sub,
             "step": "sensor update + normalise + mean pose + systematic resample (FP64 CDF)",
             "value": P * Npts * steps / (float(np.sum(ms)) / 1000.0), "unit": UNIT,
             "ms_per_step": float(np.mean(ms)),
             "roofline": {"bound": "hbm", "achieved": alg / (kmed / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / (kmed / 1000.0) / 1e9 / peak, "traffic": None, "kernel": "eval_tiled_kernel",
-                         "kernel_ms": kmed, "peak_source": peak_src, "algorithmic_bytes": alg}}
+                         "frac": alg / (kmed / 1000.0) / 1e9 / peak,
+                         "traffic": MEASURED_TRAFFIC.get(("global", P, Npts, "compact", "fast")),
+                         "kernel": "eval_tiled_kernel", "kernel_ms": kmed, "peak_source": peak_src,
+                         "algorithmic_bytes": alg}}
 
 
 def sub_measurements(args, local: int, ctx, stream, flush, plain_value: float) -> dict:
@@ -782,6 +848,11 @@ def sub_measurements(args, local: int, ctx, stream, flush, plain_value: float) -
     b = batch_measure(args, local, worlds, specs, ctx, stream, maps, flush)
     b["vs_plain"] = b["value"] / plain_value
     out["batch"] = b
+    # small filters (1k-10k particles), where one filter alone leaves most SMs idle
+    _, small = batch_workload(args.filters, seed=12, worlds=worlds, p_range=(1000, 10_000))
+    bs = batch_measure(args, local, worlds, small, ctx, stream, maps, flush)
+    bs["vs_plain"] = bs["value"] / plain_value
+    out["batch_small"] = bs
     sv = served_measure(args, local, worlds, ctx, stream, maps, args.served_seconds)
     sv["vs_plain"] = sv["value"] / plain_value
     out["served"] = sv
@@ -931,10 +1002,7 @@ def main():
     alg = roofline_bytes(P, Npts, args.layout)
     peak, peak_src = measured_peaks()
     achieved = alg / (kmed / 1000.0) / 1e9
-    # DRAM bytes of one scoring launch from an ncu capture of this exact workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum, single pass, full size;
-    # profiles/eval_tiled_kernel_building_100k_x_8192.md)
-    measured_traffic = {("building", 100_000, 8192, "compact", "fast"): 1.326252e9 + 0.054576e9}
+    measured_traffic = MEASURED_TRAFFIC
     traffic = measured_traffic.get((args.workload, P, Npts, args.layout, args.kernel))
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": "eval_tiled_kernel" if (args.kernel == "fast" and info["fast_index"])

@@ -100,6 +100,13 @@ int tsdfl_ctx_workspace_bytes(const tsdfl_ctx* ctx, size_t* eval_bytes, size_t* 
 #define TSDFL_MAP_DENSE 1u
 #define TSDFL_MAP_FORCE_F32 2u    /* keep float slots */
 #define TSDFL_MAP_F16 4u
+/* TSDFL_MAP_HASH: index the allocated bricks in a sparse hash ({brick, rank},
+ * 8 bytes a slot at a load of at most 1/2) instead of the bitmap -- what
+ * TSDFL_MAP_DENSE builds by itself when the bitmap of the brick grid would
+ * exceed 128 KB (bounding boxes of more than 524,288 bricks of 1 m, mostly
+ * empty).  The tiled kernel then reads the rank from this L2-resident table
+ * instead of the brick table. */
+#define TSDFL_MAP_HASH 8u
 int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
                      float sigma, uint32_t flags, tsdfl_map** out);
 /* Same map from 16-bit slot codes (code c < 600: likelihood of |tsdf| = c mm;
@@ -111,8 +118,9 @@ int tsdfl_map_destroy(tsdfl_map* map);
 typedef struct tsdfl_map_info {
     uint64_t grid_occ_size, data_size, bricks;
     uint64_t device_bytes;     /* all device memory the map holds */
-    int32_t storage;           /* 0 = 16-bit codes, 1 = float */
-    int32_t dense;             /* dense layout present */
+    int32_t storage;           /* 0 = 16-bit codes, 1 = float, 2 = half (TSDFL_MAP_F16) */
+    int32_t dense;             /* brick rank index: 0 = brick table only, 1 = bitmap (compact layout),
+                                  2 = sparse brick hash */
     int32_t fast_index;        /* division-free slot indexing verified for this resolution */
     int32_t reserved;
 } tsdfl_map_info;

@@ -375,3 +375,51 @@ def test_best_particle(ctx):
             w[50] = np.float32(1e-30)
         parts[:, 6] = w
         assert best_gpu(parts) == best_ref(parts[:, 6])
+
+
+def _sparse_room(seed=4):
+    """The room at 0.064 m plus one chunk about 200 m away: the bounding box
+    holds about 840,000 bricks, too many for the shared-memory bitmap, almost
+    all of them empty."""
+    from tsdf_localization_gb300 import build_map_codes
+    wl = synth.make_workload(synth.ROOM, seed, 64, 2048, 600, 16, 1024, edge=16, name="room+far")
+    pos, raw = synth.World(synth.ROOM, seed).tsdf_chunks(64, edge=16)
+    busy = int(np.argmax((raw >> 16).astype(bool).sum(1)))
+    pos = np.concatenate([pos, np.array([[195, 195, 19]], np.int32)])
+    raw = np.concatenate([raw, raw[busy:busy + 1]])
+    names = ["%d_%d_%d" % tuple(p) for p in pos]
+    order = sorted(range(len(names)), key=lambda i: names[i].encode())
+    coef, go, codes, _ = build_map_codes(pos[order], raw[order], 16, 64, 0.1, want_free=False)
+    return wl, coef, go, codes
+
+
+@pytest.mark.parametrize("case", ["sparse", "forced"])
+def test_sparse_brick_hash(ctx, case):
+    """The sparse brick hash: built by the compact layout on its own when the
+    brick bitmap exceeds shared memory ("sparse"), or on request
+    (TSDFL_MAP_HASH, "forced"); slot codes and hit counts equal the oracle's,
+    the weights the brick-table kernel's, within 1e-5 of FP64."""
+    from tsdf_localization_gb300.evaluator import code_values
+    if case == "sparse":
+        wl, coef, go, codes = _sparse_room()
+        assert coef.grid_occ_size > 524_288
+        dmap = DeviceMap(ctx, coef, go, codes=codes, dense=True)
+    else:
+        wl = synth.room_workload(seed=11, n_particles=600, n_points=2048)
+        coef, go, codes = wl.coef, wl.grid_occ, wl.codes
+        dmap = DeviceMap(ctx, coef, go, codes=codes, hash_index=True)
+    info = dmap.info()
+    assert info["dense"] == 2 and info["fast_index"] in (1, 2)
+    vals = np.append(code_values(0.1, coef.init_value), np.float32(coef.init_value))
+    om = O.OracleMap(O.coef_from(coef), go, vals[codes])
+    rng = np.random.default_rng(3)
+    pts = np.concatenate([wl.points, rng.uniform(-1.0, 0.3, size=(200, 3)).astype(np.float32)])
+    ref = _oracle_eval(om, wl, points=pts)
+    d = TSDFEvaluator(dmap).evaluate_debug(wl.particles.copy(), pts, wl.tf, voxel_index=True)
+    assert np.array_equal(d["hits"], ref["hits"])
+    assert np.array_equal(d["voxel_index"] & 0xFFFF, _codes_of(ref["voxel_index"], codes, coef.data_size))
+    assert np.allclose(d["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+    brick = DeviceMap(ctx, coef, go, codes=codes)
+    assert brick.info()["dense"] == 0
+    e = TSDFEvaluator(brick).evaluate_debug(wl.particles.copy(), pts, wl.tf)
+    assert np.array_equal(e["raw"], d["raw"]) and np.array_equal(e["hits"], d["hits"])

@@ -96,6 +96,8 @@ struct tsdfl_map {
     uint16_t* h16 = nullptr;      // TSDFL_MAP_F16: half-precision slot values
     uint32_t* occ = nullptr;      // compact layout (TSDFL_MAP_DENSE): brick bitmap and prefix counts
     uint32_t occ_bytes = 0;
+    uint2* hash = nullptr;        // sparse brick hash (TSDFL_MAP_HASH, or DENSE with a bitmap too large)
+    uint32_t hash_slots = 0, hash_probes = 0;
     float* values = nullptr;      // kNumCodes likelihood values (device)
     float max_value = 0;
     uint64_t bricks = 0;
@@ -380,6 +382,11 @@ void fill_view(tsdfl_map* m)
     v.occ = m->occ;
     v.occ_bytes = m->occ_bytes;
     v.occ_mask = m->occ_bytes ? (m->occ_bytes - 1u) & ~7u : 0u;
+    v.hash = m->hash;
+    v.hash_mask = m->hash_slots ? m->hash_slots - 1u : 0u;
+    v.hash_shift = 32u;
+    for (uint32_t sz = m->hash_slots; sz > 1u; sz >>= 1) v.hash_shift -= 1u;
+    v.hash_probes = m->hash_probes;
     v.codes_sent = (uint32_t)c.data_size;
     // tiled fast path: the packed pipeline's float sums are exact integers
     // (largest brick index a fast lookup forms below 2^23, sub-voxel offsets
@@ -441,6 +448,44 @@ int build_compact(tsdfl_map* m, const int32_t* go)
     return TSDFL_OK;
 }
 
+// Sparse brick hash: {brick index, rank} of every allocated brick in a table
+// of 2^k >= 2n slots, linear probing from (brick * 0x9E3779B1) >> (32 - k).
+// hash_probes bounds both a key's distance from its home and the run a miss
+// walks to the empty slot that ends it.
+int build_hash(tsdfl_map* m, const int32_t* go)
+{
+    const tsdfl_map_coef& c = m->coef;
+    if (!m->codes || m->codes_pre != c.sub_dim * c.sub_dim_2) return TSDFL_OK;
+    uint64_t n = 0;
+    for (uint64_t up = 0; up < c.grid_occ_size; ++up) n += go[up] >= 0 ? 1 : 0;
+    uint32_t k = 4;
+    while ((1ull << k) < 2 * n) ++k;
+    if (k > 30) return TSDFL_OK;
+    const uint32_t slots = 1u << k, mask = slots - 1u;
+    std::vector<uint2> table(slots, make_uint2(kHashEmpty, 0u));
+    uint32_t longest = 0, rank = 0;
+    for (uint64_t up = 0; up < c.grid_occ_size; ++up) {
+        if (go[up] < 0) continue;
+        const uint32_t key = (uint32_t)up;
+        const uint32_t h = (uint32_t)(key * 0x9E3779B1u) >> (32 - k);
+        uint32_t t = 0;
+        while (table[(h + t) & mask].x != kHashEmpty) ++t;
+        table[(h + t) & mask] = make_uint2(key, rank++);
+        longest = std::max(longest, t);
+    }
+    uint32_t run = 0, longest_run = 0;   // occupied slots in a row, around the wrap
+    for (uint32_t i = 0; i < 2 * slots; ++i) {
+        run = table[i & mask].x == kHashEmpty ? 0 : run + 1;
+        longest_run = std::max(longest_run, run);
+    }
+    CUDA_TRY(cudaMalloc(&m->hash, sizeof(uint2) * slots));
+    CUDA_TRY(cudaMemcpy(m->hash, table.data(), sizeof(uint2) * slots, cudaMemcpyHostToDevice));
+    m->hash_slots = slots;
+    m->hash_probes = std::max(longest, longest_run) + 1;
+    m->bytes += sizeof(uint2) * slots;
+    return TSDFL_OK;
+}
+
 // grid_occ: the caller's brick table (host)
 int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, const int32_t* grid_occ, uint32_t flags)
 {
@@ -458,9 +503,16 @@ int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, const int32_t* grid_occ, uint32_t f
         fill_view(m);
         return TSDFL_OK;
     }
-    if ((flags & TSDFL_MAP_DENSE) && m->codes) {
+    if ((flags & TSDFL_MAP_HASH) && m->codes) {
+        int rc = build_hash(m, grid_occ);
+        if (rc) return rc;
+    } else if ((flags & TSDFL_MAP_DENSE) && m->codes) {
         int rc = build_compact(m, grid_occ);
         if (rc) return rc;
+        if (!m->occ) {   // the bitmap does not fit shared memory: index the bricks in a hash
+            rc = build_hash(m, grid_occ);
+            if (rc) return rc;
+        }
     }
     fill_view(m);
     CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -476,6 +528,7 @@ void destroy_map(tsdfl_map* m)
     cudaFree(m->data);
     cudaFree(m->h16);
     cudaFree(m->occ);
+    cudaFree(m->hash);
     cudaFree(m->values);
     delete m;
 }
@@ -852,7 +905,7 @@ int tsdfl_map_get_info(const tsdfl_map* m, tsdfl_map_info* info)
     info->bricks = m->bricks;
     info->device_bytes = m->bytes;
     info->storage = m->h16 ? 2 : (m->codes ? 0 : 1);
-    info->dense = m->occ ? 1 : 0;
+    info->dense = m->occ ? 1 : (m->hash ? 2 : 0);
     info->fast_index = m->view.tiled ? m->view.sub_fast : 0;
     info->reserved = 0;
     return TSDFL_OK;

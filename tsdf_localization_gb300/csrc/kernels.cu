@@ -555,9 +555,13 @@ constexpr int kLut16Bytes = kNumCodes * 16;
 // allocated), kCodeLater (the exact slow tiers decide: offset outside
 // [0, mmax + 1) on x or y, outside (-1, mmax + 1) on z; `slow` is set) or
 // kCodeNone (a padding point, valid false).
-// DENSE: the brick's rank from the shared-memory bitmap `occ`; otherwise the
-// brick table grid_occ.
-template <bool DENSE>
+// LAY: where the brick's rank comes from -- kLayBitmap: the shared-memory
+// bitmap `occ`; kLayHash: the sparse brick hash (allocated bricks only, for
+// maps whose bitmap does not fit shared memory); kLayTable: the brick table
+// grid_occ (the reference's own).
+constexpr int kLayTable = 0, kLayBitmap = 1, kLayHash = 2;
+
+template <int LAY>
 __device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned char* occ, uint32_t ox_b,
                                               uint32_t oy_b, float oz, uint32_t upb, uint32_t slb, bool valid,
                                               bool& slow)
@@ -567,7 +571,28 @@ __device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned c
     const bool inside = valid && fast && upb < m.upb_lim;
     uint32_t idx;
     bool ok;
-    if (DENSE) {
+    if (LAY == kLayHash) {
+        // open addressing, linear probing: every key lies within hash_probes
+        // slots of its home, and every run of keys ends at an empty slot within
+        // that bound (measured when the table is built)
+        const uint32_t up = upb - kMagic;
+        uint32_t rank = 0;
+        bool found = false;
+        if (inside) {
+            const uint32_t h = (up * 0x9E3779B1u) >> m.hash_shift;
+            for (uint32_t t = 0; t < m.hash_probes; ++t) {
+                const uint2 e = __ldg(m.hash + ((h + t) & m.hash_mask));
+                if (e.x == up) {
+                    rank = e.y;
+                    found = true;
+                    break;
+                }
+                if (e.x == kHashEmpty) break;
+            }
+        }
+        ok = found;
+        idx = rank * m.sub_dim_3 + slb;
+    } else if (LAY == kLayBitmap) {
         // the masked offset stays inside the staged table whatever upb is
         const uint2 wb = *reinterpret_cast<const uint2*>(occ + ((upb >> 2) & m.occ_mask));
         const uint32_t v = __funnelshift_r(wb.x, 0u, upb);   // word >> (brick & 31)
@@ -630,7 +655,7 @@ __device__ __forceinline__ PosePairs pose_pairs(const float* pose12)
 // the gathered codes k0, k1, whether the exact slow tiers must decide them
 // (s0, s1), and the transformed points (for the deferral).  v0 / v1: the
 // lookup is a real point (false: padding, kCodeNone).
-template <bool DENSE, bool TWO, bool MIN0>
+template <int LAY, bool TWO, bool MIN0>
 __device__ __forceinline__ void pair_lookup(const MapView& m, const unsigned char* occ, const PosePairs& P,
                                             const PipeConsts& K, f2_t X, f2_t Y, f2_t Z, bool v0, bool v1,
                                             uint32_t& k0, uint32_t& k1, bool& s0, bool& s1, f2_t& TX, f2_t& TY,
@@ -666,10 +691,10 @@ __device__ __forceinline__ void pair_lookup(const MapView& m, const unsigned cha
     const f2_t UPB = fma2_rn(FZ, K.UXY, fma2_rn(FY, K.UX, MX));   // 2^23 + mx + my Ux + mz Ux Uy
     float ox0, ox1, oy0, oy1, oz0, oz1, u0, u1, l0, l1;
     upk(OX, ox0, ox1); upk(OY, oy0, oy1); upk(OZ, oz0, oz1); upk(UPB, u0, u1); upk(SLB, l0, l1);
-    k0 = fast_code<DENSE>(m, occ, __float_as_uint(ox0), __float_as_uint(oy0), oz0, __float_as_uint(u0),
-                          __float_as_uint(l0), v0, s0);
-    k1 = fast_code<DENSE>(m, occ, __float_as_uint(ox1), __float_as_uint(oy1), oz1, __float_as_uint(u1),
-                          __float_as_uint(l1), v1, s1);
+    k0 = fast_code<LAY>(m, occ, __float_as_uint(ox0), __float_as_uint(oy0), oz0, __float_as_uint(u0),
+                        __float_as_uint(l0), v0, s0);
+    k1 = fast_code<LAY>(m, occ, __float_as_uint(ox1), __float_as_uint(oy1), oz1, __float_as_uint(u1),
+                        __float_as_uint(l1), v1, s1);
 }
 
 #ifndef TSDFL_TILED_THREADS
@@ -746,7 +771,7 @@ struct TiledParams {
 // TWO: the sub-voxel index needs the two-term multiplier (sub_fast 1);
 // DBG: per-point codes are written to the debug buffer; MIN0: the map's min
 // corner is the origin, so offsets are the transformed coordinates.
-template <bool DENSE, bool TWO, bool DBG, bool MIN0>
+template <int LAY, bool TWO, bool DBG, bool MIN0>
 __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m, const MapView* s_map,
                                            const unsigned char* occ, const float4* sxy, const float2* spz,
                                            const LutEntry* lut, float4* ring, int n, int chunk_pts, int group,
@@ -775,7 +800,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
             uint32_t k0, k1;
             bool s0, s1;
             f2_t TX, TY, TZ;
-            pair_lookup<DENSE, TWO, MIN0>(m, occ, R, K, pk(xy.x, xy.y), pk(xy.z, xy.w), pk(zz.x, zz.y),
+            pair_lookup<LAY, TWO, MIN0>(m, occ, R, K, pk(xy.x, xy.y), pk(xy.z, xy.w), pk(zz.x, zz.y),
                                           !partial || 64 * blk + lane < cn, !partial || 64 * blk + 32 + lane < cn,
                                           k0, k1, s0, s1, TX, TY, TZ);
             // lanes the fast path cannot decide are deferred to the warp's ring and
@@ -840,7 +865,7 @@ __device__ __forceinline__ void fill_lut16(LutEntry* lut, const long long* lut_f
     }
 }
 
-template <bool DENSE, bool TWO, bool DBG, bool MIN0>
+template <int LAY, bool TWO, bool DBG, bool MIN0>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -852,7 +877,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const int n = p.n1 - p.n0;
     const int npairs = ((n + 63) >> 6) * 32;
     if (threadIdx.x == 0) s_map = m;
-    const uint32_t occ_bytes = DENSE ? m.occ_bytes : 0u;
+    const uint32_t occ_bytes = LAY == kLayBitmap ? m.occ_bytes : 0u;
     unsigned char* occ = smem + kLut16Bytes;
     float4* sxy = reinterpret_cast<float4*>(occ + occ_bytes);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
@@ -876,8 +901,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const int nwarps = gridDim.x * kTiledWarps;
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
-        tiled_item<DENSE, TWO, DBG, MIN0>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp,
-                                          lane);
+        tiled_item<LAY, TWO, DBG, MIN0>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp,
+                                        lane);
     }
 }
 
@@ -945,8 +970,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_subsample_kernel(SubPar
             uint32_t k0, k1;
             bool s0, s1;
             f2_t TX, TY, TZ;
-            pair_lookup<DENSE, TWO, MIN0>(m, occ, R, K, pk(xa, xb), pk(ya, yb), pk(za, zb), va, vb, k0, k1, s0, s1,
-                                          TX, TY, TZ);
+            pair_lookup<DENSE ? kLayBitmap : kLayTable, TWO, MIN0>(m, occ, R, K, pk(xa, xb), pk(ya, yb), pk(za, zb),
+                                                                   va, vb, k0, k1, s0, s1, TX, TY, TZ);
             if (__any_sync(0xffffffffu, s0 || s1)) {
                 float tx, ty, tz, u;
                 upk(TX, tx, u); upk(TY, ty, u); upk(TZ, tz, u);
@@ -1082,8 +1107,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             if (j >= (uint32_t)kBatchItems || item >= s_seg.items) break;
             const EvalParams& p = s_seg.e;
             const int chunk = item / s_seg.groups, grp = item - chunk * s_seg.groups;
-            tiled_item<DENSE, TWO, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n, s_seg.chunk, s_seg.group,
-                                                 chunk, grp, lane);
+            tiled_item<DENSE ? kLayBitmap : kLayTable, TWO, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n,
+                                                                          s_seg.chunk, s_seg.group, chunk, grp,
+                                                                          lane);
         }
         __syncthreads();   // every warp is done with s_batch and the staged segment
     }
@@ -2064,17 +2090,24 @@ size_t eval_smem_bytes(bool serial, int n)
 
 using TiledKernel = void (*)(TiledParams);
 
-template <bool DENSE, bool TWO>
+template <int LAY, bool TWO>
 TiledKernel pick_tiled_2(bool dbg, bool min0)
 {
-    return dbg ? (min0 ? eval_tiled_kernel<DENSE, TWO, true, true> : eval_tiled_kernel<DENSE, TWO, true, false>)
-               : (min0 ? eval_tiled_kernel<DENSE, TWO, false, true> : eval_tiled_kernel<DENSE, TWO, false, false>);
+    return dbg ? (min0 ? eval_tiled_kernel<LAY, TWO, true, true> : eval_tiled_kernel<LAY, TWO, true, false>)
+               : (min0 ? eval_tiled_kernel<LAY, TWO, false, true> : eval_tiled_kernel<LAY, TWO, false, false>);
 }
 
-TiledKernel pick_tiled(bool dense, bool two, bool dbg, bool min0)
+template <int LAY>
+TiledKernel pick_tiled_1(bool two, bool dbg, bool min0)
 {
-    return dense ? (two ? pick_tiled_2<true, true>(dbg, min0) : pick_tiled_2<true, false>(dbg, min0))
-                 : (two ? pick_tiled_2<false, true>(dbg, min0) : pick_tiled_2<false, false>(dbg, min0));
+    return two ? pick_tiled_2<LAY, true>(dbg, min0) : pick_tiled_2<LAY, false>(dbg, min0);
+}
+
+TiledKernel pick_tiled(int lay, bool two, bool dbg, bool min0)
+{
+    return lay == kLayBitmap ? pick_tiled_1<kLayBitmap>(two, dbg, min0)
+                             : (lay == kLayHash ? pick_tiled_1<kLayHash>(two, dbg, min0)
+                                                : pick_tiled_1<kLayTable>(two, dbg, min0));
 }
 
 size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
@@ -2127,7 +2160,10 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
         // sub_fast 2: floor(s * sub_inv) is the sub-voxel index; 1: the two-term multiplier
         const bool two = m.sub_fast == 1, dbg = p.dbg != nullptr;
-        auto k = pick_tiled(dense, two, dbg, m.min0 != 0);
+        // the brick rank: from the shared-memory bitmap, else the sparse brick hash
+        // when the map has one, else the brick table
+        const int lay = dense ? kLayBitmap : (m.hash ? kLayHash : kLayTable);
+        auto k = pick_tiled(lay, two, dbg, m.min0 != 0);
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (first) {

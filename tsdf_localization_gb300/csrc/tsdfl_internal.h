@@ -73,6 +73,14 @@ struct MapView {
     const uint32_t* occ;
     uint32_t occ_bytes;            // staged bytes (power of two), 0 without the compact layout
     uint32_t occ_mask;             // (occ_bytes - 1) & ~7
+    // Sparse brick hash (TSDFL_MAP_HASH, or TSDFL_MAP_DENSE on maps whose bitmap
+    // does not fit shared memory): {brick index, rank} of the allocated bricks
+    // only, open addressing with linear probing from slot
+    // (brick * 0x9E3779B1) >> hash_shift; empty slots hold kHashEmpty; every key
+    // sits within hash_probes slots of its home and every run of keys ends
+    // within that bound.
+    const uint2* hash;
+    uint32_t hash_mask, hash_shift, hash_probes;
     // Both code arrays end in kSentinels extra entries {kCodeMiss, kCodeLater,
     // kCodeNone, kCodeNone}: the fast path gathers a lookup that falls outside
     // the allocated slots from there, so every gather yields the final code.
@@ -95,6 +103,7 @@ struct MapView {
 };
 
 constexpr int kSentinels = 4;
+constexpr uint32_t kHashEmpty = 0xffffffffu;
 
 #ifdef __CUDACC__
 
