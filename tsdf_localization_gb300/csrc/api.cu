@@ -148,6 +148,10 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
     size_t o_sums = take(sizeof(double) * 16);
     size_t o_wsf = take(sizeof(float) * 4);
     size_t o_st = take(sizeof(int32_t) * 4);
+    size_t o_ord = take(sizeof(uint32_t) * nP);
+    size_t o_pk = take(sizeof(uint32_t) * nP);
+    size_t o_ph = take(sizeof(int32_t) * 4096);
+    size_t o_ce = take(sizeof(float) * 4);
     if (base) {
         char* b = base;
         e->pose12 = reinterpret_cast<float*>(b + o_pose);
@@ -172,6 +176,10 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
         e->sums = reinterpret_cast<double*>(b + o_sums);
         e->weight_sum_f = reinterpret_cast<float*>(b + o_wsf);
         e->status = reinterpret_cast<int32_t*>(b + o_st);
+        e->order = reinterpret_cast<uint32_t*>(b + o_ord);
+        e->pkeys = reinterpret_cast<uint32_t*>(b + o_pk);
+        e->phist = reinterpret_cast<int32_t*>(b + o_ph);
+        e->cloud_ext = reinterpret_cast<float4*>(b + o_ce);
     }
     return off;
 }
@@ -585,6 +593,8 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     if (rc) return rc;
     rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
     if (rc) return rc;
+    rc = launch_particle_order(d_particles, (int)P, b, s);
+    if (rc) return rc;
     bool dense = map->occ != nullptr;
     const bool tiled = !serial && map->view.storage == 0 && map->view.tiled && !(flags & TSDFL_EVAL_GENERIC);
     size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
@@ -644,6 +654,8 @@ int run_eval_sub(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, flo
     rc = launch_pose_kernel(tf, (int)P, b, s);
     if (rc) return rc;
     rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
+    if (rc) return rc;
+    rc = launch_particle_order(d_particles, (int)P, b, s);
     if (rc) return rc;
     if (c->timing) CUDA_TRY(cudaEventRecord(c->ev0, s));
     rc = launch_eval_subsample(map->view, mdl->a_hit, (int)P, (int)N, (int)K, seed, c_in, b, c->sm_count, s);

@@ -206,6 +206,8 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
                 e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
             }
             s_wide = fmaxf(e.z - e.x, e.w - e.y) > kWideCloud ? 1 : 0;   // no particles: -inf
+            b.counts[2] = s_wide;   // the particles are put in spatial order too
+            b.cloud_ext[0] = e;
         }
     }
     for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) bins[i] = 0;
@@ -291,6 +293,89 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
         int t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_counts[w];
         b.counts[0] = t;
+    }
+}
+
+// Spatial order of a spread cloud's particles (global localisation): 64 x 64
+// cells over the particles' x / y extent, numbered along a Morton curve; a
+// counting sort puts the particles in cell order.  The tiled kernel then walks
+// regions of consecutive particles, so that at any time the grid scores
+// particles from one part of the map and the gathers stay in the L2.  The
+// order within a cell depends on the atomics, which changes nothing: every
+// particle's sums are exact integers written to its own index.
+constexpr int kCellBits = 6;
+constexpr int kCellBins = 1 << (2 * kCellBits);
+constexpr int kCellScanThreads = 1024;
+static_assert(kCellBins == 4 * kCellScanThreads, "four bins per thread in the scan");
+
+__device__ __forceinline__ uint32_t morton2(uint32_t x, uint32_t y)
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < kCellBits; ++k) m |= (((x >> k) & 1u) << (2 * k)) | (((y >> k) & 1u) << (2 * k + 1));
+    return m;
+}
+
+__global__ void particle_cells_kernel(const float* particles, int P, EvalBuffers b)
+{
+    if (b.counts[2] == 0) return;   // a compact cloud keeps its order
+    const float4 e = b.cloud_ext[0];
+    const float n = (float)(1 << kCellBits);
+    const float sx = n / fmaxf(e.z - e.x, 1e-3f), sy = n / fmaxf(e.w - e.y, 1e-3f);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        const float x = particles[7 * (size_t)i], y = particles[7 * (size_t)i + 1];
+        // fmaxf / fminf also send NaN positions to cell 0
+        const uint32_t cx = (uint32_t)fminf(fmaxf((x - e.x) * sx, 0.0f), n - 1.0f);
+        const uint32_t cy = (uint32_t)fminf(fmaxf((y - e.y) * sy, 0.0f), n - 1.0f);
+        const uint32_t key = morton2(cx, cy);
+        b.pkeys[i] = key;
+        atomicAdd(&b.phist[key], 1);
+    }
+}
+
+__global__ void __launch_bounds__(kCellScanThreads) particle_scan_kernel(EvalBuffers b)
+{
+    if (b.counts[2] == 0) return;
+    __shared__ int warp_sums[kCellScanThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int c[4], v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        c[k] = b.phist[4 * t + k];
+        v += c[k];
+    }
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        warp_sums[lane] = w;   // inclusive over warps
+    }
+    __syncthreads();
+    int run = (warp ? warp_sums[warp - 1] : 0) + incl - v;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        b.phist[4 * t + k] = run;
+        run += c[k];
+    }
+}
+
+__global__ void particle_scatter_kernel(int P, EvalBuffers b)
+{
+    if (b.counts[2] == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        const int q = atomicAdd(&b.phist[b.pkeys[i]], 1);
+        b.order[q] = (uint32_t)i;
     }
 }
 
@@ -384,6 +469,8 @@ struct EvalParams {
     float* raw;          // serial mode
     uint32_t* hits;
     uint32_t* dbg;       // optional: P x N_total slot index (brick) / code (dense)
+    const uint32_t* order;   // spatial order of the particles (used when *sched != 0)
+    const int32_t* sched;    // the staging kernel's spread-cloud flag (null: original order)
     int32_t* status;
     int P;
     int n0, n1;          // point range of this pass
@@ -742,6 +829,8 @@ __device__ __noinline__ Partial drain(const MapView* m, const LutEntry* lut, con
 
 constexpr int kTiledChunk = 1024;     // scan points per work item
 constexpr int kTiledGroup = 4;        // particles per work item
+constexpr int kSpreadChunk = 512;     // scan points per work item, spread clouds
+constexpr int kRegionGroups = 2048;   // particle groups per region, spread clouds
 
 struct TiledParams {
     EvalParams e;
@@ -775,7 +864,7 @@ template <int LAY, bool TWO, bool DBG, bool MIN0>
 __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m, const MapView* s_map,
                                            const unsigned char* occ, const float4* sxy, const float2* spz,
                                            const LutEntry* lut, float4* ring, int n, int chunk_pts, int group,
-                                           int chunk, int grp, int lane)
+                                           int chunk, int grp, int lane, const uint32_t* order = nullptr)
 {
     const PipeConsts K = pipe_consts(m);
     uint32_t head = 0, tail = 0;
@@ -783,8 +872,9 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
     const int cn = min(chunk_pts, n - c0);
     const int b0 = c0 >> 6, nblk = (cn + 63) >> 6, nfull = cn >> 6;
     for (int k = 0; k < group; ++k) {
-        const int pi = grp * group + k;
-        if (pi >= p.P) break;
+        const int q = grp * group + k;
+        if (q >= p.P) break;
+        const int pi = order ? (int)order[q] : q;   // the particle at position q
         const PosePairs R = pose_pairs(p.pose12 + 12 * (size_t)pi);
         long long acc = 0;
         uint32_t hits = 0;
@@ -899,6 +989,23 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     float4* ring = reinterpret_cast<float4*>(spz + npairs) + (threadIdx.x >> 5) * kRing;
     const int gwarp = blockIdx.x * kTiledWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kTiledWarps;
+    if (p.sched && *p.sched) {
+        // spread cloud: the particles in spatial order, walked region by region
+        // (kRegionGroups groups of neighbouring particles, all chunks, chunk-major
+        // within the region), with shorter chunks, so that the grid's gathers at
+        // any time fall in one part of one band of the map
+        const int chunk_pts = kSpreadChunk;
+        const int chunks = (n + chunk_pts - 1) / chunk_pts, items = chunks * tp.groups;
+        const int per_region = chunks * kRegionGroups;
+        for (int item = gwarp; item < items; item += nwarps) {
+            const int r = item / per_region, rem = item - r * per_region;
+            const int g0 = r * kRegionGroups, rg = min(kRegionGroups, tp.groups - g0);
+            const int chunk = rem / rg, grp = g0 + (rem - chunk * rg);
+            tiled_item<LAY, TWO, DBG, MIN0>(p, m, &s_map, occ, sxy, spz, lut, ring, n, chunk_pts, tp.group, chunk,
+                                            grp, lane, p.order);
+        }
+        return;
+    }
     for (int item = gwarp; item < tp.items; item += nwarps) {
         const int chunk = item / tp.groups, grp = item - chunk * tp.groups;
         tiled_item<LAY, TWO, DBG, MIN0>(p, m, &s_map, occ, sxy, spz, lut, ring, n, tp.chunk, tp.group, chunk, grp,
@@ -955,7 +1062,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_subsample_kernel(SubPar
     const uint32_t N = (uint32_t)p.n_total, Ks = (uint32_t)sp.K;
     const int gwarp = blockIdx.x * kTiledWarps + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * kTiledWarps;
-    for (int pi = gwarp; pi < p.P; pi += nwarps) {
+    const bool ordered = p.sched && *p.sched;
+    for (int q = gwarp; q < p.P; q += nwarps) {
+        const int pi = ordered ? (int)p.order[q] : q;   // neighbouring warps take neighbouring particles
         const PosePairs R = pose_pairs(p.pose12 + 12 * (size_t)pi);
         const uint64_t st = sub_particle_state(sp.seed, (uint64_t)pi);
         long long acc = 0;
@@ -2071,6 +2180,18 @@ int launch_prepare(const float* points, int N, int npad, int P, float max_range_
     return check(cudaGetLastError());
 }
 
+int launch_particle_order(const float* particles, int P, const EvalBuffers& b, cudaStream_t s)
+{
+    if (P <= 0) return TSDFL_OK;
+    cudaMemsetAsync(b.phist, 0, sizeof(int32_t) * kCellBins, s);
+    const int blocks = std::min((P + 255) / 256, 4096);
+    particle_cells_kernel<<<blocks, 256, 0, s>>>(particles, P, b);
+    particle_scan_kernel<<<1, kCellScanThreads, 0, s>>>(b);
+    particle_scatter_kernel<<<blocks, 256, 0, s>>>(P, b);
+    g_launches += 3;
+    return check(cudaGetLastError());
+}
+
 int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s)
 {
     Tf16 t;
@@ -2140,6 +2261,8 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
     p.raw = b.raw;
     p.hits = b.hits;
     p.dbg = b.dbg_index;
+    p.order = b.order;
+    p.sched = b.counts + 2;
     p.status = b.status;
     p.P = P; p.n0 = n0; p.n1 = n1; p.n_total = n_total; p.first_pass = first ? 1 : 0;
     p.a_hit = a_hit;
@@ -2208,6 +2331,8 @@ int launch_eval_subsample(const MapView& m, float a_hit, int P, int N, int K, un
     p.lut_fx = b.lut_fx;
     p.sum_fx = b.sum_fx;
     p.hits = b.hits;
+    p.order = b.order;
+    p.sched = b.counts + 2;
     p.status = b.status;
     p.P = P; p.n0 = 0; p.n1 = N; p.n_total = N; p.first_pass = 1;
     p.a_hit = a_hit;

@@ -189,12 +189,23 @@ struct EvalBuffers {
     float* weight_sum_f;     // [1]
     int32_t* status;         // per-evaluation device status word
     uint32_t* dbg_index;     // optional P x N
+    // Spread clouds (global localisation): the particles in spatial order --
+    // counts[2] is set by the staging kernel when the cloud is spread, then
+    // order[q] is the particle at position q of a Morton order of 64 x 64
+    // cells over the cloud's x / y extent (cloud_ext).
+    uint32_t* order;         // P
+    uint32_t* pkeys;         // P: each particle's cell
+    int32_t* phist;          // kCellBins: cell counts, then offsets
+    float4* cloud_ext;       // [1]: min x, min y, max x, max y of the particles
 };
 
 // Runs after launch_pose_kernel for the same buffers (reads the cloud's extent).
 int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s);
 int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
+// Runs after launch_prepare: orders the particles of a spread cloud by cell
+// (b.order); for a compact cloud its kernels return at once.
+int launch_particle_order(const float* particles, int P, const EvalBuffers& b, cudaStream_t s);
 size_t eval_smem_bytes(bool serial, int n);
 // Scan points one pass of the tiled kernel stages (0: the kernel cannot hold
 // this map's occupancy bitmap beside any points).
