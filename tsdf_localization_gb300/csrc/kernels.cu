@@ -829,8 +829,8 @@ __device__ __noinline__ Partial drain(const MapView* m, const LutEntry* lut, con
 
 constexpr int kTiledChunk = 1024;     // scan points per work item
 constexpr int kTiledGroup = 4;        // particles per work item
-constexpr int kSpreadChunk = 512;     // scan points per work item, spread clouds
-constexpr int kRegionGroups = 2048;   // particle groups per region, spread clouds
+constexpr int kSpreadChunk = 1024;    // scan points per work item, spread clouds
+constexpr int kRegionGroups = 1024;   // particle groups per region, spread clouds
 
 struct TiledParams {
     EvalParams e;
@@ -992,8 +992,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     if (p.sched && *p.sched) {
         // spread cloud: the particles in spatial order, walked region by region
         // (kRegionGroups groups of neighbouring particles, all chunks, chunk-major
-        // within the region), with shorter chunks, so that the grid's gathers at
-        // any time fall in one part of one band of the map
+        // within the region), so that the grid's gathers at any time fall in one
+        // part of the map
         const int chunk_pts = kSpreadChunk;
         const int chunks = (n + chunk_pts - 1) / chunk_pts, items = chunks * tp.groups;
         const int per_region = chunks * kRegionGroups;
