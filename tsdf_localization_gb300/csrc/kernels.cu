@@ -1144,7 +1144,7 @@ struct BatchSeg {
 // LUT, its map's occupancy bitmap, the pass's scan points) before its warps
 // score the items.  Per-item scoring is eval_tiled_kernel's, so every filter's
 // sums equal its single-filter sums bit for bit.
-template <bool DENSE, bool TWO>
+template <bool DENSE, bool TWO, bool MIN0>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const BatchSeg* __restrict__ segs, int nseg,
                                                                       uint32_t total_batches, uint32_t* counter,
                                                                       int32_t* status)
@@ -1216,7 +1216,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             if (j >= (uint32_t)kBatchItems || item >= s_seg.items) break;
             const EvalParams& p = s_seg.e;
             const int chunk = item / s_seg.groups, grp = item - chunk * s_seg.groups;
-            tiled_item<DENSE ? kLayBitmap : kLayTable, TWO, false, false>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n,
+            tiled_item<DENSE ? kLayBitmap : kLayTable, TWO, false, MIN0>(p, p.m, &p.m, occ, sxy, spz, lut, ring, n,
                                                                           s_seg.chunk, s_seg.group, chunk, grp,
                                                                           lane);
         }
@@ -2368,13 +2368,13 @@ uint32_t build_batch_segs(const BatchSegSpec* specs, int nseg, int chunk, int gr
     });
     uint32_t total = 0;
     int o = 0;
-    for (int kind = 0; kind < 4; ++kind) {   // bit 1: compact layout, bit 0: two-term multiplier
+    for (int kind = 0; kind < 8; ++kind) {   // bit 2: min at the origin, bit 1: compact, bit 0: two-term
         kinds->first[kind] = o;
         kinds->count[kind] = 0;
         uint32_t batches = 0;
         for (int oi = 0; oi < nseg; ++oi) {
             const BatchSegSpec& sp = specs[order[oi]];
-            const int k = (sp.dense ? 2 : 0) + (sp.m.sub_fast == 1 ? 1 : 0);
+            const int k = (sp.m.min0 ? 4 : 0) + (sp.dense ? 2 : 0) + (sp.m.sub_fast == 1 ? 1 : 0);
             if (k != kind) continue;
             const EvalBuffers& b = sp.b;
             BatchSeg g{};
@@ -2414,11 +2414,15 @@ int launch_eval_batch(const void* d_segs, const BatchKinds& kinds, uint32_t* cou
 {
     const BatchSeg* segs = static_cast<const BatchSeg*>(d_segs);
     const size_t smem = batch_smem_bytes();
-    for (int kind = 0; kind < 4; ++kind) {
+    using BatchKernel = void (*)(const BatchSeg*, int, uint32_t, uint32_t*, int32_t*);
+    static const BatchKernel kKinds[8] = {
+        eval_batch_kernel<false, false, false>, eval_batch_kernel<false, true, false>,
+        eval_batch_kernel<true, false, false>,  eval_batch_kernel<true, true, false>,
+        eval_batch_kernel<false, false, true>,  eval_batch_kernel<false, true, true>,
+        eval_batch_kernel<true, false, true>,   eval_batch_kernel<true, true, true>};
+    for (int kind = 0; kind < 8; ++kind) {
         if (kinds.count[kind] == 0 || kinds.batches[kind] == 0) continue;
-        auto k = kind == 3 ? eval_batch_kernel<true, true>
-                           : kind == 2 ? eval_batch_kernel<true, false>
-                                       : kind == 1 ? eval_batch_kernel<false, true> : eval_batch_kernel<false, false>;
+        auto k = kKinds[kind];
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
         unsigned blocks = (unsigned)sm_count;

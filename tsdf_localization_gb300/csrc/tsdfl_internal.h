@@ -234,11 +234,12 @@ struct BatchSegSpec {
     bool dense;
     EvalBuffers b;
 };
-// The segments of each map-layout kind (bit 1: compact layout, bit 0:
-// two-term sub-voxel multiplier) form one queue and one persistent launch.
+// The segments of each map-layout kind (bit 2: min corner at the origin, bit 1:
+// compact layout, bit 0: two-term sub-voxel multiplier) form one queue and one
+// persistent launch.
 struct BatchKinds {
-    int first[4], count[4];
-    uint32_t batches[4];
+    int first[8], count[8];
+    uint32_t batches[8];
 };
 size_t batch_seg_bytes();
 // Writes nseg segment records (nseg * batch_seg_bytes() bytes at host_out),
