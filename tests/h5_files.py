@@ -8,8 +8,9 @@ Structures follow the HDF5 file format specification:
   the reference's case (HighFive with default property lists);
 - "v2": superblock version 2, version 2 object headers, groups with compact
   link messages -- the latest-format settings.
-Datasets are 1-D 4-byte integers, stored contiguously by default.  Checksums
-of version 2 structures are written as zero (the reader does not check them).
+Datasets are 1-D 4-byte integers, stored contiguously by default.  Version 2
+structures carry the format's metadata checksum: Bob Jenkins' lookup3
+hashlittle (2006) of the structure's bytes with initial value 0.
 """
 from __future__ import annotations
 
@@ -19,6 +20,48 @@ import numpy as np
 
 UNDEF = 0xFFFFFFFFFFFFFFFF
 SIGNATURE = b"\x89HDF\r\n\x1a\n"
+
+
+def lookup3(data: bytes, init: int = 0) -> int:
+    """lookup3's hashlittle (Jenkins 2006) of data, 32-bit."""
+    M = 0xFFFFFFFF
+
+    def rot(x, r):
+        return ((x << r) | (x >> (32 - r))) & M
+
+    n = len(data)
+    a = b = c = (0xDEADBEEF + n + init) & M
+    k = 0
+    while n - k > 12:
+        a = (a + int.from_bytes(data[k:k + 4], "little")) & M
+        b = (b + int.from_bytes(data[k + 4:k + 8], "little")) & M
+        c = (c + int.from_bytes(data[k + 8:k + 12], "little")) & M
+        a = (a - c) & M; a ^= rot(c, 4); c = (c + b) & M
+        b = (b - a) & M; b ^= rot(a, 6); a = (a + c) & M
+        c = (c - b) & M; c ^= rot(b, 8); b = (b + a) & M
+        a = (a - c) & M; a ^= rot(c, 16); c = (c + b) & M
+        b = (b - a) & M; b ^= rot(a, 19); a = (a + c) & M
+        c = (c - b) & M; c ^= rot(b, 4); b = (b + a) & M
+        k += 12
+    rest = data[k:]
+    if not rest:
+        return c
+    a = (a + int.from_bytes(rest[0:4], "little")) & M
+    b = (b + int.from_bytes(rest[4:8], "little")) & M
+    c = (c + int.from_bytes(rest[8:12], "little")) & M
+    c ^= b; c = (c - rot(b, 14)) & M
+    a ^= c; a = (a - rot(c, 11)) & M
+    b ^= a; b = (b - rot(a, 25)) & M
+    c ^= b; c = (c - rot(b, 16)) & M
+    a ^= c; a = (a - rot(c, 4)) & M
+    b ^= a; b = (b - rot(a, 14)) & M
+    c ^= b; c = (c - rot(b, 24)) & M
+    return c
+
+
+def _sealed(body: bytes) -> bytes:
+    """A version 2 structure: its bytes followed by their checksum."""
+    return body + struct.pack("<I", lookup3(body))
 
 
 class Dataset:
@@ -112,14 +155,14 @@ def _v2_block(msgs) -> bytes:
 
 def _v2_header(w: _Buf, msgs, split=False) -> int:
     if split and len(msgs) > 1:
-        tail = b"OCHK" + _v2_block(msgs[1:]) + b"\0" * 4
+        tail = _sealed(b"OCHK" + _v2_block(msgs[1:]))
         cont = w.add(tail)
         body = _v2_block(msgs[:1] + [(0x10, struct.pack("<QQ", cont, len(tail)))])
     else:
         body = _v2_block(msgs)
     body += b"\0\0"   # a gap shorter than a message prefix
     flags = 0x01      # chunk-0 size in 2 bytes
-    return w.add(b"OHDR" + struct.pack("<BBH", 2, flags, len(body)) + body + b"\0" * 4)
+    return w.add(_sealed(b"OHDR" + struct.pack("<BBH", 2, flags, len(body)) + body))
 
 
 def _symbol_group(w: _Buf, children: dict[str, int], leaf_k: int, internal_k: int) -> tuple[int, int, int]:
@@ -211,6 +254,10 @@ def write(path, chunks: dict[str, Dataset], fmt: str = "v0", leaf_k: int = 4, in
         base_field = {0: 24, 1: 28}.get(sbv, 12)
         data = bytearray(data)
         data[userblock + base_field:userblock + base_field + 8] = struct.pack("<Q", userblock)
+        data = bytes(data)
+    if v2:   # the superblock's checksum over its 44 bytes before it
+        data = bytearray(data)
+        data[userblock + 44:userblock + 48] = struct.pack("<I", lookup3(bytes(data[userblock:userblock + 44])))
         data = bytes(data)
     with open(path, "wb") as f:
         f.write(data)

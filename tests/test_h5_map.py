@@ -177,3 +177,37 @@ def test_corrupted_files_fail_cleanly(tmp_path, fmt):
             assert e.code in (N.TSDFL_ERR_INVALID_ARG, N.TSDFL_ERR_UNSUPPORTED, N.TSDFL_ERR_OUT_OF_MEMORY)
             continue
         assert pos.shape == (raw.shape[0], 3) and (raw.shape[0] == 0 or raw.shape[1] == edge ** 3)
+
+
+def test_lookup3_known_values():
+    """The checksum the test files carry is lookup3's hashlittle: the values
+    its author published with the function."""
+    assert H.lookup3(b"", 0) == 0xDEADBEEF
+    assert H.lookup3(b"", 0xDEADBEEF) == 0xBD5B7DDE
+    assert H.lookup3(b"Four score and seven years ago", 0) == 0x17770551
+    assert H.lookup3(b"Four score and seven years ago", 1) == 0xCD628161
+
+
+@pytest.mark.parametrize("superblock", [2, 3])
+@pytest.mark.parametrize("where", ["superblock", "object header", "continuation"])
+def test_version2_checksums_verified(tmp_path, superblock, where):
+    """A byte changed inside a checksummed version 2 structure is reported
+    (TSDFL_ERR_INVALID_ARG); the intact file reads."""
+    chunks = {"0_0_0": H.Dataset(np.arange(8, dtype=np.uint32), split_header=True),
+              "0_0_1": H.Dataset(np.arange(8, 16, dtype=np.uint32))}
+    path = tmp_path / "v2.h5"
+    H.write(path, chunks, fmt="v2", superblock=superblock)
+    pos, raw, edge = read_map_h5(path)
+    assert edge == 2 and np.array_equal(raw[1], np.arange(8, 16))
+    data = bytearray(path.read_bytes())
+    if where == "superblock":
+        at = 20    # inside the base / extension addresses
+    else:
+        sig = b"OHDR" if where == "object header" else b"OCHK"
+        at = data.index(sig) + 6
+    data[at] ^= 0x40
+    bad = tmp_path / "bad.h5"
+    bad.write_bytes(bytes(data))
+    with pytest.raises(TsdflError) as e:
+        read_map_h5(bad)
+    assert e.value.code == N.TSDFL_ERR_INVALID_ARG and "checksum" in str(e.value)

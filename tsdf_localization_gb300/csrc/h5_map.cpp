@@ -12,8 +12,11 @@
 // B-tree of group nodes, local heap, symbol table nodes) or as compact link
 // messages; dataspace, datatype (4-byte fixed point, either byte order), fill
 // value and data layout (contiguous or compact) messages.  Dense link storage,
-// chunked, filtered or external datasets are reported as unsupported, and
-// checksums of version 2 structures are not verified.
+// chunked, filtered or external datasets are reported as unsupported.  The
+// checksums of the version 2 structures read (superblock versions 2 and 3,
+// version 2 object headers and their continuation blocks) are verified: the
+// format's metadata checksum is Bob Jenkins' lookup3 hash ("hashlittle",
+// published 2006) of the structure's bytes with initial value 0.
 #include <algorithm>
 #include <cctype>
 #include <cerrno>
@@ -54,6 +57,45 @@ uint64_t le(const uint8_t* p, int n)
     uint64_t v = 0;
     for (int i = n - 1; i >= 0; --i) v = (v << 8) | p[i];
     return v;
+}
+
+// lookup3's hashlittle (Jenkins 2006), byte by byte: the metadata checksum of
+// the HDF5 file format for every version 2 structure.
+uint32_t lookup3(const uint8_t* k, size_t n, uint32_t init)
+{
+    auto rot = [](uint32_t x, int r) { return (x << r) | (x >> (32 - r)); };
+    uint32_t a, b, c;
+    a = b = c = 0xdeadbeefu + (uint32_t)n + init;
+    auto word = [&](const uint8_t* p, size_t m) {   // up to 4 bytes, little-endian
+        uint32_t v = 0;
+        for (size_t i = 0; i < m; ++i) v |= (uint32_t)p[i] << (8 * i);
+        return v;
+    };
+    while (n > 12) {
+        a += word(k, 4);
+        b += word(k + 4, 4);
+        c += word(k + 8, 4);
+        a -= c; a ^= rot(c, 4);  c += b;
+        b -= a; b ^= rot(a, 6);  a += c;
+        c -= b; c ^= rot(b, 8);  b += a;
+        a -= c; a ^= rot(c, 16); c += b;
+        b -= a; b ^= rot(a, 19); a += c;
+        c -= b; c ^= rot(b, 4);  b += a;
+        n -= 12;
+        k += 12;
+    }
+    if (n == 0) return c;
+    a += word(k, n < 4 ? n : 4);
+    if (n > 4) b += word(k + 4, n < 8 ? n - 4 : 4);
+    if (n > 8) c += word(k + 8, n - 8);
+    c ^= b; c -= rot(b, 14);
+    a ^= c; a -= rot(c, 11);
+    b ^= a; b -= rot(a, 25);
+    c ^= b; c -= rot(b, 16);
+    a ^= c; a -= rot(c, 4);
+    b ^= a; b -= rot(a, 14);
+    c ^= b; c -= rot(b, 24);
+    return c;
 }
 
 struct Msg {
@@ -136,7 +178,9 @@ public:
             read(pos + q, s, (size_t)w);
             const uint64_t chunk0 = le(s, w);
             q += (uint64_t)w;
-            if (chunk0 > size_) fail(TSDFL_ERR_INVALID_ARG, "object header chunk larger than the file");
+            if (chunk0 > size_ || pos + q + chunk0 + 4 > size_)
+                fail(TSDFL_ERR_INVALID_ARG, "object header chunk larger than the file");
+            verify_checksum(pos, q + chunk0, "object header");
             blocks.push_back({pos + q, pos + q + chunk0});
         } else if (h[0] == 1) {
             const uint64_t hsize = le(h + 8, 4);
@@ -172,8 +216,9 @@ public:
                     if (v2) {
                         uint8_t sig[4];
                         read(cpos, sig, 4);
-                        if (std::memcmp(sig, "OCHK", 4) != 0 || clen < 8)
+                        if (std::memcmp(sig, "OCHK", 4) != 0 || clen < 8 || cpos + clen > size_)
                             fail(TSDFL_ERR_INVALID_ARG, "bad object header continuation block");
+                        verify_checksum(cpos, clen - 4, "object header continuation block");
                         blocks.push_back({cpos + 4, cpos + clen - 4});   // signature .. checksum
                     } else {
                         blocks.push_back({cpos, cpos + clen});
@@ -379,6 +424,16 @@ public:
 private:
     uint64_t addr_of(const uint8_t* p) const { return addr(p); }
 
+    // The n bytes at pos are followed by their lookup3 checksum.
+    void verify_checksum(uint64_t pos, uint64_t n, const char* what) const
+    {
+        if (n > (1ull << 30) || pos + n + 4 > size_) fail(TSDFL_ERR_INVALID_ARG, std::string(what) + " outside the file");
+        std::vector<uint8_t> buf((size_t)n + 4);
+        read(pos, buf.data(), buf.size());
+        if (lookup3(buf.data(), (size_t)n, 0) != (uint32_t)le(buf.data() + n, 4))
+            fail(TSDFL_ERR_INVALID_ARG, std::string(what) + " checksum mismatch");
+    }
+
     void superblock()
     {
         static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
@@ -405,6 +460,7 @@ private:
             so_ = sb[9];
             sl_ = sb[10];
             check_sizes();
+            verify_checksum(pos, 12 + 4 * (uint64_t)so_, "superblock");
             base_ = le(sb + 12, so_);
             root_ = addr(sb + 12 + 3 * (size_t)so_);   // after base, extension, end of file
         } else {
