@@ -614,7 +614,6 @@ __device__ __forceinline__ f2_t or2(f2_t a, f2_t b)
 }
 
 constexpr uint32_t kMagic = 0x4B000000u;     // bits of 2^23
-constexpr uint32_t kMagic15 = 0x4B400000u;   // bits of 1.5 * 2^23
 
 // Code of a point the fast path does not cover: finite offsets go through the
 // signed second tier, NaN / infinite / huge ones through the 64-bit emulation.
@@ -626,18 +625,18 @@ __device__ __forceinline__ uint32_t slow_code(const MapView& m, float x, float y
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
 
-// Likelihood table entry in shared memory: the fixed-point value and whether
-// the code is a slot (a hit); one 16-byte read per lookup gives both.
-struct __align__(16) LutEntry {
+// Likelihood table entry in shared memory: the fixed-point value of a code.
+// Entries 8 bytes apart spread a warp's random reads over 16 bank pairs (a
+// 16-byte entry with the hit flag beside it left 8 and cost more shared-memory
+// wavefronts than the hit compare saves).
+struct __align__(8) LutEntry {
     long long v;
-    uint32_t hit;
-    uint32_t pad;
 };
-constexpr int kLut16Bytes = kNumCodes * 16;
+constexpr int kLutTableBytes = ((kNumCodes * 8 + 15) / 16) * 16;
 
 // Branch-free fast path of one lookup, from the packed pipeline's outputs: the
 // offsets' float bits (x, y) and value (z), upb = kMagic + brick index and
-// slb = kMagic15 + sub-voxel offset.  Returns the gathered code: the slot's, or
+// slb = bits(1.5 * 2^23) + sub-voxel offset.  Returns the gathered code: the slot's, or
 // a sentinel's -- kCodeMiss (fast, but the brick is outside the grid or not
 // allocated), kCodeLater (the exact slow tiers decide: offset outside
 // [0, mmax + 1) on x or y, outside (-1, mmax + 1) on z; `slow` is set) or
@@ -820,7 +819,7 @@ __device__ __noinline__ Partial drain(const MapView* m, const LutEntry* lut, con
         const float4 e = ring[(head + (uint32_t)lane) & (kRing - 1)];
         const uint32_t code = slow_code(*m, e.x, e.y, e.z);
         r.acc = lut[code].v;
-        r.hits = lut[code].hit;
+        r.hits = code <= (uint32_t)kCodeInit ? 1u : 0u;
         if (dbg_row) dbg_row[perm[__float_as_int(e.w)]] = code | kDbgSlow;
     }
     __syncwarp();
@@ -923,7 +922,7 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
             }
             const LutEntry e0 = lut[k0], e1 = lut[k1];
             acc += e0.v + e1.v;
-            hits += e0.hit + e1.hit;
+            hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
         };
         for (int blk = 0; blk < nfull; ++blk) step(blk, false);
         if (nfull < nblk) step(nfull, true);
@@ -942,15 +941,13 @@ __device__ __forceinline__ void tiled_item(const EvalParams& p, const MapView& m
     }
 }
 
-// Shared memory of the tiled kernels: the 16-byte likelihood table, the brick
-// bitmap (compact layout), then the staged pass and the deferral rings.
-__device__ __forceinline__ void fill_lut16(LutEntry* lut, const long long* lut_fx)
+// Shared memory of the tiled kernels: the likelihood table, the brick bitmap
+// (compact layout), then the staged pass and the deferral rings.
+__device__ __forceinline__ void fill_lut(LutEntry* lut, const long long* lut_fx)
 {
     for (int c = threadIdx.x; c < kNumCodes; c += blockDim.x) {
         LutEntry e;
         e.v = lut_fx[c];
-        e.hit = c <= kCodeInit ? 1u : 0u;
-        e.pad = 0u;
         lut[c] = e;
     }
 }
@@ -968,10 +965,10 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParam
     const int npairs = ((n + 63) >> 6) * 32;
     if (threadIdx.x == 0) s_map = m;
     const uint32_t occ_bytes = LAY == kLayBitmap ? m.occ_bytes : 0u;
-    unsigned char* occ = smem + kLut16Bytes;
+    unsigned char* occ = smem + kLutTableBytes;
     float4* sxy = reinterpret_cast<float4*>(occ + occ_bytes);
     float2* spz = reinterpret_cast<float2*>(sxy + npairs);
-    fill_lut16(lut, p.lut_fx);
+    fill_lut(lut, p.lut_fx);
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1038,10 +1035,10 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_subsample_kernel(SubPar
     const MapView& m = p.m;
     LutEntry* lut = reinterpret_cast<LutEntry*>(smem);
     const uint32_t occ_bytes = DENSE ? m.occ_bytes : 0u;
-    unsigned char* occ = smem + kLut16Bytes;
+    unsigned char* occ = smem + kLutTableBytes;
     float4* rings = reinterpret_cast<float4*>(occ + occ_bytes);
     if (threadIdx.x == 0) s_map = m;
-    fill_lut16(lut, p.lut_fx);
+    fill_lut(lut, p.lut_fx);
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     bool staged = true;
@@ -1102,7 +1099,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_subsample_kernel(SubPar
             }
             const LutEntry e0 = lut[k0], e1 = lut[k1];
             acc += e0.v + e1.v;
-            hits += e0.hit + e1.hit;
+            hits += (k0 <= (uint32_t)kCodeInit ? 1u : 0u) + (k1 <= (uint32_t)kCodeInit ? 1u : 0u);
         }
         if (tail != head) {
             const Partial d = drain(&s_map, lut, ring, head, (int)(tail - head), lane, nullptr, nullptr);
@@ -1156,7 +1153,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
     __shared__ uint32_t s_next;
     __shared__ int s_segi;
     LutEntry* lut = reinterpret_cast<LutEntry*>(smem);
-    unsigned char* occ = smem + kLut16Bytes;
+    unsigned char* occ = smem + kLutTableBytes;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
@@ -1193,7 +1190,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) eval_batch_kernel(const Batc
             sxy = reinterpret_cast<float4*>(occ + occ_bytes);
             spz = reinterpret_cast<float2*>(sxy + npairs);
             ring = reinterpret_cast<float4*>(spz + npairs) + warp * kRing;
-            fill_lut16(lut, p.lut_fx);
+            fill_lut(lut, p.lut_fx);
             if (threadIdx.x == 0) {
                 mbar_expect_tx(&bar, (uint32_t)npairs * 24u + occ_bytes);
                 bulk_g2s(sxy, p.pxy + p.n0 / 2, (uint32_t)npairs * 16u, &bar);
@@ -1689,6 +1686,53 @@ constexpr int kChainThreads = 512;
 // shared memory.  Negative or non-finite weights set *ws.serial: only the
 // literal loop reproduces them.  With s monotone, the draws each particle emits
 // then follow from the draw segments in parallel (resample_assign_sums_kernel).
+// One weight in units u = 2^(b-52) of the running sum's binade [2^b, 2^(b+1)),
+// from the float's bits alone (integer shifts, no FP64 operation -- the block
+// walks a million weights on one SM): q = floor(w / u), whether the remainder is
+// exactly half a unit (a tie) or above it, and whether w >= 2^(b+1).
+struct FloatSplit {
+    unsigned long long q;
+    bool tie, above, big;
+};
+
+__device__ __forceinline__ FloatSplit split_weight(float w, int b)
+{
+    FloatSplit o{0ull, false, false, false};
+    const uint32_t bits = __float_as_uint(w);
+    int ex = (int)((bits >> 23) & 0xffu);
+    unsigned long long man = bits & 0x7fffffu;
+    if (man == 0ull && ex == 0) return o;   // +0
+    if (ex) man |= 0x800000ull;
+    else ex = 1;                            // subnormal: man * 2^-149
+    // w = man * 2^(ex - 150); big: w >= 2^(b+1)
+    if (man >= 0x800000ull) {
+        o.big = ex - 127 >= b + 1;
+    } else {
+        const int k = b + 1 + 149;          // man >= 2^k
+        o.big = k <= 0 ? true : (k >= 23 ? false : man >= (1ull << k));
+    }
+    if (o.big) return o;
+    const int sh = ex - 150 + 52 - b;       // w / u = man * 2^sh
+    if (sh >= 0) {
+        o.q = man << sh;                    // below 2^53: w < 2^(b+1)
+    } else {
+        const int n = -sh;
+        if (n >= 64) return o;              // far below half a unit
+        o.q = n >= 32 ? 0ull : man >> n;
+        const unsigned long long rem = n >= 32 ? man : man & ((1ull << n) - 1ull);
+        const unsigned long long half = 1ull << (n - 1);
+        o.tie = rem == half;
+        o.above = rem > half;
+    }
+    return o;
+}
+
+// V * 2^(b-52) for V in [2^52, 2^53): the double's bits directly.
+__device__ __forceinline__ double binade_value(unsigned long long V, int b)
+{
+    return __longlong_as_double((long long)(((unsigned long long)(b + 1023) << 52) | (V - (1ull << 52))));
+}
+
 constexpr int kSumsThreads = 1024;
 constexpr int kSumsItems = 4;
 constexpr int kSumsChunk = kSumsThreads * kSumsItems;
@@ -1750,7 +1794,7 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
                 continue;
             }
             const int b = (int)((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;   // s in [2^b, 2^(b+1))
-            const double u = pow2(b - 52), uinv = pow2(52 - b), top = pow2(b + 1);
+            const double uinv = pow2(52 - b);
             const unsigned long long P0 = (unsigned long long)(s * uinv);   // in [2^52, 2^53)
             const unsigned long long LIM = 1ull << 53;
             unsigned long long q[kSumsItems], r[kSumsItems];
@@ -1759,17 +1803,18 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
             for (int j = 0; j < kSumsItems; ++j) {
                 const int i = pos + kSumsItems * tid + j;
                 valid[j] = i < t;
-                const double wd = valid[j] ? (double)sw[i] : 0.0;
-                big[j] = valid[j] && wd >= top;
                 q[j] = 0;
                 r[j] = 0;
                 tie[j] = false;
-                if (valid[j] && !big[j]) {
-                    const double tt = wd * uinv;   // exact scaling
-                    q[j] = (unsigned long long)tt;
-                    const double f = tt - (double)q[j];
-                    tie[j] = f == 0.5;
-                    r[j] = q[j] + (f > 0.5 ? 1ull : 0ull);
+                big[j] = false;
+                if (valid[j]) {
+                    const FloatSplit x = split_weight(sw[i], b);
+                    big[j] = x.big;
+                    if (!x.big) {
+                        q[j] = x.q;
+                        tie[j] = x.tie;
+                        r[j] = x.q + (x.above ? 1ull : 0ull);
+                    }
                 }
                 agg = parity_combine(agg, tie[j] ? ParityPrefix{1u, 0u} : ParityPrefix{0u, (uint32_t)(r[j] & 1)});
             }
@@ -1818,10 +1863,10 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
             }
             __syncthreads();
             const int e = s_e;
-            for (int j = 0; j < kSumsItems; ++j) {
+            for (int j = 0; j < kSumsItems; ++j) {   // below e every sum stays in the binade
                 const int i = pos + kSumsItems * tid + j;
-                if (i < e) ws.sums[c0 + i] = (double)(P0 + incl[j]) * u;
-                if (i == e - 1) s_prev = (double)(P0 + incl[j]) * u;
+                if (i < e) ws.sums[c0 + i] = binade_value(P0 + incl[j], b);
+                if (i == e - 1) s_prev = binade_value(P0 + incl[j], b);
             }
             __syncthreads();
             if (tid == 0) {
@@ -2233,7 +2278,7 @@ TiledKernel pick_tiled(int lay, bool two, bool dbg, bool min0)
 
 size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
 {
-    return (size_t)kLut16Bytes + (dense ? (size_t)m.occ_bytes : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
+    return (size_t)kLutTableBytes + (dense ? (size_t)m.occ_bytes : 0) + (size_t)(32 * ((n + 63) / 64)) * 24 +
            sizeof(float4) * kRing * kTiledWarps;
 }
 
@@ -2343,7 +2388,7 @@ int launch_eval_subsample(const MapView& m, float a_hit, int P, int N, int K, un
     const bool dense = m.occ_bytes != 0, two = m.sub_fast == 1;
     auto k = dense ? (two ? pick_sub_2<true, true>(m.min0 != 0) : pick_sub_2<true, false>(m.min0 != 0))
                    : (two ? pick_sub_2<false, true>(m.min0 != 0) : pick_sub_2<false, false>(m.min0 != 0));
-    const size_t smem = (size_t)kLut16Bytes + (dense ? (size_t)m.occ_bytes : 0) + sizeof(float4) * kRing * kTiledWarps;
+    const size_t smem = (size_t)kLutTableBytes + (dense ? (size_t)m.occ_bytes : 0) + sizeof(float4) * kRing * kTiledWarps;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int blocks = sm_count;
     const int need = (P + kTiledWarps - 1) / kTiledWarps;
