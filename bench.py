@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--filters", type=int, default=64, help="filters of the batch workload")
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--points", type=int, default=None)
-    ap.add_argument("--layout", default="compact", choices=["compact", "brick"])
+    ap.add_argument("--layout", default="compact", choices=["compact", "grid", "brick"])
     ap.add_argument("--kernel", default="fast", choices=["fast", "generic"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -938,7 +938,8 @@ def main():
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
-    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=(args.layout == "compact"))
+    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=(args.layout == "compact"),
+                     grid=(args.layout == "grid"))
     info = dmap.info()
     model = N.Model(0.9, 0.1, 0.0, 100.0)
     tf = np.ascontiguousarray(wl.tf, np.float32)

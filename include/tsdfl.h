@@ -107,6 +107,15 @@ int tsdfl_ctx_workspace_bytes(const tsdfl_ctx* ctx, size_t* eval_bytes, size_t* 
  * empty).  The tiled kernel then reads the rank from this L2-resident table
  * instead of the brick table. */
 #define TSDFL_MAP_HASH 8u
+/* TSDFL_MAP_GRID: also store the codes of every brick of the bounding box in
+ * brick order (unallocated bricks as misses; each brick of the lowest layer
+ * behind a copy of what getIndex reads below its first slot, the tail of the
+ * previous allocated brick), so the tiled kernel finds a slot from the brick
+ * index alone, with no rank lookup.  Costs (bricks of the bounding box + bricks
+ * of one layer) x sub_dim^3 x 2 bytes beside the code array.  Skipped under the
+ * same conditions as the compact layout, or when the array would pass 2^31
+ * codes. */
+#define TSDFL_MAP_GRID 16u
 int tsdfl_map_create(tsdfl_ctx* ctx, const tsdfl_map_coef* coef, const int32_t* grid_occ, const float* data,
                      float sigma, uint32_t flags, tsdfl_map** out);
 /* Same map from 16-bit slot codes (code c < 600: likelihood of |tsdf| = c mm;
@@ -120,7 +129,7 @@ typedef struct tsdfl_map_info {
     uint64_t device_bytes;     /* all device memory the map holds */
     int32_t storage;           /* 0 = 16-bit codes, 1 = float, 2 = half (TSDFL_MAP_F16) */
     int32_t dense;             /* brick rank index: 0 = brick table only, 1 = bitmap (compact layout),
-                                  2 = sparse brick hash */
+                                  2 = sparse brick hash, 3 = none needed (TSDFL_MAP_GRID) */
     int32_t fast_index;        /* division-free slot indexing verified for this resolution */
     int32_t reserved;
 } tsdfl_map_info;

@@ -1,7 +1,7 @@
 """GPU parity on the workloads the bench reports, against the oracle.
 
 - the 100x100x10 m building at 0.05 m with 100,000 Gaussian particles x 8,192
-  points (compact layout, two-term sub-voxel multiplier, points below the
+  points (compact and grid layouts, two-term sub-voxel multiplier, points below the
   map's floor, the compact-cloud scan order): a particle sample against the
   oracle, and all 100,000 particles across the two scoring kernels;
 - global localisation on the seed-3 building: 1,000,000 particles uniform over
@@ -51,41 +51,48 @@ def _codes_of(ref_idx, codes, data_size):
 
 
 def _check_against_oracle(ctx, wl, parts, serial_n):
-    """Compact layout: tiled kernel (debug and production instantiations) and
-    serial kernel against the oracle on the given particles."""
-    dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=True)
-    info = dmap.info()
-    assert info["dense"] == 1 and info["fast_index"] in (1, 2)
+    """Compact and grid layouts: tiled kernel (debug and production
+    instantiations) and serial kernel against the oracle on the given
+    particles."""
     om = O.OracleMap(O.coef_from(wl.coef), wl.grid_occ, wl.float_data())
     p_ref = parts.copy()
     ref = O.evaluate(om, p_ref, wl.points, wl.tf, want_idx=True)
     assert ref["rc"] == 0
     f64 = ref["sum64"]
-    ev = TSDFEvaluator(dmap)
-    p = parts.copy()
-    d = ev.evaluate_debug(p, wl.points, wl.tf, voxel_index=True)
-    assert np.array_equal(d["hits"], ref["hits"])
     want_codes = _codes_of(ref["voxel_index"], wl.codes, wl.coef.data_size)
-    assert np.array_equal(d["voxel_index"] & 0xFFFF, want_codes)
-    err_gpu = np.abs(d["raw"].astype(np.float64) - f64)
     err_ref = np.abs(ref["raw"].astype(np.float64) - f64)
-    assert np.all(err_gpu <= WEIGHT_RTOL * f64)
-    assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
-    w64 = f64 / f64.sum()
-    assert np.all(np.abs(p[:, 6].astype(np.float64) - w64) <= WEIGHT_RTOL * w64)
-    # the production (debug-free) instantiation gives the same sums
-    p2 = parts.copy()
-    d2 = ev.evaluate_debug(p2, wl.points, wl.tf)
-    assert np.array_equal(d2["raw"], d["raw"]) and np.array_equal(d2["hits"], d["hits"])
-    assert np.array_equal(p2[:, 6], p[:, 6])
-    # serial mode: the reference's point-order float sums, bit for bit
     sub = parts[:serial_n].copy()
     ref_s = O.evaluate(om, sub.copy(), wl.points, wl.tf)
-    ds = TSDFEvaluator(dmap, serial_sums=True).evaluate_debug(sub, wl.points, wl.tf)
-    assert np.array_equal(ds["raw"], ref_s["raw"])
-    assert np.array_equal(ds["hits"], ref_s["hits"])
-    return {"max_rel": float((err_gpu / f64).max()), "ref_max_rel": float((err_ref / f64).max()),
-            "hits": d["hits"]}
+    out = {}
+    for layout, want_dense in (("compact", 1), ("grid", 3)):
+        dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=layout == "compact",
+                         grid=layout == "grid")
+        info = dmap.info()
+        assert info["dense"] == want_dense and info["fast_index"] in (1, 2)
+        ev = TSDFEvaluator(dmap)
+        p = parts.copy()
+        d = ev.evaluate_debug(p, wl.points, wl.tf, voxel_index=True)
+        assert np.array_equal(d["hits"], ref["hits"])
+        assert np.array_equal(d["voxel_index"] & 0xFFFF, want_codes)
+        err_gpu = np.abs(d["raw"].astype(np.float64) - f64)
+        assert np.all(err_gpu <= WEIGHT_RTOL * f64)
+        assert np.all(err_gpu <= err_ref + WEIGHT_RTOL * f64)
+        w64 = f64 / f64.sum()
+        assert np.all(np.abs(p[:, 6].astype(np.float64) - w64) <= WEIGHT_RTOL * w64)
+        # the production (debug-free) instantiation gives the same sums
+        p2 = parts.copy()
+        d2 = ev.evaluate_debug(p2, wl.points, wl.tf)
+        assert np.array_equal(d2["raw"], d["raw"]) and np.array_equal(d2["hits"], d["hits"])
+        assert np.array_equal(p2[:, 6], p[:, 6])
+        # serial mode: the reference's point-order float sums, bit for bit
+        ds = TSDFEvaluator(dmap, serial_sums=True).evaluate_debug(sub.copy(), wl.points, wl.tf)
+        assert np.array_equal(ds["raw"], ref_s["raw"])
+        assert np.array_equal(ds["hits"], ref_s["hits"])
+        if out:
+            assert np.array_equal(d["raw"], out["raw"])   # both layouts: the same fixed-point sums
+        out = {"max_rel": float((err_gpu / f64).max()), "ref_max_rel": float((err_ref / f64).max()),
+               "hits": d["hits"], "raw": d["raw"]}
+    return out
 
 
 def test_building_sample_matches_oracle(ctx, building):
@@ -99,8 +106,8 @@ def test_building_sample_matches_oracle(ctx, building):
 
 
 def test_building_full_size_kernels_agree(ctx, building):
-    """All 100,000 x 8,192: the tiled kernel on the compact layout and the
-    generic kernel on the brick table give identical fixed-point sums (so
+    """All 100,000 x 8,192: the tiled kernel on the compact and grid layouts and
+    the generic kernel on the brick table give identical fixed-point sums (so
     identical weights and hit counts), and the weights sum to 1."""
     compact = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, dense=True)
     brick = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, dense=False)
@@ -109,6 +116,11 @@ def test_building_full_size_kernels_agree(ctx, building):
     b = TSDFEvaluator(brick, generic=True).evaluate_debug(pb, building.points, building.tf)
     assert np.array_equal(a["raw"], b["raw"]) and np.array_equal(a["hits"], b["hits"])
     assert abs(float(pb[:, 6].astype(np.float64).sum()) - 1.0) < 1e-4
+    del compact
+    grid = DeviceMap(ctx, building.coef, building.grid_occ, codes=building.codes, grid=True)
+    assert grid.info()["dense"] == 3
+    g = TSDFEvaluator(grid).evaluate_debug(building.particles.copy(), building.points, building.tf)
+    assert np.array_equal(g["raw"], b["raw"]) and np.array_equal(g["hits"], b["hits"])
 
 
 def test_global_sample_matches_oracle(ctx, global_wl):

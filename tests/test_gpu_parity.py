@@ -73,9 +73,10 @@ def _codes_of(ref_idx, codes, data_size):
 
 
 @pytest.mark.parametrize("kernel", ["fast", "generic"])
-@pytest.mark.parametrize("layout", ["brick", "dense"])
+@pytest.mark.parametrize("layout", ["brick", "dense", "grid"])
 def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
-    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"))
+    dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=(layout == "dense"),
+                     grid=(layout == "grid"))
     assert dmap.info()["fast_index"] in (1, 2)
     ev = TSDFEvaluator(dmap, generic=(kernel == "generic"))
     ref = _oracle_eval(room_oracle, room)
@@ -84,7 +85,7 @@ def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
     if kernel == "fast":
         d["voxel_index"] &= 0xFFFF   # drop the slow-path flag of the tiled kernel
     assert np.array_equal(d["hits"], ref["hits"])
-    if layout == "brick" and kernel == "generic":
+    if layout != "dense" and kernel == "generic":
         assert np.array_equal(d["voxel_index"], _as_u32_index(ref["voxel_index"], room.coef.data_size))
     else:  # these kernels report slot codes
         assert np.array_equal(d["voxel_index"], _codes_of(ref["voxel_index"], room.codes, room.coef.data_size))
@@ -102,7 +103,7 @@ def test_exact_mode_matches_oracle(ctx, room, room_oracle, layout, kernel):
 @pytest.mark.parametrize("voxel_mm", [50, 32])
 def test_fast_index_with_residual_correction(ctx, voxel_mm):
     """Resolutions whose sub-voxel multiplier can be one short (0.05 m, 0.032 m):
-    the tiled kernel's FMA residual test, both layouts, against the oracle's
+    the tiled kernel's FMA residual test, all three layouts, against the oracle's
     getIndex, including points in the (-1, 0) m band and outside the map."""
     wl = synth.make_workload(synth.ROOM, 13, voxel_mm, 1500, 96, 16, 512, edge=64, name="room@res")
     om = O.OracleMap(O.coef_from(wl.coef), wl.grid_occ, wl.float_data())
@@ -110,12 +111,39 @@ def test_fast_index_with_residual_correction(ctx, voxel_mm):
     pts = np.concatenate([wl.points, rng.uniform(-1.0, 0.3, size=(200, 3)).astype(np.float32),
                           rng.uniform(-30, 30, size=(200, 3)).astype(np.float32)])
     ref = _oracle_eval(om, wl, points=pts)
-    for dense in (False, True):
-        dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=dense)
+    for dense, grid in ((False, False), (True, False), (False, True)):
+        dmap = DeviceMap(ctx, wl.coef, wl.grid_occ, codes=wl.codes, dense=dense, grid=grid)
         assert dmap.info()["fast_index"] == 1
         d = TSDFEvaluator(dmap).evaluate_debug(wl.particles.copy(), pts, wl.tf, voxel_index=True)
         assert np.array_equal(d["hits"], ref["hits"])
         assert np.array_equal(d["voxel_index"] & 0xFFFF, _codes_of(ref["voxel_index"], wl.codes, wl.coef.data_size))
+        assert np.allclose(d["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
+
+
+def test_map_min_corner_off_origin(ctx, room):
+    """A map whose min corner is not the origin (the tiled kernel subtracts it
+    from every transformed point): the room's bricks moved to (-1.3, -0.7,
+    -0.45) m with the particles, all layouts against the oracle, including
+    points in the (-1, 0) m band below the moved floor."""
+    from tsdf_localization_gb300 import _native as N
+    shift = np.array([-1.3, -0.7, -0.45], np.float32)
+    coef = N.MapCoef.from_buffer_copy(bytes(room.coef))
+    coef.min_x, coef.min_y, coef.min_z = (float(v) for v in shift)
+    coef.max_x, coef.max_y, coef.max_z = (float(np.float32(getattr(room.coef, k)) + v)
+                                          for k, v in zip(("max_x", "max_y", "max_z"), shift))
+    om = O.OracleMap(O.coef_from(coef), room.grid_occ, room.float_data())
+    parts = room.particles.copy()
+    parts[:, :3] += shift
+    rng = np.random.default_rng(17)
+    pts = np.concatenate([room.points, rng.uniform(-1.0, 0.3, size=(300, 3)).astype(np.float32) + shift])
+    ref = O.evaluate(om, parts.copy(), pts, room.tf, want_idx=True)
+    want = _codes_of(ref["voxel_index"], room.codes, coef.data_size)
+    for dense, grid in ((False, False), (True, False), (False, True)):
+        dmap = DeviceMap(ctx, coef, room.grid_occ, codes=room.codes, dense=dense, grid=grid)
+        assert dmap.info()["fast_index"] in (1, 2)
+        d = TSDFEvaluator(dmap).evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)
+        assert np.array_equal(d["hits"], ref["hits"])
+        assert np.array_equal(d["voxel_index"] & 0xFFFF, want)
         assert np.allclose(d["raw"], ref["sum64"], rtol=WEIGHT_RTOL, atol=0)
 
 
@@ -170,8 +198,8 @@ def test_points_outside_map_and_negative_offsets(ctx, room, room_oracle):
     ]).astype(np.float32)
     parts = synth.particles_gaussian([0.3, 0.4, 0.2, 0, 0, 0], 0.6, 0.2, 64, 9)
     ref = _oracle_eval(room_oracle, room, particles=parts, points=pts)
-    for dense in (False, True):
-        dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=dense)
+    for dense, grid in ((False, False), (True, False), (False, True)):
+        dmap = DeviceMap(ctx, room.coef, room.grid_occ, codes=room.codes, dense=dense, grid=grid)
         for serial, generic in ((True, False), (False, False), (False, True)):
             ev = TSDFEvaluator(dmap, serial_sums=serial, generic=generic)
             d = ev.evaluate_debug(parts.copy(), pts, room.tf, voxel_index=True)

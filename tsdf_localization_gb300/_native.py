@@ -23,6 +23,7 @@ TSDFL_MAP_DENSE = 1
 TSDFL_MAP_FORCE_F32 = 2
 TSDFL_MAP_F16 = 4
 TSDFL_MAP_HASH = 8
+TSDFL_MAP_GRID = 16
 TSDFL_SUM_EXACT = 0
 TSDFL_SUM_SERIAL = 1
 TSDFL_EVAL_GENERIC = 4

@@ -97,6 +97,8 @@ struct tsdfl_map {
     uint32_t* occ = nullptr;      // compact layout (TSDFL_MAP_DENSE): brick bitmap and prefix counts
     uint32_t occ_bytes = 0;
     uint2* hash = nullptr;        // sparse brick hash (TSDFL_MAP_HASH, or DENSE with a bitmap too large)
+    uint16_t* grid = nullptr;     // grid layout (TSDFL_MAP_GRID): every brick of the bounding box
+    uint64_t grid_codes = 0;      // codes in grid before the sentinels
     uint32_t hash_slots = 0, hash_probes = 0;
     float* values = nullptr;      // kNumCodes likelihood values (device)
     float max_value = 0;
@@ -422,9 +424,43 @@ void fill_view(tsdfl_map* m)
     v.sent_later = v.sent_miss + 1u;
     v.sent_none = v.sent_miss + 2u;
     v.codes_b = (unsigned long long)(uintptr_t)m->codes - 2ull * kMag15;
+    v.grid_uxy1 = c.up_dim_2 ? (uint32_t)(c.up_dim_2 - 1) : 0u;
+    v.grid_b = 0;
+    v.gsent_miss = v.gsent_later = v.gsent_none = 0;
+    if (m->grid) {
+        v.grid_b = (unsigned long long)(uintptr_t)m->grid + 2ull * S3 - 2ull * kMag15;
+        v.gsent_miss = (uint32_t)(m->grid_codes - S3) + kMag15;
+        v.gsent_later = v.gsent_miss + 1u;
+        v.gsent_none = v.gsent_miss + 2u;
+    }
 }
 
 
+
+// Grid layout (TSDFL_MAP_GRID): the codes of every brick of the bounding box,
+// so the tiled kernel addresses a slot by the brick index alone.  A lookup
+// with a negative sub-voxel offset (oz in (-1, 0), the lowest layer only) reads
+// the skirt in front of its brick, which holds what the reference's index
+// reads there: the tail of the previous allocated brick.  Built under the
+// compact layout's conditions; the biased 32-bit index must stay below 2^32,
+// which the 2^31-code limit leaves room for.
+int build_grid(tsdfl_map* m, cudaStream_t s)
+{
+    const tsdfl_map_coef& c = m->coef;
+    const uint64_t S3 = c.sub_dim * c.sub_dim_2;
+    if (max_sub_index(c.resolution) >= c.sub_dim || !m->codes || m->codes_pre != S3 || c.grid_occ_size == 0 ||
+        c.grid_occ_size >= (1ull << 23))
+        return TSDFL_OK;
+    const uint64_t n = (c.grid_occ_size + c.up_dim_2) * S3;
+    if (n >= (1ull << 31)) return TSDFL_OK;
+    CUDA_TRY(cudaMalloc(&m->grid, sizeof(uint16_t) * (n + kSentinels)));
+    int rc = launch_grid_fill(m->codes, m->grid_occ, c.up_dim_2, S3, n, m->grid, s);
+    if (rc) return rc;
+    CUDA_TRY(write_sentinels(m->grid, n, s));
+    m->grid_codes = n;
+    m->bytes += sizeof(uint16_t) * (n + kSentinels);
+    return TSDFL_OK;
+}
 
 // Compact layout (TSDFL_MAP_DENSE): the code array itself, with the brick's
 // rank read from a bitmap of the brick grid staged in shared memory instead of
@@ -511,6 +547,10 @@ int finish_map(tsdfl_ctx* ctx, tsdfl_map* m, const int32_t* grid_occ, uint32_t f
         fill_view(m);
         return TSDFL_OK;
     }
+    if ((flags & TSDFL_MAP_GRID) && m->codes) {
+        int rc = build_grid(m, ctx->stream);
+        if (rc) return rc;
+    }
     if ((flags & TSDFL_MAP_HASH) && m->codes) {
         int rc = build_hash(m, grid_occ);
         if (rc) return rc;
@@ -537,6 +577,7 @@ void destroy_map(tsdfl_map* m)
     cudaFree(m->h16);
     cudaFree(m->occ);
     cudaFree(m->hash);
+    cudaFree(m->grid);
     cudaFree(m->values);
     delete m;
 }
@@ -595,8 +636,8 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     if (rc) return rc;
     rc = launch_particle_order(d_particles, (int)P, b, s);
     if (rc) return rc;
-    bool dense = map->occ != nullptr;
     const bool tiled = !serial && map->view.storage == 0 && map->view.tiled && !(flags & TSDFL_EVAL_GENERIC);
+    bool dense = map->occ != nullptr && !(tiled && map->grid);   // the grid layout needs no bitmap
     size_t pass = serial ? kSerialPassPoints : (size_t)kMaxPassPoints;
     if (tiled) {
         int tp = tiled_pass_points(map->view, dense);
@@ -917,7 +958,7 @@ int tsdfl_map_get_info(const tsdfl_map* m, tsdfl_map_info* info)
     info->bricks = m->bricks;
     info->device_bytes = m->bytes;
     info->storage = m->h16 ? 2 : (m->codes ? 0 : 1);
-    info->dense = m->occ ? 1 : (m->hash ? 2 : 0);
+    info->dense = m->grid ? 3 : (m->occ ? 1 : (m->hash ? 2 : 0));
     info->fast_index = m->view.tiled ? m->view.sub_fast : 0;
     info->reserved = 0;
     return TSDFL_OK;

@@ -644,8 +644,9 @@ constexpr int kLutTableBytes = ((kNumCodes * 8 + 15) / 16) * 16;
 // LAY: where the brick's rank comes from -- kLayBitmap: the shared-memory
 // bitmap `occ`; kLayHash: the sparse brick hash (allocated bricks only, for
 // maps whose bitmap does not fit shared memory); kLayTable: the brick table
-// grid_occ (the reference's own).
-constexpr int kLayTable = 0, kLayBitmap = 1, kLayHash = 2;
+// grid_occ (the reference's own); kLayGrid: no rank, the grid layout's codes
+// of every brick of the bounding box are addressed by the brick index.
+constexpr int kLayTable = 0, kLayBitmap = 1, kLayHash = 2, kLayGrid = 3;
 
 template <int LAY>
 __device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned char* occ, uint32_t ox_b,
@@ -678,6 +679,11 @@ __device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned c
         }
         ok = found;
         idx = rank * m.sub_dim_3 + slb;
+    } else if (LAY == kLayGrid) {
+        // every brick of the bounding box is stored: a miss is a miss code there
+        const uint32_t up = upb - kMagic;
+        ok = inside;
+        idx = (up + min(up, m.grid_uxy1)) * m.sub_dim_3 + slb;
     } else if (LAY == kLayBitmap) {
         // the masked offset stays inside the staged table whatever upb is
         const uint2 wb = *reinterpret_cast<const uint2*>(occ + ((upb >> 2) & m.occ_mask));
@@ -688,6 +694,10 @@ __device__ __forceinline__ uint32_t fast_code(const MapView& m, const unsigned c
         const int32_t base = __ldg(m.grid_occ + (inside ? upb - kMagic : 0u));
         ok = inside && base >= 0;
         idx = (uint32_t)base + slb;
+    }
+    if (LAY == kLayGrid) {
+        const uint32_t sent = valid ? (fast ? m.gsent_miss : m.gsent_later) : m.gsent_none;
+        return __ldg(reinterpret_cast<const uint16_t*>(m.grid_b + 2ull * (ok ? idx : sent)));
     }
     const uint32_t sent = valid ? (fast ? m.sent_miss : m.sent_later) : m.sent_none;
     return __ldg(reinterpret_cast<const uint16_t*>(m.codes_b + 2ull * (ok ? idx : sent)));
@@ -2177,6 +2187,23 @@ __global__ void halves_kernel(const uint16_t* codes, const float* values, const 
     }
 }
 
+// Grid layout: output brick j of the bounding box order with skirts -- for
+// j < 2 up_dim_2 brick j / 2 of the lowest layer (odd j) behind its skirt (even
+// j), beyond that brick j - up_dim_2 -- copied from the code array, whose
+// leading miss brick is what the skirt of the first allocated brick reads.
+__global__ void grid_fill_kernel(const uint16_t* codes, const int32_t* grid_occ, uint64_t uxy, uint64_t s3,
+                                 uint64_t n, uint16_t* grid)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t j = i / s3, t = i - j * s3;
+        const bool low = j < 2 * uxy;
+        const uint64_t up = low ? j >> 1 : j - uxy;
+        const bool skirt = low && (j & 1) == 0;
+        const int32_t base = grid_occ[up];
+        grid[i] = base < 0 ? (uint16_t)kCodeMiss : codes[(int64_t)base + (int64_t)t - (skirt ? (int64_t)s3 : 0)];
+    }
+}
+
 __global__ void codes_from_floats_kernel(const float* data, size_t n, const float* values, float init_value,
                                          uint16_t* codes, int32_t* fail)
 {
@@ -2271,9 +2298,12 @@ TiledKernel pick_tiled_1(bool two, bool dbg, bool min0)
 
 TiledKernel pick_tiled(int lay, bool two, bool dbg, bool min0)
 {
-    return lay == kLayBitmap ? pick_tiled_1<kLayBitmap>(two, dbg, min0)
-                             : (lay == kLayHash ? pick_tiled_1<kLayHash>(two, dbg, min0)
-                                                : pick_tiled_1<kLayTable>(two, dbg, min0));
+    switch (lay) {
+    case kLayBitmap: return pick_tiled_1<kLayBitmap>(two, dbg, min0);
+    case kLayHash: return pick_tiled_1<kLayHash>(two, dbg, min0);
+    case kLayGrid: return pick_tiled_1<kLayGrid>(two, dbg, min0);
+    default: return pick_tiled_1<kLayTable>(two, dbg, min0);
+    }
 }
 
 size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
@@ -2328,9 +2358,10 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
         // sub_fast 2: floor(s * sub_inv) is the sub-voxel index; 1: the two-term multiplier
         const bool two = m.sub_fast == 1, dbg = p.dbg != nullptr;
-        // the brick rank: from the shared-memory bitmap, else the sparse brick hash
-        // when the map has one, else the brick table
-        const int lay = dense ? kLayBitmap : (m.hash ? kLayHash : kLayTable);
+        // the slot: from the brick index alone on the grid layout; else the brick
+        // rank from the shared-memory bitmap, the sparse brick hash when the map
+        // has one, or the brick table
+        const int lay = m.grid_b ? kLayGrid : (dense ? kLayBitmap : (m.hash ? kLayHash : kLayTable));
         auto k = pick_tiled(lay, two, dbg, m.min0 != 0);
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
@@ -2590,6 +2621,13 @@ int launch_codes_from_floats(const float* data, size_t n, const float* code_valu
                              uint16_t* codes, int32_t* fail, cudaStream_t s)
 {
     if (n) codes_from_floats_kernel<<<1024, 256, 0, s>>>(data, n, code_values, init_value, codes, fail);
+    return check(cudaGetLastError());
+}
+
+int launch_grid_fill(const uint16_t* codes, const int32_t* grid_occ, uint64_t up_dim_2, uint64_t sub_dim_3,
+                     uint64_t n, uint16_t* grid, cudaStream_t s)
+{
+    if (n) grid_fill_kernel<<<4096, 256, 0, s>>>(codes, grid_occ, up_dim_2, sub_dim_3, n, grid);
     return check(cudaGetLastError());
 }
 

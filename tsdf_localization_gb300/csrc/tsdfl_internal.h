@@ -100,6 +100,19 @@ struct MapView {
     uint32_t upb_lim;              // kMagic + grid_occ_size
     uint32_t sent_miss, sent_later, sent_none;   // sentinels in the biased index
     unsigned long long codes_b;
+    // Grid layout (TSDFL_MAP_GRID): the codes of every brick of the bounding
+    // box in brick order, so no rank is needed.  Brick up starts at
+    // (up + min(up, up_dim_2 - 1) + 1) sub_dim^3: a brick of the lowest layer
+    // (up < up_dim_2) sits behind a skirt of sub_dim^3 codes holding what the
+    // reference reads at its negative sub-voxel offsets (the tail of the
+    // previous allocated brick, or misses), every other brick directly behind
+    // its predecessor.  Unallocated bricks and skirts hold kCodeMiss; the
+    // kSentinels codes follow the last brick.  Gathers address
+    // grid_b + 2 ((up + min(up, grid_uxy1)) sub_dim^3 + bits(...)),
+    // grid_b = grid + 2 (sub_dim^3 - kMagic15) (bytes); grid_b is 0 without it.
+    unsigned long long grid_b;
+    uint32_t grid_uxy1;            // up_dim_2 - 1
+    uint32_t gsent_miss, gsent_later, gsent_none;   // sentinels in the grid's biased index
 };
 
 constexpr int kSentinels = 4;
@@ -262,6 +275,10 @@ int launch_best_particle(const float* particles, size_t M, unsigned long long* k
                          cudaStream_t s);
 int launch_codes_from_floats(const float* data, size_t n, const float* code_values, float init_value,
                              uint16_t* codes, int32_t* fail, cudaStream_t s);
+// Grid layout (MapView::grid_b): n = (grid_occ_size + up_dim_2) sub_dim_3 codes
+// from the code array (with its leading miss brick) and the brick table.
+int launch_grid_fill(const uint16_t* codes, const int32_t* grid_occ, uint64_t up_dim_2, uint64_t sub_dim_3,
+                     uint64_t n, uint16_t* grid, cudaStream_t s);
 // Half-precision slot values (round to nearest): from codes through the
 // code -> value table, or from float slots when codes is null.
 int launch_halves(const uint16_t* codes, const float* code_values, const float* data, size_t n, uint16_t* h16,

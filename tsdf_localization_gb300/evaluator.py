@@ -68,17 +68,20 @@ class DeviceMap:
     f16=True stores half-precision likelihood values instead (TSDFL_MAP_F16,
     an accuracy variant); hash_index=True indexes the allocated bricks in a
     sparse hash (TSDFL_MAP_HASH), which dense=True also builds for maps whose
-    brick bitmap is too large for shared memory."""
+    brick bitmap is too large for shared memory.  grid=True also stores the
+    codes of every brick of the bounding box (TSDFL_MAP_GRID), which the tiled
+    kernel addresses by brick index with no rank lookup."""
 
     def __init__(self, ctx: Context, coef: N.MapCoef, grid_occ: np.ndarray, data: np.ndarray | None = None,
                  codes: np.ndarray | None = None, sigma: float = 0.1, dense: bool = False, force_f32: bool = False,
-                 f16: bool = False, hash_index: bool = False):
+                 f16: bool = False, hash_index: bool = False, grid: bool = False):
         self.ctx = ctx
         self.coef = coef
         lib = N.lib()
         go = np.ascontiguousarray(grid_occ, dtype=np.int32)
         flags = ((N.TSDFL_MAP_DENSE if dense else 0) | (N.TSDFL_MAP_FORCE_F32 if force_f32 else 0) |
-                 (N.TSDFL_MAP_F16 if f16 else 0) | (N.TSDFL_MAP_HASH if hash_index else 0))
+                 (N.TSDFL_MAP_F16 if f16 else 0) | (N.TSDFL_MAP_HASH if hash_index else 0) |
+                 (N.TSDFL_MAP_GRID if grid else 0))
         h = C.c_void_p()
         if codes is not None:
             cd = np.ascontiguousarray(codes, dtype=np.uint16)
