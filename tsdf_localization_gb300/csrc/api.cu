@@ -2597,10 +2597,10 @@ namespace {
 
 constexpr size_t kStaticResampleParticles = size_t(1) << 18;   // largest M the static scratch holds
 // Upper bound of resample_workspace_bytes(kStaticResampleParticles): the
-// fixed-point prefix sums (8 bytes a particle), two tile tables and the
-// segment table with headroom.  Checked against the launcher's own figure on
-// every call.
-constexpr size_t kStaticResampleBytes = 8 * (kStaticResampleParticles + 2 * (kStaticResampleParticles / 256 + 2)) +
+// fixed-point prefix sums (8 bytes a particle), three tile tables, the
+// segment table and the chunk table of the double sums, with headroom.
+// Checked against the launcher's own figure on every call.
+constexpr size_t kStaticResampleBytes = 8 * (kStaticResampleParticles + 3 * (kStaticResampleParticles / 256 + 2)) +
                                         64 * 1024;
 constexpr int kStaticMaxDevices = 64;
 

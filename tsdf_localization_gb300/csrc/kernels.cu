@@ -1444,6 +1444,22 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kMaxSegments = 1024;
+constexpr int kSumsThreads = 1024;
+constexpr int kSumsItems = 4;
+constexpr int kSumsChunk = kSumsThreads * kSumsItems;   // a whole number of scan tiles
+static_assert(kSumsChunk % kScanTile == 0, "chunks of the double sums are made of scan tiles");
+static_assert(kSumsThreads == 1024, "the double sums scan one aggregate per warp in one warp");
+constexpr int kNoBinade = 0x7fffffff;
+
+// One chunk of kSumsChunk weights in the fallback's double sums (below).
+struct SumsChunk {
+    unsigned long long R0;   // the chunk's increment in units 2^(b-52), for a start of even parity
+    unsigned long long P;    // the sum before the chunk in those units (par set)
+    int b;                   // binade of every serial sum the chunk touches, or kNoBinade
+    int delta;               // increment for an odd start minus R0 (+-1 at the first tie, else 0)
+    int ok;                  // no weight reaches 2^(b+1): R0 and delta hold
+    int par;                 // the chunk's sums are written by resample_chunk_write_kernel
+};
 
 struct Segment {
     double u_start;   // exact float value
@@ -1463,6 +1479,8 @@ struct ResampleWs {
     int* serial;            // 1 when only the literal loop reproduces it
     double* sums;           // M serial double prefix sums (aliases cdf; used when !exact_ok)
     const float* u0p;       // the draw in device memory (replaces u0 when set)
+    double* tile_dsum;      // tiles: double sum of each scan tile's weights (any order)
+    SumsChunk* chunks;      // ceil(M / kSumsChunk)
 };
 
 // Weight as an exact multiple of 2^-52 (its value in those units), or -1 when
@@ -1487,24 +1505,36 @@ __device__ __forceinline__ long long weight_fx52(float w)
 }
 
 // Tile-local inclusive scan of the fixed-point weights (exact integers).
+// Also the tile's double sum of the weights for the fallback below, and
+// *ws.serial for a negative or non-finite weight (only the literal loop
+// reproduces those).
 __global__ void resample_scan_kernel(const float* w, int stride, int M, ResampleWs ws)
 {
     __shared__ long long warp_tot[kScanThreads / 32];
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
+    __shared__ double warp_d[kScanThreads / 32];
+    __shared__ int bad, wild;
+    if (threadIdx.x == 0) bad = wild = 0;
     __syncthreads();
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     long long v[kScanItems];
     long long run = 0;
+    double dsum = 0.0;
     for (int k = 0; k < kScanItems; ++k) {
         int i = base + k;
         long long f = 0;
         if (i < M) {
-            f = weight_fx52(w[(size_t)i * stride]);
+            const float x = w[(size_t)i * stride];
+            f = weight_fx52(x);
             if (f < 0) { bad = 1; f = 0; }
+            if (!(x >= 0.0f) || !(x < INFINITY)) wild = 1;
+            else dsum += (double)x;
         }
         run += f;
         v[k] = run;
+    }
+    {
+        const double d = warp_sum_d(dsum);
+        if ((threadIdx.x & 31) == 0) warp_d[threadIdx.x >> 5] = d;
     }
     // inclusive scan of per-thread totals across the block
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1523,8 +1553,14 @@ __global__ void resample_scan_kernel(const float* w, int stride, int M, Resample
         if (i < M) ws.cdf[i] = excl + v[k];
     }
     if (threadIdx.x == kScanThreads - 1) ws.tile_sums[blockIdx.x] = excl + run;
+    if (threadIdx.x == 0) {
+        double d = 0.0;
+        for (int k = 0; k < kScanThreads / 32; ++k) d += warp_d[k];
+        ws.tile_dsum[blockIdx.x] = d;
+    }
     __syncthreads();
     if (threadIdx.x == 0 && bad) atomicExch(ws.exact_ok, 0);
+    if (threadIdx.x == 0 && wild) atomicExch(ws.serial, 1);
 }
 
 // 2^k for -1022 <= k <= 1023, exactly.
@@ -1692,14 +1728,25 @@ constexpr int kChainThreads = 512;
 // binade's start) XOR the low bits of the increments since: a segmented XOR
 // scan.  Where the exact sum leaves the binade (or a weight reaches 2^(b+1))
 // one ordinary double addition is made and the scan restarts; that happens
-// about once per binade.  One block walks the weights in chunks staged in
-// shared memory.  Negative or non-finite weights set *ws.serial: only the
-// literal loop reproduces them.  With s monotone, the draws each particle emits
-// then follow from the draw segments in parallel (resample_assign_sums_kernel).
+// about once per binade.
+// The weights are cut into chunks of kSumsChunk.  Approximate double sums of
+// the scan tiles tell which chunks keep every serial sum they touch inside one
+// binade with a margin far above the sums' rounding (all but a few: a chunk
+// per binade the running sum crosses).  Such a chunk's increment depends on
+// the sum before it only through that sum's parity, at the chunk's first tie,
+// so it is formed for both parities by one block per chunk
+// (resample_chunk_transfer_kernel); one block then chains the chunks' starts,
+// walking the others weight by weight (resample_sums_kernel), after which one
+// block per chunk writes the chained chunks' sums (resample_chunk_write_kernel).
+// The chain verifies each transfer it applies (the start in the chunk's binade,
+// the end below the binade's top), so the margin only decides speed, never the
+// result.  Negative or non-finite weights set *ws.serial: only the literal loop
+// reproduces them.  With s monotone, the draws each particle emits then follow
+// from the draw segments in parallel (resample_assign_sums_kernel).
 // One weight in units u = 2^(b-52) of the running sum's binade [2^b, 2^(b+1)),
-// from the float's bits alone (integer shifts, no FP64 operation -- the block
-// walks a million weights on one SM): q = floor(w / u), whether the remainder is
-// exactly half a unit (a tie) or above it, and whether w >= 2^(b+1).
+// from the float's bits alone (integer shifts, no FP64 operation): q =
+// floor(w / u), whether the remainder is exactly half a unit (a tie) or above
+// it, and whether w >= 2^(b+1).
 struct FloatSplit {
     unsigned long long q;
     bool tie, above, big;
@@ -1743,9 +1790,15 @@ __device__ __forceinline__ double binade_value(unsigned long long V, int b)
     return __longlong_as_double((long long)(((unsigned long long)(b + 1023) << 52) | (V - (1ull << 52))));
 }
 
-constexpr int kSumsThreads = 1024;
-constexpr int kSumsItems = 4;
-constexpr int kSumsChunk = kSumsThreads * kSumsItems;
+// The binade of a positive normal double, and its value in units 2^(b-52).
+__device__ __forceinline__ int binade_of(double s)
+{
+    return (int)((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;
+}
+__device__ __forceinline__ unsigned long long binade_units(double s)
+{
+    return ((unsigned long long)__double_as_longlong(s) & ((1ull << 52) - 1ull)) | (1ull << 52);
+}
 
 struct ParityPrefix {   // segmented XOR: the parity state after a run of items
     uint32_t reset;     // a tie occurred in the run: the parity restarted at 0 there
@@ -1757,6 +1810,181 @@ __device__ __forceinline__ ParityPrefix parity_combine(ParityPrefix a, ParityPre
     return b.reset ? b : ParityPrefix{a.reset, a.x ^ b.x};
 }
 
+// The increments of the staged weights sw[pos, t) in units 2^(b-52) for a
+// running sum of parity p0 before item pos.  Thread k of the block's
+// kSumsThreads takes items pos + kSumsItems k + j; incl[j] is the sum of the
+// increments up to and including its item j.  Increments of weights that
+// reach 2^(b+1) are 0 (big set); increments are clamped at 2^53 (where the
+// sum leaves the binade anyway).  The block's threads all call it; red_par and
+// red_sum are read after the call returns, so the caller synchronises before
+// calling again.
+struct BinadeRun {
+    unsigned long long q[kSumsItems], r[kSumsItems], incl[kSumsItems];
+    bool tie[kSumsItems], big[kSumsItems], valid[kSumsItems];
+};
+
+__device__ __forceinline__ void binade_increments(const float* sw, int pos, int t, int b, uint32_t p0, BinadeRun& x,
+                                                  ParityPrefix* red_par, unsigned long long* red_sum)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long LIM = 1ull << 53;
+    ParityPrefix agg{0u, 0u};
+    for (int j = 0; j < kSumsItems; ++j) {
+        const int i = pos + kSumsItems * tid + j;
+        x.valid[j] = i < t;
+        x.q[j] = 0;
+        x.r[j] = 0;
+        x.tie[j] = false;
+        x.big[j] = false;
+        if (x.valid[j]) {
+            const FloatSplit f = split_weight(sw[i], b);
+            x.big[j] = f.big;
+            if (!f.big) {
+                x.q[j] = f.q;
+                x.tie[j] = f.tie;
+                x.r[j] = f.q + (f.above ? 1ull : 0ull);
+            }
+        }
+        agg = parity_combine(agg, x.tie[j] ? ParityPrefix{1u, 0u} : ParityPrefix{0u, (uint32_t)(x.r[j] & 1)});
+    }
+    // exclusive segmented-XOR scan of the threads' aggregates
+    ParityPrefix px = agg;
+    for (int o = 1; o < 32; o <<= 1) {
+        ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, o), __shfl_up_sync(0xffffffffu, px.x, o)};
+        if (lane >= o) px = parity_combine(y, px);
+    }
+    if (lane == 31) red_par[warp] = px;
+    __syncthreads();
+    // the warps' aggregates before this warp: every warp scans the 32 of them
+    ParityPrefix wx = red_par[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+        ParityPrefix y{__shfl_up_sync(0xffffffffu, wx.reset, o), __shfl_up_sync(0xffffffffu, wx.x, o)};
+        if (lane >= o) wx = parity_combine(y, wx);
+    }
+    ParityPrefix before{__shfl_sync(0xffffffffu, wx.reset, (warp + 31) & 31),
+                        __shfl_sync(0xffffffffu, wx.x, (warp + 31) & 31)};
+    if (warp == 0) before = ParityPrefix{0u, 0u};
+    {
+        ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, 1), __shfl_up_sync(0xffffffffu, px.x, 1)};
+        if (lane > 0) before = parity_combine(before, y);
+    }
+    uint32_t par = before.reset ? before.x : (p0 & 1u) ^ before.x;   // parity before the first item
+    unsigned long long tsum = 0;
+    for (int j = 0; j < kSumsItems; ++j) {
+        if (x.tie[j]) {   // round half to even: +1 when the sum before plus q is odd
+            x.r[j] = x.q[j] + ((par ^ (uint32_t)(x.q[j] & 1)) & 1u);
+            par = 0u;
+        } else {
+            par ^= (uint32_t)(x.r[j] & 1);
+        }
+        if (x.r[j] > LIM) x.r[j] = LIM;
+        tsum += x.r[j];
+    }
+    // exclusive sum scan of the threads' increments
+    unsigned long long xs = tsum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, xs, o);
+        if (lane >= o) xs += y;
+    }
+    if (lane == 31) red_sum[warp] = xs;
+    __syncthreads();
+    unsigned long long ws_ = red_sum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, ws_, o);
+        if (lane >= o) ws_ += y;
+    }
+    const unsigned long long wbefore = __shfl_sync(0xffffffffu, ws_, (warp + 31) & 31);
+    unsigned long long run = xs - tsum + (warp ? wbefore : 0ull);
+    for (int j = 0; j < kSumsItems; ++j) {
+        run += x.r[j];
+        x.incl[j] = run;
+    }
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* red)
+{
+    v = warp_sum_d(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    __syncthreads();
+    return t;
+}
+
+// Stages chunk c's weights in shared memory; returns its length.
+__device__ __forceinline__ int stage_chunk(const float* __restrict__ w, int stride, int M, int c, float* sw)
+{
+    const int c0 = c * kSumsChunk, t = min(kSumsChunk, M - c0);
+    for (int i = threadIdx.x; i < t; i += blockDim.x) sw[i] = w[(size_t)(c0 + i) * stride];
+    return t;
+}
+
+// One block per chunk: the chunk's binade (the serial sums' bounds from the
+// tiles' double sums, widened by far more than their rounding), and for a
+// chunk inside one binade its increment R0 from an even start and the change
+// delta for an odd one.
+__global__ void __launch_bounds__(kSumsThreads) resample_chunk_transfer_kernel(const float* __restrict__ w,
+                                                                               int stride, int M, ResampleWs ws)
+{
+    __shared__ float sw[kSumsChunk];
+    __shared__ unsigned long long red_sum[kSumsThreads / 32];
+    __shared__ ParityPrefix red_par[kSumsThreads / 32];
+    __shared__ double red_d[kSumsThreads / 32];
+    __shared__ int s_b, s_first, s_big;
+    if (*ws.exact_ok || *ws.serial) return;
+    const int c = blockIdx.x, tid = threadIdx.x;
+    constexpr int kTilesPerChunk = kSumsChunk / kScanTile;
+    const int tiles = (M + kScanTile - 1) / kScanTile;
+    const int t0 = c * kTilesPerChunk, t1 = min(t0 + kTilesPerChunk, tiles);
+    double a = 0.0, e = 0.0;
+    for (int i = tid; i < t0; i += kSumsThreads) a += ws.tile_dsum[i];
+    for (int i = t0 + tid; i < t1; i += kSumsThreads) e += ws.tile_dsum[i];
+    a = block_sum_d(a, red_d);
+    e = block_sum_d(e, red_d);
+    if (tid == 0) {
+        // |serial - approximate| <= (M + tiles + 2 kScanTile) 2^-53 relative: widen by 4x that
+        const double eps = ((double)M + (double)tiles + 2.0 * kScanTile) * 0x1p-51;
+        const double lo = a * (1.0 - eps), hi = (a + e) * (1.0 + eps);
+        int b = kNoBinade;
+        if (a > 0.0 && lo > 0.0 && binade_of(lo) == binade_of(hi)) b = binade_of(lo);
+        s_b = b;
+        s_first = kSumsChunk;
+        s_big = 0;
+        SumsChunk& k = ws.chunks[c];
+        k.b = b;
+        k.ok = 0;
+        k.par = 0;
+        k.delta = 0;
+        k.R0 = 0;
+        k.P = 0;
+    }
+    __syncthreads();
+    const int b = s_b;
+    if (b == kNoBinade) return;
+    const int t = stage_chunk(w, stride, M, c, sw);
+    __syncthreads();
+    BinadeRun x;
+    binade_increments(sw, 0, t, b, 0u, x, red_par, red_sum);
+    bool big = false;
+    for (int j = 0; j < kSumsItems; ++j) {
+        big |= x.big[j];
+        if (x.tie[j]) atomicMin(&s_first, kSumsItems * tid + j);
+    }
+    if (big) s_big = 1;
+    __syncthreads();
+    SumsChunk& k = ws.chunks[c];
+    for (int j = 0; j < kSumsItems; ++j)   // r(odd start) - r(even start) at the first tie
+        if (kSumsItems * tid + j == s_first) k.delta = x.r[j] == x.q[j] ? 1 : -1;
+    if (tid == kSumsThreads - 1) {
+        k.R0 = x.incl[kSumsItems - 1];
+        k.ok = s_big ? 0 : 1;
+    }
+}
+
+// The chain: one block walks the chunks in order, applying the transfers of
+// chunks inside one binade (thread 0, checked) and forming the others' sums
+// weight by weight.
 __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
                                                                      ResampleWs ws)
 {
@@ -1764,23 +1992,40 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
     __shared__ unsigned long long red_sum[kSumsThreads / 32];
     __shared__ ParityPrefix red_par[kSumsThreads / 32];
     __shared__ double s_s, s_prev;
-    __shared__ int s_pos, s_e;
-    if (*ws.exact_ok) return;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_s = 0.0;
-    for (int c0 = 0; c0 < M; c0 += kSumsChunk) {
-        const int t = min(kSumsChunk, M - c0);
-        bool bad = false;
-        for (int i = tid; i < t; i += kSumsThreads) {
-            const float x = w[(size_t)(c0 + i) * stride];
-            bad |= !(x >= 0.0f) || !(x < INFINITY);
-            sw[i] = x;
+    __shared__ int s_pos, s_e, s_c;
+    if (*ws.exact_ok || *ws.serial) return;
+    const int tid = threadIdx.x;
+    const int chunks = (M + kSumsChunk - 1) / kSumsChunk;
+    const unsigned long long LIM = 1ull << 53;
+    if (tid == 0) {
+        s_s = 0.0;
+        s_c = 0;
+    }
+    __syncthreads();
+    for (;;) {
+        if (tid == 0) {   // chunks inside one binade: only their starts
+            int c = s_c;
+            double sum = s_s;
+            for (; c < chunks; ++c) {
+                SumsChunk& k = ws.chunks[c];
+                if (k.b == kNoBinade || !k.ok || !(sum > 0.0) || binade_of(sum) != k.b) break;
+                const unsigned long long P = binade_units(sum);
+                const unsigned long long E = P + k.R0 + ((P & 1ull) ? (unsigned long long)(long long)k.delta : 0ull);
+                if (E >= LIM) break;
+                k.P = P;
+                k.par = 1;
+                sum = binade_value(E, k.b);
+            }
+            s_c = c;
+            s_s = sum;
         }
+        __syncthreads();
+        const int c = s_c;
+        if (c >= chunks) break;
+        const int c0 = c * kSumsChunk;
+        const int t = stage_chunk(w, stride, M, c, sw);
         if (tid == 0) s_pos = 0;
-        if (__syncthreads_or(bad ? 1 : 0)) {
-            if (tid == 0) *ws.serial = 1;
-            return;
-        }
+        __syncthreads();
         for (int guard = 0; guard <= kSumsChunk; ++guard) {   // one pass per event: at most t + 1
             const int pos = s_pos;
             if (pos >= t) break;
@@ -1803,80 +2048,21 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
                 __syncthreads();
                 continue;
             }
-            const int b = (int)((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;   // s in [2^b, 2^(b+1))
-            const double uinv = pow2(52 - b);
-            const unsigned long long P0 = (unsigned long long)(s * uinv);   // in [2^52, 2^53)
-            const unsigned long long LIM = 1ull << 53;
-            unsigned long long q[kSumsItems], r[kSumsItems];
-            bool tie[kSumsItems], big[kSumsItems], valid[kSumsItems];
-            ParityPrefix agg{0u, 0u};
+            const int b = binade_of(s);   // s in [2^b, 2^(b+1))
+            const unsigned long long P0 = binade_units(s);
+            BinadeRun x;
+            binade_increments(sw, pos, t, b, (uint32_t)(P0 & 1ull), x, red_par, red_sum);
             for (int j = 0; j < kSumsItems; ++j) {
                 const int i = pos + kSumsItems * tid + j;
-                valid[j] = i < t;
-                q[j] = 0;
-                r[j] = 0;
-                tie[j] = false;
-                big[j] = false;
-                if (valid[j]) {
-                    const FloatSplit x = split_weight(sw[i], b);
-                    big[j] = x.big;
-                    if (!x.big) {
-                        q[j] = x.q;
-                        tie[j] = x.tie;
-                        r[j] = x.q + (x.above ? 1ull : 0ull);
-                    }
-                }
-                agg = parity_combine(agg, tie[j] ? ParityPrefix{1u, 0u} : ParityPrefix{0u, (uint32_t)(r[j] & 1)});
-            }
-            // exclusive segmented-XOR scan of the threads' aggregates
-            ParityPrefix px = agg;
-            for (int o = 1; o < 32; o <<= 1) {
-                ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, o), __shfl_up_sync(0xffffffffu, px.x, o)};
-                if (lane >= o) px = parity_combine(y, px);
-            }
-            if (lane == 31) red_par[warp] = px;
-            __syncthreads();
-            ParityPrefix before{0u, 0u};
-            for (int k = 0; k < warp; ++k) before = parity_combine(before, red_par[k]);
-            {
-                ParityPrefix y{__shfl_up_sync(0xffffffffu, px.reset, 1), __shfl_up_sync(0xffffffffu, px.x, 1)};
-                if (lane > 0) before = parity_combine(before, y);
-            }
-            uint32_t par = before.reset ? before.x : (uint32_t)(P0 & 1) ^ before.x;   // parity before the first item
-            unsigned long long tsum = 0;
-            for (int j = 0; j < kSumsItems; ++j) {
-                if (tie[j]) {   // round half to even: +1 when the sum before plus q is odd
-                    r[j] = q[j] + ((par ^ (uint32_t)(q[j] & 1)) & 1u);
-                    par = 0u;
-                } else {
-                    par ^= (uint32_t)(r[j] & 1);
-                }
-                if (r[j] > LIM) r[j] = LIM;   // the sum leaves the binade there anyway
-                tsum += r[j];
-            }
-            // exclusive sum scan of the threads' increments
-            unsigned long long xs = tsum;
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned long long y = __shfl_up_sync(0xffffffffu, xs, o);
-                if (lane >= o) xs += y;
-            }
-            if (lane == 31) red_sum[warp] = xs;
-            __syncthreads();
-            unsigned long long run = xs - tsum;
-            for (int k = 0; k < warp; ++k) run += red_sum[k];
-            unsigned long long incl[kSumsItems];
-            for (int j = 0; j < kSumsItems; ++j) {
-                const int i = pos + kSumsItems * tid + j;
-                if (valid[j] && (big[j] || P0 + run + q[j] >= LIM)) atomicMin(&s_e, i);   // leaves the binade
-                run += r[j];
-                incl[j] = run;
+                const unsigned long long before = x.incl[j] - x.r[j];
+                if (x.valid[j] && (x.big[j] || P0 + before + x.q[j] >= LIM)) atomicMin(&s_e, i);   // leaves the binade
             }
             __syncthreads();
             const int e = s_e;
             for (int j = 0; j < kSumsItems; ++j) {   // below e every sum stays in the binade
                 const int i = pos + kSumsItems * tid + j;
-                if (i < e) ws.sums[c0 + i] = binade_value(P0 + incl[j], b);
-                if (i == e - 1) s_prev = binade_value(P0 + incl[j], b);
+                if (i < e) ws.sums[c0 + i] = binade_value(P0 + x.incl[j], b);
+                if (i == e - 1) s_prev = binade_value(P0 + x.incl[j], b);
             }
             __syncthreads();
             if (tid == 0) {
@@ -1893,7 +2079,30 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
             }
             __syncthreads();
         }
+        if (tid == 0) s_c = c + 1;
         __syncthreads();
+    }
+}
+
+// One block per chained chunk: its sums from the start the chain gave it.
+__global__ void __launch_bounds__(kSumsThreads) resample_chunk_write_kernel(const float* __restrict__ w, int stride,
+                                                                            int M, ResampleWs ws)
+{
+    __shared__ float sw[kSumsChunk];
+    __shared__ unsigned long long red_sum[kSumsThreads / 32];
+    __shared__ ParityPrefix red_par[kSumsThreads / 32];
+    if (*ws.exact_ok || *ws.serial) return;
+    const int c = blockIdx.x;
+    const SumsChunk k = ws.chunks[c];
+    if (!k.par) return;
+    const int t = stage_chunk(w, stride, M, c, sw);
+    __syncthreads();
+    BinadeRun x;
+    binade_increments(sw, 0, t, k.b, (uint32_t)(k.P & 1ull), x, red_par, red_sum);
+    const int c0 = c * kSumsChunk;
+    for (int j = 0; j < kSumsItems; ++j) {
+        const int i = kSumsItems * threadIdx.x + j;
+        if (x.valid[j]) ws.sums[c0 + i] = binade_value(k.P + x.incl[j], k.b);
     }
 }
 
@@ -2542,7 +2751,9 @@ int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s)
 size_t resample_workspace_bytes(size_t M)
 {
     size_t tiles = (M + kScanTile - 1) / kScanTile + 1;
-    return 8 * (M + 2 * tiles) + sizeof(Segment) * kMaxSegments + 64;   // flags: 16 + 16 + 8 + 4 + 4 <= 64
+    size_t chunks = (M + kSumsChunk - 1) / kSumsChunk + 1;
+    // flags: 16 + 16 + 8 + 4 + 4 <= 64
+    return 8 * (M + 3 * tiles) + sizeof(Segment) * kMaxSegments + 64 + sizeof(SumsChunk) * chunks;
 }
 
 int launch_resample_impl(const float* particles, const float* w, int stride, size_t M, float u0, float* out,
@@ -2560,9 +2771,12 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     ws.exact_ok = reinterpret_cast<int*>(p); p += 16;
     ws.total = reinterpret_cast<long long*>(p); p += 8;
     int* err = reinterpret_cast<int*>(p); p += 4;
-    ws.serial = reinterpret_cast<int*>(p);
+    ws.serial = reinterpret_cast<int*>(p); p += 4;
+    ws.tile_dsum = reinterpret_cast<double*>(p); p += 8 * (tiles + 1);
+    ws.chunks = reinterpret_cast<SumsChunk*>(p);
     ws.sums = reinterpret_cast<double*>(ws.cdf);
     ws.u0p = u0p;
+    const unsigned chunks = (unsigned)((M + kSumsChunk - 1) / kSumsChunk);
     // the literal loop reuses the prefix-sum array for counts and offsets
     uint32_t* cnt = reinterpret_cast<uint32_t*>(ws.cdf);
     uint32_t* off = cnt + M;
@@ -2574,7 +2788,9 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     resample_assign_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out, ws,
                                                   status);
     // exact fallbacks: serial double sums + parallel assignment, else the literal loop
+    resample_chunk_transfer_kernel<<<chunks ? chunks : 1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
     resample_sums_kernel<<<1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
+    resample_chunk_write_kernel<<<chunks ? chunks : 1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
     resample_segments_sums_kernel<<<1, 32, 0, s>>>((int)M, u0, ws);
     resample_assign_sums_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out,
                                                        ws, status);
@@ -2582,7 +2798,7 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
                                                          u0p);
     resample_scatter_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, cnt, off, total, err, ws.serial, out,
                                                    idx_out, (long long)cap, count_out, status);
-    g_launches += 9;
+    g_launches += 11;
     return check(cudaGetLastError());
 }
 
