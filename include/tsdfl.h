@@ -215,6 +215,12 @@ int tsdfl_evaluate_device(tsdfl_ctx* ctx, const tsdfl_map* map, const tsdfl_mode
  * always M.  Bit-exact with the reference for the same weights and u0. */
 int tsdfl_resample_systematic(tsdfl_ctx* ctx, const float* weights, size_t M, float u0, uint32_t* idx_out,
                               size_t cap, size_t* count_out);
+/* The same on the particle cloud itself (M x 7 floats, the weight last), as
+ * SystematicResampler::resample reads the weights from its particles
+ * (novel_resampling.h:41-72): no weight array to gather on the host, the
+ * cloud goes over in one copy. */
+int tsdfl_resample_systematic_particles(tsdfl_ctx* ctx, const float* particles, size_t M, float u0,
+                                        uint32_t* idx_out, size_t cap, size_t* count_out);
 /* Device form: gathers the resampled particles (P x 7 floats) from d_particles
  * into d_particles_out (capacity cap particles) and writes the count to
  * *d_count (device).  Weights are the last field of every particle. */

@@ -35,6 +35,7 @@
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -201,14 +202,31 @@ void resample_systematic(Context& ctx, std::vector<ParticleT>& particles, float 
 {
     const size_t M = particles.size();
     if (M == 0) return;
-    std::vector<float> w(M);
-    for (size_t i = 0; i < M; ++i) w[i] = particles[i].second;
     std::vector<uint32_t> idx(2 * M + 16);
     size_t count = 0;
-    check(tsdfl_resample_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+    // the reference's Particle (pose floats, then the weight) is the M x 7
+    // float cloud the particles form reads: pass it as it lies
+    const char* p0 = reinterpret_cast<const char*>(particles.data());
+    const bool cloud = std::is_same<decltype(particles[0].second), float>::value &&
+                       sizeof(ParticleT) == 7 * sizeof(float) &&
+                       reinterpret_cast<const char*>(&particles[0].second) - p0 == 6 * sizeof(float);
+    std::vector<float> w;
+    auto call = [&]() {
+        if (cloud) {
+            check(tsdfl_resample_systematic_particles(ctx.get(), reinterpret_cast<const float*>(p0), M, u0,
+                                                      idx.data(), idx.size(), &count));
+        } else {
+            if (w.empty()) {
+                w.resize(M);
+                for (size_t i = 0; i < M; ++i) w[i] = particles[i].second;
+            }
+            check(tsdfl_resample_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+        }
+    };
+    call();
     if (count > idx.size()) {   // more draws than the first guess held: ask again with room for all
         idx.resize(count);
-        check(tsdfl_resample_systematic(ctx.get(), w.data(), M, u0, idx.data(), idx.size(), &count));
+        call();
     }
     std::vector<ParticleT> out;
     out.reserve(count);

@@ -40,4 +40,5 @@ def test_calls_without_a_device_fail_cleanly():
     assert lib.tsdfl_evaluate(None, None, None, None, 0, None, 0, None, 0, None) == N.TSDFL_ERR_INVALID_ARG
     assert lib.tsdfl_last_error()
     assert lib.tsdfl_resample_systematic(None, None, 0, 0.0, None, 0, None) == N.TSDFL_ERR_INVALID_ARG
+    assert lib.tsdfl_resample_systematic_particles(None, None, 0, 0.0, None, 0, None) == N.TSDFL_ERR_INVALID_ARG
     assert lib.tsdfl_version()

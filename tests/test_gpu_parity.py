@@ -317,12 +317,15 @@ def test_resample_bit_exact(ctx, m, kind):
     rng = np.random.default_rng(m * 31 + len(kind))
     w = _random_weights(rng, m, kind)
     rs = SystematicResampler(ctx, seed=m)
+    parts = rng.random((m, 7)).astype(np.float32)   # the same weights inside a particle cloud
+    parts[:, 6] = w
     for u0 in (0.0, float(np.float32(0.5 / m)), float(np.nextafter(np.float32(1.0 / m), np.float32(0))),
                rs.draw(m)):
         got = rs.resample_indices(w, u0)
         exp = O.resample_systematic(w, u0)
         assert got.shape == exp.shape
         assert np.array_equal(got, exp)
+        assert np.array_equal(rs.resample_particle_indices(parts, u0), exp)
 
 
 @pytest.mark.parametrize("m", [1, 2, 7, 1000, 65537, 250000])

@@ -116,6 +116,7 @@ SIGNATURES = [
     ("tsdfl_evaluate_debug", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, C.c_uint32, P, C.POINTER(EvalDebug)]),
     ("tsdfl_evaluate_device", I, [P, P, C.POINTER(Model), P, SZ, P, SZ, P, C.c_uint32, P]),
     ("tsdfl_resample_systematic", I, [P, P, SZ, F, P, SZ, C.POINTER(SZ)]),
+    ("tsdfl_resample_systematic_particles", I, [P, P, SZ, F, P, SZ, C.POINTER(SZ)]),
     ("tsdfl_resample_systematic_device", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_systematic_static", I, [P, P, SZ, F, P, SZ, P]),
     ("tsdfl_resample_residual_systematic", I, [P, P, SZ, F, P, SZ, P]),

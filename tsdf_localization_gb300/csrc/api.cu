@@ -1120,40 +1120,57 @@ uint32_t tsdfl_subsample_index(uint64_t seed, uint64_t particle, uint32_t N, uin
     return sub_point(sub_particle_state(seed, particle), N, K, k);
 }
 
-int tsdfl_resample_systematic(tsdfl_ctx* c, const float* weights, size_t M, float u0, uint32_t* idx_out, size_t cap,
-                              size_t* count_out)
+// Host forms of the systematic resampler: the M weights are every stride-th
+// float of src starting at src[offset] (stride 1: a weight array; stride 7,
+// offset 6: the particle cloud).  The whole source is copied in one transfer.
+int resample_systematic_host(tsdfl_ctx* c, const char* fn, const float* src, size_t stride, size_t offset, size_t M,
+                             float u0, uint32_t* idx_out, size_t cap, size_t* count_out)
 {
-    if (!c || (M && !weights) || (cap && !idx_out) || !count_out) {
-        set_error("tsdfl_resample_systematic: invalid argument");
+    if (!c || (M && !src) || (cap && !idx_out) || !count_out) {
+        set_error("%s: invalid argument", fn);
         return TSDFL_ERR_INVALID_ARG;
     }
     *count_out = 0;
     if (M == 0) return TSDFL_OK;
     if (M >= (1ull << 24)) {
-        set_error("tsdfl_resample_systematic: at most 2^24-1 particles");
+        set_error("%s: at most 2^24-1 particles", fn);
         return TSDFL_ERR_UNSUPPORTED;
     }
     int rc = set_device(c->device);
     if (rc) return rc;
     rc = ensure_resample_ws(c, M);
     if (rc) return rc;
-    size_t w_b = align_up(sizeof(float) * M, 256);
+    size_t w_b = align_up(sizeof(float) * stride * M, 256);
     size_t i_b = align_up(sizeof(uint32_t) * (cap ? cap : 1), 256);
     rc = ensure_io(c, w_b + i_b + 256);
     if (rc) return rc;
     char* io = static_cast<char*>(c->io);
-    float* d_w = reinterpret_cast<float*>(io);
+    float* d_src = reinterpret_cast<float*>(io);
     uint32_t* d_idx = reinterpret_cast<uint32_t*>(io + w_b);
     uint32_t* d_cnt = reinterpret_cast<uint32_t*>(io + w_b + i_b);
     cudaStream_t s = c->stream;
-    CUDA_TRY(cudaMemcpyAsync(d_w, weights, sizeof(float) * M, cudaMemcpyHostToDevice, s));
-    rc = launch_resample_impl(nullptr, d_w, 1, M, u0, nullptr, d_idx, cap, d_cnt, c->rs_ws, c->status, s);
+    CUDA_TRY(cudaMemcpyAsync(d_src, src, sizeof(float) * stride * M, cudaMemcpyHostToDevice, s));
+    rc = launch_resample_impl(nullptr, d_src + offset, (int)stride, M, u0, nullptr, d_idx, cap, d_cnt, c->rs_ws,
+                              c->status, s);
     if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(c->h_count, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     if (cap) CUDA_TRY(cudaMemcpyAsync(idx_out, d_idx, sizeof(uint32_t) * cap, cudaMemcpyDeviceToHost, s));
     int st = tsdfl_ctx_sync(c);
     *count_out = c->h_count[0];
     return st;
+}
+
+int tsdfl_resample_systematic(tsdfl_ctx* c, const float* weights, size_t M, float u0, uint32_t* idx_out, size_t cap,
+                              size_t* count_out)
+{
+    return resample_systematic_host(c, "tsdfl_resample_systematic", weights, 1, 0, M, u0, idx_out, cap, count_out);
+}
+
+int tsdfl_resample_systematic_particles(tsdfl_ctx* c, const float* particles, size_t M, float u0, uint32_t* idx_out,
+                                        size_t cap, size_t* count_out)
+{
+    return resample_systematic_host(c, "tsdfl_resample_systematic_particles", particles, 7, 6, M, u0, idx_out, cap,
+                                    count_out);
 }
 
 int tsdfl_resample_systematic_device(tsdfl_ctx* c, const float* d_particles, size_t M, float u0,

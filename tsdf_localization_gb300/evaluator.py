@@ -296,8 +296,25 @@ class SystematicResampler:
                                                   C.byref(cnt)))
         return out[: cnt.value]
 
+    def resample_particle_indices(self, particles: np.ndarray, u0: float | None = None,
+                                  cap: int | None = None) -> np.ndarray:
+        """The same indices from the (M, 7) particle array itself (its last
+        column holds the weights; tsdfl_resample_systematic_particles)."""
+        p = np.ascontiguousarray(particles, dtype=np.float32)
+        if p.ndim != 2 or p.shape[1] != 7:
+            raise ValueError("particles must be an (M, 7) array")
+        m = p.shape[0]
+        if u0 is None:
+            u0 = self.draw(m)
+        cap = cap if cap is not None else 2 * m + 16
+        out = np.zeros(max(cap, 1), np.uint32)
+        cnt = C.c_size_t()
+        N.check(N.lib().tsdfl_resample_systematic_particles(self.ctx.handle, _ptr(p), m, np.float32(u0), _ptr(out),
+                                                            cap, C.byref(cnt)))
+        return out[: cnt.value]
+
     def resample(self, particles: np.ndarray, u0: float | None = None) -> np.ndarray:
-        idx = self.resample_indices(particles[:, 6], u0)
+        idx = self.resample_particle_indices(particles, u0)
         return particles[idx].copy()
 
 
