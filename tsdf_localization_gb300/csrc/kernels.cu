@@ -104,6 +104,19 @@ __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v)
     return v;
 }
 
+// First statement of every kernel of the update and resampling chain, which
+// the launchers start with programmatic dependent launch: the grid may be
+// scheduled while the previous kernel in the stream is still running, so it
+// waits here until that kernel has completed and its writes are visible, then
+// lets its own successor be scheduled once all of its CTAs have started (the
+// successor waits in turn).  Both instructions do nothing for a grid launched
+// without the attribute.
+__device__ __forceinline__ void chain_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Element-wise min (x, y) / max (z, w) over the warp; NaN entries are ignored.
 __device__ __forceinline__ float4 warp_extent(float4 e)
 {
@@ -184,6 +197,7 @@ __device__ __forceinline__ int spatial_bin(float x, float y, float z, bool wide)
 // the pose kernel (it reads the cloud's extent).
 __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParams p, EvalBuffers b)
 {
+    chain_enter();
     __shared__ int warp_counts[32];
     __shared__ int bins[kSortBins];
     __shared__ uint16_t sbin[kBinCache];
@@ -318,6 +332,7 @@ __device__ __forceinline__ uint32_t morton2(uint32_t x, uint32_t y)
 
 __global__ void particle_cells_kernel(const float* particles, int P, EvalBuffers b)
 {
+    chain_enter();
     if (b.counts[2] == 0) return;   // a compact cloud keeps its order
     const float4 e = b.cloud_ext[0];
     const float n = (float)(1 << kCellBits);
@@ -335,6 +350,7 @@ __global__ void particle_cells_kernel(const float* particles, int P, EvalBuffers
 
 __global__ void __launch_bounds__(kCellScanThreads) particle_scan_kernel(EvalBuffers b)
 {
+    chain_enter();
     if (b.counts[2] == 0) return;
     __shared__ int warp_sums[kCellScanThreads / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -372,6 +388,7 @@ __global__ void __launch_bounds__(kCellScanThreads) particle_scan_kernel(EvalBuf
 
 __global__ void particle_scatter_kernel(int P, EvalBuffers b)
 {
+    chain_enter();
     if (b.counts[2] == 0) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
         const int q = atomicAdd(&b.phist[b.pkeys[i]], 1);
@@ -387,10 +404,22 @@ struct Tf16 {
 // rounded to float (the correctly rounded sin/cos), products and sums in the
 // reference's order without contraction.
 // Also: the x / y extent of the block's particles (min x, min y, max x, max y)
-// into extent[block], for the scan staging's choice of point order.
-__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6, float4* extent)
+// into extent[block], for the scan staging's choice of point order; and zeros
+// in the scoring sums and the cell histogram, so no memset breaks the chain of
+// kernels.
+__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6, float4* extent,
+                            long long* sum_fx, uint32_t* hits, int32_t* phist)
 {
+    chain_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // the tiled kernel's per-particle sums and the particle order's cell
+    // histogram start at zero (the kernels of this update run after this one)
+    if (i < P) {
+        sum_fx[i] = 0;
+        hits[i] = 0;
+    }
+    if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k < kCellBins; k += blockDim.x) phist[k] = 0;
     {
         __shared__ float4 s_ext[32];
         const float inf = __int_as_float(0x7f800000);
@@ -965,6 +994,7 @@ __device__ __forceinline__ void fill_lut(LutEntry* lut, const long long* lut_fx)
 template <int LAY, bool TWO, bool DBG, bool MIN0>
 __global__ void __launch_bounds__(kTiledThreads, 1) eval_tiled_kernel(TiledParams tp)
 {
+    chain_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint64_t bar;
     __shared__ MapView s_map;   // the map view the slow tiers read
@@ -1290,6 +1320,7 @@ struct NormParams {
 // weighted pose sums of tsdf_evaluator.cpp:198-217.
 __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* sum_f64)
 {
+    chain_enter();
     double acc[kNormSums];
     for (int k = 0; k < kNormSums; ++k) acc[k] = 0.0;
     const double n_in_all = (double)b.counts[0];
@@ -1338,6 +1369,7 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
 // reduction tree (so the result does not depend on timing).
 __global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, float* pose_out)
 {
+    chain_enter();
     __shared__ double red[kNormSums][kNormBlocks / 32];
     __shared__ double s[kNormSums];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -1375,6 +1407,7 @@ __global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, 
 // the sum was degenerate so the caller's particles stay untouched.
 __global__ void normalize_kernel(int P, EvalBuffers b, float* particles_out)
 {
+    chain_enter();
     if (*b.status == TSDFL_ERR_DEGENERATE) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
@@ -1510,6 +1543,7 @@ __device__ __forceinline__ long long weight_fx52(float w)
 // reproduces those).
 __global__ void resample_scan_kernel(const float* w, int stride, int M, ResampleWs ws)
 {
+    chain_enter();
     __shared__ long long warp_tot[kScanThreads / 32];
     __shared__ double warp_d[kScanThreads / 32];
     __shared__ int bad, wild;
@@ -1638,6 +1672,7 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
 // prefix offsets, lane 0 walks the binades (scalings by powers of two only).
 __global__ void resample_segments_kernel(int M, float u0, int tiles, ResampleWs ws)
 {
+    chain_enter();
     if (ws.u0p) u0 = *ws.u0p;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x >= 32 || blockIdx.x != 0) return;
@@ -1688,6 +1723,7 @@ __device__ long long count_below(const Segment* seg, int ns, double s)
 __global__ void resample_assign_kernel(const float* particles, int M, float* out, uint32_t* idx_out, long long cap,
                                        uint32_t* count_out, ResampleWs ws, int32_t* status)
 {
+    chain_enter();
     __shared__ Segment seg[kMaxSegments];
     if (!*ws.exact_ok) return;
     const int ns = *ws.nseg;
@@ -1927,6 +1963,7 @@ __device__ __forceinline__ int stage_chunk(const float* __restrict__ w, int stri
 __global__ void __launch_bounds__(kSumsThreads) resample_chunk_transfer_kernel(const float* __restrict__ w,
                                                                                int stride, int M, ResampleWs ws)
 {
+    chain_enter();
     __shared__ float sw[kSumsChunk];
     __shared__ unsigned long long red_sum[kSumsThreads / 32];
     __shared__ ParityPrefix red_par[kSumsThreads / 32];
@@ -1988,6 +2025,7 @@ __global__ void __launch_bounds__(kSumsThreads) resample_chunk_transfer_kernel(c
 __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
                                                                      ResampleWs ws)
 {
+    chain_enter();
     __shared__ float sw[kSumsChunk];
     __shared__ unsigned long long red_sum[kSumsThreads / 32];
     __shared__ ParityPrefix red_par[kSumsThreads / 32];
@@ -2088,6 +2126,7 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
 __global__ void __launch_bounds__(kSumsThreads) resample_chunk_write_kernel(const float* __restrict__ w, int stride,
                                                                             int M, ResampleWs ws)
 {
+    chain_enter();
     __shared__ float sw[kSumsChunk];
     __shared__ unsigned long long red_sum[kSumsThreads / 32];
     __shared__ ParityPrefix red_par[kSumsThreads / 32];
@@ -2109,6 +2148,7 @@ __global__ void __launch_bounds__(kSumsThreads) resample_chunk_write_kernel(cons
 // Draw segments up to the serial sum's total, for the fallback above.
 __global__ void resample_segments_sums_kernel(int M, float u0, ResampleWs ws)
 {
+    chain_enter();
     if (ws.u0p) u0 = *ws.u0p;
     if (threadIdx.x != 0 || blockIdx.x != 0 || *ws.exact_ok || *ws.serial) return;
     if (!build_segments(M, u0, ws.sums[M - 1], ws)) *ws.serial = 1;
@@ -2118,6 +2158,7 @@ __global__ void resample_segments_sums_kernel(int M, float u0, ResampleWs ws)
 __global__ void resample_assign_sums_kernel(const float* particles, int M, float* out, uint32_t* idx_out,
                                             long long cap, uint32_t* count_out, ResampleWs ws, int32_t* status)
 {
+    chain_enter();
     __shared__ Segment seg[kMaxSegments];
     if (*ws.exact_ok || *ws.serial) return;
     const int ns = *ws.nseg;
@@ -2143,6 +2184,7 @@ __global__ void resample_assign_sums_kernel(const float* particles, int M, float
 
 __global__ void set_flags_kernel(int* exact_ok, int* serial, int* err)
 {
+    chain_enter();
     *exact_ok = 1;
     *serial = 0;
     *err = 0;
@@ -2162,6 +2204,7 @@ __global__ void __launch_bounds__(kChainThreads) systematic_chain_kernel(const f
                                                                          unsigned long long* total, int* err,
                                                                          const int* run, const float* u0p)
 {
+    chain_enter();
     if (u0p) u0 = *u0p;
     __shared__ float sw[kChainTile];
     __shared__ uint32_t sc[kChainTile], so[kChainTile];
@@ -2325,6 +2368,7 @@ __global__ void resample_scatter_kernel(const float* particles, int M, const uin
                                         float* out, uint32_t* idx_out, long long cap, uint32_t* count_out,
                                         int32_t* status)
 {
+    chain_enter();
     if (run && !*run) return;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (*err) {
@@ -2381,6 +2425,7 @@ __global__ void best_index_kernel(const unsigned long long* key, uint32_t* index
 // Carries a per-evaluation error into the context's sticky status word.
 __global__ void fold_status_kernel(int32_t* ev, int32_t* sticky)
 {
+    chain_enter();
     int v = *ev;
     if (v && *sticky == 0) *sticky = v;
 }
@@ -2451,12 +2496,32 @@ int check(cudaError_t e)
 
 // ------------------------------------------------------------------ launchers
 
+// Launches a kernel of the update / resampling chain with programmatic
+// dependent launch (the kernel opens with chain_enter()), so its launch
+// overlaps the end of the previous kernel instead of following it.
+template <typename... Params, typename... Args>
+void launch_chained(void (*kernel)(Params...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                    Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
 {
     PointParams p{points, N, npad, 32 * ((N + 63) / 64), b.extent, P > 0 ? (P + 255) / 256 : 0,
                   max_range_sq, c_in, c_out, code_values, shift};
-    prepare_points_kernel<<<1, kPrepThreads, 0, s>>>(p, b);
+    launch_chained(prepare_points_kernel, 1, kPrepThreads, 0, s, p, b);
     g_launches += 1;
     return check(cudaGetLastError());
 }
@@ -2464,11 +2529,11 @@ int launch_prepare(const float* points, int N, int npad, int P, float max_range_
 int launch_particle_order(const float* particles, int P, const EvalBuffers& b, cudaStream_t s)
 {
     if (P <= 0) return TSDFL_OK;
-    cudaMemsetAsync(b.phist, 0, sizeof(int32_t) * kCellBins, s);
-    const int blocks = std::min((P + 255) / 256, 4096);
-    particle_cells_kernel<<<blocks, 256, 0, s>>>(particles, P, b);
-    particle_scan_kernel<<<1, kCellScanThreads, 0, s>>>(b);
-    particle_scatter_kernel<<<blocks, 256, 0, s>>>(P, b);
+    // the cell histogram was cleared by pose_kernel
+    const unsigned blocks = (unsigned)std::min((P + 255) / 256, 4096);
+    launch_chained(particle_cells_kernel, blocks, 256, 0, s, particles, P, b);
+    launch_chained(particle_scan_kernel, 1, kCellScanThreads, 0, s, b);
+    launch_chained(particle_scatter_kernel, blocks, 256, 0, s, P, b);
     g_launches += 3;
     return check(cudaGetLastError());
 }
@@ -2478,7 +2543,8 @@ int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_
     Tf16 t;
     for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
     if (P > 0) {
-        pose_kernel<<<(P + 255) / 256, 256, 0, s>>>(b.particles, P, t, b.pose12, b.trig6, b.extent);
+        launch_chained(pose_kernel, (unsigned)((P + 255) / 256), 256, 0, s, b.particles, P, t, b.pose12, b.trig6,
+                       b.extent, b.sum_fx, b.hits, b.phist);
         g_launches += 1;
     }
     return check(cudaGetLastError());
@@ -2574,14 +2640,11 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         auto k = pick_tiled(lay, two, dbg, m.min0 != 0);
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
-        if (first) {
-            cudaMemsetAsync(b.sum_fx, 0, sizeof(long long) * (size_t)P, s);
-            cudaMemsetAsync(b.hits, 0, sizeof(uint32_t) * (size_t)P, s);
-        }
+        // pose_kernel cleared sum_fx and hits before the first pass
         int blocks = sm_count;
         int need = (tp.items + kTiledWarps - 1) / kTiledWarps;
         if (need < blocks) blocks = need > 0 ? need : 1;
-        k<<<blocks, kTiledThreads, tsmem, s>>>(tp);
+        launch_chained(k, (unsigned)blocks, kTiledThreads, tsmem, s, tp);
         g_launches += 1;
     } else {
         auto k = dense && !f32 ? eval_exact_kernel<true, 0>
@@ -2724,8 +2787,8 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
                 const uint32_t* nin, bool log_domain)
 {
     NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points, nin};
-    norm_partial_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(q, b, sum_f64);
-    norm_final_kernel<<<1, kNormBlocks, 0, s>>>(b, pose_out);
+    launch_chained(norm_partial_kernel, kNormBlocks, kNormThreads, 0, s, q, b, sum_f64);
+    launch_chained(norm_final_kernel, 1, kNormBlocks, 0, s, b, pose_out);
     g_launches += 2;
     if (P > 0 && log_domain) {
         cudaMemsetAsync(b.counts + 1, 0, sizeof(int32_t), s);
@@ -2735,7 +2798,7 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
         normalize_log_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
         g_launches += 4;
     } else if (P > 0) {
-        normalize_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
+        launch_chained(normalize_kernel, (unsigned)((P + 255) / 256), 256, 0, s, P, b, particles_out);
         g_launches += 1;
     }
     return check(cudaGetLastError());
@@ -2743,7 +2806,7 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
 
 int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s)
 {
-    fold_status_kernel<<<1, 1, 0, s>>>(eval_status, sticky);
+    launch_chained(fold_status_kernel, 1, 1, 0, s, eval_status, sticky);
     g_launches += 1;
     return check(cudaGetLastError());
 }
@@ -2782,22 +2845,23 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
     uint32_t* off = cnt + M;
     unsigned long long* total = reinterpret_cast<unsigned long long*>(ws.total);
     const unsigned blocks = (unsigned)((M + 255) / 256);
-    set_flags_kernel<<<1, 1, 0, s>>>(ws.exact_ok, ws.serial, err);
-    resample_scan_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(w, stride, (int)M, ws);
-    resample_segments_kernel<<<1, 32, 0, s>>>((int)M, u0, (int)tiles, ws);
-    resample_assign_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out, ws,
-                                                  status);
+    launch_chained(set_flags_kernel, 1, 1, 0, s, ws.exact_ok, ws.serial, err);
+    launch_chained(resample_scan_kernel, (unsigned)tiles, kScanThreads, 0, s, w, stride, (int)M, ws);
+    launch_chained(resample_segments_kernel, 1, 32, 0, s, (int)M, u0, (int)tiles, ws);
+    launch_chained(resample_assign_kernel, blocks, 256, 0, s, particles, (int)M, out, idx_out, (long long)cap,
+                   count_out, ws, status);
     // exact fallbacks: serial double sums + parallel assignment, else the literal loop
-    resample_chunk_transfer_kernel<<<chunks ? chunks : 1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
-    resample_sums_kernel<<<1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
-    resample_chunk_write_kernel<<<chunks ? chunks : 1, kSumsThreads, 0, s>>>(w, stride, (int)M, ws);
-    resample_segments_sums_kernel<<<1, 32, 0, s>>>((int)M, u0, ws);
-    resample_assign_sums_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, out, idx_out, (long long)cap, count_out,
-                                                       ws, status);
-    systematic_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err, ws.serial,
-                                                         u0p);
-    resample_scatter_kernel<<<blocks, 256, 0, s>>>(particles, (int)M, cnt, off, total, err, ws.serial, out,
-                                                   idx_out, (long long)cap, count_out, status);
+    launch_chained(resample_chunk_transfer_kernel, chunks ? chunks : 1u, kSumsThreads, 0, s, w, stride, (int)M, ws);
+    launch_chained(resample_sums_kernel, 1, kSumsThreads, 0, s, w, stride, (int)M, ws);
+    launch_chained(resample_chunk_write_kernel, chunks ? chunks : 1u, kSumsThreads, 0, s, w, stride, (int)M, ws);
+    launch_chained(resample_segments_sums_kernel, 1, 32, 0, s, (int)M, u0, ws);
+    launch_chained(resample_assign_sums_kernel, blocks, 256, 0, s, particles, (int)M, out, idx_out, (long long)cap,
+                   count_out, ws, status);
+    launch_chained(systematic_chain_kernel, 1, kChainThreads, 0, s, w, stride, (int)M, u0, cnt, off, total, err,
+                   ws.serial, u0p);
+    launch_chained(resample_scatter_kernel, blocks, 256, 0, s, particles, (int)M, (const uint32_t*)cnt,
+                   (const uint32_t*)off, (const unsigned long long*)total, (const int*)err, (const int*)ws.serial,
+                   out, idx_out, (long long)cap, count_out, status);
     g_launches += 11;
     return check(cudaGetLastError());
 }
