@@ -15,8 +15,10 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session", autouse=True)
 def _built():
+    from oracle.build import build as build_checker
     from tsdf_localization_gb300._build import build
     build()
+    build_checker()
     yield
 
 

@@ -6,7 +6,7 @@ from pathlib import Path
 
 import pytest
 
-from tsdf_localization_gb300._build import REFERENCE
+from oracle.build import REFERENCE
 
 ROOT = Path(__file__).resolve().parent.parent
 

@@ -3,11 +3,8 @@
 Products (git-ignored, rebuilt on every machine):
   tsdf_localization_gb300/_lib/libtsdfl.so        CUDA library behind include/tsdfl.h
   tsdf_localization_gb300/_lib/libtsdfl_synth.so  synthetic workload generator (host)
-Test infrastructure built by the same call:
-  oracle/_build/liboracle.so   CPU restatement of the reference sensor update
-  oracle/_ref/libref.so        the reference's own CPU sources, compiled from the
-                               reference tree when it is present on this machine
-  oracle/_ref/ref_gpu.cubin    the reference's own CUDA kernels (device code), same
+The oracle and the reference's own sources (test infrastructure) have their
+own recipe, oracle/build.py.
 """
 from __future__ import annotations
 
@@ -23,8 +20,6 @@ PKG = ROOT / "tsdf_localization_gb300"
 CSRC = PKG / "csrc"
 LIB = PKG / "_lib"
 OBJ = PKG / "_lib" / "obj"
-ORACLE = ROOT / "oracle"
-REFERENCE = Path(os.environ.get("TSDFL_REFERENCE_DIR", "/root/reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-std=c++17"]
@@ -76,33 +71,6 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     synth = LIB / "libtsdfl_synth.so"
     if force or _stale(synth, [CSRC / "synth.cpp"]):
         jobs.append(["g++", *HOST_FLAGS, "-shared", str(CSRC / "synth.cpp"), "-o", str(synth)])
-    orc_dir = ORACLE / "_build"
-    orc_dir.mkdir(parents=True, exist_ok=True)
-    orc = orc_dir / "liboracle.so"
-    if force or _stale(orc, [ORACLE / "tsdf_oracle.c", ORACLE / "tsdf_oracle.h"]):
-        jobs.append(["gcc", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-std=gnu11", "-shared",
-                     str(ORACLE / "tsdf_oracle.c"), "-o", str(orc), "-lm"])
-    ref_built = None
-    if (REFERENCE / "src" / "evaluation" / "tsdf_evaluator.cpp").exists():
-        ref_dir = ORACLE / "_ref"
-        ref_dir.mkdir(parents=True, exist_ok=True)
-        ref = ref_dir / "libref.so"
-        ref_srcs = [REFERENCE / "src" / "evaluation" / "tsdf_evaluator.cpp",
-                    REFERENCE / "src" / "evaluation" / "model" / "likelihood_evaluation.cpp",
-                    REFERENCE / "src" / "particle_cloud.cpp",
-                    REFERENCE / "src" / "util" / "util.cpp",
-                    REFERENCE / "src" / "resampling" / "wheel_resampler.cpp"]
-        if force or _stale(ref, [ORACLE / "ref_driver.cpp"] + ref_srcs + sorted((ORACLE / "shim").rglob("*"))):
-            jobs.append(["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-fopenmp", "-shared",
-                         f"-DTSDFL_REF_OMP_THREADS={os.cpu_count() or 8}",
-                         "-I", str(ORACLE / "shim"), "-I", str(REFERENCE / "include"),
-                         str(ORACLE / "ref_driver.cpp"), *map(str, ref_srcs), "-o", str(ref)])
-        ref_built = str(ref)
-        # the reference's CUDA kernels as device code only (loaded through the driver API)
-        cubin = ref_dir / "ref_gpu.cubin"
-        if force or _stale(cubin, [ORACLE / "ref_gpu_kernels.cu"] + sorted((REFERENCE / "include").rglob("*.h"))):
-            jobs.append([nvcc, "-cubin", *ARCH, "-O3", "-std=c++17", "-I", str(ORACLE / "shim"), "-I",
-                         str(REFERENCE / "include"), str(ORACLE / "ref_gpu_kernels.cu"), "-o", str(cubin)])
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
@@ -111,7 +79,7 @@ def build(verbose: bool = False, force: bool = False) -> dict:
         _run([nvcc, *ARCH, "-shared", *map(str, objs), "-o", str(lib), "-Xcompiler", "-fopenmp", "-lgomp"])
     if verbose:
         print(f"built {lib}")
-    return {"lib": str(lib), "synth": str(synth), "oracle": str(orc), "ref": ref_built}
+    return {"lib": str(lib), "synth": str(synth)}
 
 
 if __name__ == "__main__":
