@@ -1603,6 +1603,12 @@ __device__ __forceinline__ double pow2(int k)
     return __longlong_as_double((long long)(k + 1023) << 52);
 }
 
+// V * 2^(b-52) for V in [2^52, 2^53): the double's bits directly.
+__device__ __forceinline__ double binade_value(unsigned long long V, int b)
+{
+    return __longlong_as_double((long long)(((unsigned long long)(b + 1023) << 52) | (V - (1ull << 52))));
+}
+
 // Builds the piecewise-arithmetic description of the reference's float draw
 // sequence U_{k+1} = (float)((double)U_k + 1.0/M) (novel_resampling.h:59-63)
 // for all draws below s_total: inside one binade of float the step is constant
@@ -1613,32 +1619,60 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
 {
     bool ok = true;
     const double inv_m = 1.0 / (double)M;
+    // 1/M = Mi 2^(Ei - 52): the binade arithmetic below is integer work on the
+    // doubles' bits (one lane walks the binades; GB300's FP64 pipe is narrow)
+    const unsigned long long ib = (unsigned long long)__double_as_longlong(inv_m);
+    const unsigned long long Mi = (ib & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const int Ei = (int)((ib >> 52) & 0x7ff) - 1023;
+    const unsigned long long kHalf29 = 1ull << 28, kMask29 = (1ull << 29) - 1ull, kTop = 1ull << 53;
     double U = (double)u0;
     long long j = 0;
     int ns = 0;
     for (int iter = 0; U < s_total; ++iter) {
         if (ns == kMaxSegments || iter > 4 * kMaxSegments) { ok = false; break; }
-        float uf = (float)U;
         bool regular = false;
         long long cnt = 0;
+        int e = 0;
+        unsigned long long Ui = 0, D = 0;
         double delta = 0.0;
-        if (uf >= 1.17549435e-38f) {     // normal float: binade [2^e, 2^(e+1))
-            const int e = (int)((__double_as_longlong(U) >> 52) & 0x7ff) - 1023;
-            const double u = pow2(e - 23);     // float ulp in the binade
-            const double g = pow2(e - 52);     // double ulp in the binade
-            const double ginv = pow2(52 - e);
-            const double y = rint(inv_m * ginv) * g;   // (double)U + inv_m - U, while inside the binade
-            const double r = y * pow2(23 - e);          // y / u
-            double frac = r - floor(r);
-            if (frac == 0.5) { ok = false; break; }   // step would depend on the parity of U
-            delta = rint(r) * u;
-            if (delta <= 0.0) { ok = false; break; }  // U would stop advancing
-            // values U + i*delta with U + i*delta + y < 2^(e+1) take the regular step
-            double top = pow2(e + 1) - y;
-            if (U < top) {
-                long long Ui = (long long)(U * ginv), Di = (long long)(delta * ginv), Ti = (long long)(top * ginv);
-                cnt = (Ti - Ui + Di - 1) / Di;
-                regular = cnt > 0;
+        if (U >= 1.17549435e-38) {   // normal float: binade [2^e, 2^(e+1))
+            const unsigned long long ub = (unsigned long long)__double_as_longlong(U);
+            e = (int)((ub >> 52) & 0x7ff) - 1023;
+            Ui = (ub & ((1ull << 52) - 1ull)) | (1ull << 52);   // U in units g = 2^(e-52)
+            // Y = rint(inv_m / g): (double)U + inv_m = U + Y g while inside the binade
+            const int sh = Ei - e;
+            unsigned long long Y = 0, low;   // low: Y's bits below the float ulp u = 2^29 g
+            bool big = false;                // Y >= 2^53: the first step leaves the binade
+            if (sh >= 0) {
+                low = sh >= 29 ? 0ull : (Mi & ((1ull << (29 - sh)) - 1ull)) << sh;
+                if (sh >= 11) {
+                    big = true;
+                } else {
+                    Y = Mi << sh;
+                    big = Y >= kTop;
+                }
+            } else {
+                const int n = -sh;
+                if (n < 64) {   // round half to even
+                    const unsigned long long q = Mi >> n, rem = Mi & ((1ull << n) - 1ull), half = 1ull << (n - 1);
+                    Y = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+                }
+                low = Y & kMask29;
+            }
+            if (low == kHalf29) { ok = false; break; }   // step would depend on the parity of U
+            if (!big) {
+                // delta = rint(Y g / u) u = R 2^29 g
+                const unsigned long long R = (Y >> 29) + (low > kHalf29 ? 1ull : 0ull);
+                if (R == 0) { ok = false; break; }        // U would stop advancing
+                D = R << 29;
+                delta = (double)R * pow2(e - 23);   // exact: R < 2^25
+                // values U + i delta below top = 2^(e+1) - Y g take the regular step
+                const unsigned long long T = kTop - Y;
+                if (Ui < T) {
+                    const unsigned long long num = (T - Ui + D - 1ull) >> 29;   // below 2^24
+                    cnt = (long long)((uint32_t)num / (uint32_t)R);
+                    regular = cnt > 0;
+                }
             }
         }
         if (regular) {
@@ -1648,7 +1682,8 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
             ws.segs[ns].n = cnt;
             ++ns;
             j += cnt;
-            U = U + (double)cnt * delta;   // exact: a float value of this binade or 2^(e+1)
+            const unsigned long long V = Ui + (unsigned long long)cnt * D;   // at most 2^53 (a float value)
+            U = V >= kTop ? pow2(e + 1) : binade_value(V, e);
         } else {
             ws.segs[ns].u_start = U;
             ws.segs[ns].delta = 0.0;
@@ -1820,11 +1855,6 @@ __device__ __forceinline__ FloatSplit split_weight(float w, int b)
     return o;
 }
 
-// V * 2^(b-52) for V in [2^52, 2^53): the double's bits directly.
-__device__ __forceinline__ double binade_value(unsigned long long V, int b)
-{
-    return __longlong_as_double((long long)(((unsigned long long)(b + 1023) << 52) | (V - (1ull << 52))));
-}
 
 // The binade of a positive normal double, and its value in units 2^(b-52).
 __device__ __forceinline__ int binade_of(double s)
