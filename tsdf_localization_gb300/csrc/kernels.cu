@@ -2659,6 +2659,17 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         tp.e = p;
         tp.chunk = kTiledChunk;
         tp.group = kTiledGroup;
+        // small filters: smaller work items (fewer particles, then fewer points)
+        // until the grid has about two per warp; the sums are exact integers,
+        // so the shape changes no result
+        auto items_of = [&](int chunk, int group) {
+            return (long long)((n1 - n0 + chunk - 1) / chunk) * (long long)((P + group - 1) / group);
+        };
+        const long long want = 2ll * sm_count * kTiledWarps;
+        while (items_of(tp.chunk, tp.group) < want && (tp.group > 1 || tp.chunk > 256)) {
+            if (tp.group > 1) tp.group /= 2;
+            else tp.chunk /= 2;
+        }
         tp.groups = (P + tp.group - 1) / tp.group;
         tp.items = ((n1 - n0 + tp.chunk - 1) / tp.chunk) * tp.groups;
         // sub_fast 2: floor(s * sub_inv) is the sub-voxel index; 1: the two-term multiplier
