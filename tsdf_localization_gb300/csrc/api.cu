@@ -142,7 +142,7 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
     size_t o_pxy = take(sizeof(float) * 4 * npairs);
     size_t o_pz = take(sizeof(float) * 2 * npairs);
     size_t o_perm = take(sizeof(int32_t) * 2 * npairs);
-    size_t o_ext = take(sizeof(float) * 4 * ((nP + 255) / 256));
+    size_t o_ext = take(sizeof(float) * 4 * pose_blocks(nP));   // one x / y extent per pose block
     size_t o_lfx = take(sizeof(long long) * kNumCodes);
     size_t o_lf = take(sizeof(float) * kNumCodes);
     size_t o_cnt = take(sizeof(int32_t) * 16);

@@ -402,83 +402,85 @@ struct Tf16 {
 
 // Laser pose of every particle (tsdf_evaluator.cpp:102-147): trig in double,
 // rounded to float (the correctly rounded sin/cos), products and sums in the
-// reference's order without contraction.
+// reference's order without contraction.  Three lanes per particle, ten
+// particles a warp (lanes 30 and 31 idle): lane 3p + k forms the sine and
+// cosine of angle k (roll, pitch, yaw), the three exchange them by shuffles,
+// and lane 3p + r forms row r of the 3 x 4 laser pose, so the FP64 latency of
+// the three sincos is spread over three lanes.
 // Also: the x / y extent of the block's particles (min x, min y, max x, max y)
 // into extent[block], for the scan staging's choice of point order; and zeros
 // in the scoring sums and the cell histogram, so no memset breaks the chain of
 // kernels.
-__global__ void pose_kernel(const float* particles, int P, Tf16 tf, float* pose12, float* trig6, float4* extent,
-                            long long* sum_fx, uint32_t* hits, int32_t* phist)
+__global__ void __launch_bounds__(kPoseThreads) pose_kernel(const float* particles, int P, Tf16 tf, float* pose12,
+                                                            float* trig6, float4* extent, long long* sum_fx,
+                                                            uint32_t* hits, int32_t* phist)
 {
     chain_enter();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int slot = lane / 3, k = lane - 3 * slot;
+    const int i = (blockIdx.x * (kPoseThreads / 32) + (threadIdx.x >> 5)) * kPoseSlots + slot;
+    const bool active = slot < kPoseSlots && i < P;
     // the tiled kernel's per-particle sums and the particle order's cell
     // histogram start at zero (the kernels of this update run after this one)
-    if (i < P) {
+    if (active && k == 0) {
         sum_fx[i] = 0;
         hits[i] = 0;
     }
     if (blockIdx.x == 0)
-        for (int k = threadIdx.x; k < kCellBins; k += blockDim.x) phist[k] = 0;
+        for (int c = threadIdx.x; c < kCellBins; c += blockDim.x) phist[c] = 0;
+    const float* p = particles + 7 * (size_t)(active ? i : 0);
     {
-        __shared__ float4 s_ext[32];
+        __shared__ float4 s_ext[kPoseThreads / 32];
         const float inf = __int_as_float(0x7f800000);
         float4 e = make_float4(inf, inf, -inf, -inf);
-        if (i < P) {
-            const float x = particles[7 * (size_t)i], y = particles[7 * (size_t)i + 1];
-            e = make_float4(x, y, x, y);
-        }
+        if (active && k == 0) e = make_float4(p[0], p[1], p[0], p[1]);
         e = warp_extent(e);
-        if ((threadIdx.x & 31) == 0) s_ext[threadIdx.x >> 5] = e;
+        if (lane == 0) s_ext[threadIdx.x >> 5] = e;
         __syncthreads();
         if (threadIdx.x == 0) {
-            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            for (int w = 1; w < kPoseThreads / 32; ++w) {
                 const float4 v = s_ext[w];
                 e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
             }
             extent[blockIdx.x] = e;
         }
     }
-    if (i >= P) return;
-    const float* p = particles + 7 * (size_t)i;
-    float px = p[0], py = p[1], pz = p[2];
-    double s, c;
-    sincos((double)p[3], &s, &c);
-    float sin_alpha = (float)s, cos_alpha = (float)c;
-    sincos((double)p[4], &s, &c);
-    float sin_beta = (float)s, cos_beta = (float)c;
-    sincos((double)p[5], &s, &c);
-    float sin_gamma = (float)s, cos_gamma = (float)c;
-    float t[12];
-    t[0] = __fmul_rn(cos_beta, cos_gamma);
-    t[4] = __fmul_rn(cos_beta, sin_gamma);
-    t[8] = -sin_beta;
-    t[3] = px;
-    t[1] = __fsub_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), cos_gamma), __fmul_rn(cos_alpha, sin_gamma));
-    t[5] = __fadd_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), sin_gamma), __fmul_rn(cos_alpha, cos_gamma));
-    t[9] = __fmul_rn(sin_alpha, cos_beta);
-    t[7] = py;
-    t[2] = __fadd_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), cos_gamma), __fmul_rn(sin_alpha, sin_gamma));
-    t[6] = __fsub_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), sin_gamma), __fmul_rn(sin_alpha, cos_gamma));
-    t[10] = __fmul_rn(cos_alpha, cos_beta);
-    t[11] = pz;
-    const float* f = tf.v;
-    float o[12];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        const float* a = t + 4 * r;
-        o[4 * r + 0] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[0]), __fmul_rn(a[1], f[4])), __fmul_rn(a[2], f[8]));
-        o[4 * r + 1] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[1]), __fmul_rn(a[1], f[5])), __fmul_rn(a[2], f[9]));
-        o[4 * r + 2] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[2]), __fmul_rn(a[1], f[6])), __fmul_rn(a[2], f[10]));
-        o[4 * r + 3] = __fadd_rn(
-            __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[3]), __fmul_rn(a[1], f[7])), __fmul_rn(a[2], f[11])), a[3]);
+    double sd, cd;
+    sincos((double)p[3 + (k < 3 ? k : 0)], &sd, &cd);
+    const float sv = (float)sd, cv = (float)cd;
+    const int base = 3 * slot;
+    auto from = [&](float v, int j) { return __shfl_sync(0xffffffffu, v, min(base + j, 31)); };
+    const float sin_alpha = from(sv, 0), cos_alpha = from(cv, 0);
+    const float sin_beta = from(sv, 1), cos_beta = from(cv, 1);
+    const float sin_gamma = from(sv, 2), cos_gamma = from(cv, 2);
+    if (!active) return;
+    float a[4];   // row k of the particle's transform
+    if (k == 0) {
+        a[0] = __fmul_rn(cos_beta, cos_gamma);
+        a[1] = __fsub_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), cos_gamma), __fmul_rn(cos_alpha, sin_gamma));
+        a[2] = __fadd_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), cos_gamma), __fmul_rn(sin_alpha, sin_gamma));
+        a[3] = p[0];
+    } else if (k == 1) {
+        a[0] = __fmul_rn(cos_beta, sin_gamma);
+        a[1] = __fadd_rn(__fmul_rn(__fmul_rn(sin_alpha, sin_beta), sin_gamma), __fmul_rn(cos_alpha, cos_gamma));
+        a[2] = __fsub_rn(__fmul_rn(__fmul_rn(cos_alpha, sin_beta), sin_gamma), __fmul_rn(sin_alpha, cos_gamma));
+        a[3] = p[1];
+    } else {
+        a[0] = -sin_beta;
+        a[1] = __fmul_rn(sin_alpha, cos_beta);
+        a[2] = __fmul_rn(cos_alpha, cos_beta);
+        a[3] = p[2];
     }
-    float4* dst = reinterpret_cast<float4*>(pose12 + 12 * (size_t)i);
-    dst[0] = make_float4(o[0], o[1], o[2], o[3]);
-    dst[1] = make_float4(o[4], o[5], o[6], o[7]);
-    dst[2] = make_float4(o[8], o[9], o[10], o[11]);
+    const float* f = tf.v;
+    float o[4];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        o[c] = __fadd_rn(__fadd_rn(__fmul_rn(a[0], f[c]), __fmul_rn(a[1], f[4 + c])), __fmul_rn(a[2], f[8 + c]));
+    o[3] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a[0], f[3]), __fmul_rn(a[1], f[7])), __fmul_rn(a[2], f[11])), a[3]);
+    reinterpret_cast<float4*>(pose12 + 12 * (size_t)i)[k] = make_float4(o[0], o[1], o[2], o[3]);
     float* tg = trig6 + 6 * (size_t)i;
-    tg[0] = sin_alpha; tg[1] = cos_alpha; tg[2] = sin_beta; tg[3] = cos_beta; tg[4] = sin_gamma; tg[5] = cos_gamma;
+    tg[2 * k] = sv;
+    tg[2 * k + 1] = cv;
 }
 
 struct EvalParams {
@@ -1365,16 +1367,17 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
 
 // Final weight sum, the "No particle is valid!" check (tsdf_evaluator.cpp:159)
 // and the mean pose with circular means of the angles (:219-221).  One block
-// of kNormBlocks threads: thread t takes block t's partial sums, then a fixed
-// reduction tree (so the result does not depend on timing).
-__global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, float* pose_out)
+// of kNormBlocks threads: thread t takes block t's partial sums (nb blocks ran),
+// then a fixed reduction tree (so the result does not depend on timing); the
+// position and the three angles are formed by four threads side by side.
+__global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, float* pose_out, int nb)
 {
     chain_enter();
     __shared__ double red[kNormSums][kNormBlocks / 32];
     __shared__ double s[kNormSums];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     for (int k = 0; k < kNormSums; ++k) {
-        const double v = warp_sum_d(b.partials[t * kNormSums + k]);
+        const double v = warp_sum_d(t < nb ? b.partials[t * kNormSums + k] : 0.0);
         if (lane == 0) red[k][warp] = v;
     }
     __syncthreads();
@@ -1385,21 +1388,20 @@ __global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, 
         b.sums[t] = v;
     }
     __syncthreads();
-    if (t != 0) return;
-    float wsum = (float)s[0];
-    b.weight_sum_f[0] = wsum;
-    if (!(wsum != 0.0f) || !isfinite(s[0])) {
-        atomicExch(b.status, TSDFL_ERR_DEGENERATE);
-        return;
+    if (t >= 4) return;
+    const bool degenerate = !((float)s[0] != 0.0f) || !isfinite(s[0]);
+    if (t == 0) {
+        b.weight_sum_f[0] = (float)s[0];
+        if (degenerate) atomicExch(b.status, TSDFL_ERR_DEGENERATE);
     }
-    if (pose_out) {
-        double inv = 1.0 / s[0];
+    if (degenerate || !pose_out) return;
+    const double inv = 1.0 / s[0];
+    if (t == 0) {
         pose_out[0] = (float)(s[1] * inv);
         pose_out[1] = (float)(s[2] * inv);
         pose_out[2] = (float)(s[3] * inv);
-        pose_out[3] = (float)atan2(s[4] * inv, s[5] * inv);
-        pose_out[4] = (float)atan2(s[6] * inv, s[7] * inv);
-        pose_out[5] = (float)atan2(s[8] * inv, s[9] * inv);
+    } else {
+        pose_out[2 + t] = (float)atan2(s[2 + 2 * t] * inv, s[3 + 2 * t] * inv);
     }
 }
 
@@ -2549,7 +2551,7 @@ void launch_chained(void (*kernel)(Params...), unsigned grid, unsigned block, si
 int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
                    const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
 {
-    PointParams p{points, N, npad, 32 * ((N + 63) / 64), b.extent, P > 0 ? (P + 255) / 256 : 0,
+    PointParams p{points, N, npad, 32 * ((N + 63) / 64), b.extent, P > 0 ? (int)pose_blocks((size_t)P) : 0,
                   max_range_sq, c_in, c_out, code_values, shift};
     launch_chained(prepare_points_kernel, 1, kPrepThreads, 0, s, p, b);
     g_launches += 1;
@@ -2573,8 +2575,8 @@ int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_
     Tf16 t;
     for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
     if (P > 0) {
-        launch_chained(pose_kernel, (unsigned)((P + 255) / 256), 256, 0, s, b.particles, P, t, b.pose12, b.trig6,
-                       b.extent, b.sum_fx, b.hits, b.phist);
+        launch_chained(pose_kernel, (unsigned)pose_blocks((size_t)P), kPoseThreads, 0, s, b.particles, P, t, b.pose12,
+                       b.trig6, b.extent, b.sum_fx, b.hits, b.phist);
         g_launches += 1;
     }
     return check(cudaGetLastError());
@@ -2827,9 +2829,12 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s,
                 const uint32_t* nin, bool log_domain)
 {
+    // one block per kNormThreads particles, at most kNormBlocks: the block count
+    // depends on P alone, so the sums' order does too
+    const int nb = std::max(1, std::min(kNormBlocks, (P + kNormThreads - 1) / kNormThreads));
     NormParams q{P, mode, shift, a_hit, c_in, c_out, n_points, nin};
-    launch_chained(norm_partial_kernel, kNormBlocks, kNormThreads, 0, s, q, b, sum_f64);
-    launch_chained(norm_final_kernel, 1, kNormBlocks, 0, s, b, pose_out);
+    launch_chained(norm_partial_kernel, (unsigned)nb, kNormThreads, 0, s, q, b, sum_f64);
+    launch_chained(norm_final_kernel, 1, kNormBlocks, 0, s, b, pose_out, nb);
     g_launches += 2;
     if (P > 0 && log_domain) {
         cudaMemsetAsync(b.counts + 1, 0, sizeof(int32_t), s);

@@ -116,6 +116,12 @@ struct MapView {
 };
 
 constexpr int kSentinels = 4;
+
+// pose_kernel: three lanes per particle, kPoseSlots particles a warp.
+constexpr int kPoseThreads = 256;
+constexpr int kPoseSlots = 10;
+constexpr int kPoseParticlesPerBlock = (kPoseThreads / 32) * kPoseSlots;
+inline size_t pose_blocks(size_t P) { return (P + kPoseParticlesPerBlock - 1) / kPoseParticlesPerBlock; }
 constexpr uint32_t kHashEmpty = 0xffffffffu;
 
 #ifdef __CUDACC__
