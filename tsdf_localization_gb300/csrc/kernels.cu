@@ -1755,6 +1755,48 @@ __device__ long long count_below(const Segment* seg, int ns, double s)
     return g.j0 + i;
 }
 
+// count_below for s = c_fx 2^-52 (0 <= c_fx < 2^53), with integer operations
+// only (the FP64 pipe is narrow): positive doubles order like their bits, and
+// the draws of a regular segment are (A + k R) u with u = 2^(e-23) the float
+// ulp of its binade, A = u_start / u, R = delta / u, so the count of those
+// below s is ceil((ceil(s / u) - A) / R), clamped to [0, n].
+__device__ __forceinline__ long long count_below_fx(const Segment* seg, int ns, long long c_fx)
+{
+    constexpr unsigned long long kM52 = (1ull << 52) - 1ull;
+    long long sb = 0;   // bits of the double c_fx 2^-52 (exact)
+    if (c_fx > 0) {
+        const int lz = __clzll(c_fx);   // at least 11
+        sb = ((long long)(63 - lz - 52 + 1023) << 52) | (long long)(((unsigned long long)c_fx << (lz - 11)) & kM52);
+    }
+    int lo = 0, hi = ns;   // first segment with u_start >= s
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__double_as_longlong(seg[mid].u_start) < sb) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo == 0) return 0;
+    const Segment& g = seg[lo - 1];
+    const unsigned long long db = (unsigned long long)__double_as_longlong(g.delta);
+    if (db == 0ull) return g.j0 + 1;
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(g.u_start);
+    const int e = (int)((ub >> 52) & 0x7ff) - 1023, ed = (int)((db >> 52) & 0x7ff) - 1023;
+    const unsigned long long A = ((ub & kM52) | (1ull << 52)) >> 29;
+    const unsigned long long R = ((db & kM52) | (1ull << 52)) >> (e + 29 - ed);
+    const unsigned long long L = A + (unsigned long long)g.n * R;   // the segment's end, below 2^50
+    const int t = -29 - e;   // s / u = c_fx 2^t
+    unsigned long long S;    // ceil(s / u), or L when it is at least L
+    if (t >= 0) {
+        S = (t >= 50 || ((unsigned long long)c_fx >> (63 - t)) != 0ull) ? L : (unsigned long long)c_fx << t;
+        if (S > L) S = L;
+    } else {
+        const int n = -t;
+        S = n >= 63 ? 1ull : ((unsigned long long)c_fx + (1ull << n) - 1ull) >> n;
+    }
+    if (S >= L) return g.j0 + g.n;
+    if (S <= A) return g.j0;
+    return g.j0 + (long long)((S - A + R - 1ull) / R);
+}
+
 // Particle m receives the draws in [cdf_{m-1}, cdf_m) (novel_resampling.h:52-68):
 // writes their indices and, when asked, copies of the particle.
 __global__ void resample_assign_kernel(const float* particles, int M, float* out, uint32_t* idx_out, long long cap,
@@ -1771,8 +1813,8 @@ __global__ void resample_assign_kernel(const float* particles, int M, float* out
     const long long c_hi_fx = ws.cdf[m] + ws.tile_off[m / kScanTile];
     long long c_lo_fx = 0;
     if (m > 0) c_lo_fx = ws.cdf[m - 1] + ws.tile_off[(m - 1) / kScanTile];
-    long long lo = count_below(seg, ns, ldexp((double)c_lo_fx, -52));
-    long long hi = count_below(seg, ns, ldexp((double)c_hi_fx, -52));
+    long long lo = count_below_fx(seg, ns, c_lo_fx);
+    long long hi = count_below_fx(seg, ns, c_hi_fx);
     if (m == M - 1) {
         *count_out = (uint32_t)hi;
         if (hi > cap) atomicExch(status, TSDFL_ERR_CAPACITY);
