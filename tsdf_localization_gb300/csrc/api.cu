@@ -142,7 +142,6 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
     size_t o_pxy = take(sizeof(float) * 4 * npairs);
     size_t o_pz = take(sizeof(float) * 2 * npairs);
     size_t o_perm = take(sizeof(int32_t) * 2 * npairs);
-    size_t o_ext = take(sizeof(float) * 4 * pose_blocks(nP));   // one x / y extent per pose block
     size_t o_lfx = take(sizeof(long long) * kNumCodes);
     size_t o_lf = take(sizeof(float) * kNumCodes);
     size_t o_cnt = take(sizeof(int32_t) * 16);
@@ -170,7 +169,6 @@ size_t eval_layout(size_t nP, size_t nN, char* base, EvalBuffers* e, double** su
         e->pxy = reinterpret_cast<float4*>(b + o_pxy);
         e->pz = reinterpret_cast<float2*>(b + o_pz);
         e->perm = reinterpret_cast<int32_t*>(b + o_perm);
-        e->extent = reinterpret_cast<float4*>(b + o_ext);
         e->lut_fx = reinterpret_cast<long long*>(b + o_lfx);
         e->lut_f = reinterpret_cast<float*>(b + o_lf);
         e->counts = reinterpret_cast<int32_t*>(b + o_cnt);
@@ -630,9 +628,8 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
     }
     const int npad = (int)align_up(N, 4);
     cudaStream_t s = c->stream;
-    rc = launch_pose_kernel(tf, (int)P, b, s);
-    if (rc) return rc;
-    rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
+    rc = launch_pose_prepare(tf, d_particles, (int)P, d_points, (int)N, npad, max_range_sq, c_in, c_out, map->values,
+                             shift, b, s);
     if (rc) return rc;
     rc = launch_particle_order(d_particles, (int)P, b, s);
     if (rc) return rc;
@@ -692,9 +689,8 @@ int run_eval_sub(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, flo
     }
     const int npad = (int)align_up(N, 4);
     cudaStream_t s = c->stream;
-    rc = launch_pose_kernel(tf, (int)P, b, s);
-    if (rc) return rc;
-    rc = launch_prepare(d_points, (int)N, npad, (int)P, max_range_sq, c_in, c_out, map->values, shift, b, s);
+    rc = launch_pose_prepare(tf, d_particles, (int)P, d_points, (int)N, npad, max_range_sq, c_in, c_out, map->values,
+                             shift, b, s);
     if (rc) return rc;
     rc = launch_particle_order(d_particles, (int)P, b, s);
     if (rc) return rc;
@@ -1516,10 +1512,9 @@ int batch_record(tsdfl_batch* B)
         if (F.N == 0) continue;
         const float inv_max_range = (float)(1.0 / (double)F.model.max_range);
         const float c_in = F.model.a_range * inv_max_range;
-        int rc = launch_pose_kernel(F.tf, (int)F.P, q.b, s);
-        if (rc) return rc;
-        rc = launch_prepare(F.d_points, (int)F.N, q.npad, (int)F.P, F.model.max_range * F.model.max_range, c_in,
-                            F.model.a_max, F.map->values, q.shift, q.b, s);
+        int rc = launch_pose_prepare(F.tf, F.d_particles, (int)F.P, F.d_points, (int)F.N, q.npad,
+                                     F.model.max_range * F.model.max_range, c_in, F.model.a_max, F.map->values,
+                                     q.shift, q.b, s);
         if (rc) return rc;
     }
     int rc = batch_score(B, s);

@@ -146,11 +146,15 @@ __device__ __forceinline__ uint32_t dense_code(const MapView& m, float x, float 
     return idx == kMissIndex ? (uint32_t)kCodeMiss : (uint32_t)__ldg(m.codes + idx);
 }
 
+// Spread clouds' particle order: 2^kCellBits x 2^kCellBits cells (below).
+constexpr int kCellBits = 6;
+constexpr int kCellBins = 1 << (2 * kCellBits);
+
 struct PointParams {
     const float* points;  // N x 3
     int N, npad, npairs;
-    const float4* extent;  // the pose kernel's per-block cloud extents
-    int n_ext;
+    const float* particles;  // P x 7 (the cloud's extent is taken from a sample)
+    int P;
     float max_range_sq, c_in, c_out;
     const float* code_values;  // kNumCodes floats (device)
     int shift;                 // fixed-point scale 2^shift
@@ -193,23 +197,30 @@ __device__ __forceinline__ int spatial_bin(float x, float y, float z, bool wide)
 // score constant of tsdf_evaluator.cpp:56-65 and the number of points inside
 // max_range; the pair layout of the tiled kernels in spatial order (a counting
 // sort by spatial_bin; perm records each position's scan index); also the
-// likelihood tables for this scan.  One block of kPrepThreads, launched after
-// the pose kernel (it reads the cloud's extent).
-__global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParams p, EvalBuffers b)
+// likelihood tables for this scan.  Block 0 of pose_prepare_kernel, beside the
+// pose blocks.  Which order suits the cloud (compact or spread) is decided on
+// the x / y extent of a sample of at most kExtentSample particles, and the
+// particle order's cells span that extent (clamped at its edges); both only
+// decide how fast the scoring runs, never what it returns.
+constexpr int kExtentSample = 4096;
+
+__device__ __forceinline__ void prepare_points_block(const PointParams& p, const EvalBuffers& b)
 {
-    chain_enter();
     __shared__ int warp_counts[32];
     __shared__ int bins[kSortBins];
     __shared__ uint16_t sbin[kBinCache];
     __shared__ float4 s_ext[32];
     __shared__ int s_wide;
     if (threadIdx.x == 0) *b.status = 0;
-    {   // the cloud's x / y extent from the pose kernel's per-block partials
+    for (int c = threadIdx.x; c < kCellBins; c += blockDim.x) b.phist[c] = 0;   // the particle order's histogram
+    {   // the cloud's x / y extent from a sample of the particles
         const float inf = __int_as_float(0x7f800000);
         float4 e = make_float4(inf, inf, -inf, -inf);
-        for (int k = threadIdx.x; k < p.n_ext; k += blockDim.x) {
-            const float4 v = p.extent[k];
-            e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
+        const int n_s = min(p.P, kExtentSample), stride = max(1, p.P / kExtentSample);
+        for (int k = threadIdx.x; k < n_s; k += blockDim.x) {
+            const float* q = p.particles + 7 * (size_t)k * (size_t)stride;
+            const float x = q[0], y = q[1];
+            e = make_float4(fminf(e.x, x), fminf(e.y, y), fmaxf(e.z, x), fmaxf(e.w, y));
         }
         e = warp_extent(e);
         if ((threadIdx.x & 31) == 0) s_ext[threadIdx.x >> 5] = e;
@@ -317,8 +328,6 @@ __global__ void __launch_bounds__(kPrepThreads) prepare_points_kernel(PointParam
 // particles from one part of the map and the gathers stay in the L2.  The
 // order within a cell depends on the atomics, which changes nothing: every
 // particle's sums are exact integers written to its own index.
-constexpr int kCellBits = 6;
-constexpr int kCellBins = 1 << (2 * kCellBits);
 constexpr int kCellScanThreads = 1024;
 static_assert(kCellBins == 4 * kCellScanThreads, "four bins per thread in the scan");
 
@@ -406,45 +415,21 @@ struct Tf16 {
 // particles a warp (lanes 30 and 31 idle): lane 3p + k forms the sine and
 // cosine of angle k (roll, pitch, yaw), the three exchange them by shuffles,
 // and lane 3p + r forms row r of the 3 x 4 laser pose, so the FP64 latency of
-// the three sincos is spread over three lanes.
-// Also: the x / y extent of the block's particles (min x, min y, max x, max y)
-// into extent[block], for the scan staging's choice of point order; and zeros
-// in the scoring sums and the cell histogram, so no memset breaks the chain of
-// kernels.
-__global__ void __launch_bounds__(kPoseThreads) pose_kernel(const float* particles, int P, Tf16 tf, float* pose12,
-                                                            float* trig6, float4* extent, long long* sum_fx,
-                                                            uint32_t* hits, int32_t* phist)
+// the three sincos is spread over three lanes.  Also zeros in the scoring
+// sums, so no memset breaks the chain of kernels.  `blk` numbers the pose
+// blocks of pose_prepare_kernel.
+__device__ __forceinline__ void pose_block(int blk, const float* particles, int P, const Tf16& tf, float* pose12,
+                                           float* trig6, long long* sum_fx, uint32_t* hits)
 {
-    chain_enter();
     const int lane = threadIdx.x & 31;
     const int slot = lane / 3, k = lane - 3 * slot;
-    const int i = (blockIdx.x * (kPoseThreads / 32) + (threadIdx.x >> 5)) * kPoseSlots + slot;
+    const int i = (blk * (kPoseThreads / 32) + (int)(threadIdx.x >> 5)) * kPoseSlots + slot;
     const bool active = slot < kPoseSlots && i < P;
-    // the tiled kernel's per-particle sums and the particle order's cell
-    // histogram start at zero (the kernels of this update run after this one)
-    if (active && k == 0) {
+    if (active && k == 0) {   // the tiled kernel's per-particle sums start at zero
         sum_fx[i] = 0;
         hits[i] = 0;
     }
-    if (blockIdx.x == 0)
-        for (int c = threadIdx.x; c < kCellBins; c += blockDim.x) phist[c] = 0;
     const float* p = particles + 7 * (size_t)(active ? i : 0);
-    {
-        __shared__ float4 s_ext[kPoseThreads / 32];
-        const float inf = __int_as_float(0x7f800000);
-        float4 e = make_float4(inf, inf, -inf, -inf);
-        if (active && k == 0) e = make_float4(p[0], p[1], p[0], p[1]);
-        e = warp_extent(e);
-        if (lane == 0) s_ext[threadIdx.x >> 5] = e;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < kPoseThreads / 32; ++w) {
-                const float4 v = s_ext[w];
-                e = make_float4(fminf(e.x, v.x), fminf(e.y, v.y), fmaxf(e.z, v.z), fmaxf(e.w, v.w));
-            }
-            extent[blockIdx.x] = e;
-        }
-    }
     double sd, cd;
     sincos((double)p[3 + (k < 3 ? k : 0)], &sd, &cd);
     const float sv = (float)sd, cv = (float)cd;
@@ -481,6 +466,16 @@ __global__ void __launch_bounds__(kPoseThreads) pose_kernel(const float* particl
     float* tg = trig6 + 6 * (size_t)i;
     tg[2 * k] = sv;
     tg[2 * k + 1] = cv;
+}
+
+// First kernel of an update: block 0 stages the scan (prepare_points_block),
+// the others form the laser poses (pose_block); the two parts share no data,
+// so they run side by side.
+__global__ void __launch_bounds__(kPoseThreads) pose_prepare_kernel(Tf16 tf, PointParams p, EvalBuffers b)
+{
+    chain_enter();
+    if (blockIdx.x == 0) prepare_points_block(p, b);
+    else pose_block((int)blockIdx.x - 1, p.particles, p.P, tf, b.pose12, b.trig6, b.sum_fx, b.hits);
 }
 
 struct EvalParams {
@@ -2590,12 +2585,16 @@ void launch_chained(void (*kernel)(Params...), unsigned grid, unsigned block, si
     cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
-                   const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s)
+int launch_pose_prepare(const float* tf, const float* particles, int P, const float* points, int N, int npad,
+                        float max_range_sq, float c_in, float c_out, const float* code_values, int shift,
+                        const EvalBuffers& b, cudaStream_t s)
 {
-    PointParams p{points, N, npad, 32 * ((N + 63) / 64), b.extent, P > 0 ? (int)pose_blocks((size_t)P) : 0,
-                  max_range_sq, c_in, c_out, code_values, shift};
-    launch_chained(prepare_points_kernel, 1, kPrepThreads, 0, s, p, b);
+    Tf16 t;
+    for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
+    PointParams p{points, N, npad, 32 * ((N + 63) / 64), particles, P, max_range_sq, c_in, c_out, code_values,
+                  shift};
+    launch_chained(pose_prepare_kernel, (unsigned)(1 + pose_blocks((size_t)(P > 0 ? P : 0))), kPoseThreads, 0, s,
+                   t, p, b);
     g_launches += 1;
     return check(cudaGetLastError());
 }
@@ -2603,24 +2602,12 @@ int launch_prepare(const float* points, int N, int npad, int P, float max_range_
 int launch_particle_order(const float* particles, int P, const EvalBuffers& b, cudaStream_t s)
 {
     if (P <= 0) return TSDFL_OK;
-    // the cell histogram was cleared by pose_kernel
+    // the cell histogram was cleared by pose_prepare_kernel
     const unsigned blocks = (unsigned)std::min((P + 255) / 256, 4096);
     launch_chained(particle_cells_kernel, blocks, 256, 0, s, particles, P, b);
     launch_chained(particle_scan_kernel, 1, kCellScanThreads, 0, s, b);
     launch_chained(particle_scatter_kernel, blocks, 256, 0, s, P, b);
     g_launches += 3;
-    return check(cudaGetLastError());
-}
-
-int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s)
-{
-    Tf16 t;
-    for (int k = 0; k < 16; ++k) t.v[k] = tf[k];
-    if (P > 0) {
-        launch_chained(pose_kernel, (unsigned)pose_blocks((size_t)P), kPoseThreads, 0, s, b.particles, P, t, b.pose12,
-                       b.trig6, b.extent, b.sum_fx, b.hits, b.phist);
-        g_launches += 1;
-    }
     return check(cudaGetLastError());
 }
 
@@ -2725,7 +2712,7 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
         auto k = pick_tiled(lay, two, dbg, m.min0 != 0);
         size_t tsmem = tiled_smem_bytes(m, dense, n1 - n0);
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
-        // pose_kernel cleared sum_fx and hits before the first pass
+        // pose_prepare_kernel cleared sum_fx and hits before the first pass
         int blocks = sm_count;
         int need = (tp.items + kTiledWarps - 1) / kTiledWarps;
         if (need < blocks) blocks = need > 0 ? need : 1;

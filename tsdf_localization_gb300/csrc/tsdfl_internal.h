@@ -117,8 +117,9 @@ struct MapView {
 
 constexpr int kSentinels = 4;
 
-// pose_kernel: three lanes per particle, kPoseSlots particles a warp.
-constexpr int kPoseThreads = 256;
+// pose_prepare_kernel: blocks of kPoseThreads; in the pose blocks three lanes
+// per particle, kPoseSlots particles a warp.
+constexpr int kPoseThreads = 1024;
 constexpr int kPoseSlots = 10;
 constexpr int kPoseParticlesPerBlock = (kPoseThreads / 32) * kPoseSlots;
 inline size_t pose_blocks(size_t P) { return (P + kPoseParticlesPerBlock - 1) / kPoseParticlesPerBlock; }
@@ -193,7 +194,6 @@ struct EvalBuffers {
     float4* pxy;             // point pairs (x_a, x_b, y_a, y_b) per 64-point block, spatial order
     float2* pz;              // point pairs (z_a, z_b)
     int32_t* perm;           // scan index of each point of the pair layout
-    float4* extent;          // per 256 particles: min x, min y, max x, max y
     float* pose12;           // P x 12 laser poses
     float* trig6;            // P x 6: sin/cos of roll, pitch, yaw
     long long* sum_fx;       // P: fixed-point likelihood sums
@@ -218,12 +218,14 @@ struct EvalBuffers {
     float4* cloud_ext;       // [1]: min x, min y, max x, max y of the particles
 };
 
-// Runs after launch_pose_kernel for the same buffers (reads the cloud's extent).
-int launch_prepare(const float* points, int N, int npad, int P, float max_range_sq, float c_in, float c_out,
-                   const float* code_values, int shift, const EvalBuffers& b, cudaStream_t s);
-int launch_pose_kernel(const float* tf, int P, const EvalBuffers& b, cudaStream_t s);
-// Runs after launch_prepare: orders the particles of a spread cloud by cell
-// (b.order); for a compact cloud its kernels return at once.
+// First kernel of an update: the particles' laser poses (tf: the sensor's
+// 4 x 4 transform) beside the scan staging (pair layout in spatial order,
+// likelihood tables, per-point constants); also clears the scoring sums.
+int launch_pose_prepare(const float* tf, const float* particles, int P, const float* points, int N, int npad,
+                        float max_range_sq, float c_in, float c_out, const float* code_values, int shift,
+                        const EvalBuffers& b, cudaStream_t s);
+// Runs after launch_pose_prepare: orders the particles of a spread cloud by
+// cell (b.order); for a compact cloud its kernels return at once.
 int launch_particle_order(const float* particles, int P, const EvalBuffers& b, cudaStream_t s);
 size_t eval_smem_bytes(bool serial, int n);
 // Scan points one pass of the tiled kernel stages (0: the kernel cannot hold
