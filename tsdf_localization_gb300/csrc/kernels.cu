@@ -2088,19 +2088,23 @@ __global__ void __launch_bounds__(kSumsThreads) resample_chunk_transfer_kernel(c
     }
 }
 
+__device__ void systematic_chain_block(const float* __restrict__ w, int stride, int M, float u0,
+                                       uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
+                                       unsigned long long* total, int* err);
+
 // The chain: one block walks the chunks in order, applying the transfers of
 // chunks inside one binade (thread 0, checked) and forming the others' sums
-// weight by weight.
-__global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
-                                                                     ResampleWs ws)
+// weight by weight; then thread 0 describes the draws below the total as
+// segments.  Where only the literal loop reproduces the reference (*ws.serial:
+// set by the scan for negative or non-finite weights, or here when the draws
+// cannot be described), the block walks that instead.
+__device__ void serial_sums_block(const float* __restrict__ w, int stride, int M, float u0, ResampleWs ws)
 {
-    chain_enter();
     __shared__ float sw[kSumsChunk];
     __shared__ unsigned long long red_sum[kSumsThreads / 32];
     __shared__ ParityPrefix red_par[kSumsThreads / 32];
     __shared__ double s_s, s_prev;
     __shared__ int s_pos, s_e, s_c;
-    if (*ws.exact_ok || *ws.serial) return;
     const int tid = threadIdx.x;
     const int chunks = (M + kSumsChunk - 1) / kSumsChunk;
     const unsigned long long LIM = 1ull << 53;
@@ -2189,6 +2193,20 @@ __global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float
         if (tid == 0) s_c = c + 1;
         __syncthreads();
     }
+    if (tid == 0 && !build_segments(M, u0, s_s, ws)) *ws.serial = 1;   // s_s: the total
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSumsThreads) resample_sums_kernel(const float* __restrict__ w, int stride, int M,
+                                                                     float u0, ResampleWs ws, uint32_t* cnt,
+                                                                     uint32_t* off, unsigned long long* total,
+                                                                     int* err)
+{
+    chain_enter();
+    if (*ws.exact_ok) return;
+    if (ws.u0p) u0 = *ws.u0p;
+    if (!*ws.serial) serial_sums_block(w, stride, M, u0, ws);
+    if (*ws.serial) systematic_chain_block(w, stride, M, u0, cnt, off, total, err);
 }
 
 // One block per chained chunk: its sums from the start the chain gave it.
@@ -2214,22 +2232,25 @@ __global__ void __launch_bounds__(kSumsThreads) resample_chunk_write_kernel(cons
     }
 }
 
-// Draw segments up to the serial sum's total, for the fallback above.
-__global__ void resample_segments_sums_kernel(int M, float u0, ResampleWs ws)
-{
-    chain_enter();
-    if (ws.u0p) u0 = *ws.u0p;
-    if (threadIdx.x != 0 || blockIdx.x != 0 || *ws.exact_ok || *ws.serial) return;
-    if (!build_segments(M, u0, ws.sums[M - 1], ws)) *ws.serial = 1;
-}
+__device__ void scatter_block(const float* particles, int M, const uint32_t* cnt, const uint32_t* off,
+                              const unsigned long long* total, const int* err, float* out, uint32_t* idx_out,
+                              long long cap, uint32_t* count_out, int32_t* status);
 
-// Particle m receives the draws in [s_{m-1}, s_m) of the serial double sums.
-__global__ void resample_assign_sums_kernel(const float* particles, int M, float* out, uint32_t* idx_out,
-                                            long long cap, uint32_t* count_out, ResampleWs ws, int32_t* status)
+// The fallbacks' assignment: from the literal loop's counts and offsets
+// (*ws.serial), else particle m receives the draws in [s_{m-1}, s_m) of the
+// serial double sums.
+__global__ void resample_fallback_assign_kernel(const float* particles, int M, float* out, uint32_t* idx_out,
+                                                long long cap, uint32_t* count_out, ResampleWs ws, int32_t* status,
+                                                const uint32_t* cnt, const uint32_t* off,
+                                                const unsigned long long* total, const int* err)
 {
     chain_enter();
     __shared__ Segment seg[kMaxSegments];
-    if (*ws.exact_ok || *ws.serial) return;
+    if (*ws.exact_ok) return;
+    if (*ws.serial) {
+        scatter_block(particles, M, cnt, off, total, err, out, idx_out, cap, count_out, status);
+        return;
+    }
     const int ns = *ws.nseg;
     for (int k = threadIdx.x; k < ns; k += blockDim.x) seg[k] = ws.segs[k];
     __syncthreads();
@@ -2264,21 +2285,16 @@ __global__ void set_flags_kernel(int* exact_ok, int* serial, int* err)
 // one thread walks it over tiles of weights the block stages in shared memory,
 // writing every particle's count and exclusive offset; the copies are made in
 // parallel afterwards.  A draw that stops advancing or a count beyond 4M + 16
-// (the reference would never finish) stops the walk and sets *err.  Runs only
-// when *run is set (neither parallel form applies).
-__global__ void __launch_bounds__(kChainThreads) systematic_chain_kernel(const float* __restrict__ w, int stride,
-                                                                         int M, float u0,
-                                                                         uint32_t* __restrict__ cnt,
-                                                                         uint32_t* __restrict__ off,
-                                                                         unsigned long long* total, int* err,
-                                                                         const int* run, const float* u0p)
+// (the reference would never finish) stops the walk and sets *err.  Run by
+// resample_sums_kernel's block when *ws.serial is set (neither parallel form
+// applies).
+__device__ void systematic_chain_block(const float* __restrict__ w, int stride, int M, float u0,
+                                       uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
+                                       unsigned long long* total, int* err)
 {
-    chain_enter();
-    if (u0p) u0 = *u0p;
     __shared__ float sw[kChainTile];
     __shared__ uint32_t sc[kChainTile], so[kChainTile];
     __shared__ int s_stop;
-    if (!*run) return;
     const double inv_m = 1.0 / (double)M;
     float u = u0;
     double s = 0.0;
@@ -2432,13 +2448,10 @@ __global__ void __launch_bounds__(kChainThreads) residual_chain_kernel(const flo
 
 // Copies particle m (7 floats) to its cnt[m] output slots below cap, or writes
 // its index there; thread 0 reports the count (and the chain's failure).
-__global__ void resample_scatter_kernel(const float* particles, int M, const uint32_t* cnt, const uint32_t* off,
-                                        const unsigned long long* total, const int* err, const int* run,
-                                        float* out, uint32_t* idx_out, long long cap, uint32_t* count_out,
-                                        int32_t* status)
+__device__ void scatter_block(const float* particles, int M, const uint32_t* cnt, const uint32_t* off,
+                              const unsigned long long* total, const int* err, float* out, uint32_t* idx_out,
+                              long long cap, uint32_t* count_out, int32_t* status)
 {
-    chain_enter();
-    if (run && !*run) return;
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (*err) {
         if (m == 0) {
@@ -2461,6 +2474,13 @@ __global__ void resample_scatter_kernel(const float* particles, int M, const uin
             for (int k = 0; k < 7; ++k) dst[k] = src[k];
         }
     }
+}
+
+__global__ void resample_scatter_kernel(const float* particles, int M, const uint32_t* cnt, const uint32_t* off,
+                                        const unsigned long long* total, const int* err, float* out,
+                                        uint32_t* idx_out, long long cap, uint32_t* count_out, int32_t* status)
+{
+    scatter_block(particles, M, cnt, off, total, err, out, idx_out, cap, count_out, status);
 }
 
 __global__ void set_int_kernel(int* p, int v) { *p = v; }
@@ -2927,17 +2947,12 @@ int launch_resample_impl(const float* particles, const float* w, int stride, siz
                    count_out, ws, status);
     // exact fallbacks: serial double sums + parallel assignment, else the literal loop
     launch_chained(resample_chunk_transfer_kernel, chunks ? chunks : 1u, kSumsThreads, 0, s, w, stride, (int)M, ws);
-    launch_chained(resample_sums_kernel, 1, kSumsThreads, 0, s, w, stride, (int)M, ws);
+    launch_chained(resample_sums_kernel, 1, kSumsThreads, 0, s, w, stride, (int)M, u0, ws, cnt, off, total, err);
     launch_chained(resample_chunk_write_kernel, chunks ? chunks : 1u, kSumsThreads, 0, s, w, stride, (int)M, ws);
-    launch_chained(resample_segments_sums_kernel, 1, 32, 0, s, (int)M, u0, ws);
-    launch_chained(resample_assign_sums_kernel, blocks, 256, 0, s, particles, (int)M, out, idx_out, (long long)cap,
-                   count_out, ws, status);
-    launch_chained(systematic_chain_kernel, 1, kChainThreads, 0, s, w, stride, (int)M, u0, cnt, off, total, err,
-                   ws.serial, u0p);
-    launch_chained(resample_scatter_kernel, blocks, 256, 0, s, particles, (int)M, (const uint32_t*)cnt,
-                   (const uint32_t*)off, (const unsigned long long*)total, (const int*)err, (const int*)ws.serial,
-                   out, idx_out, (long long)cap, count_out, status);
-    g_launches += 11;
+    launch_chained(resample_fallback_assign_kernel, blocks, 256, 0, s, particles, (int)M, out, idx_out,
+                   (long long)cap, count_out, ws, status, (const uint32_t*)cnt, (const uint32_t*)off,
+                   (const unsigned long long*)total, (const int*)err);
+    g_launches += 8;
     return check(cudaGetLastError());
 }
 
@@ -2953,8 +2968,8 @@ int launch_resample_residual(const float* particles, const float* w, int stride,
     set_int_kernel<<<1, 1, 0, s>>>(err, 0);
     residual_chain_kernel<<<1, kChainThreads, 0, s>>>(w, stride, (int)M, u0, cnt, off, total, err);
     resample_scatter_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(particles, (int)M, cnt, off, total, err,
-                                                                         nullptr, out, idx_out, (long long)cap,
-                                                                         count_out, status);
+                                                                         out, idx_out, (long long)cap, count_out,
+                                                                         status);
     g_launches += 3;
     return check(cudaGetLastError());
 }
