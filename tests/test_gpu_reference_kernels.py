@@ -1,7 +1,7 @@
 """The reference's own CUDA kernels (cudaEvaluateParticlesOrdered, compiled
 from the reference tree for sm_103a and loaded through the driver API) beside
-ours on the same GPU, timed on the room (C1) and building (C2) workloads (run
-with -s to see the timings).  Their raw weights follow the reference's GPU
+ours on the same GPU, timed on the room (C1), building (C2) and global
+localisation (C3) workloads (run with -s to see the timings).  Their raw weights follow the reference's GPU
 semantics, which differ from its CPU path that we reproduce: float-to-unsigned
 conversions saturate negative map offsets to 0 (a slot of the first brick
 where the CPU path misses), and sinf/cosf and FMA contraction change the
@@ -75,12 +75,14 @@ def ours(ctx, wl, parts):
     return raw, float(np.median(times[1:]))
 
 
-@pytest.mark.parametrize("name", ["room", "building"])
+@pytest.mark.parametrize("name", ["room", "building", "global"])
 def test_reference_kernels_beside_ours(name):
     if name == "room":
         wl = synth.room_workload(seed=1, n_particles=1024, n_points=2048)
-    else:
+    elif name == "building":
         wl = synth.building_workload(seed=2, n_particles=100_032, n_points=8192)
+    else:   # C3: 1M particles uniform over the building's free space
+        wl = synth.global_workload(seed=3, n_particles=1_000_000, n_points=2048)
     parts = np.ascontiguousarray(wl.particles, np.float32)
     assert parts.shape[0] % 64 == 0   # the reference kernel has no thread-index bound check
     ctx = Context(0)
