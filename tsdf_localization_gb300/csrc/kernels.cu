@@ -1852,7 +1852,7 @@ constexpr int kChainThreads = 512;
 // the end below the binade's top), so the margin only decides speed, never the
 // result.  Negative or non-finite weights set *ws.serial: only the literal loop
 // reproduces them.  With s monotone, the draws each particle emits then follow
-// from the draw segments in parallel (resample_assign_sums_kernel).
+// from the draw segments in parallel (resample_fallback_assign_kernel).
 // One weight in units u = 2^(b-52) of the running sum's binade [2^b, 2^(b+1)),
 // from the float's bits alone (integer shifts, no FP64 operation): q =
 // floor(w / u), whether the remainder is exactly half a unit (a tie) or above
