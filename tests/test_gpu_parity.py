@@ -319,8 +319,10 @@ def test_resample_bit_exact(ctx, m, kind):
     rs = SystematicResampler(ctx, seed=m)
     parts = rng.random((m, 7)).astype(np.float32)   # the same weights inside a particle cloud
     parts[:, 6] = w
-    for u0 in (0.0, float(np.float32(0.5 / m)), float(np.nextafter(np.float32(1.0 / m), np.float32(0))),
-               rs.draw(m)):
+    # u0 from 0 and subnormal values up to just below 1/M: the draws' segments
+    # cross many float binades before the first regular step
+    for u0 in (0.0, float(np.float32(1e-42)), float(np.float32(1e-30)), float(np.float32(0.5 / m)),
+               float(np.nextafter(np.float32(1.0 / m), np.float32(0))), rs.draw(m)):
         got = rs.resample_indices(w, u0)
         exp = O.resample_systematic(w, u0)
         assert got.shape == exp.shape
