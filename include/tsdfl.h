@@ -291,6 +291,11 @@ int tsdfl_batch_hits(tsdfl_batch* batch, size_t i, uint32_t* hits);
 /* Work in the persistent launch: segments, batches of work items, and the
  * filters scored outside it (maps without the tiled path). */
 int tsdfl_batch_info(const tsdfl_batch* batch, uint32_t* segments, uint32_t* batches, uint32_t* outside);
+/* Filters whose scans fill the GPU by themselves (about two of the
+ * single-filter kernel's work items per warp): the batch's update scores them
+ * with the single-filter kernel instead of the persistent launch, which
+ * measured faster per lookup; results are the same either way. */
+int tsdfl_batch_single(const tsdfl_batch* batch, uint32_t* single);
 
 /* ---- served sessions ----
  * No counterpart in the reference (mcl_3d runs one filter per process).  A

@@ -1,5 +1,6 @@
 """Batched filters (tsdfl_batch): many filters with uneven particle counts and
-scan sizes over several maps, scored in one persistent launch, give every
+scan sizes over several maps, scored in one persistent launch (filters that
+fill the GPU by themselves with the single-filter kernel), give every
 filter exactly its single-filter results -- weights, mean pose, resampled
 particles and counts, bit for bit -- eagerly, replayed from a captured CUDA
 graph, and after the autotuner changed the work-item shape."""
@@ -97,7 +98,9 @@ def test_gpu_batch_equals_single_filters(ctx, maps):
     fs, keep = make_filters(maps, SIZES, 10)
     b = FilterBatch(ctx, fs)
     info = b.info()
-    assert info["outside"] == 2 and info["segments"] >= 8
+    # two float-slot filters outside the tiled path, two that fill the GPU by
+    # themselves (single-filter kernel), the rest in the persistent launch
+    assert info["outside"] == 2 and info["single"] == 2 and info["segments"] >= 6
     torch.cuda.synchronize()
     b.run()
     ctx.sync()

@@ -140,6 +140,7 @@ SIGNATURES = [
     ("tsdfl_batch_autotune", I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(F)]),
     ("tsdfl_batch_hits", I, [P, SZ, P]),
     ("tsdfl_batch_info", I, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
+    ("tsdfl_batch_single", I, [P, C.POINTER(U32)]),
     ("tsdfl_server_create", I, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     ("tsdfl_server_destroy", I, [P]),
     ("tsdfl_session_open", I, [P, P, P, SZ, P, C.POINTER(Model), C.c_uint64, C.POINTER(U32)]),

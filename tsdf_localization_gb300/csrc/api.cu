@@ -1397,6 +1397,7 @@ struct tsdfl_batch {
         int npad = 4;
         bool tiled = false;
         bool dense = false;
+        bool big = false;            // scored by the single-filter kernel, not the persistent queue
         size_t pass = 0;
         int32_t* sticky = nullptr;   // where device errors of this filter go (null: the context's status)
     };
@@ -1432,8 +1433,12 @@ int batch_build_segments(tsdfl_batch* B, void* pinned = nullptr)
     return TSDFL_OK;
 }
 
-// Per-filter settings that depend on the filter's map and scan size.
-void per_configure(tsdfl_batch::Per& q, const tsdfl_filter& F)
+// Per-filter settings that depend on the filter's map and scan size.  A filter
+// whose first pass alone makes about two of the single-filter kernel's work
+// items per warp of the GPU is scored by that kernel (it fills the GPU by
+// itself, and measured faster per lookup than the persistent queue); the
+// queue takes the others, which alone would leave most SMs idle.
+void per_configure(tsdfl_batch::Per& q, const tsdfl_filter& F, int sm_count)
 {
     q.b.particles = F.d_particles;
     q.npad = (int)align_up(F.N, 4);
@@ -1453,6 +1458,12 @@ void per_configure(tsdfl_batch::Per& q, const tsdfl_filter& F)
         q.pass = (size_t)(tp > 0 ? tp : kMaxPassPoints);
     }
     if (!q.tiled) q.pass = (size_t)kMaxPassPoints;
+    q.big = false;
+    if (q.tiled && F.N) {
+        const size_t n1 = F.N < q.pass ? F.N : q.pass;
+        const unsigned long long items = (unsigned long long)((n1 + 1023) / 1024) * ((F.P + 3) / 4);
+        q.big = items >= 2ull * (unsigned long long)sm_count * (unsigned long long)tiled_warps_per_cta();
+    }
 }
 
 // The persistent launch's segments of filter i (one per pass).
@@ -1460,7 +1471,7 @@ void append_specs(tsdfl_batch* B, size_t i)
 {
     const tsdfl_filter& F = B->f[i];
     const tsdfl_batch::Per& q = B->per[i];
-    if (!q.tiled || !F.N) return;
+    if (!q.tiled || q.big || !F.N) return;
     for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
         BatchSegSpec sp;
         sp.m = F.map->view;
@@ -1477,17 +1488,32 @@ void append_specs(tsdfl_batch* B, size_t i)
 
 cudaStream_t batch_stream(const tsdfl_batch* B) { return B->stream ? B->stream : B->ctx->stream; }
 
-// Scoring of every filter: the persistent launch, then the filters it does not take.
+// Scoring of every filter: the persistent launch, the filters that fill the
+// GPU by themselves with the single-filter kernel (in their particle order for
+// a spread cloud), then the filters neither takes.
 int batch_score(tsdfl_batch* B, cudaStream_t s)
 {
     tsdfl_ctx* c = B->ctx;
     for (size_t i = 0; i < B->f.size(); ++i) {
-        if (!B->per[i].tiled || B->f[i].N == 0) continue;
+        if (!B->per[i].tiled || B->per[i].big || B->f[i].N == 0) continue;
         CUDA_TRY(cudaMemsetAsync(B->per[i].b.sum_fx, 0, sizeof(long long) * B->f[i].P, s));
         CUDA_TRY(cudaMemsetAsync(B->per[i].b.hits, 0, sizeof(uint32_t) * B->f[i].P, s));
     }
     int rc = launch_eval_batch(B->d_segs, B->kinds, B->d_counter, c->status, c->sm_count, s);
     if (rc) return rc;
+    for (size_t i = 0; i < B->f.size(); ++i) {   // pose_prepare_kernel cleared their sums
+        const tsdfl_filter& F = B->f[i];
+        const tsdfl_batch::Per& q = B->per[i];
+        if (!q.big || F.N == 0) continue;
+        rc = launch_particle_order(F.d_particles, (int)F.P, q.b, s);
+        if (rc) return rc;
+        for (size_t n0 = 0; n0 < F.N; n0 += q.pass) {
+            size_t n1 = n0 + q.pass < F.N ? n0 + q.pass : F.N;
+            rc = launch_eval_pass(F.map->view, F.model.a_hit, (int)F.P, (int)n0, (int)n1, (int)F.N, n0 == 0, false,
+                                  q.dense, false, q.b, q.sum_f64, c->sm_count, s);
+            if (rc) return rc;
+        }
+    }
     for (size_t i = 0; i < B->f.size(); ++i) {
         const tsdfl_filter& F = B->f[i];
         const tsdfl_batch::Per& q = B->per[i];
@@ -1604,7 +1630,7 @@ int tsdfl_batch_create(tsdfl_ctx* c, const tsdfl_filter* filters, size_t n, uint
         tsdfl_batch::Per& q = B->per[i];
         eval_layout(F.P, F.N, base + eval_off[i], &q.b, &q.sum_f64);
         q.rs_ws = base + rs_off[i];
-        per_configure(q, F);
+        per_configure(q, F, c->sm_count);
         append_specs(B, i);
     }
     if (B->specs.size() > 2 * n + 1) {   // more passes than the segment buffer holds: grow it
@@ -1781,6 +1807,15 @@ int tsdfl_batch_info(const tsdfl_batch* B, uint32_t* segments, uint32_t* batches
     return TSDFL_OK;
 }
 
+int tsdfl_batch_single(const tsdfl_batch* B, uint32_t* single)
+{
+    if (!B || !single) return TSDFL_ERR_INVALID_ARG;
+    uint32_t n = 0;
+    for (size_t i = 0; i < B->f.size(); ++i) n += (B->per[i].big && B->f[i].N) ? 1u : 0u;
+    *single = n;
+    return TSDFL_OK;
+}
+
 // ------------------------------------------------ served sessions
 
 struct tsdfl_server {
@@ -1948,7 +1983,7 @@ int server_launch(tsdfl_server* S, int k)
         F.d_count = sl.d_count + r;
         B.f.push_back(F);
         tsdfl_batch::Per pq = se.per;
-        per_configure(pq, F);
+        per_configure(pq, F, B.ctx->sm_count);
         pq.sticky = sl.d_status + r;
         B.per.push_back(pq);
         const size_t before = B.specs.size();

@@ -2668,6 +2668,8 @@ size_t tiled_smem_bytes(const MapView& m, bool dense, int n)
            sizeof(float4) * kRing * kTiledWarps;
 }
 
+int tiled_warps_per_cta() { return kTiledWarps; }
+
 int tiled_pass_points(const MapView& m, bool dense)
 {
     const size_t budget = 227 * 1024 - 1024;   // dynamic shared memory left beside the static part

@@ -231,6 +231,8 @@ size_t eval_smem_bytes(bool serial, int n);
 // Scan points one pass of the tiled kernel stages (0: the kernel cannot hold
 // this map's occupancy bitmap beside any points).
 int tiled_pass_points(const MapView& m, bool dense);
+// Warps per CTA of the tiled scoring kernel (one CTA per SM).
+int tiled_warps_per_cta();
 int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n_total, bool first, bool serial,
                      bool dense, bool generic, const EvalBuffers& b, double* sum_f64, int sm_count, cudaStream_t s);
 // nin: per-particle points within max_range when the particles scored

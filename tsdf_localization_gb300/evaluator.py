@@ -522,7 +522,9 @@ class FilterBatch:
     def info(self):
         a, b, o = C.c_uint32(), C.c_uint32(), C.c_uint32()
         N.check(N.lib().tsdfl_batch_info(self.handle, C.byref(a), C.byref(b), C.byref(o)))
-        return {"segments": a.value, "batches": b.value, "outside": o.value}
+        n1 = C.c_uint32()
+        N.check(N.lib().tsdfl_batch_single(self.handle, C.byref(n1)))
+        return {"segments": a.value, "batches": b.value, "outside": o.value, "single": n1.value}
 
     def close(self) -> None:
         if getattr(self, "handle", None):
