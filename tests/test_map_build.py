@@ -9,8 +9,9 @@ table, every slot's value bit for bit and the free-space cells -- with the
 oracle's createTSDFMap restatement and, where the reference's sources were
 compiled on this machine, with the reference's own map built from the same
 tuples.  The worlds are the bench's and the batch's: a room at 0.064 m (the
-reference's 64-cell chunks) and at 0.05 m, the 100x100x10 m building at 0.05 m
-in 8^3 chunks, a warehouse and a tunnel at 0.1 m in 16^3 chunks.
+reference's 64-cell chunks) and at 0.05 m, a 25 x 25 m part of the
+100x100x10 m building at 0.05 m in 8^3 chunks, a warehouse and a tunnel at
+0.1 m in 16^3 chunks.
 """
 import numpy as np
 import pytest
@@ -45,18 +46,25 @@ def test_code_values_equal_oracle_likelihood(sigma):
     assert vals[0] == vals.max()
 
 
+# (name, world, seed, voxel mm, chunk edge, chunks kept along x and y from the
+# low corner or None for all): the building is checked on a 25 x 25 m part of
+# its chunks (every floor, the same cells and chunking), which runs in a tenth
+# of the whole building's time.
 WORLDS = [
-    ("room@0.064/64", synth.ROOM, 4, 64, 64),
-    ("room@0.05/8", synth.ROOM, 21, 50, 8),
-    ("building@0.05/8", synth.BUILDING, 2, 50, 8),
-    ("warehouse@0.1/16", synth.WAREHOUSE, 23, 100, 16),
-    ("tunnel@0.1/16", synth.TUNNEL, 24, 100, 16),
+    ("room@0.064/64", synth.ROOM, 4, 64, 64, None),
+    ("room@0.05/8", synth.ROOM, 21, 50, 8, None),
+    ("building@0.05/8 25x25m", synth.BUILDING, 2, 50, 8, 62),
+    ("warehouse@0.1/16", synth.WAREHOUSE, 23, 100, 16, None),
+    ("tunnel@0.1/16", synth.TUNNEL, 24, 100, 16, None),
 ]
 
 
-@pytest.mark.parametrize("name,kind,seed,voxel_mm,edge", WORLDS, ids=[w[0] for w in WORLDS])
-def test_map_build_equals_oracle_and_reference(name, kind, seed, voxel_mm, edge):
+@pytest.mark.parametrize("name,kind,seed,voxel_mm,edge,crop", WORLDS, ids=[w[0] for w in WORLDS])
+def test_map_build_equals_oracle_and_reference(name, kind, seed, voxel_mm, edge, crop):
     pos, raw = synth.World(kind, seed).tsdf_chunks(voxel_mm, edge)
+    if crop is not None:
+        keep = (pos[:, 0] < pos[:, 0].min() + crop) & (pos[:, 1] < pos[:, 1].min() + crop)
+        pos, raw = pos[keep], raw[keep]
     pos, raw = _named_order(pos, raw)
     coef, grid_occ, codes, free_xyz = build_map_codes(pos, raw, edge, voxel_mm, 0.1, want_free=True)
     om, ofree = O.OracleMap.from_chunks(pos, raw, voxel_mm, 0.1, edge=edge)
