@@ -1312,6 +1312,32 @@ struct NormParams {
     const uint32_t* nin; // per-particle points within max_range (subsampled scans), else null
 };
 
+// The block's sums of ten values per thread (blockDim.x == kNormThreads), in a
+// fixed order: the values go to shared memory, 160 threads add sixteen each,
+// ten threads add those sixteen partial sums.  Few FP64 instructions: a
+// warp-shuffle tree would spend five FP64 additions a warp for every sum, and
+// GB300's FP64 pipe is narrow.  Valid in threads 0..9 (out[k]).
+constexpr int kNormSumsParts = 16;
+static_assert(kNormSums * kNormSumsParts <= kNormThreads && kNormThreads % kNormSumsParts == 0,
+              "the block's threads cover the partial sums");
+__device__ __forceinline__ double block_sums10(const double (&acc)[kNormSums], double (*red)[kNormThreads],
+                                               double (*red2)[kNormSumsParts])
+{
+    for (int k = 0; k < kNormSums; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < kNormSums * kNormSumsParts) {
+        const int k = threadIdx.x / kNormSumsParts, part = threadIdx.x % kNormSumsParts;
+        double v = 0.0;
+        for (int j = 0; j < kNormThreads / kNormSumsParts; ++j) v += red[k][part + kNormSumsParts * j];
+        red2[k][part] = v;
+    }
+    __syncthreads();
+    double v = 0.0;
+    if (threadIdx.x < kNormSums)
+        for (int j = 0; j < kNormSumsParts; ++j) v += red2[threadIdx.x][j];
+    return v;
+}
+
 // Forms each particle's un-normalised weight from its likelihood sum and
 // accumulates, in double and in a fixed order, the weight sum and the
 // weighted pose sums of tsdf_evaluator.cpp:198-217.
@@ -1347,17 +1373,10 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
         acc[8] += (double)tg[4] * w;
         acc[9] += (double)tg[5] * w;
     }
-    __shared__ double red[kNormSums][kNormThreads / 32];
-    for (int k = 0; k < kNormSums; ++k) {
-        double v = warp_sum_d(acc[k]);
-        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kNormSums) {
-        double v = 0.0;
-        for (int w = 0; w < kNormThreads / 32; ++w) v += red[threadIdx.x][w];
-        b.partials[blockIdx.x * kNormSums + threadIdx.x] = v;
-    }
+    __shared__ double red[kNormSums][kNormThreads];
+    __shared__ double red2[kNormSums][kNormSumsParts];
+    const double v = block_sums10(acc, red, red2);
+    if (threadIdx.x < kNormSums) b.partials[blockIdx.x * kNormSums + threadIdx.x] = v;
 }
 
 // Final weight sum, the "No particle is valid!" check (tsdf_evaluator.cpp:159)
@@ -1368,17 +1387,15 @@ __global__ void norm_partial_kernel(NormParams q, EvalBuffers b, const double* s
 __global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, float* pose_out, int nb)
 {
     chain_enter();
-    __shared__ double red[kNormSums][kNormBlocks / 32];
+    static_assert(kNormBlocks == kNormThreads, "one partial per thread");
+    __shared__ double red[kNormSums][kNormThreads];
+    __shared__ double red2[kNormSums][kNormSumsParts];
     __shared__ double s[kNormSums];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    for (int k = 0; k < kNormSums; ++k) {
-        const double v = warp_sum_d(t < nb ? b.partials[t * kNormSums + k] : 0.0);
-        if (lane == 0) red[k][warp] = v;
-    }
-    __syncthreads();
+    const int t = threadIdx.x;
+    double acc[kNormSums];
+    for (int k = 0; k < kNormSums; ++k) acc[k] = t < nb ? b.partials[t * kNormSums + k] : 0.0;
+    const double v = block_sums10(acc, red, red2);
     if (t < kNormSums) {
-        double v = 0.0;
-        for (int w = 0; w < kNormBlocks / 32; ++w) v += red[t][w];
         s[t] = v;
         b.sums[t] = v;
     }
