@@ -1642,14 +1642,22 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
     double U = (double)u0;
     long long j = 0;
     int ns = 0;
-    for (int iter = 0; U < s_total; ++iter) {
+    if (!(s_total >= 0.0) || !(s_total < INFINITY)) {   // no sum of non-negative finite weights
+        *ws.nseg = 0;
+        return false;
+    }
+    // the draws' and the sums' doubles are compared on their bits (a sum here
+    // is >= +0, and a double >= +0 orders like its bits as a signed integer)
+    const long long s_bits = __double_as_longlong(s_total);
+    const long long kFltMinBits = 0x3810000000000000ll;   // 2^-126, the smallest normal float
+    for (int iter = 0; __double_as_longlong(U) < s_bits; ++iter) {
         if (ns == kMaxSegments || iter > 4 * kMaxSegments) { ok = false; break; }
         bool regular = false;
         long long cnt = 0;
         int e = 0;
         unsigned long long Ui = 0, D = 0;
         double delta = 0.0;
-        if (U >= 1.17549435e-38) {   // normal float: binade [2^e, 2^(e+1))
+        if (__double_as_longlong(U) >= kFltMinBits) {   // normal float: binade [2^e, 2^(e+1))
             const unsigned long long ub = (unsigned long long)__double_as_longlong(U);
             e = (int)((ub >> 52) & 0x7ff) - 1023;
             Ui = (ub & ((1ull << 52) - 1ull)) | (1ull << 52);   // U in units g = 2^(e-52)
@@ -1679,7 +1687,11 @@ __device__ bool build_segments(int M, float u0, double s_total, ResampleWs ws)
                 const unsigned long long R = (Y >> 29) + (low > kHalf29 ? 1ull : 0ull);
                 if (R == 0) { ok = false; break; }        // U would stop advancing
                 D = R << 29;
-                delta = (double)R * pow2(e - 23);   // exact: R < 2^25
+                {   // delta = R 2^(e-23), built from its bits (R < 2^25)
+                    const int lz = __clzll((long long)R);
+                    delta = __longlong_as_double(((long long)(63 - lz + e - 23 + 1023) << 52) |
+                                                 (long long)((R << (lz - 11)) & ((1ull << 52) - 1ull)));
+                }
                 // values U + i delta below top = 2^(e+1) - Y g take the regular step
                 const unsigned long long T = kTop - Y;
                 if (Ui < T) {
