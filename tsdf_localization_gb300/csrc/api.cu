@@ -656,10 +656,8 @@ int run_eval(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, float* 
         c->timed = true;
     }
     const int mode = serial ? 2 : (map->view.storage != 0 ? 1 : 0);
-    rc = launch_norm((int)P, mode, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)N, c->sum_f64,
-                     d_particles, d_pose, b, s, nullptr, (flags & TSDFL_NORM_LOG) != 0);
-    if (rc) return rc;
-    return launch_fold_status(c->status + 1, c->status, s);
+    return launch_norm((int)P, mode, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)N, c->sum_f64,
+                       d_particles, d_pose, b, s, c->status, nullptr, (flags & TSDFL_NORM_LOG) != 0);
 }
 
 // Seeded per-particle subsampling: K of the N points per particle
@@ -701,10 +699,8 @@ int run_eval_sub(tsdfl_ctx* c, const tsdfl_map* map, const tsdfl_model* mdl, flo
         CUDA_TRY(cudaEventRecord(c->ev1, s));
         c->timed = true;
     }
-    rc = launch_norm((int)P, 0, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)K, c->sum_f64,
-                     d_particles, d_pose, b, s, b.nin);
-    if (rc) return rc;
-    return launch_fold_status(c->status + 1, c->status, s);
+    return launch_norm((int)P, 0, shift, (double)mdl->a_hit, (double)c_in, (double)c_out, (int)K, c->sum_f64,
+                       d_particles, d_pose, b, s, c->status, b.nin);
 }
 
 int check_sub_args(const char* fn, size_t P, size_t N, size_t K)
@@ -1552,11 +1548,9 @@ int batch_record(tsdfl_batch* B)
         const float inv_max_range = (float)(1.0 / (double)F.model.max_range);
         const float c_in = F.model.a_range * inv_max_range;
         const int mode = F.map->view.storage != 0 ? 1 : 0;
-        rc = launch_norm((int)F.P, mode, q.shift, (double)F.model.a_hit, (double)c_in, (double)F.model.a_max,
-                         (int)F.N, q.sum_f64, F.d_particles, F.d_pose_out, q.b, s);
-        if (rc) return rc;
         int32_t* sticky = q.sticky ? q.sticky : c->status;
-        rc = launch_fold_status(q.b.status, sticky, s);
+        rc = launch_norm((int)F.P, mode, q.shift, (double)F.model.a_hit, (double)c_in, (double)F.model.a_max,
+                         (int)F.N, q.sum_f64, F.d_particles, F.d_pose_out, q.b, s, sticky);
         if (rc) return rc;
         if (F.d_u0 && F.d_resampled && F.P)
             rc = launch_resample_impl(F.d_particles, F.d_particles + 6, 7, F.P, 0.0f, F.d_resampled, nullptr,

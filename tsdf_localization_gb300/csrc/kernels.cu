@@ -1419,9 +1419,20 @@ __global__ void __launch_bounds__(kNormBlocks) norm_final_kernel(EvalBuffers b, 
 
 // particles[i].second = raw / weight_sum (tsdf_evaluator.cpp:203), skipped when
 // the sum was degenerate so the caller's particles stay untouched.
-__global__ void normalize_kernel(int P, EvalBuffers b, float* particles_out)
+// Also the last step of an evaluation: thread 0 carries its device status into
+// the sticky status word (when one is given and still clear).
+__device__ __forceinline__ void fold_status(const int32_t* ev, int32_t* sticky)
+{
+    if (sticky && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int v = *ev;
+        if (v && *sticky == 0) *sticky = v;
+    }
+}
+
+__global__ void normalize_kernel(int P, EvalBuffers b, float* particles_out, int32_t* sticky)
 {
     chain_enter();
+    fold_status(b.status, sticky);
     if (*b.status == TSDFL_ERR_DEGENERATE) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
@@ -1476,8 +1487,9 @@ __global__ void __launch_bounds__(kNormBlocks) log_final_kernel(EvalBuffers b)
     }
 }
 
-__global__ void normalize_log_kernel(int P, EvalBuffers b, float* particles_out)
+__global__ void normalize_log_kernel(int P, EvalBuffers b, float* particles_out, int32_t* sticky)
 {
+    fold_status(b.status, sticky);
     if (*b.status == TSDFL_ERR_DEGENERATE) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
@@ -2540,14 +2552,6 @@ __global__ void best_index_kernel(const unsigned long long* key, uint32_t* index
     *index_out = k ? 0xffffffffu - (uint32_t)(k & 0xffffffffu) : 0xffffffffu;
 }
 
-// Carries a per-evaluation error into the context's sticky status word.
-__global__ void fold_status_kernel(int32_t* ev, int32_t* sticky)
-{
-    chain_enter();
-    int v = *ev;
-    if (v && *sticky == 0) *sticky = v;
-}
-
 // ------------------------------------------------------------- map layouts
 
 __global__ void halves_kernel(const uint16_t* codes, const float* values, const float* data, size_t n,
@@ -2907,7 +2911,7 @@ int launch_eval_batch(const void* d_segs, const BatchKinds& kinds, uint32_t* cou
 
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s,
-                const uint32_t* nin, bool log_domain)
+                int32_t* sticky, const uint32_t* nin, bool log_domain)
 {
     // one block per kNormThreads particles, at most kNormBlocks: the block count
     // depends on P alone, so the sums' order does too
@@ -2921,19 +2925,12 @@ int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_
         log_max_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(P, b);
         log_sum_kernel<<<kNormBlocks, kNormThreads, 0, s>>>(P, b);
         log_final_kernel<<<1, kNormBlocks, 0, s>>>(b);
-        normalize_log_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out);
+        normalize_log_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, b, particles_out, sticky);
         g_launches += 4;
     } else if (P > 0) {
-        launch_chained(normalize_kernel, (unsigned)((P + 255) / 256), 256, 0, s, P, b, particles_out);
+        launch_chained(normalize_kernel, (unsigned)((P + 255) / 256), 256, 0, s, P, b, particles_out, sticky);
         g_launches += 1;
     }
-    return check(cudaGetLastError());
-}
-
-int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s)
-{
-    launch_chained(fold_status_kernel, 1, 1, 0, s, eval_status, sticky);
-    g_launches += 1;
     return check(cudaGetLastError());
 }
 

@@ -238,15 +238,16 @@ int launch_eval_pass(const MapView& m, float a_hit, int P, int n0, int n1, int n
 // nin: per-particle points within max_range when the particles scored
 // different point subsets (n_points each), else null (the scan's count).
 // log_domain: weights from ln raw - LSE in double (TSDFL_NORM_LOG).
+// sticky: where the evaluation's device status is carried at its end (the
+// context's or the filter's sticky word).
 int launch_norm(int P, int mode, int shift, double a_hit, double c_in, double c_out, int n_points,
                 const double* sum_f64, float* particles_out, float* pose_out, const EvalBuffers& b, cudaStream_t s,
-                const uint32_t* nin = nullptr, bool log_domain = false);
+                int32_t* sticky, const uint32_t* nin = nullptr, bool log_domain = false);
 // Seeded per-particle subsampling (subsample.h): K of the N staged points per
 // particle, exact fixed-point sums, hits and in-range counts into b.sum_fx,
 // b.hits, b.nin.  Needs a map on the tiled path (TSDFL_ERR_UNSUPPORTED else).
 int launch_eval_subsample(const MapView& m, float a_hit, int P, int N, int K, unsigned long long seed, float c_in,
                           const EvalBuffers& b, int sm_count, cudaStream_t s);
-int launch_fold_status(int32_t* eval_status, int32_t* sticky, cudaStream_t s);
 
 // Many filters' scoring in one persistent launch (eval_batch_kernel).  One
 // segment per (filter, pass) of a filter whose map takes the tiled path.
