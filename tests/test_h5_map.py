@@ -4,9 +4,15 @@ files written byte by byte from the HDF5 file format specification
 groups, version 1 object headers: the reference's case) and the latest
 (superblock 2, compact link messages, version 2 object headers).
 
-No HDF5 file written by the HDF5 library itself (or by the reference) exists
-on this machine, so compatibility with such files rests on the specification:
-parity of this row is unpinned."""
+No map file written by the reference exists on this machine.  The one file
+here that the HDF5 library itself wrote (SciPy's MATLAB 7.3 test file) pins
+the structures the library writes by default, which are those of the
+reference's map files: the reader walks it and finds its dataset's type,
+shape, storage and values.  The "/map" layout itself rests on the reference's
+writer code (global_map.cpp)."""
+import subprocess
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -211,3 +217,43 @@ def test_version2_checksums_verified(tmp_path, superblock, where):
     with pytest.raises(TsdflError) as e:
         read_map_h5(bad)
     assert e.value.code == N.TSDFL_ERR_INVALID_ARG and "checksum" in str(e.value)
+
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _libhdf5_file():
+    """SciPy's MATLAB 7.3 test file, written by the HDF5 library: a 512-byte
+    MATLAB header as the user block, then the library's default structures
+    (superblock 0, a symbol-table root group, version 1 object headers, a
+    contiguous dataset).  Its one variable is SciPy's ``testdouble`` case,
+    pi/4 * (0..8) as a 1x9 double (scipy/io/matlab/tests/test_mio.py)."""
+    mio = pytest.importorskip("scipy.io.matlab")
+    p = Path(mio.__file__).parent / "tests" / "data" / "testhdf5_7.4_GLNX86.mat"
+    if not p.exists():
+        pytest.skip("SciPy's HDF5 test file is not installed")
+    return p
+
+
+def test_reader_walks_a_file_written_by_libhdf5(tmp_path):
+    src = _libhdf5_file()
+    exe = tmp_path / "h5_walk"
+    subprocess.run(["g++", "-O1", "-std=c++17", "-I", str(ROOT / "include"),
+                    "-I", str(ROOT / "tsdf_localization_gb300" / "csrc"),
+                    str(ROOT / "tests" / "native" / "h5_walk.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), str(src)], capture_output=True, text=True, check=True).stdout.splitlines()
+    links = [ln.split() for ln in out if ln.startswith("link ")]
+    assert len(links) == 1, out
+    f = links[0]
+    assert f[1] == "testdouble", out
+    got = dict(zip(f[2::2], f[3::2]))
+    # floating point, 8 bytes, little-endian; MATLAB's 1x9 stored column-major as 9x1
+    assert (got["class"], got["elem"], got["order"], got["dims"]) == ("1", "8", "le", "9,1"), out
+    data = src.read_bytes()
+    at = int(got["address"])
+    assert at >= 512   # addresses are relative to the superblock after the user block
+    values = np.frombuffer(data[at:at + 72], "<f8")
+    assert np.array_equal(values, np.pi / 4 * np.arange(9, dtype=float))
+    # the map entry point reads the same file and reports the missing group
+    status = [ln for ln in out if ln.startswith("map ")][0].split(maxsplit=4)
+    assert int(status[1]) == N.TSDFL_ERR_INVALID_ARG and 'no object "map"' in status[4], out

@@ -10,13 +10,14 @@
 // specification: superblock versions 0 to 3; object header versions 1 and 2
 // with their continuation blocks; groups stored as symbol tables (version 1
 // B-tree of group nodes, local heap, symbol table nodes) or as compact link
-// messages; dataspace, datatype (4-byte fixed point, either byte order), fill
-// value and data layout (contiguous or compact) messages.  Dense link storage,
-// chunked, filtered or external datasets are reported as unsupported.  The
-// checksums of the version 2 structures read (superblock versions 2 and 3,
-// version 2 object headers and their continuation blocks) are verified: the
-// format's metadata checksum is Bob Jenkins' lookup3 hash ("hashlittle",
-// published 2006) of the structure's bytes with initial value 0.
+// messages; dataspace, datatype (class, size and byte order; a map chunk must
+// be 4-byte fixed point), fill value and data layout (contiguous or compact)
+// messages.  Dense link storage, chunked, filtered or external datasets are
+// reported as unsupported.  The checksums of the version 2 structures read
+// (superblock versions 2 and 3, version 2 object headers and their
+// continuation blocks) are verified: the format's metadata checksum is Bob
+// Jenkins' lookup3 hash ("hashlittle", published 2006) of the structure's
+// bytes with initial value 0.
 #include <algorithm>
 #include <cctype>
 #include <cerrno>
@@ -105,10 +106,13 @@ struct Msg {
 };
 
 struct DatasetInfo {
+    std::vector<uint64_t> dims;   // dataspace extents, slowest first
     uint64_t count = 0;     // elements
+    int type_class = -1;    // datatype class: 0 fixed point, 1 floating point, ...
+    uint32_t elem = 0;      // bytes per element
     uint64_t address = kUndef;   // absolute file position of the data, kUndef: none stored
     bool big_endian = false;
-    uint32_t fill = 0;
+    uint32_t fill = 0;      // fill value of a 4-byte type
     std::vector<uint8_t> compact;   // compact layout: the data itself
 };
 
@@ -269,7 +273,9 @@ public:
         fail(TSDFL_ERR_INVALID_ARG, "no object \"" + name + "\"");
     }
 
-    DatasetInfo dataset(uint64_t addr) const
+    // The dataset whose object header is at addr: its dataspace, element type
+    // and storage, checked against the file's size.
+    DatasetInfo describe(uint64_t addr) const
     {
         DatasetInfo info;
         bool have_space = false, have_type = false, have_layout = false;
@@ -294,10 +300,12 @@ public:
                     fail(TSDFL_ERR_UNSUPPORTED, "dataspace version " + std::to_string(ver));
                 }
                 need(q + (size_t)rank * sl_);
+                info.dims.clear();
                 for (int r = 0; r < rank; ++r) {
                     const uint64_t dim = len(d.data() + q + (size_t)r * sl_);
                     if (dim && n > UINT64_MAX / dim) fail(TSDFL_ERR_INVALID_ARG, "dataspace too large");
                     n *= dim;
+                    info.dims.push_back(dim);
                 }
                 info.count = n;
                 have_space = true;
@@ -305,9 +313,10 @@ public:
             }
             case 0x03: {   // datatype
                 need(8);
-                if ((d[0] & 0x0f) != 0) fail(TSDFL_ERR_UNSUPPORTED, "datasets of a non-integer type");
-                if (le(d.data() + 4, 4) != 4) fail(TSDFL_ERR_UNSUPPORTED, "integers of other than 4 bytes");
-                info.big_endian = (d[1] & 1) != 0;
+                info.type_class = d[0] & 0x0f;
+                info.elem = (uint32_t)le(d.data() + 4, 4);
+                if (info.elem == 0) fail(TSDFL_ERR_INVALID_ARG, "datatype of 0 bytes");
+                info.big_endian = (d[1] & 1) != 0;   // byte order of the fixed- and floating-point classes
                 have_type = true;
                 break;
             }
@@ -393,12 +402,22 @@ public:
             }
         }
         if (!have_space || !have_type || !have_layout) fail(TSDFL_ERR_INVALID_ARG, "object is not a dataset");
-        if (info.count > UINT64_MAX / 4 || (layout_size != UINT64_MAX && layout_size < 4 * info.count))
+        const uint64_t e = info.elem;
+        if (info.count > UINT64_MAX / e || (layout_size != UINT64_MAX && layout_size < e * info.count))
             fail(TSDFL_ERR_INVALID_ARG, "dataset storage smaller than its dataspace");
-        if (info.address != kUndef && (info.address > size_ || 4 * info.count > size_ - info.address))
+        if (info.address != kUndef && (info.address > size_ || e * info.count > size_ - info.address))
             fail(TSDFL_ERR_INVALID_ARG, "dataset storage outside the file");
         if (info.address == kUndef && info.compact.empty() && info.count > kMaxCells)
             fail(TSDFL_ERR_INVALID_ARG, "dataset without storage larger than a chunk can be");
+        return info;
+    }
+
+    // A map chunk: a dataset of 4-byte integers (tsdf.h:11-33, TSDFValue's raw word).
+    DatasetInfo dataset(uint64_t addr) const
+    {
+        DatasetInfo info = describe(addr);
+        if (info.type_class != 0) fail(TSDFL_ERR_UNSUPPORTED, "datasets of a non-integer type");
+        if (info.elem != 4) fail(TSDFL_ERR_UNSUPPORTED, "integers of other than 4 bytes");
         return info;
     }
 
